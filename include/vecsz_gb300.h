@@ -1,0 +1,233 @@
+/*
+ * vecsz_gb300.h -- C ABI of the GB300-native dual-quantization compressor (the SZ / vecSZ path).
+ *
+ * Every entry point takes plain pointers and sizes.  Device pointers are named d_*, host pointers
+ * h_*; `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).  Device-side
+ * entry points are stream-ordered and do not synchronise unless their comment says so.
+ *
+ * Field layout is the reference's: dims[0] is the fastest axis (x), dims[1] y, dims[2] z; a field
+ * with ndim < 3 ignores the trailing dims.  dict_size is the reference's `-d` (quantization radius
+ * = dict_size / 2), block_size its `-b`, eb its `-e`, mode its `-m`.
+ *
+ * Each entry point names the reference function (szcompressor/vecSZ, file:line) it replaces.
+ * The ctypes bindings a Python caller uses, and the C++ a host caller adds, are in INTEGRATION.md.
+ */
+#ifndef VECSZ_GB300_H
+#define VECSZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: the reference calls exit(); every entry point here returns one --------- */
+typedef int vsz_status;
+#define VSZ_OK 0
+#define VSZ_ERR_INVALID 1     /* bad argument (dims, eb, dict_size, block_size, null pointer) */
+#define VSZ_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define VSZ_ERR_CORRUPT 3     /* archive or bitstream does not parse */
+#define VSZ_ERR_CAPACITY 4    /* caller buffer or workspace too small */
+#define VSZ_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
+#define VSZ_ERR_UNSUPPORTED 6 /* accepted by the reference, not supported here (documented) */
+#define VSZ_ERR_RANGE 7       /* r2r with zero value range: the reference exits (src/types.cc:51-54) */
+#define VSZ_ERR_NOMEM 8       /* device or host allocation failed */
+#define VSZ_ERR_NO_DEVICE 9   /* no CUDA device */
+
+#define VSZ_MODE_ABS 0 /* -m abs */
+#define VSZ_MODE_R2R 1 /* -m r2r: eb relative to the value range */
+
+#define VSZ_LOSSLESS_NONE 0
+#define VSZ_LOSSLESS_ZSTD 1 /* -L zstd: host library, level 3 (src/lossless.hh:179-200) */
+#define VSZ_LOSSLESS_GZIP 2 /* -L gzip: host library, level 3 */
+
+/* Compression settings: the ArgParse fields that reach the path
+ * (src/argument_parser/argparse.hh:62-77; reference defaults eb 1e-4, dict 4096, block 8). */
+typedef struct vsz_params {
+    double eb;      /* -e */
+    int mode;       /* -m: VSZ_MODE_ABS | VSZ_MODE_R2R */
+    int dict_size;  /* -d: number of quant bins, even, 2..65536 */
+    int block_size; /* -b: Lorenzo block edge: 8, 16, 32 or 64 */
+    int lossless;   /* -L: VSZ_LOSSLESS_* (applied by the host entry points only) */
+} vsz_params;
+
+/* What a compress produced (device-side vsz_compress writes these 8 u64 into d_result). */
+typedef struct vsz_result {
+    uint64_t data_size;    /* bytes of the packed block (the reference's data_size) */
+    uint64_t trailer_size; /* bytes of this library's index trailer after the packed block */
+    uint64_t n_outlier;    /* the reference's num_outlier */
+    uint64_t huff_bytes;   /* Huffman section: 8 + tree bytes + payload */
+    uint64_t payload_bits; /* Huffman bitstream length */
+    uint64_t status;       /* VSZ_OK or the first device-side error */
+    uint64_t max_code_len; /* longest codeword of the tree */
+    uint64_t node_count;   /* Huffman tree nodes (2 * used symbols - 1) */
+} vsz_result;
+
+/* Parsed archive: the reference's packed block (src/utils/datapack.hh:17-56) plus, when present,
+ * this library's trailer (r2r-final eb, block size, dict size and a decode index). */
+typedef struct vsz_archive_desc {
+    int ndim;
+    uint64_t dims[3];
+    double eb;              /* eb field of the packed block: the user's eb */
+    uint64_t n_pad, huff_bytes, n_outlier;
+    uint64_t header_bytes;  /* 4 (ndim + 1) + 8 + 24 */
+    uint64_t huff_offset;   /* byte offset of the Huffman section */
+    uint32_t node_count;
+    uint64_t tree_bytes;
+    uint64_t payload_offset;
+    uint64_t payload_bytes;
+    uint64_t outlier_offset;
+    uint64_t data_size;     /* packed block bytes */
+    int has_trailer;
+    double eb_final;        /* trailer: absolute eb actually used */
+    double value_range;     /* trailer: r2r value range (0 for abs) */
+    int mode, dict_size, block_size;
+    uint32_t chunk_syms;    /* trailer: codewords per index entry */
+    uint64_t n_chunks;
+    uint64_t index_offset;  /* trailer: byte offset of u16 bits-per-chunk, 8-byte aligned */
+    uint64_t trailer_size;
+} vsz_archive_desc;
+
+/* Options a decompressor needs that the packed block does not store (the reference takes them
+ * from the command line, src/vecsz_interface.hh:270-285).  Ignored where the trailer has them. */
+typedef struct vsz_decompress_opts {
+    int dict_size;      /* -d used at compression */
+    int block_size;     /* -b used at compression */
+    int mode;           /* -m used at compression */
+    double value_range; /* r2r: value range of the original field (the reference re-reads it) */
+} vsz_decompress_opts;
+
+/* Size in bytes of the device-resident constant block written by vsz_eb_setup. */
+#define VSZ_CONSTS_BYTES 64
+
+const char* vsz_status_string(vsz_status status);
+const char* vsz_version(void);
+
+/* =============================================================================================
+ * Stage-level entry points (device buffers).  Each replaces one reference routine; together they
+ * are the compress/decompress workflow of src/vecsz_interface.hh.
+ * ============================================================================================= */
+
+/* Error-bound family on the device.  r2r: min/max pass over d_in, range = (float)max - (float)min.
+ * Replaces GetDatumValueRange (src/types.cc:28-35), ChangeToRelativeMode (:49-60) and
+ * InitializeErrorBoundFamily (:84-92).  d_consts: VSZ_CONSTS_BYTES; d_tmp: 16 bytes. */
+vsz_status vsz_eb_setup(const vsz_params* p, const float* d_in, size_t n, void* d_consts, void* d_tmp, void* stream);
+/* Reads {eb_final, 2 eb, 1/(2 eb), value range} and the constants' status.  Synchronises. */
+vsz_status vsz_consts_read(const void* d_consts, double h_out[4], int* h_status, void* stream);
+
+/* Number of 128-wide row segments used to rank outliers: d1 * d2 * ceil(d0 / 128). */
+size_t vsz_outlier_segments(int ndim, const size_t dims[3]);
+
+/* Prequant + Lorenzo + quant codes, fused with the code histogram and per-segment outlier
+ * ranking.  Replaces c_lorenzo_{1,2,3}d1l (src/dualquant.hh:19-913) and the histogram loop of
+ * initHuffman (src/huffman.hh:239-242).  d_code: n u16; d_scratch: segments * 128 floats;
+ * d_seg_count: segments bytes; d_hist: dict_size u64, accumulated (zero it first). */
+vsz_status vsz_dualquant(int ndim, const size_t dims[3], int block_size, int dict_size, const float* d_in,
+                         const void* d_consts, uint16_t* d_code, float* d_scratch, uint8_t* d_seg_count,
+                         uint64_t* d_hist, void* stream);
+
+/* Outlier values in row-major order of code == 0 (src/vecsz_interface.hh:166-170) into d_out
+ * (aligned floats); *d_count = their number.  d_tmp: vsz_outlier_gather_tmp_bytes. */
+size_t vsz_outlier_gather_tmp_bytes(int ndim, const size_t dims[3]);
+vsz_status vsz_outlier_gather(int ndim, const size_t dims[3], const uint8_t* d_seg_count, const float* d_scratch,
+                              float* d_out, uint64_t* d_count, void* d_tmp, size_t tmp_bytes, void* stream);
+
+/* Heap-tree Huffman codebook from a histogram, bit-identical to initHuffman + build_code +
+ * convert_HuffTree_to_bytes_anyStates (src/huffman.hh:116-266, 374-502).
+ * d_codebook: vsz_codebook_bytes(dict); d_huff_head: 8 + tree bytes, [BE nodeCount][BE dict][tree]
+ * (capacity vsz_huff_head_max(dict)); d_info: 4 u32 {node count, tree bytes, max len, nodes}. */
+size_t vsz_codebook_bytes(int dict_size);
+size_t vsz_huff_head_max(int dict_size);
+size_t vsz_huffman_build_tmp_bytes(int dict_size);
+vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_codebook, uint8_t* d_huff_head,
+                             uint32_t* d_info, void* d_tmp, size_t tmp_bytes, void* stream);
+
+/* Bit packing of codes with a codebook: the payload of HuffmanEncode (src/huffman.hh:268-341),
+ * MSB-first codewords, ceil(bits / 8) bytes, written at d_payload (any alignment; the bytes of its
+ * first 32-bit word before d_payload are preserved; 4 writable bytes past the end are needed).
+ * *d_bits = payload length in bits; d_chunk_bits (optional): bits per 512 codes. */
+size_t vsz_huffman_encode_tmp_bytes(size_t n);
+vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_codebook, int dict_size,
+                              uint8_t* d_payload, uint64_t* d_bits, uint16_t* d_chunk_bits, void* d_tmp,
+                              size_t tmp_bytes, void* stream);
+
+/* Decode n codes from a Huffman section [BE nodeCount][BE dict][tree][payload] (decode_withTree,
+ * src/huffman.hh:679-691) without an index, by self-synchronising chunk decoding.  d_huff needs
+ * 8 readable bytes past huff_bytes.  Synchronises (the synchronisation rounds are host-driven). */
+size_t vsz_huffman_decode_tmp_bytes(size_t huff_bytes, size_t n, int dict_size);
+vsz_status vsz_huffman_decode(const uint8_t* d_huff, size_t huff_bytes, size_t n, int dict_size, uint16_t* d_code,
+                              void* d_tmp, size_t tmp_bytes, void* stream);
+
+/* Reverse prediction-quantization: outlier placement + x_lorenzo_{1,2,3}d1l
+ * (src/vecsz_interface.hh:313-354, src/dualquant.hh:915-1043).  d_outliers: the compact outlier
+ * list (aligned), n_outlier entries. */
+size_t vsz_dualquant_decompress_tmp_bytes(int ndim, const size_t dims[3]);
+vsz_status vsz_dualquant_decompress(int ndim, const size_t dims[3], int block_size, int dict_size,
+                                    const uint16_t* d_code, const float* d_outliers, uint64_t n_outlier,
+                                    const void* d_consts, float* d_out, void* d_tmp, size_t tmp_bytes, void* stream);
+
+/* =============================================================================================
+ * Whole-field entry points (device buffers, stream-ordered, no host synchronisation):
+ * the Compress / Decompress workflow of src/vecsz_interface.hh:31-229 and :232-375.
+ * ============================================================================================= */
+
+/* Workspace and archive capacity for one field. */
+vsz_status vsz_compress_bounds(const vsz_params* p, int ndim, const size_t dims[3], size_t* ws_bytes,
+                               size_t* archive_capacity);
+/* Packed block (byte-identical to the reference's Compress output without -L) followed by this
+ * library's trailer, into d_archive; 8 u64 of vsz_result into d_result (device memory). */
+vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], const float* d_in, void* d_ws,
+                        size_t ws_bytes, uint8_t* d_archive, size_t archive_capacity, uint64_t* d_result,
+                        void* stream);
+
+/* Parse a packed block (+ optional trailer) held in host memory. */
+vsz_status vsz_archive_parse(const uint8_t* h_archive, size_t len, vsz_archive_desc* desc);
+vsz_status vsz_decompress_bounds(const vsz_archive_desc* desc, const vsz_decompress_opts* opts, size_t* ws_bytes);
+/* Decompress a device-resident archive (d_archive needs 16 readable bytes past its end).
+ * *d_status (device int, optional) receives VSZ_OK or the first device-side error.  Archives
+ * without this library's trailer are decoded by self-synchronisation, which synchronises the
+ * stream. */
+vsz_status vsz_decompress(const vsz_archive_desc* desc, const vsz_decompress_opts* opts, const uint8_t* d_archive,
+                          void* d_ws, size_t ws_bytes, float* d_out, int* d_status, void* stream);
+
+/* =============================================================================================
+ * Host entry points: the reference's interface, host buffers in and out, device memory managed
+ * by the library (cached between calls).  Synchronous.
+ * ============================================================================================= */
+
+/* vecsz::interface::Compress<float,int> (src/vecsz_interface.hh:31): returns a malloc'd buffer
+ * holding the packed block (or its lossless frame when p->lossless != NONE) followed by the
+ * trailer.  *data_size, *lossless_size, *n_outlier as the reference reports them;
+ * *out_bytes = total bytes in *h_out.  Free with vsz_free_host. */
+vsz_status vsz_compress_host(const vsz_params* p, int ndim, const size_t dims[3], const float* h_in, uint8_t** h_out,
+                             size_t* out_bytes, size_t* data_size, size_t* lossless_size, size_t* n_outlier);
+/* Same, into a caller buffer (pinned memory gives full-speed copies); *out_bytes as above. */
+vsz_status vsz_compress_host_into(const vsz_params* p, int ndim, const size_t dims[3], const float* h_in,
+                                  uint8_t* h_out, size_t out_capacity, size_t* out_bytes, size_t* data_size,
+                                  size_t* lossless_size, size_t* n_outlier);
+/* Capacity vsz_compress_host_into needs for this field. */
+vsz_status vsz_compress_host_bound(const vsz_params* p, int ndim, const size_t dims[3], size_t* out_capacity);
+
+/* vecsz::interface::Decompress<float,int> (src/vecsz_interface.hh:232).  h_archive holds the
+ * packed block (data_size bytes) or its lossless frame (lossless_size bytes, > 0), optionally
+ * followed by this library's trailer; len = all bytes available.  *h_out malloc'd, *n floats. */
+vsz_status vsz_decompress_host(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
+                               const vsz_decompress_opts* opts, float** h_out, size_t* n);
+/* Same, into a caller buffer of out_capacity floats. */
+vsz_status vsz_decompress_host_into(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
+                                    const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, size_t* n);
+void vsz_free_host(void* p);
+
+/* Lossless pass on host memory (src/lossless.hh:179-221): level 3 zstd or zlib through the
+ * system libzstd / libz.  *h_out malloc'd.  VSZ_ERR_UNSUPPORTED when the library is absent. */
+vsz_status vsz_lossless_compress(int which, const uint8_t* h_in, size_t len, uint8_t** h_out, size_t* out_len);
+vsz_status vsz_lossless_decompress(const uint8_t* h_in, size_t len, size_t target, uint8_t** h_out, size_t* out_len);
+/* 1 zstd frame, 2 zlib stream, 0 neither (is_lossless_compressed_data, src/lossless.hh:59-76). */
+int vsz_lossless_detect(const uint8_t* h_in, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VECSZ_GB300_H */

@@ -1,0 +1,188 @@
+"""Parity of the CUDA path (through the C ABI) with the reference: every stage bit-exact against
+the golden fixtures the reference produced, whole archives byte-identical, reconstructions
+bit-identical, and random settings checked against the pinned oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+import vecsz_gb300 as V
+from vecsz_gb300 import api, fields
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+CASES = golden_cases()
+
+
+def dev(cuda, a):
+    return cuda.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_stages_match_reference(cuda, name):
+    g = load_golden(name)
+    x = dev(cuda, g["x"])
+    consts, info, st = api.eb_setup(x, g["eb"], "r2r" if g["r2r"] else "abs")
+    assert st == 0
+    assert info["eb_final"] == g["eb_final"]
+    code, hist, scratch, segc = api.dualquant(x, g["dims"], g["bs"], g["dict_size"], consts)
+    cuda.cuda.synchronize()
+    code_h = code.cpu().numpy().view(np.uint16)
+    np.testing.assert_array_equal(code_h, g["code"])
+    np.testing.assert_array_equal(hist.cpu().numpy(), np.bincount(g["code"].astype(np.int64),
+                                                                  minlength=g["dict_size"]))
+    outl = api.outlier_gather(g["dims"], segc, scratch)
+    np.testing.assert_array_equal(outl.cpu().numpy().view(np.uint32), g["outliers"].view(np.uint32))
+    cb, head, binfo = api.huffman_build(hist, g["dict_size"])
+    nc, tree_bytes = int(binfo[0]), int(binfo[1])
+    head_len = 8 + tree_bytes
+    assert head.cpu().numpy()[:head_len].tobytes() == g["huff"][:head_len].tobytes()
+    for off in (0, 1, 3):
+        pay, bits, chunks = api.huffman_encode(code, cb, g["dict_size"], offset=off)
+        nbytes = (bits + 7) // 8
+        assert pay.cpu().numpy()[off:off + nbytes].tobytes() == g["huff"][head_len:].tobytes()
+    # reconstruction from the reference's own codes and outliers
+    d_out = api.dualquant_decompress(g["dims"], g["bs"], g["dict_size"], code, outl, consts)
+    np.testing.assert_array_equal(d_out.cpu().numpy().view(np.uint32), g["xhat"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_huffman_decode_reference_section(cuda, name):
+    g = load_golden(name)
+    huff = np.concatenate([g["huff"], np.zeros(16, np.uint8)])
+    d = dev(cuda, huff)
+    out = api.huffman_decode(d, g["huff"].size, g["code"].size, g["dict_size"])
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint16), g["code"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_archive_and_roundtrip_match_reference(cuda, name):
+    g = load_golden(name)
+    codec = V.DeviceCodec(g["dims"], eb=g["eb"], mode="r2r" if g["r2r"] else "abs", dict_size=g["dict_size"],
+                          block_size=g["bs"])
+    x = dev(cuda, g["x"])
+    codec.compress(x)
+    r = codec.result_host()
+    assert r.data_size == g["data_size"] and r.n_outlier == g["n_outlier"]
+    ab = codec.archive_bytes()
+    assert ab[: r.data_size] == g["archive"].tobytes()
+    # our archive (with trailer -> indexed decode)
+    codec.prepare_decompress(ab)
+    assert codec._desc.has_trailer
+    out = cuda.empty(g["x"].size, dtype=cuda.float32, device="cuda")
+    d_arch = dev(cuda, np.concatenate([np.frombuffer(ab, np.uint8), np.zeros(64, np.uint8)]))
+    codec.decompress(d_arch, out)
+    assert codec.decompress_status() == 0
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), g["xhat"].view(np.uint32))
+    # the reference's archive (no trailer -> self-synchronising decode), -d/-b/-m as given
+    vr = O.value_range(g["x"]) if g["r2r"] else 0.0
+    y = V.decompress(g["archive"].tobytes(), g["data_size"], 0, g["dict_size"], g["bs"],
+                     "r2r" if g["r2r"] else "abs", vr)
+    np.testing.assert_array_equal(y.view(np.uint32), g["xhat"].view(np.uint32))
+
+
+def test_reference_zstd_archive(cuda):
+    g = load_golden("d2_bump_64x45")
+    try:
+        y = V.decompress(g["zstd_frame"].tobytes(), g["data_size"], g["zstd_frame"].size, g["dict_size"], g["bs"])
+    except V.VszError as e:
+        if e.status == 6:
+            pytest.skip("libzstd not present")
+        raise
+    np.testing.assert_array_equal(y.view(np.uint32), g["xhat"].view(np.uint32))
+
+
+def _random_case(seed):
+    rng = np.random.default_rng(1000 + seed)
+    ndim = 1 + seed % 3
+    if ndim == 1:
+        dims = (int(rng.integers(1, 300000)),)
+    elif ndim == 2:
+        dims = (int(rng.integers(1, 700)), int(rng.integers(1, 400)))
+    else:
+        dims = tuple(int(rng.integers(1, 70)) for _ in range(3))
+    n = int(np.prod(dims))
+    bs = int(rng.choice([8, 8, 16, 32, 64]))
+    dct = int(rng.choice([256, 1024, 1024, 4096, 65536]))
+    eb = float(10 ** rng.uniform(-6, -1))
+    kind = seed % 4
+    if kind == 0:
+        x = (np.cumsum(rng.standard_normal(n)) * 10 ** rng.uniform(-2, 3)).astype(np.float32)
+    elif kind == 1:
+        x = rng.standard_normal(n).astype(np.float32)
+    elif kind == 2:
+        x = (rng.standard_normal(n) * 1e6).astype(np.float32)  # |s| well above 2^24
+    else:
+        x = np.sin(np.arange(n) * 0.01).astype(np.float32) + 2.0
+    r2r = bool(rng.integers(0, 2))
+    return dims, bs, dct, eb, r2r, x
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_settings_match_oracle(cuda, seed):
+    dims, bs, dct, eb, r2r, x = _random_case(seed)
+    if r2r and O.value_range(x) == 0:
+        r2r = False
+    a_or, meta = O.compress(x, dims, bs, dct, eb, r2r)
+    c = V.compress(x, dims, eb, "r2r" if r2r else "abs", dct, bs)
+    assert c.data_size == len(a_or)
+    assert c.data[: c.data_size] == a_or
+    assert c.n_outlier == meta["n_outlier"]
+    y = V.decompress(c)
+    y_or = O.decompress(a_or, bs, dct, O.value_range(x) if r2r else 0.0)
+    np.testing.assert_array_equal(y.view(np.uint32), y_or.view(np.uint32))
+
+
+@pytest.mark.parametrize("dims", [(1,), (7,), (128,), (129,), (1, 1), (3, 1), (1, 9), (130, 2), (8, 8), (9, 9),
+                                  (1, 1, 1), (2, 3, 5), (1, 1, 9), (129, 1, 1), (8, 8, 8), (9, 9, 9)])
+def test_edge_shapes_match_oracle(cuda, dims):
+    rng = np.random.default_rng(sum(dims))
+    x = np.cumsum(rng.standard_normal(int(np.prod(dims)))).astype(np.float32)
+    for bs in (8, 16):
+        a_or, _ = O.compress(x, dims, bs, 1024, 1e-3, False)
+        c = V.compress(x, dims, 1e-3, "abs", 1024, bs)
+        assert c.data[: c.data_size] == a_or
+        y = V.decompress(c)
+        np.testing.assert_array_equal(y.view(np.uint32), O.decompress(a_or, bs, 1024).view(np.uint32))
+
+
+def test_large_3d_roundtrip_properties(cuda):
+    """256^3 r2r field: deterministic archive, error bound (reference overshoot <= 2 ulp),
+    indexed and self-synchronising decoders agree."""
+    torch = cuda
+    xt = fields.grf_3d_torch(256, 256, 256, seed=5)
+    codec = V.DeviceCodec((256, 256, 256), eb=1e-4, mode="r2r", dict_size=1024, block_size=8)
+    codec.compress(xt)
+    a1 = codec.archive_bytes()
+    codec.compress(xt)
+    assert codec.archive_bytes() == a1
+    r = codec.result_host()
+    codec.prepare_decompress(a1)
+    out = torch.empty_like(xt)
+    d_arch = torch.from_numpy(np.concatenate([np.frombuffer(a1, np.uint8), np.zeros(64, np.uint8)])).cuda()
+    codec.decompress(d_arch, out)
+    assert codec.decompress_status() == 0
+    ebf = codec._desc.eb_final
+    err = (out.double() - xt.double()).abs()
+    ulp = torch.from_numpy(np.spacing(np.abs(xt.cpu().numpy())).astype(np.float64)).cuda()
+    assert bool((err <= ebf + 2 * ulp).all())
+    # the same bytes without the trailer go through self-synchronisation
+    y = V.decompress(a1[: r.data_size], r.data_size, 0, 1024, 8, "r2r", codec._desc.value_range)
+    np.testing.assert_array_equal(y, out.cpu().numpy().ravel())
+
+
+def test_corrupt_archive_is_reported(cuda):
+    g = load_golden("d3_tail_19x23x29")
+    bad = bytearray(g["archive"].tobytes())
+    hoff = 4 * 4 + 8 + 24
+    bad[hoff:hoff + 4] = (10 ** 6).to_bytes(4, "big")  # node count larger than the tree
+    with pytest.raises(V.VszError):
+        V.decompress(bytes(bad), g["data_size"], 0, g["dict_size"], g["bs"])
+    with pytest.raises(V.VszError):
+        V.decompress(g["archive"].tobytes()[:100], g["data_size"], 0, g["dict_size"], g["bs"])
+
+
+def test_zero_range_r2r_is_an_error(cuda):
+    x = np.full(1000, 3.0, np.float32)
+    with pytest.raises(V.VszError) as e:
+        V.compress(x, (1000,), 1e-3, "r2r", 1024, 8)
+    assert e.value.status == 7

@@ -1,0 +1,140 @@
+"""ctypes binding of libvecsz_gb300.so (the C ABI in include/vecsz_gb300.h).
+
+There is no fallback: if the shared library is missing or cannot load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+VSZ_OK = 0
+VSZ_ERR_INVALID = 1
+VSZ_ERR_CUDA = 2
+VSZ_ERR_CORRUPT = 3
+VSZ_ERR_CAPACITY = 4
+VSZ_ERR_TIMEOUT = 5
+VSZ_ERR_UNSUPPORTED = 6
+VSZ_ERR_RANGE = 7
+VSZ_ERR_NOMEM = 8
+VSZ_ERR_NO_DEVICE = 9
+
+MODE_ABS = 0
+MODE_R2R = 1
+LOSSLESS_NONE = 0
+LOSSLESS_ZSTD = 1
+LOSSLESS_GZIP = 2
+CONSTS_BYTES = 64
+
+
+class VszError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = lib().vsz_status_string(status).decode() if _LIB is not None else str(status)
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+
+
+class Params(C.Structure):
+    _fields_ = [("eb", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
+                ("lossless", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("data_size", "trailer_size", "n_outlier", "huff_bytes", "payload_bits",
+                                          "status", "max_code_len", "node_count")]
+
+
+class ArchiveDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("dims", C.c_uint64 * 3), ("eb", C.c_double), ("n_pad", C.c_uint64),
+                ("huff_bytes", C.c_uint64), ("n_outlier", C.c_uint64), ("header_bytes", C.c_uint64),
+                ("huff_offset", C.c_uint64), ("node_count", C.c_uint32), ("tree_bytes", C.c_uint64),
+                ("payload_offset", C.c_uint64), ("payload_bytes", C.c_uint64), ("outlier_offset", C.c_uint64),
+                ("data_size", C.c_uint64), ("has_trailer", C.c_int), ("eb_final", C.c_double),
+                ("value_range", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
+                ("chunk_syms", C.c_uint32), ("n_chunks", C.c_uint64), ("index_offset", C.c_uint64),
+                ("trailer_size", C.c_uint64)]
+
+
+class DecompressOpts(C.Structure):
+    _fields_ = [("dict_size", C.c_int), ("block_size", C.c_int), ("mode", C.c_int), ("value_range", C.c_double)]
+
+
+_LIB = None
+
+_p, _sz, _i, _d, _u64p, _u32p = C.c_void_p, C.c_size_t, C.c_int, C.c_double, C.c_void_p, C.c_void_p
+_PROTOS = {
+    "vsz_status_string": ([_i], C.c_char_p),
+    "vsz_version": ([], C.c_char_p),
+    "vsz_eb_setup": ([C.POINTER(Params), _p, _sz, _p, _p, _p], _i),
+    "vsz_consts_read": ([_p, C.POINTER(C.c_double), C.POINTER(C.c_int), _p], _i),
+    "vsz_outlier_segments": ([_i, C.POINTER(C.c_size_t)], _sz),
+    "vsz_dualquant": ([_i, C.POINTER(C.c_size_t), _i, _i, _p, _p, _p, _p, _p, _p, _p], _i),
+    "vsz_outlier_gather_tmp_bytes": ([_i, C.POINTER(C.c_size_t)], _sz),
+    "vsz_outlier_gather": ([_i, C.POINTER(C.c_size_t), _p, _p, _p, _p, _p, _sz, _p], _i),
+    "vsz_codebook_bytes": ([_i], _sz),
+    "vsz_huff_head_max": ([_i], _sz),
+    "vsz_huffman_build_tmp_bytes": ([_i], _sz),
+    "vsz_huffman_build": ([_p, _i, _p, _p, _p, _p, _sz, _p], _i),
+    "vsz_huffman_encode_tmp_bytes": ([_sz], _sz),
+    "vsz_huffman_encode": ([_p, _sz, _p, _i, _p, _p, _p, _p, _sz, _p], _i),
+    "vsz_huffman_decode_tmp_bytes": ([_sz, _sz, _i], _sz),
+    "vsz_huffman_decode": ([_p, _sz, _sz, _i, _p, _p, _sz, _p], _i),
+    "vsz_dualquant_decompress_tmp_bytes": ([_i, C.POINTER(C.c_size_t)], _sz),
+    "vsz_dualquant_decompress": ([_i, C.POINTER(C.c_size_t), _i, _i, _p, _p, C.c_uint64, _p, _p, _p, _sz, _p], _i),
+    "vsz_compress_bounds": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                             C.POINTER(C.c_size_t)], _i),
+    "vsz_compress": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), _p, _p, _sz, _p, _sz, _p, _p], _i),
+    "vsz_archive_parse": ([_p, _sz, C.POINTER(ArchiveDesc)], _i),
+    "vsz_decompress_bounds": ([C.POINTER(ArchiveDesc), C.POINTER(DecompressOpts), C.POINTER(C.c_size_t)], _i),
+    "vsz_decompress": ([C.POINTER(ArchiveDesc), C.POINTER(DecompressOpts), _p, _p, _sz, _p, _p, _p], _i),
+    "vsz_compress_host": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), _p, C.POINTER(C.c_void_p),
+                           C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                           C.POINTER(C.c_size_t)], _i),
+    "vsz_compress_host_into": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), _p, _p, _sz, C.POINTER(C.c_size_t),
+                                C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], _i),
+    "vsz_compress_host_bound": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], _i),
+    "vsz_decompress_host": ([_p, _sz, _sz, _sz, C.POINTER(DecompressOpts), C.POINTER(C.c_void_p),
+                             C.POINTER(C.c_size_t)], _i),
+    "vsz_decompress_host_into": ([_p, _sz, _sz, _sz, C.POINTER(DecompressOpts), _p, _sz, C.POINTER(C.c_size_t)], _i),
+    "vsz_free_host": ([_p], None),
+    "vsz_lossless_compress": ([_i, _p, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
+    "vsz_lossless_decompress": ([_p, _sz, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
+    "vsz_lossless_detect": ([_p, _sz], _i),
+}
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True) -> C.CDLL:
+    """Load libvecsz_gb300.so (building it with nvcc first if it is missing or stale)."""
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB
+        if build_if_missing and (not os.path.exists(path) or _build._stale()):
+            _build.build()
+        if not os.path.exists(path):
+            raise ImportError(f"vecsz_gb300: native library {path} is missing; run vecsz_gb300._build.build()")
+        L = C.CDLL(path, mode=C.RTLD_GLOBAL)
+        for name, (args, res) in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def exported_symbols() -> list[str]:
+    return list(_PROTOS)
+
+
+def check(status: int, what: str = "") -> None:
+    if status != VSZ_OK:
+        raise VszError(status, what)
+
+
+def dims_arg(dims) -> C.Array:
+    d = list(int(v) for v in dims) + [1] * (3 - len(dims))
+    return (C.c_size_t * 3)(*d)

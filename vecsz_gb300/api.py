@@ -1,0 +1,277 @@
+"""Python host API over the C ABI.
+
+Mirrors the reference's workflow (src/vecsz_interface.hh): `compress` is Compress<float,int>,
+`decompress` is Decompress<float,int>, both on host arrays.  `DeviceCodec` keeps a field's
+workspace resident on the GPU for repeated device-to-device compress/decompress (torch tensors
+provide the device memory and streams).  Stage functions expose each kernel stage for tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import (ArchiveDesc, DecompressOpts, Params, Result, VszError, check, dims_arg, lib)
+
+_MODES = {"abs": L.MODE_ABS, "r2r": L.MODE_R2R}
+_LOSSLESS = {None: L.LOSSLESS_NONE, "none": L.LOSSLESS_NONE, "zstd": L.LOSSLESS_ZSTD, "gzip": L.LOSSLESS_GZIP}
+
+
+def make_params(eb=1e-4, mode="abs", dict_size=4096, block_size=8, lossless=None) -> Params:
+    m = _MODES[mode] if isinstance(mode, str) else int(mode)
+    ll = _LOSSLESS[lossless] if (lossless is None or isinstance(lossless, str)) else int(lossless)
+    return Params(float(eb), m, int(dict_size), int(block_size), ll)
+
+
+@dataclass
+class Compressed:
+    """What Compress returns: the bytes main() writes after its 16-byte header, and the sizes."""
+    data: bytes           # packed block (or lossless frame) followed by this library's trailer
+    data_size: int        # packed block bytes (the reference's data_size)
+    lossless_size: int    # lossless frame bytes, 0 without -L
+    n_outlier: int
+
+    def file_bytes(self) -> bytes:
+        """The .sz file: u64 lossless_size, u64 data_size, payload (src/vecsz.cc:103-105)."""
+        return (np.array([self.lossless_size, self.data_size], np.uint64).tobytes() + self.data)
+
+
+def compress(data: np.ndarray, dims=None, eb: float = 1e-4, mode="abs", dict_size: int = 4096, block_size: int = 8,
+             lossless=None) -> Compressed:
+    """Compress a float32 field held in host memory (vecsz::interface::Compress)."""
+    x = np.ascontiguousarray(data, dtype=np.float32)
+    if dims is None:
+        dims = tuple(reversed(x.shape))  # numpy (z, y, x) -> reference (x, y, z)
+    p = make_params(eb, mode, dict_size, block_size, lossless)
+    out = C.c_void_p(0)
+    ob, ds, ls, no = C.c_size_t(0), C.c_size_t(0), C.c_size_t(0), C.c_size_t(0)
+    check(lib().vsz_compress_host(C.byref(p), len(dims), dims_arg(dims), x.ctypes.data_as(C.c_void_p), C.byref(out),
+                                  C.byref(ob), C.byref(ds), C.byref(ls), C.byref(no)), "compress")
+    try:
+        buf = C.string_at(out.value, ob.value)
+    finally:
+        lib().vsz_free_host(out)
+    return Compressed(buf, ds.value, ls.value, no.value)
+
+
+def decompress(archive, data_size: int = 0, lossless_size: int = 0, dict_size: int = 4096, block_size: int = 8,
+               mode="abs", value_range: float = 0.0) -> np.ndarray:
+    """Decompress (vecsz::interface::Decompress).  `archive` is a Compressed or raw bytes; the
+    -d/-b/-m options matter only for archives without this library's trailer."""
+    if isinstance(archive, Compressed):
+        data_size, lossless_size, archive = archive.data_size, archive.lossless_size, archive.data
+    a = np.frombuffer(archive, np.uint8)
+    o = DecompressOpts(int(dict_size), int(block_size), _MODES[mode] if isinstance(mode, str) else int(mode),
+                       float(value_range))
+    out = C.c_void_p(0)
+    n = C.c_size_t(0)
+    check(lib().vsz_decompress_host(a.ctypes.data_as(C.c_void_p), a.size, int(data_size), int(lossless_size),
+                                    C.byref(o), C.byref(out), C.byref(n)), "decompress")
+    try:
+        res = np.frombuffer(C.string_at(out.value, n.value * 4), np.float32).copy()
+    finally:
+        lib().vsz_free_host(out)
+    return res
+
+
+def parse_archive(buf) -> ArchiveDesc:
+    a = np.frombuffer(buf, np.uint8)
+    d = ArchiveDesc()
+    check(lib().vsz_archive_parse(a.ctypes.data_as(C.c_void_p), a.size, C.byref(d)), "archive_parse")
+    return d
+
+
+def read_sz_file(path: str):
+    """(data, data_size, lossless_size) of a .sz file written by the reference or by this library."""
+    raw = open(path, "rb").read()
+    lossless_size, data_size = np.frombuffer(raw[:16], np.uint64)
+    return raw[16:], int(data_size), int(lossless_size)
+
+
+# ------------------------------------------------------------------------------------------------
+# Device-resident codec (torch provides device memory and streams)
+# ------------------------------------------------------------------------------------------------
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream=None) -> C.c_void_p:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class DeviceCodec:
+    """Compress / decompress one field shape repeatedly with resident buffers.
+
+    compress(d_in) writes the archive into self.archive (a uint8 CUDA tensor) and the vsz_result
+    record into self.result (8 uint64); nothing is copied to the host unless you ask."""
+
+    def __init__(self, dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8, device="cuda"):
+        torch = _torch()
+        self.dims = tuple(int(v) for v in dims)
+        self.n = int(np.prod(self.dims))
+        self.params = make_params(eb, mode, dict_size, block_size)
+        ws, cap = C.c_size_t(0), C.c_size_t(0)
+        check(lib().vsz_compress_bounds(C.byref(self.params), len(self.dims), dims_arg(self.dims), C.byref(ws),
+                                        C.byref(cap)), "compress_bounds")
+        self.ws = torch.empty(ws.value, dtype=torch.uint8, device=device)
+        self.archive = torch.zeros(cap.value + 64, dtype=torch.uint8, device=device)
+        self.archive_cap = cap.value
+        self.result = torch.zeros(8, dtype=torch.int64, device=device)
+        self._dws = None
+        self._desc = None
+
+    def compress(self, d_in, stream=None) -> None:
+        check(lib().vsz_compress(C.byref(self.params), len(self.dims), dims_arg(self.dims), _ptr(d_in), _ptr(self.ws),
+                                 self.ws.numel(), _ptr(self.archive), self.archive_cap, _ptr(self.result),
+                                 _stream_ptr(stream)), "compress")
+
+    def result_host(self) -> Result:
+        r = self.result.cpu().numpy().view(np.uint64)
+        res = Result(*[int(v) for v in r])
+        if res.status != 0:
+            raise VszError(int(res.status), "compress (device)")
+        return res
+
+    def archive_bytes(self) -> bytes:
+        r = self.result_host()
+        return self.archive[: r.data_size + r.trailer_size].cpu().numpy().tobytes()
+
+    def prepare_decompress(self, archive_host: bytes, opts: DecompressOpts | None = None) -> None:
+        """Parse the archive's header on the host once and size the decompress workspace."""
+        torch = _torch()
+        self._desc = parse_archive(archive_host)
+        self._opts = opts or DecompressOpts(self.params.dict_size, self.params.block_size, self.params.mode, 0.0)
+        ws = C.c_size_t(0)
+        check(lib().vsz_decompress_bounds(C.byref(self._desc), C.byref(self._opts), C.byref(ws)), "decompress_bounds")
+        if self._dws is None or self._dws.numel() < ws.value:
+            self._dws = torch.empty(ws.value, dtype=torch.uint8, device=self.archive.device)
+        self._dstatus = torch.zeros(1, dtype=torch.int32, device=self.archive.device)
+
+    def decompress(self, d_archive, d_out, stream=None) -> None:
+        check(lib().vsz_decompress(C.byref(self._desc), C.byref(self._opts), _ptr(d_archive), _ptr(self._dws),
+                                   self._dws.numel(), _ptr(d_out), _ptr(self._dstatus), _stream_ptr(stream)),
+              "decompress")
+
+    def decompress_status(self) -> int:
+        return int(self._dstatus.item())
+
+
+# ------------------------------------------------------------------------------------------------
+# Stage-level calls on torch CUDA tensors (one per reference routine)
+# ------------------------------------------------------------------------------------------------
+
+def eb_setup(d_in, eb, mode="abs"):
+    """Device constants for eb; returns (consts tensor, {eb_final, c, r, range}, status)."""
+    torch = _torch()
+    p = make_params(eb, mode, 2, 8)
+    consts = torch.zeros(L.CONSTS_BYTES, dtype=torch.uint8, device=d_in.device)
+    tmp = torch.zeros(16, dtype=torch.uint8, device=d_in.device)
+    check(lib().vsz_eb_setup(C.byref(p), _ptr(d_in), d_in.numel(), _ptr(consts), _ptr(tmp), _stream_ptr()), "eb_setup")
+    out = (C.c_double * 4)()
+    st = C.c_int(0)
+    check(lib().vsz_consts_read(_ptr(consts), out, C.byref(st), _stream_ptr()), "consts_read")
+    return consts, {"eb_final": out[0], "c": out[1], "r": out[2], "range": out[3]}, st.value
+
+
+def dualquant(d_in, dims, block_size, dict_size, consts):
+    """Codes (u16 as int32 tensor), histogram (int64), scratch, segment counts."""
+    torch = _torch()
+    dev = d_in.device
+    n = int(np.prod(dims))
+    nseg = lib().vsz_outlier_segments(len(dims), dims_arg(dims))
+    code = torch.zeros(n + 8, dtype=torch.int16, device=dev)
+    scratch = torch.zeros(nseg * 128 + 4, dtype=torch.float32, device=dev)
+    segc = torch.zeros(nseg + 16, dtype=torch.uint8, device=dev)
+    hist = torch.zeros(dict_size, dtype=torch.int64, device=dev)
+    check(lib().vsz_dualquant(len(dims), dims_arg(dims), block_size, dict_size, _ptr(d_in), _ptr(consts), _ptr(code),
+                              _ptr(scratch), _ptr(segc), _ptr(hist), _stream_ptr()), "dualquant")
+    return code[:n], hist, scratch, segc
+
+
+def outlier_gather(dims, segc, scratch):
+    torch = _torch()
+    dev = segc.device
+    nseg = lib().vsz_outlier_segments(len(dims), dims_arg(dims))
+    tb = lib().vsz_outlier_gather_tmp_bytes(len(dims), dims_arg(dims))
+    tmp = torch.zeros(tb, dtype=torch.uint8, device=dev)
+    out = torch.zeros(nseg * 128 + 4, dtype=torch.float32, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    check(lib().vsz_outlier_gather(len(dims), dims_arg(dims), _ptr(segc), _ptr(scratch), _ptr(out), _ptr(cnt),
+                                   _ptr(tmp), tb, _stream_ptr()), "outlier_gather")
+    k = int(cnt.item())
+    return out[:k]
+
+
+def huffman_build(hist, dict_size):
+    """(codebook tensor, huffman head bytes tensor, info [node_count, tree_bytes, max_len, nodes])."""
+    torch = _torch()
+    dev = hist.device
+    cb = torch.zeros(lib().vsz_codebook_bytes(dict_size), dtype=torch.uint8, device=dev)
+    head = torch.zeros(lib().vsz_huff_head_max(dict_size) + 16, dtype=torch.uint8, device=dev)
+    info = torch.zeros(4, dtype=torch.int32, device=dev)
+    tb = lib().vsz_huffman_build_tmp_bytes(dict_size)
+    tmp = torch.zeros(tb, dtype=torch.uint8, device=dev)
+    check(lib().vsz_huffman_build(_ptr(hist), dict_size, _ptr(cb), _ptr(head), _ptr(info), _ptr(tmp), tb,
+                                  _stream_ptr()), "huffman_build")
+    torch.cuda.synchronize()
+    st = int(tmp[:4].view(torch.int32).item())
+    if st:
+        raise VszError(st, "huffman_build")
+    return cb, head, info.cpu().numpy()
+
+
+def huffman_encode(code, cb, dict_size, max_bits_per_code=64, offset=0):
+    """Payload bytes (host), total bits, per-512 chunk bits.  `offset` places the payload at that
+    byte offset of the output buffer (to exercise unaligned starts)."""
+    torch = _torch()
+    dev = code.device
+    n = code.numel()
+    cap = offset + (n * max_bits_per_code + 7) // 8 + 64
+    out = torch.zeros(cap, dtype=torch.uint8, device=dev)
+    bits = torch.zeros(1, dtype=torch.int64, device=dev)
+    chunks = torch.zeros((n + 511) // 512 + 8, dtype=torch.int16, device=dev)
+    tb = lib().vsz_huffman_encode_tmp_bytes(n)
+    tmp = torch.zeros(tb, dtype=torch.uint8, device=dev)
+    check(lib().vsz_huffman_encode(_ptr(code), n, _ptr(cb), dict_size, C.c_void_p(out.data_ptr() + offset),
+                                   _ptr(bits), _ptr(chunks), _ptr(tmp), tb, _stream_ptr()), "huffman_encode")
+    torch.cuda.synchronize()
+    st = int(tmp[:4].view(torch.int32).item())
+    if st:
+        raise VszError(st, "huffman_encode")
+    b = int(bits.item())
+    return out, b, chunks[: (n + 511) // 512]
+
+
+def huffman_decode(d_huff, huff_bytes, n, dict_size):
+    torch = _torch()
+    dev = d_huff.device
+    out = torch.zeros(n + 8, dtype=torch.int16, device=dev)
+    tb = lib().vsz_huffman_decode_tmp_bytes(huff_bytes, n, dict_size)
+    tmp = torch.zeros(tb, dtype=torch.uint8, device=dev)
+    check(lib().vsz_huffman_decode(_ptr(d_huff), huff_bytes, n, dict_size, _ptr(out), _ptr(tmp), tb, _stream_ptr()),
+          "huffman_decode")
+    return out[:n]
+
+
+def dualquant_decompress(dims, block_size, dict_size, code, outliers, consts):
+    torch = _torch()
+    dev = code.device
+    n = int(np.prod(dims))
+    out = torch.zeros(n + 8, dtype=torch.float32, device=dev)
+    tb = lib().vsz_dualquant_decompress_tmp_bytes(len(dims), dims_arg(dims))
+    tmp = torch.zeros(tb, dtype=torch.uint8, device=dev)
+    check(lib().vsz_dualquant_decompress(len(dims), dims_arg(dims), block_size, dict_size, _ptr(code),
+                                         _ptr(outliers) if outliers.numel() else C.c_void_p(tmp.data_ptr()),
+                                         int(outliers.numel()), _ptr(consts), _ptr(out), _ptr(tmp), tb,
+                                         _stream_ptr()), "dualquant_decompress")
+    return out[:n]

@@ -1,0 +1,631 @@
+// Dual-quantization compress on sm_103a: value range (r2r), error-bound constants, fused
+// prequant + Lorenzo + quant-code + histogram + outlier ranking, and outlier compaction.
+//
+// Replaces, from szcompressor/vecSZ:
+//   GetDatumValueRange / ChangeToRelativeMode / InitializeErrorBoundFamily  src/types.cc:28-92
+//   c_lorenzo_{1,2,3}d1l                                                    src/dualquant.hh:19-913
+//   histogram loop of initHuffman                                           src/huffman.hh:239-242
+//   outlier gather                                                          src/vecsz_interface.hh:166-170
+//
+// Element rules (pinned against the reference by the oracle):
+//   s   = rint(x *f32 r_f)                       all 1D/2D elements, 3D columns x < d0 & ~7
+//   s   = (float) round((double) x * r_d)        3D tail columns x >= d0 & ~7 when d0 % 8 != 0
+//   pred: 1D s[x-1]; 2D W + (N - NW); 3D (XYZ - (XY + (XZ + YZ))) + (X + (Y + Z)),
+//         3D tail columns left to right XYZ - XY - XZ - YZ + X + Y + Z; zero halo per block
+//   e   = s - pred (always integer valued, so the reference's sqrt(e*e) < R is |e| < R)
+//   code = |e| < R ? e + R : 0;  outlier value = s where code == 0
+//   2D tail columns (d0 % 8 != 0): code 0, outlier 0.0 -- the reference skips those AVX chunks
+//   and never runs its scalar tail (src/dualquant.hh:490-495).
+#include <cstdint>
+#include <type_traits>
+
+#include "vsz_device.cuh"
+#include "vsz_kernels.h"
+
+namespace vsz {
+
+// ------------------------------------------------------------------------------------------
+// K0: min / max of the field for r2r (GetDatumValueRange, src/types.cc:28-35)
+// ------------------------------------------------------------------------------------------
+
+// Order-preserving map of floats onto unsigned integers (NaNs are skipped by the caller).
+__device__ __forceinline__ uint32_t f2key(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+__global__ void __launch_bounds__(256) k_minmax(const float* __restrict__ x, size_t n, uint32_t* __restrict__ mm) {
+    uint32_t kmax = 0u, kmin = 0xffffffffu;
+    size_t tid    = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(x) & 15u) == 0);
+    size_t n4 = aligned ? n / 4 : 0;
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    for (size_t i = tid; i < n4; i += stride) {
+        float4 v = __ldcs(&x4[i]);
+        float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (e[j] == e[j]) {
+                uint32_t k = f2key(e[j]);
+                kmax       = max(kmax, k);
+                kmin       = min(kmin, k);
+            }
+        }
+    }
+    for (size_t i = n4 * 4 + tid; i < n; i += stride) {
+        float v = x[i];
+        if (v == v) {
+            uint32_t k = f2key(v);
+            kmax       = max(kmax, k);
+            kmin       = min(kmin, k);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+        kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+    }
+    __shared__ uint32_t smax[8], smin[8];
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        smax[w] = kmax;
+        smin[w] = kmin;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
+            kmax = max(kmax, smax[i]);
+            kmin = min(kmin, smin[i]);
+        }
+        atomicMax(&mm[0], kmax);
+        atomicMin(&mm[1], kmin);
+    }
+}
+
+// Error-bound constants (one thread).  For r2r: range = (double)((float)max - (float)min), with
+// std::max_element's rule that a NaN first element wins; a zero range is VSZ_ERR_RANGE, as the
+// reference exits there (src/types.cc:49-56).
+__global__ void k_consts(int mode, double eb, const uint32_t* __restrict__ mm, const float* __restrict__ x,
+                         Consts* __restrict__ c, int* status_word) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double ebf   = eb;
+    double range = 0.0;
+    int status   = VSZ_OK;
+    if (mode == VSZ_MODE_R2R) {
+        float x0 = x[0];
+        float mx, mn;
+        if (x0 != x0) {
+            mx = x0;
+            mn = x0;
+        } else {
+            mx = key2f(mm[0]);
+            mn = key2f(mm[1]);
+        }
+        float r = __fsub_rn(mx, mn);
+        range   = (double)r;
+        if (range == 0.0) status = VSZ_ERR_RANGE;
+        ebf = __dmul_rn(ebf, range);
+    }
+    c->eb_final = ebf;
+    c->r_d      = 1.0 / __dmul_rn(2.0, ebf);  // src/types.cc:91
+    c->c_d      = __dmul_rn(2.0, ebf);        // src/types.cc:90
+    c->range    = range;
+    c->r_f      = __double2float_rn(c->r_d);
+    float ch    = __double2float_rn(c->c_d);
+    float cl    = __double2float_rn(__dsub_rn(c->c_d, (double)ch));
+    c->c_hi     = ch;
+    c->c_lo     = cl;
+    auto normal = [](float f) {
+        uint32_t e = __float_as_uint(f) & 0x7f800000u;
+        return e != 0u && e != 0x7f800000u;
+    };
+    c->dq_fast = normal(ch) && (cl == 0.0f || normal(cl));
+    c->status  = status;
+    if (status != VSZ_OK && status_word) set_status(status_word, status);
+}
+
+// ------------------------------------------------------------------------------------------
+// K1: fused prequant + Lorenzo + quant codes + histogram + outlier ranking.
+//
+// Work unit = one warp tile: 128 consecutive x (4 per lane) by 8 rows (y) by one Lorenzo block
+// of planes (z, 3D) -- or 4 consecutive 128-element tiles in 1D.  Every lane keeps its 4 x 8
+// prequantized values of the current and the previous plane in registers; the x - 1 neighbour
+// of its first column comes from the lane to its left (shuffle), the y - 1 row above a warp
+// tile that starts inside a Lorenzo block (block_size > 8) is reloaded from global memory, so
+// warps never wait on each other.  Tile widths (128) are multiples of every block size, so a
+// tile's first column always starts a Lorenzo block.
+//
+// Outliers: for each row segment (one tile row, 128 elements) the warp ranks its outliers with
+// four ballots and writes them to scratch[seg * 128 + rank]; seg_count[seg] holds the count.
+// k_outlier_gather then places them in global row-major order, as the reference's serial gather.
+// ------------------------------------------------------------------------------------------
+
+struct HistAcc {
+    // Private counters for the three most frequent codes of a smooth field (R-1, R, R+1); all
+    // other codes go to the block's shared-memory histogram.
+    uint32_t c0 = 0, c1 = 0, c2 = 0;
+    __device__ __forceinline__ void add(int code, int R, uint32_t* s_hist, int dict, unsigned long long* g_hist) {
+        int d = code - R;
+        if (d == 0) c1++;
+        else if (d == -1) c0++;
+        else if (d == 1) c2++;
+        else if (s_hist) atomicAdd(&s_hist[code], 1u);
+        else atomicAdd(&g_hist[code], 1ull);
+    }
+    __device__ __forceinline__ void flush(int R, uint32_t* s_hist, int dict, unsigned long long* g_hist) {
+        if (s_hist) {
+            if (c1) atomicAdd(&s_hist[R], c1);
+            if (c0) atomicAdd(&s_hist[R - 1], c0);
+            if (c2 && R + 1 < dict) atomicAdd(&s_hist[R + 1], c2);
+        } else {
+            if (c1) atomicAdd(&g_hist[R], (unsigned long long)c1);
+            if (c0) atomicAdd(&g_hist[R - 1], (unsigned long long)c0);
+            if (c2 && R + 1 < dict) atomicAdd(&g_hist[R + 1], (unsigned long long)c2);
+        }
+    }
+};
+
+// One row of 4 elements per lane: store codes, count histogram, rank and write outliers.
+template <bool VEC>
+__device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t xb, uint32_t xt, bool row_in,
+                                         const int code[4], const float outv[4], HistAcc& h, uint32_t* s_hist) {
+    const unsigned lane = lane_id();
+    bool in[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) in[j] = row_in && (xb + j < a.d0);
+    uint16_t* crow = a.code + row * a.d0;
+    if (VEC && in[0]) {
+        // d0 % 4 == 0: all four columns are in range together; 8-byte aligned store.
+        uint2 v;
+        v.x = (uint32_t)code[0] | ((uint32_t)code[1] << 16);
+        v.y = (uint32_t)code[2] | ((uint32_t)code[3] << 16);
+        *reinterpret_cast<uint2*>(crow + xb) = v;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (in[j]) crow[xb + j] = (uint16_t)code[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (in[j]) h.add(code[j], a.R, s_hist, a.dict, a.hist);
+    // Outlier ranking inside the row segment: element (lane, j) precedes (lane', j') iff
+    // 4 lane + j < 4 lane' + j'.
+    bool o[4];
+    unsigned m[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        o[j] = in[j] && code[j] == 0;
+        m[j] = __ballot_sync(0xffffffffu, o[j]);
+    }
+    if (!row_in) return;
+    const unsigned lt = lanemask_lt();
+    unsigned before   = __popc(m[0] & lt) + __popc(m[1] & lt) + __popc(m[2] & lt) + __popc(m[3] & lt);
+    unsigned total    = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
+    size_t seg        = row * a.nxt + xt;
+    if (lane == 0) a.seg_count[seg] = (uint8_t)total;
+    if (total) {
+        float* dst = a.scratch + seg * kSegX;
+        unsigned r = before;
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (o[j]) dst[r++] = outv[j];
+    }
+}
+
+template <int NDIM>
+__device__ __forceinline__ float prequant_at(float v, uint32_t col, uint32_t xtail, float r_f, double r_d) {
+    if (NDIM == 3 && col >= xtail) return prequant_scalar(v, r_d);
+    return prequant_vec(v, r_f);
+}
+
+// Load and prequantize 4 consecutive columns [xb, xb+4) of one row; zero outside the field.
+template <int NDIM, bool VEC>
+__device__ __forceinline__ void load_row(const DqArgs& a, const float* rowp, bool row_in, uint32_t xb, float r_f,
+                                         double r_d, float S[4]) {
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (row_in) {
+        if (VEC) {
+            if (xb < a.d0) {
+                float4 t = __ldcs(reinterpret_cast<const float4*>(rowp + xb));
+                v[0] = t.x;
+                v[1] = t.y;
+                v[2] = t.z;
+                v[3] = t.w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (xb + j < a.d0) v[j] = __ldcs(rowp + xb + j);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        bool in = row_in && (xb + j < a.d0);
+        S[j]    = in ? prequant_at<NDIM>(v[j], xb + j, a.xtail, r_f, r_d) : 0.0f;
+    }
+}
+
+template <int NDIM, int BS, bool VEC>
+__global__ void __launch_bounds__(256) k_dq_compress_23d(DqArgs a) {
+    extern __shared__ uint32_t s_hist_dyn[];
+    uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
+    const Consts c   = *a.consts;
+    if (c.status != VSZ_OK) return;  // uniform across the grid
+    if (s_hist) {
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
+        __syncthreads();
+    }
+    const float r_f   = c.r_f;
+    const double r_d  = c.r_d;
+    const float Rf    = (float)a.R;
+    const unsigned lane = lane_id();
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const bool xbound = ((lane * 4) % BS) == 0;  // my first column starts a Lorenzo block
+    HistAcc h;
+
+    for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
+        const uint32_t xt = (uint32_t)(u % a.nxt);
+        const unsigned long long r = u / a.nxt;
+        const uint32_t yg = (uint32_t)(r % a.nyg);
+        const uint32_t zb = (uint32_t)(r / a.nyg);
+        const uint32_t xb = xt * kTileX + lane * 4;
+        const uint32_t y0 = yg * 8;
+        const bool yhalo  = (BS > 8) && (y0 % BS) != 0;
+        const uint32_t z0 = (NDIM == 3) ? zb * BS : 0;
+        const int nz      = (NDIM == 3) ? (int)min((uint32_t)BS, a.d2 - z0) : 1;
+
+        float P[8][4], Ph[4], PL[8], PhL = 0.f;  // previous plane (3D): rows, halo row, x - 1 column
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            PL[i] = 0.f;
+#pragma unroll
+            for (int j = 0; j < 4; j++) P[i][j] = 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) Ph[j] = 0.f;
+
+        for (int zz = 0; zz < nz; zz++) {
+            const uint32_t z = z0 + zz;
+            float S[8][4], Sh[4], SL[8], ShL;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const uint32_t y = y0 + i;
+                const bool row_in = y < a.d1;
+                const float* rowp = a.x + ((size_t)z * a.d1 + y) * a.d0;
+                load_row<NDIM, VEC>(a, rowp, row_in, xb, r_f, r_d, S[i]);
+            }
+            if (yhalo) {
+                const float* rowp = a.x + ((size_t)z * a.d1 + (y0 - 1)) * a.d0;
+                load_row<NDIM, VEC>(a, rowp, true, xb, r_f, r_d, Sh);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) Sh[j] = 0.f;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                SL[i] = __shfl_up_sync(0xffffffffu, S[i][3], 1);
+                if (xbound) SL[i] = 0.f;
+            }
+            ShL = __shfl_up_sync(0xffffffffu, Sh[3], 1);
+            if (xbound) ShL = 0.f;
+
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const uint32_t y  = y0 + i;
+                const bool row_in = y < a.d1;
+                int code[4];
+                float outv[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint32_t col = xb + j;
+                    const float cur    = S[i][j];
+                    const float X      = j ? S[i][j - 1] : SL[i];
+                    const float Y      = i ? S[i - 1][j] : Sh[j];
+                    const float XY     = i ? (j ? S[i - 1][j - 1] : SL[i - 1]) : (j ? Sh[j - 1] : ShL);
+                    const bool tail    = col >= a.xtail;
+                    float pred;
+                    if (NDIM == 2) {
+                        pred = __fadd_rn(X, __fsub_rn(Y, XY));  // W + (N - NW)
+                    } else {
+                        const float Z   = P[i][j];
+                        const float XZ  = j ? P[i][j - 1] : PL[i];
+                        const float YZ  = i ? P[i - 1][j] : Ph[j];
+                        const float XYZ = i ? (j ? P[i - 1][j - 1] : PL[i - 1]) : (j ? Ph[j - 1] : PhL);
+                        if (!tail) {
+                            float dist1 = __fadd_rn(X, __fadd_rn(Y, Z));
+                            float dist2 = __fadd_rn(XY, __fadd_rn(XZ, YZ));
+                            pred        = __fadd_rn(__fsub_rn(XYZ, dist2), dist1);
+                        } else {
+                            pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y),
+                                             Z);
+                        }
+                    }
+                    const float e  = __fsub_rn(cur, pred);
+                    const bool q   = fabsf(e) < Rf;
+                    code[j]        = q ? (int)__fadd_rn(e, Rf) : 0;
+                    outv[j]        = cur;
+                    if (NDIM == 2 && tail) {
+                        code[j] = 0;
+                        outv[j] = 0.0f;
+                    }
+                }
+                emit_row<VEC>(a, (size_t)z * a.d1 + y, xb, xt, row_in, code, outv, h, s_hist);
+            }
+            if (NDIM == 3) {
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    PL[i] = SL[i];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) P[i][j] = S[i][j];
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) Ph[j] = Sh[j];
+                PhL = ShL;
+            }
+        }
+    }
+    h.flush(a.R, s_hist, a.dict, a.hist);
+    if (s_hist) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
+            uint32_t v = s_hist[i];
+            if (v) atomicAdd(&a.hist[i], (unsigned long long)v);
+        }
+    }
+}
+
+// 1D: 4 consecutive 128-element tiles per warp unit; the x - 1 neighbour comes from the lane to
+// the left or, at a tile start, from the previous tile's last lane.  Blocks start on multiples of
+// block_size (which divide 128), so tile starts are block starts.
+template <int BS, bool VEC>
+__global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
+    extern __shared__ uint32_t s_hist_dyn[];
+    uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
+    const Consts c   = *a.consts;
+    if (c.status != VSZ_OK) return;
+    if (s_hist) {
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
+        __syncthreads();
+    }
+    const float r_f     = c.r_f;
+    const float Rf      = (float)a.R;
+    const unsigned lane = lane_id();
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const bool xbound = ((lane * 4) % BS) == 0;
+    constexpr int U   = 4;
+    HistAcc h;
+    for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
+        float S[U][4];
+#pragma unroll
+        for (int t = 0; t < U; t++) {
+            const uint32_t xt = (uint32_t)(u * U + t);
+            load_row<1, VEC>(a, a.x, xt < a.nxt, xt * kTileX + lane * 4, r_f, 0.0, S[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < U; t++) {
+            const uint32_t xt = (uint32_t)(u * U + t);
+            const uint32_t xb = xt * kTileX + lane * 4;
+            float L           = __shfl_up_sync(0xffffffffu, S[t][3], 1);
+            if (xbound) L = 0.f;
+            int code[4];
+            float outv[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float pred = j ? S[t][j - 1] : L;
+                const float e    = __fsub_rn(S[t][j], pred);
+                const bool q     = fabsf(e) < Rf;
+                code[j]          = q ? (int)__fadd_rn(e, Rf) : 0;
+                outv[j]          = S[t][j];
+            }
+            emit_row<VEC>(a, 0, xb, xt, xt < a.nxt, code, outv, h, s_hist);
+        }
+    }
+    h.flush(a.R, s_hist, a.dict, a.hist);
+    if (s_hist) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
+            uint32_t v = s_hist[i];
+            if (v) atomicAdd(&a.hist[i], (unsigned long long)v);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Outlier compaction: exclusive scan of seg_count in segment (= row-major) order with a single
+// pass decoupled look-back, then each warp copies whole segments from scratch to their final
+// place.  The destination is a byte address (the outlier section of a packed block need not be
+// 4-byte aligned).
+// ------------------------------------------------------------------------------------------
+
+constexpr int kGatherThreads = 256;
+constexpr int kGatherPerThread = 16;
+constexpr int kGatherTile = kGatherThreads * kGatherPerThread;  // segments per tile
+
+__device__ unsigned long long lookback(unsigned long long* tile_status, uint32_t tile, unsigned long long agg,
+                                       int* status) {
+    constexpr unsigned long long FA = 1ull << 62, FP = 2ull << 62, VM = (1ull << 62) - 1;
+    if (tile == 0) {
+        st_release_u64(&tile_status[0], FP | agg);
+        return 0;
+    }
+    st_release_u64(&tile_status[tile], FA | agg);
+    unsigned long long excl = 0;
+    long long spins         = 0;
+    int t                   = (int)tile - 1;
+    while (t >= 0) {
+        unsigned long long s = ld_acquire_u64(&tile_status[t]);
+        unsigned long long f = s & (3ull << 62);
+        if (f == 0) {
+            if (++spins > kSpinLimit) {
+                set_status(status, VSZ_ERR_TIMEOUT);
+                break;
+            }
+            continue;
+        }
+        excl += s & VM;
+        if (f == FP) break;
+        t--;
+    }
+    st_release_u64(&tile_status[tile], FP | (excl + agg));
+    return excl;
+}
+
+__global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g) {
+    if (*g.status != VSZ_OK) return;  // set before this launch, so uniform across the grid
+    __shared__ uint32_t s_off[kGatherTile];
+    __shared__ uint32_t s_warp[kGatherThreads / 32];
+    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(g.tile_counter, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const size_t seg0   = (size_t)tile * kGatherTile + (size_t)threadIdx.x * kGatherPerThread;
+    uint32_t cnt[kGatherPerThread];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kGatherPerThread; k++) {
+        size_t s = seg0 + k;
+        cnt[k]   = (s < g.nseg) ? g.seg_count[s] : 0u;
+        sum += cnt[k];
+    }
+    // block exclusive scan of per-thread sums
+    const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned)o) incl += v;
+    }
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int i = 0; i < kGatherThreads / 32; i++) {
+            uint32_t v = s_warp[i];
+            s_warp[i]  = run;
+            run += v;
+        }
+        s_base = lookback(g.tile_status, tile, run, g.status);
+        if (tile == g.ntiles - 1) *g.total = s_base + run;
+    }
+    __syncthreads();
+    uint32_t run = incl - sum + s_warp[w];
+#pragma unroll
+    for (int k = 0; k < kGatherPerThread; k++) {
+        s_off[threadIdx.x * kGatherPerThread + k] = run;
+        run += cnt[k];
+    }
+    __syncthreads();
+    const unsigned long long base = s_base;
+    uint8_t* out_bytes = g.out_bytes ? g.out_bytes + g.out_off.eval() : nullptr;
+    // warp-cooperative copies, one segment at a time
+    for (int k = w; k < kGatherTile; k += kGatherThreads / 32) {
+        size_t s = (size_t)tile * kGatherTile + k;
+        if (s >= g.nseg) break;
+        uint32_t n = g.seg_count[s];
+        if (n == 0) continue;
+        const float* src          = g.scratch + s * kSegX;
+        unsigned long long dst0   = base + s_off[k];
+        for (uint32_t i = lane; i < n; i += 32) {
+            float v = src[i];
+            if (g.out_f32) {
+                g.out_f32[dst0 + i] = v;
+            } else {
+                uint8_t* d = out_bytes + 4 * (dst0 + i);
+                uint32_t b = __float_as_uint(v);
+                d[0]       = (uint8_t)b;
+                d[1]       = (uint8_t)(b >> 8);
+                d[2]       = (uint8_t)(b >> 16);
+                d[3]       = (uint8_t)(b >> 24);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host-side launchers
+// ------------------------------------------------------------------------------------------
+
+int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_consts, uint32_t* d_mm,
+                    cudaStream_t st, int* status_word) {
+    if (mode == VSZ_MODE_R2R) {
+        uint32_t init[2] = {0u, 0xffffffffu};
+        if (cudaMemcpyAsync(d_mm, init, sizeof(init), cudaMemcpyHostToDevice, st) != cudaSuccess) return VSZ_ERR_CUDA;
+        size_t nb = (n + 1023) / 1024; int blocks = (int)(nb < (size_t)(152 * 8) ? nb : (size_t)(152 * 8));
+        if (blocks < 1) blocks = 1;
+        k_minmax<<<blocks, 256, 0, st>>>(d_in, n, d_mm);
+    }
+    k_consts<<<1, 32, 0, st>>>(mode, eb, d_mm, d_in, d_consts, status_word);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+template <int NDIM, int BS>
+static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
+    if (vec) k_dq_compress_23d<NDIM, BS, true><<<grid, 256, smem, st>>>(a);
+    else k_dq_compress_23d<NDIM, BS, false><<<grid, 256, smem, st>>>(a);
+}
+
+template <int BS>
+static void launch_1d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
+    if (vec) k_dq_compress_1d<BS, true><<<grid, 256, smem, st>>>(a);
+    else k_dq_compress_1d<BS, false><<<grid, 256, smem, st>>>(a);
+}
+
+template <int NDIM>
+static int dispatch_bs(const DqArgs& a, int bs, bool vec, int grid, size_t smem, cudaStream_t st) {
+    // Block sizes must divide the 128-wide warp tile so every tile starts a Lorenzo block.
+    auto go = [&](auto bs_c) {
+        constexpr int B = decltype(bs_c)::value;
+        if constexpr (NDIM == 1) launch_1d<B>(a, vec, grid, smem, st);
+        else launch_23d<NDIM, B>(a, vec, grid, smem, st);
+    };
+    switch (bs) {
+        case 8: go(std::integral_constant<int, 8>{}); break;
+        case 16: go(std::integral_constant<int, 16>{}); break;
+        case 32: go(std::integral_constant<int, 32>{}); break;
+        case 64: go(std::integral_constant<int, 64>{}); break;
+        default: return VSZ_ERR_UNSUPPORTED;
+    }
+    return VSZ_OK;
+}
+
+int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms) {
+    const bool vec = (a.d0 % 4 == 0) && ((reinterpret_cast<uintptr_t>(a.x) & 15u) == 0) &&
+                     ((reinterpret_cast<uintptr_t>(a.code) & 7u) == 0);
+    if (a.nunits == 0) return VSZ_OK;
+    size_t smem = a.smem_hist ? (size_t)a.dict * sizeof(uint32_t) : 0;
+    long long want = (long long)((a.nunits + 7) / 8);
+    long long cap = (long long)num_sms * 8; int grid = (int)(want < cap ? want : cap);
+    if (grid < 1) grid = 1;
+    int rc;
+    if (ndim == 1) rc = dispatch_bs<1>(a, bs, vec, grid, smem, st);
+    else if (ndim == 2) rc = dispatch_bs<2>(a, bs, vec, grid, smem, st);
+    else rc = dispatch_bs<3>(a, bs, vec, grid, smem, st);
+    if (rc) return rc;
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_outlier_gather(GatherArgs g, cudaStream_t st) {
+    g.ntiles = (uint32_t)((g.nseg + kGatherTile - 1) / kGatherTile);
+    if (g.ntiles == 0) {
+        return cudaMemsetAsync(g.total, 0, sizeof(unsigned long long), st) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+    }
+    if (cudaMemsetAsync(g.tile_status, 0, sizeof(unsigned long long) * g.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
+    if (cudaMemsetAsync(g.tile_counter, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
+    k_outlier_gather<<<g.ntiles, kGatherThreads, 0, st>>>(g);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+size_t gather_tmp_bytes(size_t nseg) {
+    size_t ntiles = (nseg + kGatherTile - 1) / kGatherTile;
+    return 16 + 8 * (ntiles + 1);
+}
+
+}  // namespace vsz

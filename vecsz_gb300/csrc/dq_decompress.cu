@@ -1,0 +1,357 @@
+// Dual-quantization decompress on sm_103a: outlier placement + reverse Lorenzo + dequantization.
+//
+// Replaces, from szcompressor/vecSZ:
+//   outlier scatter           src/vecsz_interface.hh:313-317
+//   x_lorenzo_{1,2,3}d1l      src/dualquant.hh:915-1043
+//
+// Per element, in the reference's FP32 operation order (zero halo per block):
+//   s = code == 0 ? outlier : (float)(pred + (float)(code - R))
+//   pred: 1D s[x-1]; 2D (N + W) - NW; 3D XYZ - XY - XZ - YZ + X + Y + Z, left to right
+//   xhat = (float)((double) s * 2eb)                 (dequant(), vsz_device.cuh)
+// The outlier of an element with code 0 is found by its rank among the zero codes in row-major
+// order: seg_off[row segment of 256 columns] (an exclusive scan of the zero counts the Huffman
+// decoder produced) plus the zeros before it inside the segment.
+#include <cstdint>
+#include <type_traits>
+
+#include "vsz_device.cuh"
+#include "vsz_kernels.h"
+
+namespace vsz {
+
+constexpr int kDSeg = 256;  // decompress row segment (one warp of 8-wide blocks)
+
+// ------------------------------------------------------------------------------------------
+// Fast path, block size 8: one lane reconstructs one whole Lorenzo block (8 x by 8 y, plane by
+// plane in z) in registers -- the x, y and z recurrences never leave the thread.  A warp covers
+// 32 consecutive blocks (one 256-wide row segment), so code loads (16 B) and value stores (32 B)
+// of a row are contiguous across the warp.
+// ------------------------------------------------------------------------------------------
+template <int NDIM, bool VEC>
+__global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
+    const Consts c = *a.consts;
+    if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
+    const int R           = a.R;
+    const unsigned lane   = lane_id();
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const unsigned lt = lanemask_lt();
+
+    for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
+        const uint32_t xs = (uint32_t)(u % a.nxs);
+        const unsigned long long r = u / a.nxs;
+        const uint32_t yb = (NDIM >= 2) ? (uint32_t)(r % a.nyb) : 0u;
+        const uint32_t zb = (NDIM == 3) ? (uint32_t)(r / a.nyb) : 0u;
+        const uint32_t x0 = xs * kDSeg + lane * 8;
+        const uint32_t y0 = yb * 8, z0 = zb * 8;
+        const int ny = (NDIM >= 2) ? (int)min(8u, a.d1 - y0) : 1;
+        const int nz = (NDIM == 3) ? (int)min(8u, a.d2 - z0) : 1;
+
+        float P[8][8];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) P[i][k] = 0.f;
+
+        for (int zz = 0; zz < nz; zz++) {
+            float Cm[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) Cm[k] = 0.f;
+#pragma unroll
+            for (int y = 0; y < 8; y++) {
+                const bool row_in = y < ny;
+                const size_t row  = ((size_t)(z0 + zz) * a.d1 + (y0 + y));
+                // ---- codes of my 8 columns
+                uint32_t cd[8];
+                bool in[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) in[k] = row_in && (x0 + k < a.d0);
+                const uint16_t* crow = a.codes + row * a.d0;
+                if (VEC && in[0]) {
+                    uint4 v = __ldcs(reinterpret_cast<const uint4*>(crow + x0));
+                    cd[0] = v.x & 0xffffu; cd[1] = v.x >> 16; cd[2] = v.y & 0xffffu; cd[3] = v.y >> 16;
+                    cd[4] = v.z & 0xffffu; cd[5] = v.z >> 16; cd[6] = v.w & 0xffffu; cd[7] = v.w >> 16;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 8; k++) cd[k] = in[k] ? (uint32_t)crow[x0 + k] : (uint32_t)R;
+                }
+                // ---- outliers of this row segment, ranked in row-major order
+                uint32_t zm = 0;
+#pragma unroll
+                for (int k = 0; k < 8; k++) zm |= (in[k] && cd[k] == 0u) ? (1u << k) : 0u;
+                float ov[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) ov[k] = 0.f;
+                if (__any_sync(0xffffffffu, zm != 0u)) {
+                    uint32_t cnt = __popc(zm), incl = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= (unsigned)o) incl += t;
+                    }
+                    (void)lt;
+                    if (zm) {
+                        unsigned long long base = a.seg_off[row * a.nxs + xs] + (incl - cnt);
+#pragma unroll
+                        for (int k = 0; k < 8; k++)
+                            if (zm & (1u << k)) {
+                                unsigned long long oi = base + __popc(zm & ((1u << k) - 1u));
+                                if (oi < a.n_outliers) ov[k] = a.outliers[oi];
+                                else set_status(a.status, VSZ_ERR_CORRUPT);
+                            }
+                    }
+                }
+                // ---- reverse Lorenzo along the row (registers only)
+                float C[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    float pred;
+                    if (NDIM == 1) {
+                        pred = k ? C[k - 1] : 0.f;
+                    } else if (NDIM == 2) {
+                        const float X  = k ? C[k - 1] : 0.f;
+                        const float Y  = y ? Cm[k] : 0.f;
+                        const float XY = (y && k) ? Cm[k - 1] : 0.f;
+                        pred           = __fsub_rn(__fadd_rn(Y, X), XY);  // (N + W) - NW
+                    } else {
+                        const float XYZ = (y && k) ? P[y - 1][k - 1] : 0.f;
+                        const float XY  = (y && k) ? Cm[k - 1] : 0.f;
+                        const float XZ  = k ? P[y][k - 1] : 0.f;
+                        const float YZ  = y ? P[y - 1][k] : 0.f;
+                        const float X   = k ? C[k - 1] : 0.f;
+                        const float Y   = y ? Cm[k] : 0.f;
+                        const float Z   = P[y][k];
+                        pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
+                    }
+                    const float delta = (float)((int)cd[k] - R);
+                    float s           = (cd[k] == 0u) ? ov[k] : __fadd_rn(pred, delta);
+                    C[k]              = in[k] ? s : 0.f;
+                }
+                // ---- dequantize and store
+                float xo[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) xo[k] = dequant(C[k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                float* orow = a.out + row * a.d0;
+                if (VEC && in[0]) {
+                    __stcs(reinterpret_cast<float4*>(orow + x0), make_float4(xo[0], xo[1], xo[2], xo[3]));
+                    __stcs(reinterpret_cast<float4*>(orow + x0 + 4), make_float4(xo[4], xo[5], xo[6], xo[7]));
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        if (in[k]) orow[x0 + k] = xo[k];
+                }
+                if (NDIM == 3) {
+                    if (y > 0) {
+#pragma unroll
+                        for (int k = 0; k < 8; k++) P[y - 1][k] = Cm[k];
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) Cm[k] = C[k];
+                if (NDIM == 1) break;
+            }
+            if (NDIM == 3) {
+#pragma unroll
+                for (int k = 0; k < 8; k++) P[7][k] = Cm[k];
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// General block sizes (16, 32, 64; also 8): one thread per block row, skewed pipeline.
+// Thread t (row y = t of the block) visits its elements in (z, x) order one step behind thread
+// t - 1, so every neighbour it reads was written in an earlier step; planes alternate between
+// two shared-memory buffers.  A CTA runs G = 128 / bs blocks side by side.
+// 1D: one thread per block, sequential along x.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t zeros_before(const uint16_t* crow, uint32_t from, uint32_t to) {
+    uint32_t n = 0;
+    for (uint32_t x = from; x < to; x++) n += (crow[x] == 0);
+    return n;
+}
+
+template <int NDIM, int BS>
+__global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
+    constexpr int G = (128 / BS) > 0 ? (128 / BS) : 1;
+    extern __shared__ float s_buf[];  // G blocks x 2 planes x BS x BS
+    const Consts c = *a.consts;
+    if (c.status != VSZ_OK || *a.status != VSZ_OK) return;  // uniform across the grid
+    const int R = a.R;
+    if (NDIM == 1) {
+        size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+        size_t x0 = b * BS;
+        if (x0 >= a.d0) return;
+        uint32_t seg_x0 = (uint32_t)(x0 & ~(size_t)(kDSeg - 1));
+        uint32_t zb = zeros_before(a.codes, seg_x0, (uint32_t)x0);
+        float prev = 0.f;
+        for (int k = 0; k < BS; k++) {
+            size_t x = x0 + k;
+            if (x >= a.d0) break;
+            uint32_t cd = a.codes[x];
+            float s;
+            if (cd == 0u) {
+                if ((x & (kDSeg - 1)) == 0) zb = 0;
+                unsigned long long oi = a.seg_off[x / kDSeg] + zb;
+                if (oi < a.n_outliers) s = a.outliers[oi];
+                else {
+                    s = 0.f;
+                    set_status(a.status, VSZ_ERR_CORRUPT);
+                }
+                zb++;
+            } else {
+                if ((x & (kDSeg - 1)) == 0) zb = 0;
+                s = __fadd_rn(k ? prev : 0.f, (float)((int)cd - R));
+            }
+            prev     = s;
+            a.out[x] = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+        }
+        return;
+    }
+    const int g = threadIdx.x / BS, t = threadIdx.x % BS;
+    const unsigned long long blk = (unsigned long long)blockIdx.x * G + g;
+    const bool active = blk < a.nunits;
+    const uint32_t bx = active ? (uint32_t)(blk % a.nbx) : 0u;
+    const unsigned long long rr = active ? blk / a.nbx : 0ull;
+    const uint32_t by = (uint32_t)(rr % a.nyb);
+    const uint32_t bz = (NDIM == 3) ? (uint32_t)(rr / a.nyb) : 0u;
+    const uint32_t x0 = bx * BS, y = by * BS + t, z0 = bz * BS;
+    float* S0 = s_buf + (size_t)g * 2 * BS * BS;
+    float* S1 = S0 + BS * BS;
+    for (int i = t; i < 2 * BS * BS; i += BS) S0[i] = 0.f;
+    __syncthreads();
+    const int nsteps = (NDIM == 3) ? (BS * BS + BS - 1) : (2 * BS - 1);
+    uint32_t zrun = 0;  // zeros seen in the current row segment before the current x
+    for (int step = 0; step < nsteps; step++) {
+        const int q = step - t;
+        const int lim = (NDIM == 3) ? BS * BS : BS;
+        if (active && q >= 0 && q < lim) {
+            const int zl = (NDIM == 3) ? q / BS : 0, xl = (NDIM == 3) ? q % BS : q;
+            const uint32_t z = z0 + zl, x = x0 + xl;
+            float* Sc = (zl & 1) ? S1 : S0;  // plane z
+            float* Sp = (zl & 1) ? S0 : S1;  // plane z - 1
+            const bool in = (x < a.d0) && (y < a.d1) && (NDIM < 3 || z < a.d2);
+            float s = 0.f;
+            if (in) {
+                const size_t row     = (size_t)z * a.d1 + y;
+                const uint16_t* crow = a.codes + row * a.d0;
+                if (xl == 0) zrun = zeros_before(crow, x0 & ~(uint32_t)(kDSeg - 1), x0);
+                else if ((x & (kDSeg - 1)) == 0) zrun = 0;
+                uint32_t cd = crow[x];
+                float pred;
+                const float X  = xl ? Sc[t * BS + xl - 1] : 0.f;
+                const float Y  = t ? Sc[(t - 1) * BS + xl] : 0.f;
+                const float XY = (t && xl) ? Sc[(t - 1) * BS + xl - 1] : 0.f;
+                if (NDIM == 2) {
+                    pred = __fsub_rn(__fadd_rn(Y, X), XY);
+                } else {
+                    const bool zp   = zl > 0;
+                    const float XYZ = (zp && t && xl) ? Sp[(t - 1) * BS + xl - 1] : 0.f;
+                    const float XZ  = (zp && xl) ? Sp[t * BS + xl - 1] : 0.f;
+                    const float YZ  = (zp && t) ? Sp[(t - 1) * BS + xl] : 0.f;
+                    const float Z   = zp ? Sp[t * BS + xl] : 0.f;
+                    pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
+                }
+                if (cd == 0u) {
+                    unsigned long long oi = a.seg_off[row * a.nxs + (x / kDSeg)] + zrun;
+                    if (oi < a.n_outliers) s = a.outliers[oi];
+                    else set_status(a.status, VSZ_ERR_CORRUPT);
+                    zrun++;
+                } else {
+                    s = __fadd_rn(pred, (float)((int)cd - R));
+                }
+                a.out[row * a.d0 + x] = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+            }
+            Sc[t * BS + xl] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// Zero codes per 256-wide row segment, for callers that hold codes but no decoder counts.
+__global__ void __launch_bounds__(256) k_count_zeros(const uint16_t* __restrict__ codes, uint32_t d0, size_t nrows,
+                                                     uint32_t nxs, uint32_t* __restrict__ seg_zero) {
+    const unsigned lane = lane_id();
+    const size_t nseg   = nrows * nxs;
+    const size_t wtot   = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t sgi = blockIdx.x * (size_t)(blockDim.x >> 5) + (threadIdx.x >> 5); sgi < nseg; sgi += wtot) {
+        size_t row = sgi / nxs;
+        uint32_t xs = (uint32_t)(sgi - row * nxs);
+        const uint16_t* crow = codes + row * d0;
+        uint32_t z = 0;
+        for (uint32_t x = xs * kDSeg + lane; x < min(d0, (xs + 1) * kDSeg); x += 32) z += (crow[x] == 0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+        if (lane == 0) seg_zero[sgi] = z;
+    }
+}
+
+int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* seg_zero, cudaStream_t st,
+                       int num_sms) {
+    uint32_t nxs = (d0 + kDSeg - 1) / kDSeg;
+    size_t nseg  = nrows * nxs;
+    if (nseg == 0) return VSZ_OK;
+    long long want = (long long)((nseg + 7) / 8), cap = (long long)num_sms * 16;
+    int grid = (int)(want < cap ? want : cap);
+    k_count_zeros<<<grid, 256, 0, st>>>(codes, d0, nrows, nxs, seg_zero);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+template <int NDIM, int BS>
+static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
+    constexpr int G = (128 / BS) > 0 ? (128 / BS) : 1;
+    if (NDIM == 1) {
+        size_t nblk = (a.d0 + BS - 1) / BS;
+        k_dq_decompress_gen<1, BS><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(a);
+    } else {
+        size_t smem = (size_t)G * 2 * BS * BS * sizeof(float);
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_dq_decompress_gen<NDIM, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr = true;
+        }
+        unsigned grid = (unsigned)((a.nunits + G - 1) / G);
+        k_dq_decompress_gen<NDIM, BS><<<grid, G * BS, smem, st>>>(a);
+    }
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms) {
+    if (a.n == 0) return VSZ_OK;
+    if (bs == 8 && !force_general) {
+        a.nxs = (a.d0 + kDSeg - 1) / kDSeg;
+        a.nyb = (a.d1 + 7) / 8;
+        unsigned long long nzb = (ndim == 3) ? (a.d2 + 7) / 8 : 1;
+        a.nunits = (unsigned long long)a.nxs * (ndim >= 2 ? a.nyb : 1) * nzb;
+        const bool vec = (a.d0 % 8 == 0) && ((reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0) &&
+                         ((reinterpret_cast<uintptr_t>(a.out) & 15u) == 0);
+        long long want = (long long)((a.nunits + 3) / 4);
+        long long cap  = (long long)num_sms * 16;
+        int grid = (int)(want < cap ? want : cap);
+        if (grid < 1) grid = 1;
+        if (ndim == 3) vec ? k_dq_decompress_b8<3, true><<<grid, 128, 0, st>>>(a) : k_dq_decompress_b8<3, false><<<grid, 128, 0, st>>>(a);
+        else if (ndim == 2) vec ? k_dq_decompress_b8<2, true><<<grid, 128, 0, st>>>(a) : k_dq_decompress_b8<2, false><<<grid, 128, 0, st>>>(a);
+        else vec ? k_dq_decompress_b8<1, true><<<grid, 128, 0, st>>>(a) : k_dq_decompress_b8<1, false><<<grid, 128, 0, st>>>(a);
+        return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+    }
+    a.nxs = (a.d0 + kDSeg - 1) / kDSeg;
+    a.nbx = (a.d0 + bs - 1) / bs;
+    a.nyb = (a.d1 + bs - 1) / bs;
+    unsigned long long nzb = (ndim == 3) ? (a.d2 + bs - 1) / bs : 1;
+    a.nunits = (unsigned long long)a.nbx * a.nyb * nzb;
+    auto go = [&](auto bs_c) -> int {
+        constexpr int B = decltype(bs_c)::value;
+        if (ndim == 3) return launch_gen<3, B>(a, st);
+        if (ndim == 2) return launch_gen<2, B>(a, st);
+        return launch_gen<1, B>(a, st);
+    };
+    switch (bs) {
+        case 8: return go(std::integral_constant<int, 8>{});
+        case 16: return go(std::integral_constant<int, 16>{});
+        case 32: return go(std::integral_constant<int, 32>{});
+        case 64: return go(std::integral_constant<int, 64>{});
+        default: return VSZ_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace vsz

@@ -1,0 +1,816 @@
+// Tree-Huffman coding of quant codes on sm_103a, bit-compatible with vecSZ's src/huffman.hh.
+//
+//   k_huff_build    initHuffman heap build + build_code + convert_HuffTree_to_bytes_anyStates
+//                   (src/huffman.hh:169-266, 374-502): exact replay of the reference's heap, one
+//                   thread, then the serialized tree and the codebook written by the whole CTA.
+//   k_huff_encode   HuffmanEncode (src/huffman.hh:268-341): persistent CTAs, 4096 codes per tile,
+//                   bit offsets from a block scan plus decoupled look-back, codewords packed into a
+//                   shared-memory word buffer and stored MSB-first into the payload.
+//   k_huff_table    reconstruct_HuffTree_from_bytes_anyStates (src/huffman.hh:561-635): 12-bit
+//                   lookup table plus a child array for longer codes.
+//   k_huff_decode   decode (src/huffman.hh:343-372): one thread per chunk of codewords whose first
+//                   bit is known (from this library's chunk index, or found by self-synchronising
+//                   rounds k_huff_sync_* for archives written by the reference).
+#include <cstdint>
+
+#include "scan.cuh"
+#include "vsz_device.cuh"
+#include "vsz_huffman.h"
+
+namespace vsz {
+
+// ------------------------------------------------------------------------------------------
+// K2: heap-tree build
+// ------------------------------------------------------------------------------------------
+
+constexpr int kKeyShift = 20;  // heap key = freq << 20 | node  (node < 2^20, freq < 2^44)
+
+struct DfsEntry {
+    uint32_t node;
+    int32_t parent;
+    uint32_t depth_side;  // depth << 1 | side
+    uint32_t pad;
+    unsigned long long code;
+};
+
+__device__ __forceinline__ unsigned long long kfreq(unsigned long long k) { return k >> kKeyShift; }
+
+__global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
+    extern __shared__ unsigned long long s_heap_dyn[];
+    __shared__ uint32_t s_info[4];
+    __shared__ int s_fail;
+    if (*a.status != VSZ_OK) return;  // an earlier stage failed (uniform: one CTA)
+    const int dict = a.dict;
+    uint8_t* base  = reinterpret_cast<uint8_t*>(a.scratch);
+    // global scratch layout (HuffBuildScratch::bytes)
+    uint32_t* used   = reinterpret_cast<uint32_t*>(base);                        // dict
+    int32_t* lchild  = reinterpret_cast<int32_t*>(used + dict);                  // dict (internal)
+    int32_t* rchild  = lchild + dict;                                            // dict
+    uint32_t* preL   = reinterpret_cast<uint32_t*>(rchild + dict);               // 2 dict
+    uint32_t* preR   = preL + 2 * dict;
+    uint32_t* preC   = preR + 2 * dict;
+    uint8_t* preT    = reinterpret_cast<uint8_t*>(preC + 2 * dict);              // 2 dict
+    DfsEntry* stack  = reinterpret_cast<DfsEntry*>(base + a.stack_offset);       // 2 dict
+    unsigned long long* heap = a.heap_in_smem ? s_heap_dyn : reinterpret_cast<unsigned long long*>(base + a.heap_offset);
+
+    for (int i = threadIdx.x; i < dict; i += blockDim.x) {
+        a.cb_word[i] = 0ull;
+        a.cb_len[i]  = 0;
+    }
+    for (int i = threadIdx.x; i < 2 * dict; i += blockDim.x) {
+        preL[i] = 0u;
+        preR[i] = 0u;
+    }
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+
+    if (threadIdx.x == 0) {
+        // leaves in symbol order (src/huffman.hh:248-254)
+        int nused = 0;
+        int qend  = 1;
+        for (int i = 0; i < dict; i++) {
+            unsigned long long f = a.hist[i];
+            if (f == 0) continue;
+            if (f >= (1ull << (64 - kKeyShift))) s_fail = VSZ_ERR_UNSUPPORTED;
+            used[nused] = (uint32_t)i;
+            unsigned long long key = (f << kKeyShift) | (unsigned long long)nused;
+            nused++;
+            int ii = qend++, j;  // qinsert
+            while ((j = ii >> 1)) {
+                if (kfreq(heap[j]) <= kfreq(key)) break;
+                heap[ii] = heap[j];
+                ii       = j;
+            }
+            heap[ii] = key;
+        }
+        if (nused == 0) s_fail = VSZ_ERR_INVALID;
+        int nnodes = nused;
+        // merge (src/huffman.hh:262): new_node(.., qremove(), qremove()) -- the first removal is
+        // the right child, the second the left (argument evaluation order of the reference build)
+        while (!s_fail && qend > 2) {
+            unsigned long long rem[2];
+#pragma unroll
+            for (int r = 0; r < 2; r++) {  // qremove
+                unsigned long long n = heap[1];
+                qend--;
+                int i = 1, l;
+                while ((l = i << 1) < qend) {
+                    ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(&heap[l]);
+                    unsigned long long best = pr.x;
+                    if (l + 1 < qend && kfreq(pr.y) < kfreq(pr.x)) {
+                        l++;
+                        best = pr.y;
+                    }
+                    heap[i] = best;
+                    i       = l;
+                }
+                heap[i] = heap[qend];
+                rem[r]  = n;
+            }
+            int node = nnodes++;
+            rchild[node - nused] = (int32_t)(rem[0] & ((1u << kKeyShift) - 1));
+            lchild[node - nused] = (int32_t)(rem[1] & ((1u << kKeyShift) - 1));
+            unsigned long long key = ((kfreq(rem[0]) + kfreq(rem[1])) << kKeyShift) | (unsigned long long)node;
+            int ii = qend++, j;
+            while ((j = ii >> 1)) {
+                if (kfreq(heap[j]) <= kfreq(key)) break;
+                heap[ii] = heap[j];
+                ii       = j;
+            }
+            heap[ii] = key;
+        }
+        uint32_t node_count = 0, max_len = 0;
+        if (!s_fail) {
+            int root = (int)(heap[1] & ((1u << kKeyShift) - 1));
+            // preorder DFS: numbering of pad_tree_* (src/huffman.hh:374-423) and codewords of
+            // build_code (:200-227), left edge 0, right edge 1
+            int sp = 0;
+            stack[sp++] = DfsEntry{(uint32_t)root, -1, 0u, 0u, 0ull};
+            uint32_t counter = 0;
+            while (sp > 0) {
+                DfsEntry e   = stack[--sp];
+                uint32_t idx = counter++;
+                uint32_t depth = e.depth_side >> 1;
+                if (e.parent >= 0) {
+                    if (e.depth_side & 1u) preR[e.parent] = idx;
+                    else preL[e.parent] = idx;
+                }
+                if ((int)e.node < nused) {
+                    uint32_t sym = used[e.node];
+                    preC[idx]    = sym;
+                    preT[idx]    = 1;
+                    a.cb_len[sym]  = (uint8_t)(depth > 255 ? 255 : depth);
+                    a.cb_word[sym] = e.code;
+                    if (depth > max_len) max_len = depth;
+                } else {
+                    preC[idx] = 0;
+                    preT[idx] = 0;
+                    int k     = (int)e.node - nused;
+                    unsigned long long c2 = e.code << 1;
+                    stack[sp++] = DfsEntry{(uint32_t)rchild[k], (int32_t)idx, ((depth + 1) << 1) | 1u, 0u, c2 | 1ull};
+                    stack[sp++] = DfsEntry{(uint32_t)lchild[k], (int32_t)idx, ((depth + 1) << 1), 0u, c2};
+                }
+            }
+            node_count = counter;
+        }
+        s_info[0] = node_count;
+        s_info[1] = (uint32_t)tree_bytes_size(node_count);
+        s_info[2] = max_len;
+        s_info[3] = (uint32_t)nnodes;
+    }
+    __syncthreads();
+    if (s_fail) {
+        if (threadIdx.x == 0) set_status(a.status, s_fail);
+        return;
+    }
+    const uint32_t nc = s_info[0];
+    const int w       = tree_index_width(nc);
+    // [BE nodeCount][BE dict][u8 0][L][R][C u32 LE][t]  (src/huffman.hh:649-653, 438-444)
+    uint8_t* o = a.out;
+    if (threadIdx.x == 0) {
+        o[0] = (uint8_t)(nc >> 24);
+        o[1] = (uint8_t)(nc >> 16);
+        o[2] = (uint8_t)(nc >> 8);
+        o[3] = (uint8_t)nc;
+        uint32_t dh = (uint32_t)dict;
+        o[4] = (uint8_t)(dh >> 24);
+        o[5] = (uint8_t)(dh >> 16);
+        o[6] = (uint8_t)(dh >> 8);
+        o[7] = (uint8_t)dh;
+        o[8] = 0;
+    }
+    uint8_t* pL = o + 9;
+    uint8_t* pR = pL + (size_t)w * nc;
+    uint8_t* pC = pR + (size_t)w * nc;
+    uint8_t* pT = pC + 4 * (size_t)nc;
+    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
+        uint32_t l = preL[i], r = preR[i], c = preC[i];
+        for (int b = 0; b < w; b++) {
+            pL[(size_t)i * w + b] = (uint8_t)(l >> (8 * b));
+            pR[(size_t)i * w + b] = (uint8_t)(r >> (8 * b));
+        }
+        pC[4 * (size_t)i + 0] = (uint8_t)c;
+        pC[4 * (size_t)i + 1] = (uint8_t)(c >> 8);
+        pC[4 * (size_t)i + 2] = (uint8_t)(c >> 16);
+        pC[4 * (size_t)i + 3] = (uint8_t)(c >> 24);
+        pT[i]                 = preT[i];
+    }
+    if (threadIdx.x < 4) a.info[threadIdx.x] = s_info[threadIdx.x];
+}
+
+// ------------------------------------------------------------------------------------------
+// K3: encoder
+// ------------------------------------------------------------------------------------------
+
+constexpr int kEncThreads   = 256;
+constexpr int kEncPerThread = 16;
+constexpr int kEncTile      = kEncThreads * kEncPerThread;  // 4096 codes
+constexpr int kEncMaxWords  = kEncTile * 64 / 32 + 4;       // codes are at most 64 bits
+
+__global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
+    extern __shared__ uint8_t s_dyn[];
+    uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);                     // kEncMaxWords
+    unsigned long long* s_cw = reinterpret_cast<unsigned long long*>(s_words + kEncMaxWords);  // dict (if cached)
+    uint8_t* s_len = reinterpret_cast<uint8_t*>(s_cw + (a.cb_in_smem ? a.dict : 0));
+    __shared__ unsigned long long s_scan[33];
+    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_tile;
+
+    if (*a.status != VSZ_OK) return;  // set before this launch: uniform across the grid
+    if (a.build_info && (a.build_info[2] > 64u || a.build_info[0] == 0u)) {
+        // codewords longer than 64 bits (a tree deeper than any reachable in practice) or no tree
+        if (threadIdx.x == 0 && blockIdx.x == 0) set_status(a.status, a.build_info[0] ? VSZ_ERR_UNSUPPORTED : VSZ_ERR_INVALID);
+        return;
+    }
+    const unsigned long long* cw = a.cb_word;
+    const uint8_t* cl            = a.cb_len;
+    if (a.cb_in_smem) {
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
+            s_cw[i]  = a.cb_word[i];
+            s_len[i] = a.cb_len[i];
+        }
+        cw = s_cw;
+        cl = s_len;
+    }
+    __syncthreads();
+    uint8_t* out          = a.out + a.out_off.eval();
+    const uint32_t base0  = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
+    uint32_t* gw          = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
+    const unsigned lane   = threadIdx.x & 31u;
+    const unsigned warp   = threadIdx.x >> 5;
+
+    while (true) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= a.ntiles) break;
+        // ---- load 16 codes and their lengths
+        const size_t c0 = (size_t)tile * kEncTile + (size_t)threadIdx.x * kEncPerThread;
+        uint32_t sym[kEncPerThread];
+        if (c0 + kEncPerThread <= a.n && a.codes_aligned) {
+            const uint4* p = reinterpret_cast<const uint4*>(a.codes + c0);
+            uint4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+            uint32_t w8[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                sym[2 * k]     = w8[k] & 0xffffu;
+                sym[2 * k + 1] = w8[k] >> 16;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kEncPerThread; k++) sym[k] = (c0 + k < a.n) ? a.codes[c0 + k] : 0xffffffffu;
+        }
+        uint32_t bits = 0;
+#pragma unroll
+        for (int k = 0; k < kEncPerThread; k++)
+            if (sym[k] != 0xffffffffu) bits += cl[sym[k]];
+        // ---- per-warp totals feed the decode index (one entry per 512 codes)
+        uint32_t wsum = bits;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+        if (lane == 0 && a.chunk_bits) {
+            size_t chunk = (size_t)tile * (kEncTile / 512) + warp;
+            if (chunk * 512 < a.n) a.chunk_bits[chunk] = (uint16_t)wsum;
+        }
+        unsigned long long tot;
+        unsigned long long toff = block_exclusive_scan<unsigned long long>((unsigned long long)bits, s_scan, &tot);
+        if (threadIdx.x == 0) {
+            s_base = lookback_publish(a.tile_status, tile, tot, a.status);
+            if (tile == a.ntiles - 1) *a.total_bits = s_base + tot;
+        }
+        __syncthreads();
+        const unsigned long long B = s_base;
+        const unsigned long long gstart = base0 + B;  // tile's first bit on the global word grid
+        const uint32_t r0     = (uint32_t)(gstart & 31u);
+        const unsigned long long F = gstart >> 5;
+        const uint32_t nwords = (uint32_t)((r0 + tot + 31) >> 5);
+        for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) s_words[i] = 0u;
+        __syncthreads();
+        // ---- pack this thread's codewords into the word buffer; only a thread's first and last
+        // word can be shared with its neighbours, so only those use atomics
+        {
+            unsigned long long pos = r0 + toff;
+            uint32_t wi   = (uint32_t)(pos >> 5);
+            uint32_t nb   = (uint32_t)(pos & 31u);  // bits already taken in the current word
+            bool first    = true;
+            unsigned long long acc = 0;             // MSB-aligned pending bits of word wi..
+            auto emit = [&](uint32_t word) {
+                if (first && (pos & 31u)) atomicOr(&s_words[wi], word);
+                else s_words[wi] = word;
+                first = false;
+                wi++;
+            };
+            auto append = [&](unsigned long long v, uint32_t len) {  // len <= 32
+                if (len == 0) return;
+                acc |= v << (64 - nb - len);
+                nb += len;
+                if (nb >= 32) {
+                    emit((uint32_t)(acc >> 32));
+                    acc <<= 32;
+                    nb -= 32;
+                }
+            };
+#pragma unroll
+            for (int k = 0; k < kEncPerThread; k++) {
+                if (sym[k] == 0xffffffffu) continue;
+                uint32_t len          = cl[sym[k]];
+                unsigned long long v  = cw[sym[k]];
+                if (len > 32) {
+                    append(v >> 32, len - 32);
+                    append(v & 0xffffffffull, 32);
+                } else {
+                    append(v, len);
+                }
+            }
+            if (nb > 0) atomicOr(&s_words[wi], (uint32_t)(acc >> 32));
+        }
+        __syncthreads();
+        // ---- store: interior words and the last word are plain stores; a first word shared with
+        // the previous tile is OR-ed in by thread 0 after that tile's last word has landed
+        const bool first_special = (r0 != 0) || (tile == 0 && base0 != 0);
+        for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) {
+            if (i == 0 && first_special) continue;
+            gw[F + i] = bswap32(s_words[i]);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (first_special && nwords > 0) {
+                uint32_t v = bswap32(s_words[0]);
+                if (tile == 0) {
+                    // bytes before the payload start belong to the tree section: keep them
+                    uint32_t keep = (base0 == 0) ? 0u : ((1u << base0) - 1u);
+                    uint32_t old  = gw[F];
+                    gw[F]         = (old & keep) | v;
+                } else {
+                    long long spins = 0;
+                    while (atomicAdd(&a.tail_flag[tile - 1], 0u) == 0u) {
+                        if (++spins > kSpinLimit) {
+                            set_status(a.status, VSZ_ERR_TIMEOUT);
+                            break;
+                        }
+                    }
+                    atomicOr(&gw[F], v);
+                }
+            } else if (tile > 0 && nwords == 0) {
+                // empty tile (cannot happen for codes of length >= 1): keep the chain intact
+            }
+            __threadfence();
+            atomicExch(&a.tail_flag[tile], 1u);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// K4a: decode table from the serialized tree
+// ------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t rd_index(const uint8_t* p, int w) {
+    uint32_t v = 0;
+    for (int b = 0; b < w; b++) v |= (uint32_t)p[b] << (8 * b);
+    return v;
+}
+
+__global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
+    const uint8_t* h = a.huff;
+    __shared__ uint32_t s_nc;
+    __shared__ int s_bad;
+    if (threadIdx.x == 0) {
+        s_nc  = ((uint32_t)h[0] << 24) | ((uint32_t)h[1] << 16) | ((uint32_t)h[2] << 8) | (uint32_t)h[3];
+        s_bad = 0;
+        if (s_nc == 0 || s_nc > a.max_nodes || 8 + tree_bytes_size(s_nc) > a.huff_bytes) s_bad = 1;
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (threadIdx.x == 0) set_status(a.status, VSZ_ERR_CORRUPT);
+        return;
+    }
+    const uint32_t nc = s_nc;
+    const int w       = tree_index_width(nc);
+    const uint8_t* pL = h + 9;
+    const uint8_t* pR = pL + (size_t)w * nc;
+    const uint8_t* pC = pR + (size_t)w * nc;
+    const uint8_t* pT = pC + 4 * (size_t)nc;
+    uint32_t* parent  = a.parent;  // nc entries: parent << 1 | side; 0xffffffff = none
+    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) parent[i] = 0xffffffffu;
+    for (uint32_t i = threadIdx.x; i < (1u << kDecBits); i += blockDim.x) a.table[i] = 0u;
+    __syncthreads();
+    // The reference rebuilds the root as an internal node when nodeCount > 256 and from
+    // (C[0], t[0]) otherwise (src/huffman.hh:577,602,627).
+    const bool root_leaf = (nc <= 256) && pT[0];
+    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
+        bool leaf = (i == 0) ? root_leaf : (pT[i] != 0);
+        uint32_t c = (uint32_t)pC[4 * (size_t)i] | ((uint32_t)pC[4 * (size_t)i + 1] << 8) |
+                     ((uint32_t)pC[4 * (size_t)i + 2] << 16) | ((uint32_t)pC[4 * (size_t)i + 3] << 24);
+        a.node_sym[i] = leaf ? (0x80000000u | (c & 0xffffu)) : 0u;
+        if (leaf && c >= (uint32_t)a.dict) atomicExch(&s_bad, 1);
+        if (!leaf) {
+            uint32_t l = rd_index(pL + (size_t)i * w, w), r = rd_index(pR + (size_t)i * w, w);
+            if (l == 0 || r == 0 || l >= nc || r >= nc) {
+                // an internal node needs both children (the reference would dereference null)
+                atomicExch(&s_bad, 1);
+                l = r = 0;
+            } else {
+                atomicExch(&parent[l], (i << 1) | 0u);
+                atomicExch(&parent[r], (i << 1) | 1u);
+            }
+            a.child[2 * (size_t)i]     = l;
+            a.child[2 * (size_t)i + 1] = r;
+        } else {
+            a.child[2 * (size_t)i]     = 0;
+            a.child[2 * (size_t)i + 1] = 0;
+        }
+    }
+    __syncthreads();
+    if (s_bad) {
+        if (threadIdx.x == 0) set_status(a.status, VSZ_ERR_CORRUPT);
+        return;
+    }
+    if (root_leaf) {
+        if (threadIdx.x == 0) {
+            a.info[0] = 1;  // single-symbol tree: constant output, no bits
+            a.info[1] = a.node_sym[0] & 0xffffu;
+        }
+        return;
+    }
+    // depth and code of every node by walking up to the root (depth bounded by nc)
+    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
+        uint32_t depth = 0, cur = i;
+        unsigned long long code = 0;
+        bool ok = true;
+        while (cur != 0) {
+            uint32_t p = parent[cur];
+            if (p == 0xffffffffu || depth >= 64) {
+                ok = false;
+                break;
+            }
+            code |= (unsigned long long)(p & 1u) << depth;
+            depth++;
+            cur = p >> 1;
+        }
+        if (!ok) {
+            // unreachable node or a code longer than 64 bits: only the walk can reach it
+            if (depth >= 64 && parent[i] != 0xffffffffu) continue;
+            continue;
+        }
+        bool leaf = (a.node_sym[i] & 0x80000000u) != 0;
+        if (leaf && depth >= 1 && depth <= (uint32_t)kDecBits) {
+            uint32_t lo = (uint32_t)(code << (kDecBits - depth));
+            uint32_t hi = lo + (1u << (kDecBits - depth));
+            uint32_t e  = ((a.node_sym[i] & 0xffffu) << 8) | depth;
+            for (uint32_t t = lo; t < hi; t++) a.table[t] = e;
+        } else if (!leaf && depth == (uint32_t)kDecBits) {
+            a.table[(uint32_t)code] = (i << 8);  // len 0: continue bit by bit from node i
+        }
+    }
+    if (threadIdx.x == 0) {
+        a.info[0] = 0;
+        a.info[1] = 0;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// K4b: chunk decoder
+// ------------------------------------------------------------------------------------------
+
+struct BitReader {
+    const uint32_t* gw;       // aligned word base
+    unsigned long long pos;   // bit position on the word grid
+    unsigned long long buf;   // MSB-aligned bits starting at `pos`
+    int nbits;                // valid bits in buf
+    unsigned long long limit; // first bit past the payload on the word grid
+
+    __device__ __forceinline__ void init(const uint32_t* g, unsigned long long p, unsigned long long lim) {
+        gw    = g;
+        pos   = p;
+        limit = lim;
+        unsigned long long wi = p >> 5;
+        uint32_t off          = (uint32_t)(p & 31u);
+        unsigned long long hi = bswap32(__ldg(&gw[wi]));
+        unsigned long long lo = bswap32(__ldg(&gw[wi + 1]));
+        buf   = ((hi << 32) | lo) << off;
+        nbits = 64 - (int)off;
+    }
+    __device__ __forceinline__ void refill() {
+        if (nbits <= 32) {
+            unsigned long long wi = (pos + nbits) >> 5;  // word aligned: pos + nbits is a multiple of 32
+            unsigned long long v  = bswap32(__ldg(&gw[wi]));
+            buf |= v << (32 - nbits);
+            nbits += 32;
+        }
+    }
+    __device__ __forceinline__ uint32_t peek(int k) const { return (uint32_t)(buf >> (64 - k)); }
+    __device__ __forceinline__ void skip(int k) {
+        buf <<= k;
+        nbits -= k;
+        pos += k;
+    }
+};
+
+// Decode one symbol; returns 0xffffffff on a malformed walk or on running past the payload.
+__device__ __forceinline__ uint32_t decode_one(BitReader& br, const uint32_t* table, const uint32_t* child,
+                                               const uint32_t* node_sym, uint32_t max_nodes) {
+    br.refill();
+    uint32_t e   = table[br.peek(kDecBits)];
+    uint32_t len = e & 0xffu;
+    if (len) {
+        if (br.pos + len > br.limit) return 0xffffffffu;
+        br.skip((int)len);
+        return e >> 8;
+    }
+    uint32_t node = e >> 8;
+    if (node == 0 || node >= max_nodes) return 0xffffffffu;  // prefix not in the tree
+    if (br.pos + kDecBits > br.limit) return 0xffffffffu;
+    br.skip(kDecBits);
+    for (int guard = 0; guard < 4096; guard++) {
+        br.refill();
+        if (br.pos + 1 > br.limit) return 0xffffffffu;
+        uint32_t b = br.peek(1);
+        br.skip(1);
+        node = __ldg(&child[2 * (size_t)node + b]);
+        if (node == 0 || node >= max_nodes) return 0xffffffffu;
+        uint32_t s = __ldg(&node_sym[node]);
+        if (s & 0x80000000u) return s & 0xffffu;
+    }
+    return 0xffffffffu;
+}
+
+__global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
+    __shared__ uint32_t s_table[1 << kDecBits];
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    __syncthreads();
+    const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= a.nchunks) return;
+    if (*a.status != VSZ_OK) return;  // e.g. the tree failed to parse: tables are not valid
+    const unsigned long long out0 = a.out_begin ? a.out_begin[j] : (unsigned long long)j * a.chunk_syms;
+    if (out0 >= a.n) return;
+    unsigned long long cnt = a.nsym ? a.nsym[j] : (unsigned long long)a.chunk_syms;
+    if (out0 + cnt > a.n) cnt = a.n - out0;
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 3u) * 8u;
+    const uint32_t* gw   = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)3);
+    BitReader br;
+    br.init(gw, base0 + a.start_bit[j], base0 + a.payload_bits);
+    // output position -> (row, x) for the per-segment zero counts
+    unsigned long long row = out0 / a.d0;
+    uint32_t x             = (uint32_t)(out0 - row * a.d0);
+    uint32_t zeros         = 0;
+    auto flush = [&]() {
+        if (zeros && a.seg_zero) atomicAdd(&a.seg_zero[row * a.nxs + (x >> 8)], zeros);
+        zeros = 0;
+    };
+    uint16_t* out = a.codes + out0;
+    for (unsigned long long k = 0; k < cnt; k++) {
+        uint32_t s = decode_one(br, s_table, a.child, a.node_sym, a.max_nodes);
+        if (s == 0xffffffffu) {
+            set_status(a.status, VSZ_ERR_CORRUPT);
+            return;
+        }
+        out[k] = (uint16_t)s;
+        zeros += (s == 0);
+        x++;
+        if (x == a.d0) {
+            x--;
+            flush();
+            x = 0;
+            row++;
+        } else if ((x & 255u) == 0) {
+            x--;
+            flush();
+            x++;
+        }
+    }
+    flush();
+}
+
+// Constant fill for a one-symbol tree (src/huffman.hh:348-352).
+__global__ void k_huff_const(uint16_t* codes, size_t n, const uint32_t* info, uint32_t* seg_zero, uint32_t d0, uint32_t nxs,
+                             const int* status) {
+    if (*status != VSZ_OK) return;
+    const uint16_t c = (uint16_t)info[1];
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        codes[i] = c;
+        if (c == 0 && seg_zero) {
+            size_t row = i / d0;
+            uint32_t x = (uint32_t)(i - row * d0);
+            atomicAdd(&seg_zero[row * nxs + (x >> 8)], 1u);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// K4c: self-synchronising chunk boundaries for streams without an index (reference archives).
+// Chunk j owns the codewords that START in [j C, (j+1) C).  Round 0 decodes every chunk from its
+// nominal start; each later round re-decodes chunks whose start moved (the exit of chunk j - 1
+// from the previous round) until no exit changes.  Tree-Huffman codes resynchronise within a few
+// codewords, so this normally converges in two rounds.
+// ------------------------------------------------------------------------------------------
+
+__device__ void sync_decode_chunk(const HuffSyncArgs& a, const uint32_t* table, size_t j, unsigned long long start,
+                                  unsigned long long* exit_out, uint32_t* cnt_out) {
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 3u) * 8u;
+    const uint32_t* gw   = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)3);
+    const unsigned long long end = (unsigned long long)(j + 1) * a.chunk_bits;
+    BitReader br;
+    br.init(gw, base0 + start, base0 + a.payload_bits);
+    uint32_t cnt = 0;
+    while (br.pos - base0 < end && br.pos - base0 < a.payload_bits) {
+        uint32_t s = decode_one(br, table, a.child, a.node_sym, a.max_nodes);
+        if (s == 0xffffffffu) break;  // padding at the stream end, or a wrong (unsynchronised) start
+        cnt++;
+    }
+    *exit_out = br.pos - base0;
+    *cnt_out  = cnt;
+}
+
+__global__ void __launch_bounds__(256) k_huff_sync_init(HuffSyncArgs a) {
+    __shared__ uint32_t s_table[1 << kDecBits];
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    __syncthreads();
+    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= a.nchunks) return;
+    if (*a.status != VSZ_OK) {
+        a.start[j] = 0;
+        a.exit_a[j] = 0;
+        a.count[j] = 0;
+        return;
+    }
+    unsigned long long st = (unsigned long long)j * a.chunk_bits;
+    a.start[j] = st;
+    sync_decode_chunk(a, s_table, j, st, &a.exit_a[j], &a.count[j]);
+}
+
+__global__ void __launch_bounds__(256) k_huff_sync_round(HuffSyncArgs a, const unsigned long long* exit_in,
+                                                         unsigned long long* exit_out, int* changed) {
+    __shared__ uint32_t s_table[1 << kDecBits];
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    __syncthreads();
+    size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j >= a.nchunks) return;
+    if (*a.status != VSZ_OK) {
+        exit_out[j] = exit_in[j];
+        return;
+    }
+    unsigned long long want = (j == 0) ? 0ull : exit_in[j - 1];
+    if (want == a.start[j]) {
+        exit_out[j] = exit_in[j];
+        return;
+    }
+    a.start[j] = want;
+    unsigned long long ex;
+    uint32_t c;
+    if (want >= (unsigned long long)(j + 1) * a.chunk_bits || want >= a.payload_bits) {
+        ex = want;  // the previous chunk's last codeword reaches past this chunk: it owns none
+        c  = 0;
+    } else {
+        sync_decode_chunk(a, s_table, j, want, &ex, &c);
+    }
+    a.count[j]  = c;
+    exit_out[j] = ex;
+    if (ex != exit_in[j]) atomicExch(changed, 1);
+}
+
+// ------------------------------------------------------------------------------------------
+// Generic exclusive scan (decoupled look-back) of u16/u32 values into u64 offsets.
+// ------------------------------------------------------------------------------------------
+
+template <typename TIn>
+__global__ void __launch_bounds__(256) k_scan_excl(const TIn* __restrict__ in, unsigned long long* __restrict__ out,
+                                                   size_t n, unsigned long long* tile_status, uint32_t* tile_counter,
+                                                   unsigned long long* total, int* status) {
+    constexpr int PER = 16;
+    __shared__ unsigned long long s_scan[33];
+    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const size_t i0     = (size_t)tile * 256 * PER + (size_t)threadIdx.x * PER;
+    unsigned long long v[PER], sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        v[k] = (i0 + k < n) ? (unsigned long long)in[i0 + k] : 0ull;
+        sum += v[k];
+    }
+    unsigned long long tot;
+    unsigned long long ex = block_exclusive_scan<unsigned long long>(sum, s_scan, &tot);
+    if (threadIdx.x == 0) {
+        s_base = lookback_publish(tile_status, tile, tot, status);
+        if ((size_t)(tile + 1) * 256 * PER >= n && total) *total = s_base + tot;
+    }
+    __syncthreads();
+    unsigned long long run = s_base + ex;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        if (i0 + k < n) out[i0 + k] = run;
+        run += v[k];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------------
+
+int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
+    size_t heap_bytes = ((size_t)a.dict + 2) * sizeof(unsigned long long);
+    size_t smem       = 0;
+    a.heap_in_smem    = heap_bytes <= 48 * 1024 ? 1 : 0;
+    if (a.heap_in_smem) smem = heap_bytes;
+    k_huff_build<<<1, 256, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+size_t huff_build_scratch_bytes(int dict, size_t* stack_offset, size_t* heap_offset) {
+    size_t d   = (size_t)dict;
+    size_t off = 0;
+    off += 4 * d;          // used
+    off += 8 * d;          // lchild, rchild
+    off += 3 * 4 * 2 * d;  // preL, preR, preC
+    off += 2 * d;          // preT
+    off = (off + 15) & ~(size_t)15;
+    if (stack_offset) *stack_offset = off;
+    off += sizeof(DfsEntry) * 2 * d + 64;
+    off = (off + 15) & ~(size_t)15;
+    if (heap_offset) *heap_offset = off;
+    off += 8 * (d + 4);
+    return off;
+}
+
+int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
+    a.ntiles = (uint32_t)((a.n + kEncTile - 1) / kEncTile);
+    if (a.ntiles == 0) return cudaMemsetAsync(a.total_bits, 0, 8, st) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+    a.codes_aligned = (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0;
+    size_t cb_bytes = (size_t)a.dict * 9;
+    a.cb_in_smem    = cb_bytes <= 64 * 1024 ? 1 : 0;
+    size_t smem     = kEncMaxWords * 4 + (a.cb_in_smem ? cb_bytes : 0) + 16;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_huff_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024 + 64 * 1024 + 1024);
+        attr_set = true;
+    }
+    if (cudaMemsetAsync(a.tile_status, 0, 8 * (size_t)a.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
+    if (cudaMemsetAsync(a.tail_flag, 0, 4 * (size_t)a.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
+    if (cudaMemsetAsync(a.tile_counter, 0, 4, st) != cudaSuccess) return VSZ_ERR_CUDA;
+    int grid = (int)min((long long)a.ntiles, (long long)num_sms * 2);
+    k_huff_encode<<<grid, kEncThreads, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_table(HuffTableArgs a, cudaStream_t st) {
+    k_huff_table<<<1, 1024, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
+    if (a.nchunks == 0) return VSZ_OK;
+    int grid = (int)((a.nchunks + 255) / 256);
+    k_huff_decode<<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_const(uint16_t* codes, size_t n, const uint32_t* info, uint32_t* seg_zero, uint32_t d0, uint32_t nxs,
+                      const int* status, cudaStream_t st, int num_sms) {
+    int grid = (int)min((long long)((n + 255) / 256), (long long)num_sms * 8);
+    if (grid < 1) grid = 1;
+    k_huff_const<<<grid, 256, 0, st>>>(codes, n, info, seg_zero, d0, nxs, status);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_sync_init(HuffSyncArgs a, cudaStream_t st) {
+    if (a.nchunks == 0) return VSZ_OK;
+    k_huff_sync_init<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_sync_round(HuffSyncArgs a, const unsigned long long* exit_in, unsigned long long* exit_out, int* changed,
+                           cudaStream_t st) {
+    k_huff_sync_round<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a, exit_in, exit_out, changed);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+template <typename TIn>
+int launch_scan_excl_t(const TIn* in, unsigned long long* out, size_t n, unsigned long long* tile_status,
+                       uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st) {
+    size_t ntiles = (n + 4095) / 4096;
+    if (ntiles == 0) {
+        if (total) return cudaMemsetAsync(total, 0, 8, st) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+        return VSZ_OK;
+    }
+    if (cudaMemsetAsync(tile_status, 0, 8 * ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
+    if (cudaMemsetAsync(tile_counter, 0, 4, st) != cudaSuccess) return VSZ_ERR_CUDA;
+    k_scan_excl<TIn><<<(unsigned)ntiles, 256, 0, st>>>(in, out, n, tile_status, tile_counter, total, status);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_scan_u16(const uint16_t* in, unsigned long long* out, size_t n, unsigned long long* ts, uint32_t* tc,
+                    unsigned long long* total, int* status, cudaStream_t st) {
+    return launch_scan_excl_t<uint16_t>(in, out, n, ts, tc, total, status, st);
+}
+int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsigned long long* ts, uint32_t* tc,
+                    unsigned long long* total, int* status, cudaStream_t st) {
+    return launch_scan_excl_t<uint32_t>(in, out, n, ts, tc, total, status, st);
+}
+
+size_t scan_tmp_tiles(size_t n) { return (n + 4095) / 4096; }
+
+}  // namespace vsz

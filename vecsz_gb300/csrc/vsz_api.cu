@@ -1,0 +1,907 @@
+// C ABI of the library (include/vecsz_gb300.h): argument checks, workspace layout and the
+// stream-ordered compress / decompress pipelines built from the kernels in dq_*.cu and huffman.cu.
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "vsz_device.cuh"
+#include "vsz_huffman.h"
+#include "vsz_kernels.h"
+
+using namespace vsz;
+
+static_assert(sizeof(Consts) <= VSZ_CONSTS_BYTES, "Consts must fit VSZ_CONSTS_BYTES");
+
+namespace {
+
+constexpr uint32_t kTrailerMagic   = 0x545A5356u;  // "VSZT"
+constexpr uint32_t kTrailerVersion = 1;
+constexpr uint32_t kTrailerFixed   = 64;
+
+#define VSZ_TRY(x)                        \
+    do {                                  \
+        int _rc = (x);                    \
+        if (_rc != VSZ_OK) return _rc;    \
+    } while (0)
+#define VSZ_CUDA(x)                                    \
+    do {                                               \
+        if ((x) != cudaSuccess) return VSZ_ERR_CUDA;   \
+    } while (0)
+
+// Bump allocator over a caller workspace; with base == nullptr it only measures.
+struct Bump {
+    uint8_t* base;
+    size_t cap;
+    size_t off = 0;
+    template <class T>
+    T* take(size_t count, size_t align = 256) {
+        off  = (off + align - 1) & ~(align - 1);
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+    bool fits() const { return off <= cap; }
+};
+
+int g_sms[64];
+
+int num_sms() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!g_sms[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        g_sms[dev] = v > 0 ? v : 152;
+    }
+    return g_sms[dev];
+}
+
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+bool valid_dims(int ndim, const size_t* dims) {
+    if (ndim < 1 || ndim > 3 || !dims) return false;
+    size_t n = 1;
+    for (int i = 0; i < ndim; i++) {
+        if (dims[i] == 0 || dims[i] > 0x7fffffffu) return false;  // the archive stores i32 dims
+        n *= dims[i];
+        if (n > (1ull << 36)) return false;
+    }
+    return true;
+}
+
+bool valid_dict(int dict) { return dict >= 2 && dict <= 65536 && (dict % 2) == 0; }
+bool valid_bs(int bs) { return bs == 8 || bs == 16 || bs == 32 || bs == 64; }
+
+int check_params(const vsz_params* p, int ndim, const size_t* dims) {
+    if (!p || !valid_dims(ndim, dims)) return VSZ_ERR_INVALID;
+    if (!(p->eb > 0.0) || p->eb != p->eb || p->eb > 1e300) return VSZ_ERR_INVALID;
+    if (p->mode != VSZ_MODE_ABS && p->mode != VSZ_MODE_R2R) return VSZ_ERR_INVALID;
+    if (!valid_dict(p->dict_size)) return VSZ_ERR_INVALID;
+    if (p->block_size <= 0) return VSZ_ERR_INVALID;
+    if (!valid_bs(p->block_size)) return VSZ_ERR_UNSUPPORTED;
+    return VSZ_OK;
+}
+
+size_t hdr_bytes(int ndim) { return 4 * (size_t)(ndim + 1) + 8 + 24; }
+
+DqArgs make_dq_args(const Geometry& g, int bs, int dict, const float* x, const Consts* c, uint16_t* code,
+                    float* scratch, uint8_t* seg_count, unsigned long long* hist) {
+    DqArgs a{};
+    a.x = x;
+    a.code = code;
+    a.scratch = scratch;
+    a.seg_count = seg_count;
+    a.hist = hist;
+    a.consts = c;
+    a.d0 = g.d0;
+    a.d1 = g.d1;
+    a.d2 = g.d2;
+    a.nxt = g.nxt;
+    a.nyg = (g.d1 + 7) / 8;
+    a.nzb = (g.ndim == 3) ? (g.d2 + bs - 1) / bs : 1;
+    a.xtail = (g.d0 % 8) ? (g.d0 & ~7u) : g.d0;
+    a.R = dict / 2;
+    a.dict = dict;
+    a.smem_hist = dict <= 16384 ? 1 : 0;
+    if (g.ndim == 1) a.nunits = (g.nxt + 3) / 4;  // 4 tiles per unit
+    else a.nunits = (unsigned long long)g.nxt * a.nyg * a.nzb;
+    return a;
+}
+
+// ---- archive finalization --------------------------------------------------------------------
+
+struct FinalizeArgs {
+    uint8_t* archive;
+    int ndim;
+    uint32_t dims[3];
+    double eb;  // user eb (header field)
+    int mode, dict, bs;
+    size_t hdr;
+    const Consts* consts;
+    const uint32_t* build_info;             // node count, tree bytes, max len
+    const unsigned long long* payload_bits;
+    const unsigned long long* n_out;
+    const int* status;
+    unsigned long long* result;             // vsz_result
+    const uint16_t* chunk_bits;
+    unsigned long long n_chunks;
+};
+
+__device__ __forceinline__ void put_bytes(uint8_t* d, const void* src, int n) {
+    const uint8_t* s = reinterpret_cast<const uint8_t*>(src);
+    for (int i = 0; i < n; i++) d[i] = s[i];
+}
+
+__device__ __forceinline__ size_t trailer_index_pad(size_t data_size) {
+    size_t start = data_size + kTrailerFixed;
+    return ((start + 7) & ~(size_t)7) - data_size;
+}
+
+// Header, result record and trailer (one thread), then the index copy (whole grid).
+__global__ void k_finalize(FinalizeArgs f) {
+    const unsigned long long bits = *f.payload_bits;
+    const unsigned long long nout = *f.n_out;
+    const uint32_t tree           = f.build_info[1];
+    const size_t huff_bytes       = 8 + (size_t)tree + (size_t)((bits + 7) >> 3);
+    const size_t data_size        = f.hdr + huff_bytes + 4 * (size_t)nout;
+    const size_t pad              = trailer_index_pad(data_size);
+    const size_t trailer          = ((pad + 2 * (size_t)f.n_chunks) + 7) & ~(size_t)7;
+    uint8_t* t                    = f.archive + data_size;
+    const int st                  = f.consts->status != VSZ_OK ? f.consts->status : *f.status;
+    if (st != VSZ_OK) {
+        // sizes from failed stages are not meaningful: report the status, write no archive bytes
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            for (int i = 0; i < 8; i++) f.result[i] = 0;
+            f.result[5] = (unsigned long long)st;
+        }
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int32_t nd = f.ndim;
+        put_bytes(f.archive, &nd, 4);
+        for (int i = 0; i < f.ndim; i++) {
+            int32_t d = (int32_t)f.dims[i];
+            put_bytes(f.archive + 4 * (1 + i), &d, 4);
+        }
+        put_bytes(f.archive + 4 * (f.ndim + 1), &f.eb, 8);
+        unsigned long long lens[3] = {0ull, (unsigned long long)huff_bytes, nout};
+        put_bytes(f.archive + 4 * (f.ndim + 1) + 8, lens, 24);
+        // trailer fixed part
+        uint32_t u32[4] = {kTrailerMagic, kTrailerVersion, kTrailerFixed, (uint32_t)kChunkSyms};
+        put_bytes(t, u32, 16);
+        double ebf = f.consts->eb_final, vr = f.consts->range;
+        put_bytes(t + 16, &ebf, 8);
+        put_bytes(t + 24, &vr, 8);
+        int32_t i32[3] = {f.mode, f.dict, f.bs};
+        put_bytes(t + 32, i32, 12);
+        uint32_t padu = (uint32_t)pad;
+        put_bytes(t + 44, &padu, 4);
+        unsigned long long nch = f.n_chunks, tsz = trailer;
+        put_bytes(t + 48, &nch, 8);
+        put_bytes(t + 56, &tsz, 8);
+        for (size_t i = kTrailerFixed; i < pad; i++) t[i] = 0;
+        unsigned long long* r = f.result;
+        r[0] = data_size;
+        r[1] = trailer;
+        r[2] = nout;
+        r[3] = huff_bytes;
+        r[4] = bits;
+        r[5] = (unsigned long long)st;
+        r[6] = f.build_info[2];
+        r[7] = f.build_info[0];
+    }
+    uint16_t* idx = reinterpret_cast<uint16_t*>(t + pad);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < f.n_chunks; i += (size_t)gridDim.x * blockDim.x)
+        idx[i] = f.chunk_bits[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        size_t used = pad + 2 * (size_t)f.n_chunks;
+        for (size_t i = used; i < trailer; i++) t[i] = 0;
+    }
+}
+
+__global__ void k_check_zeros(const unsigned long long* total_zeros, unsigned long long n_out, int* status) {
+    if (*total_zeros != n_out) set_status(status, VSZ_ERR_CORRUPT);
+}
+
+__global__ void k_copy_status(const int* from, const Consts* c, int* to) {
+    int st = c->status != VSZ_OK ? c->status : *from;
+    *to    = st;
+}
+
+// ---- workspace layouts ------------------------------------------------------------------------
+
+struct CompressWs {
+    Consts* consts;
+    uint32_t* mm;
+    int* status;
+    unsigned long long* hist;
+    uint16_t* code;
+    uint8_t* seg_count;
+    float* scratch;
+    unsigned long long* g_tile_status;
+    uint32_t* g_counter;
+    unsigned long long* n_out;
+    uint8_t* build_scratch;
+    size_t build_stack_off, build_heap_off;
+    unsigned long long* cb_word;
+    uint8_t* cb_len;
+    uint32_t* build_info;
+    unsigned long long* e_tile_status;
+    uint32_t* e_tail;
+    uint32_t* e_counter;
+    unsigned long long* total_bits;
+    uint16_t* chunk_bits;
+    size_t n_chunks;
+    size_t bytes;
+};
+
+CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t cap) {
+    Bump b{base, cap};
+    CompressWs w{};
+    w.consts    = b.take<Consts>(1);
+    w.mm        = b.take<uint32_t>(4);
+    w.status    = b.take<int>(4);
+    w.hist      = b.take<unsigned long long>(dict);
+    w.code      = b.take<uint16_t>(g.n + 8);
+    w.seg_count = b.take<uint8_t>(g.nseg + 16);
+    w.scratch   = b.take<float>(g.nseg * kSegX);
+    size_t gt   = (g.nseg + 4095) / 4096 + 1;
+    w.g_tile_status = b.take<unsigned long long>(gt);
+    w.g_counter = b.take<uint32_t>(4);
+    w.n_out     = b.take<unsigned long long>(1);
+    size_t so, ho;
+    size_t bsz  = huff_build_scratch_bytes(dict, &so, &ho);
+    w.build_scratch   = b.take<uint8_t>(bsz);
+    w.build_stack_off = so;
+    w.build_heap_off  = ho;
+    w.cb_word    = b.take<unsigned long long>(dict);
+    w.cb_len     = b.take<uint8_t>(dict);
+    w.build_info = b.take<uint32_t>(4);
+    size_t et    = (g.n + 4095) / 4096 + 1;
+    w.e_tile_status = b.take<unsigned long long>(et);
+    w.e_tail     = b.take<uint32_t>(et);
+    w.e_counter  = b.take<uint32_t>(4);
+    w.total_bits = b.take<unsigned long long>(1);
+    w.n_chunks   = (g.n + kChunkSyms - 1) / kChunkSyms;
+    w.chunk_bits = b.take<uint16_t>(w.n_chunks + 8);
+    w.bytes      = b.off + 256;
+    return w;
+}
+
+size_t archive_capacity(const Geometry& g, int dict) {
+    size_t tree_max = tree_bytes_size((uint32_t)(2 * dict - 1));
+    size_t n_chunks = (g.n + kChunkSyms - 1) / kChunkSyms;
+    return hdr_bytes(g.ndim) + 8 + tree_max + 8 * g.n + 4 * g.n + kTrailerFixed + 8 + 2 * n_chunks + 64;
+}
+
+struct DecompressWs {
+    Consts* consts;
+    uint32_t* mm;
+    int* status;
+    uint32_t* table;
+    uint32_t* child;
+    uint32_t* node_sym;
+    uint32_t* parent;
+    uint32_t* tinfo;
+    uint16_t* code;
+    uint32_t* seg_zero;
+    unsigned long long* seg_off;
+    unsigned long long* scan_status;
+    uint32_t* scan_counter;
+    unsigned long long* scan_total;
+    unsigned long long* chunk_start;  // index path
+    unsigned long long* s_start;      // sync path
+    unsigned long long* s_exit_a;
+    unsigned long long* s_exit_b;
+    uint32_t* s_count;
+    unsigned long long* s_out_begin;
+    int* s_changed;
+    float* outliers;
+    size_t bytes;
+};
+
+DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes, size_t n_out, size_t n_index_chunks,
+                               uint8_t* base, size_t cap) {
+    Bump b{base, cap};
+    DecompressWs w{};
+    uint32_t maxn = (uint32_t)(2 * dict);
+    w.consts   = b.take<Consts>(1);
+    w.mm       = b.take<uint32_t>(4);
+    w.status   = b.take<int>(4);
+    w.table    = b.take<uint32_t>(1u << kDecBits);
+    w.child    = b.take<uint32_t>(2 * (size_t)maxn);
+    w.node_sym = b.take<uint32_t>(maxn);
+    w.parent   = b.take<uint32_t>(maxn);
+    w.tinfo    = b.take<uint32_t>(4);
+    w.code     = b.take<uint16_t>(g.n + 8);
+    uint32_t nxs = (g.d0 + 255) / 256;
+    size_t nsegd = g.nrows * nxs;
+    w.seg_zero = b.take<uint32_t>(nsegd + 1);
+    w.seg_off  = b.take<unsigned long long>(nsegd + 1);
+    size_t nsync = (payload_bytes * 8 + kSyncBits - 1) / kSyncBits + 1;
+    size_t scan_n = nsegd;
+    if (n_index_chunks > scan_n) scan_n = n_index_chunks;
+    if (nsync > scan_n) scan_n = nsync;
+    w.scan_status  = b.take<unsigned long long>(scan_tmp_tiles(scan_n) + 1);
+    w.scan_counter = b.take<uint32_t>(4);
+    w.scan_total   = b.take<unsigned long long>(1);
+    w.chunk_start  = b.take<unsigned long long>(n_index_chunks + 1);
+    w.s_start      = b.take<unsigned long long>(nsync);
+    w.s_exit_a     = b.take<unsigned long long>(nsync);
+    w.s_exit_b     = b.take<unsigned long long>(nsync);
+    w.s_count      = b.take<uint32_t>(nsync);
+    w.s_out_begin  = b.take<unsigned long long>(nsync);
+    w.s_changed    = b.take<int>(4);
+    w.outliers     = b.take<float>(n_out + 4);
+    w.bytes        = b.off + 256;
+    return w;
+}
+
+// Decode n codes from a Huffman section at d_huff.  Index path when chunk_bits != null.
+int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, size_t tree_bytes, size_t n, int dict,
+                 const uint16_t* chunk_bits, size_t n_index_chunks, uint32_t chunk_syms, const DecompressWs& w,
+                 uint32_t* seg_zero, uint32_t d0, cudaStream_t st) {
+    const uint8_t* payload   = d_huff + 8 + tree_bytes;
+    size_t payload_bytes     = huff_bytes - 8 - tree_bytes;
+    unsigned long long pbits = (unsigned long long)payload_bytes * 8ull;
+    uint32_t nxs             = (d0 + 255) / 256;
+    HuffTableArgs ta{};
+    ta.huff = d_huff;
+    ta.huff_bytes = huff_bytes;
+    ta.dict = dict;
+    ta.max_nodes = (uint32_t)(2 * dict - 1);
+    ta.table = w.table;
+    ta.child = w.child;
+    ta.node_sym = w.node_sym;
+    ta.parent = w.parent;
+    ta.info = w.tinfo;
+    ta.status = w.status;
+    VSZ_TRY(launch_huff_table(ta, st));
+    if (node_count == 1) {
+        // one-symbol tree: constant output (src/huffman.hh:348-352)
+        return launch_huff_const(w.code, n, w.tinfo, seg_zero, d0, nxs, w.status, st, num_sms());
+    }
+    HuffDecodeArgs da{};
+    da.payload = payload;
+    da.payload_bits = pbits;
+    da.table = w.table;
+    da.child = w.child;
+    da.node_sym = w.node_sym;
+    da.codes = w.code;
+    da.n = n;
+    da.seg_zero = seg_zero;
+    da.d0 = d0;
+    da.nxs = nxs;
+    da.max_nodes = (uint32_t)(2 * dict - 1);
+    da.status = w.status;
+    if (chunk_bits) {
+        VSZ_TRY(launch_scan_u16(chunk_bits, w.chunk_start, n_index_chunks, w.scan_status, w.scan_counter, nullptr,
+                                w.status, st));
+        da.start_bit = w.chunk_start;
+        da.out_begin = nullptr;
+        da.nsym = nullptr;
+        da.nchunks = n_index_chunks;
+        da.chunk_syms = chunk_syms;
+        return launch_huff_decode(da, st);
+    }
+    // self-synchronising path
+    HuffSyncArgs sa{};
+    sa.payload = payload;
+    sa.payload_bits = pbits;
+    sa.table = w.table;
+    sa.child = w.child;
+    sa.node_sym = w.node_sym;
+    sa.nchunks = (size_t)((pbits + kSyncBits - 1) / kSyncBits);
+    sa.chunk_bits = kSyncBits;
+    sa.start = w.s_start;
+    sa.exit_a = w.s_exit_a;
+    sa.count = w.s_count;
+    sa.max_nodes = (uint32_t)(2 * dict - 1);
+    sa.status = w.status;
+    if (sa.nchunks == 0) return VSZ_ERR_CORRUPT;
+    VSZ_TRY(launch_huff_sync_init(sa, st));
+    unsigned long long* ein  = w.s_exit_a;
+    unsigned long long* eout = w.s_exit_b;
+    for (size_t round = 0; round < sa.nchunks + 2; round++) {
+        VSZ_CUDA(cudaMemsetAsync(w.s_changed, 0, sizeof(int), st));
+        VSZ_TRY(launch_huff_sync_round(sa, ein, eout, w.s_changed, st));
+        int changed = 0;
+        VSZ_CUDA(cudaMemcpyAsync(&changed, w.s_changed, sizeof(int), cudaMemcpyDeviceToHost, st));
+        VSZ_CUDA(cudaStreamSynchronize(st));
+        unsigned long long* t = ein;
+        ein  = eout;
+        eout = t;
+        if (!changed) break;
+    }
+    VSZ_TRY(launch_scan_u32(w.s_count, w.s_out_begin, sa.nchunks, w.scan_status, w.scan_counter, w.scan_total,
+                            w.status, st));
+    unsigned long long total = 0;
+    VSZ_CUDA(cudaMemcpyAsync(&total, w.scan_total, 8, cudaMemcpyDeviceToHost, st));
+    VSZ_CUDA(cudaStreamSynchronize(st));
+    if (total < n) return VSZ_ERR_CORRUPT;
+    da.start_bit = w.s_start;
+    da.out_begin = w.s_out_begin;
+    da.nsym = w.s_count;
+    da.nchunks = sa.nchunks;
+    da.chunk_syms = 0;
+    return launch_huff_decode(da, st);
+}
+
+}  // namespace
+
+// =================================================================================================
+extern "C" {
+
+const char* vsz_status_string(vsz_status s) {
+    switch (s) {
+        case VSZ_OK: return "ok";
+        case VSZ_ERR_INVALID: return "invalid argument";
+        case VSZ_ERR_CUDA: return "CUDA runtime error";
+        case VSZ_ERR_CORRUPT: return "corrupt archive or bitstream";
+        case VSZ_ERR_CAPACITY: return "buffer or workspace too small";
+        case VSZ_ERR_TIMEOUT: return "device-side wait timed out";
+        case VSZ_ERR_UNSUPPORTED: return "unsupported setting";
+        case VSZ_ERR_RANGE: return "zero value range (r2r)";
+        case VSZ_ERR_NOMEM: return "out of memory";
+        case VSZ_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* vsz_version(void) { return "vecsz_gb300 0.1 (sm_103a)"; }
+
+vsz_status vsz_eb_setup(const vsz_params* p, const float* d_in, size_t n, void* d_consts, void* d_tmp, void* stream) {
+    if (!p || !d_consts || !d_tmp) return VSZ_ERR_INVALID;
+    if (p->mode == VSZ_MODE_R2R && (!d_in || n == 0)) return VSZ_ERR_INVALID;
+    if (!(p->eb > 0.0)) return VSZ_ERR_INVALID;
+    return launch_eb_setup(p->mode, p->eb, d_in, n, reinterpret_cast<Consts*>(d_consts),
+                           reinterpret_cast<uint32_t*>(d_tmp), S(stream));
+}
+
+vsz_status vsz_consts_read(const void* d_consts, double h_out[4], int* h_status, void* stream) {
+    Consts c;
+    VSZ_CUDA(cudaMemcpyAsync(&c, d_consts, sizeof(Consts), cudaMemcpyDeviceToHost, S(stream)));
+    VSZ_CUDA(cudaStreamSynchronize(S(stream)));
+    if (h_out) {
+        h_out[0] = c.eb_final;
+        h_out[1] = c.c_d;
+        h_out[2] = c.r_d;
+        h_out[3] = c.range;
+    }
+    if (h_status) *h_status = c.status;
+    return VSZ_OK;
+}
+
+size_t vsz_outlier_segments(int ndim, const size_t dims[3]) {
+    if (!valid_dims(ndim, dims)) return 0;
+    return make_geometry(ndim, dims).nseg;
+}
+
+vsz_status vsz_dualquant(int ndim, const size_t dims[3], int block_size, int dict_size, const float* d_in,
+                         const void* d_consts, uint16_t* d_code, float* d_scratch, uint8_t* d_seg_count,
+                         uint64_t* d_hist, void* stream) {
+    if (!valid_dims(ndim, dims) || !valid_dict(dict_size) || !d_in || !d_consts || !d_code || !d_scratch ||
+        !d_seg_count || !d_hist)
+        return VSZ_ERR_INVALID;
+    if (!valid_bs(block_size)) return VSZ_ERR_UNSUPPORTED;
+    Geometry g = make_geometry(ndim, dims);
+    DqArgs a   = make_dq_args(g, block_size, dict_size, d_in, reinterpret_cast<const Consts*>(d_consts), d_code,
+                              d_scratch, d_seg_count, reinterpret_cast<unsigned long long*>(d_hist));
+    return launch_dq_compress(a, ndim, block_size, S(stream), num_sms());
+}
+
+size_t vsz_outlier_gather_tmp_bytes(int ndim, const size_t dims[3]) {
+    if (!valid_dims(ndim, dims)) return 0;
+    Geometry g = make_geometry(ndim, dims);
+    return 256 + 8 * ((g.nseg + 4095) / 4096 + 1) + 256;
+}
+
+vsz_status vsz_outlier_gather(int ndim, const size_t dims[3], const uint8_t* d_seg_count, const float* d_scratch,
+                              float* d_out, uint64_t* d_count, void* d_tmp, size_t tmp_bytes, void* stream) {
+    if (!valid_dims(ndim, dims) || !d_seg_count || !d_scratch || !d_out || !d_count || !d_tmp) return VSZ_ERR_INVALID;
+    if (tmp_bytes < vsz_outlier_gather_tmp_bytes(ndim, dims)) return VSZ_ERR_CAPACITY;
+    Geometry g = make_geometry(ndim, dims);
+    Bump b{reinterpret_cast<uint8_t*>(d_tmp), tmp_bytes};
+    GatherArgs ga{};
+    ga.status       = b.take<int>(4);
+    ga.tile_counter = b.take<uint32_t>(4);
+    ga.tile_status  = b.take<unsigned long long>((g.nseg + 4095) / 4096 + 1);
+    ga.seg_count    = d_seg_count;
+    ga.scratch      = d_scratch;
+    ga.nseg         = g.nseg;
+    ga.out_f32      = d_out;
+    ga.total        = reinterpret_cast<unsigned long long*>(d_count);
+    VSZ_CUDA(cudaMemsetAsync(ga.status, 0, sizeof(int), S(stream)));
+    return launch_outlier_gather(ga, S(stream));
+}
+
+size_t vsz_codebook_bytes(int dict_size) { return (size_t)dict_size * 9 + 64; }
+size_t vsz_huff_head_max(int dict_size) { return 8 + tree_bytes_size((uint32_t)(2 * dict_size - 1)); }
+size_t vsz_huffman_build_tmp_bytes(int dict_size) { return huff_build_scratch_bytes(dict_size, nullptr, nullptr) + 512; }
+
+vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_codebook, uint8_t* d_huff_head,
+                             uint32_t* d_info, void* d_tmp, size_t tmp_bytes, void* stream) {
+    if (!valid_dict(dict_size) || !d_hist || !d_codebook || !d_huff_head || !d_info || !d_tmp) return VSZ_ERR_INVALID;
+    if (tmp_bytes < vsz_huffman_build_tmp_bytes(dict_size)) return VSZ_ERR_CAPACITY;
+    HuffBuildArgs a{};
+    a.hist    = reinterpret_cast<const unsigned long long*>(d_hist);
+    a.dict    = dict_size;
+    a.cb_word = reinterpret_cast<unsigned long long*>(d_codebook);
+    a.cb_len  = reinterpret_cast<uint8_t*>(d_codebook) + 8 * (size_t)dict_size;
+    a.out     = d_huff_head;
+    a.info    = d_info;
+    a.status  = reinterpret_cast<int*>(d_tmp);
+    a.scratch = reinterpret_cast<uint8_t*>(d_tmp) + 256;
+    huff_build_scratch_bytes(dict_size, &a.stack_offset, &a.heap_offset);
+    VSZ_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), S(stream)));
+    return launch_huff_build(a, S(stream));
+}
+
+size_t vsz_huffman_encode_tmp_bytes(size_t n) {
+    size_t nt = (n + 4095) / 4096 + 1;
+    return 1024 + 12 * nt + 256;
+}
+
+vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_codebook, int dict_size,
+                              uint8_t* d_payload, uint64_t* d_bits, uint16_t* d_chunk_bits, void* d_tmp,
+                              size_t tmp_bytes, void* stream) {
+    if (!valid_dict(dict_size) || !d_code || !d_codebook || !d_payload || !d_bits || !d_tmp) return VSZ_ERR_INVALID;
+    if (tmp_bytes < vsz_huffman_encode_tmp_bytes(n)) return VSZ_ERR_CAPACITY;
+    Bump b{reinterpret_cast<uint8_t*>(d_tmp), tmp_bytes};
+    HuffEncodeArgs a{};
+    a.status       = b.take<int>(4);
+    a.tile_counter = b.take<uint32_t>(4);
+    size_t nt      = (n + 4095) / 4096 + 1;
+    a.tile_status  = b.take<unsigned long long>(nt);
+    a.tail_flag    = b.take<uint32_t>(nt);
+    a.codes        = d_code;
+    a.n            = n;
+    a.cb_word      = reinterpret_cast<const unsigned long long*>(d_codebook);
+    a.cb_len       = reinterpret_cast<const uint8_t*>(d_codebook) + 8 * (size_t)dict_size;
+    a.dict         = dict_size;
+    a.out          = d_payload;
+    a.total_bits   = reinterpret_cast<unsigned long long*>(d_bits);
+    a.chunk_bits   = d_chunk_bits;
+    VSZ_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), S(stream)));
+    return launch_huff_encode(a, S(stream), num_sms());
+}
+
+size_t vsz_huffman_decode_tmp_bytes(size_t huff_bytes, size_t n, int dict_size) {
+    size_t dims[3] = {n, 1, 1};
+    Geometry g = make_geometry(1, dims);
+    return layout_decompress(g, dict_size, huff_bytes, 0, 0, nullptr, 0).bytes;
+}
+
+vsz_status vsz_huffman_decode(const uint8_t* d_huff, size_t huff_bytes, size_t n, int dict_size, uint16_t* d_code,
+                              void* d_tmp, size_t tmp_bytes, void* stream) {
+    if (!d_huff || !d_code || !d_tmp || n == 0 || !valid_dict(dict_size) || huff_bytes < 9) return VSZ_ERR_INVALID;
+    if (n > 0x7fffffffull) return VSZ_ERR_UNSUPPORTED;
+    size_t need = vsz_huffman_decode_tmp_bytes(huff_bytes, n, dict_size);
+    if (tmp_bytes < need) return VSZ_ERR_CAPACITY;
+    size_t dims[3] = {n, 1, 1};
+    Geometry g = make_geometry(1, dims);
+    DecompressWs w = layout_decompress(g, dict_size, huff_bytes, 0, 0, reinterpret_cast<uint8_t*>(d_tmp), tmp_bytes);
+    // node count / tree size from the big-endian header on the device: copy 4 bytes
+    uint8_t h4[4];
+    VSZ_CUDA(cudaMemcpyAsync(h4, d_huff, 4, cudaMemcpyDeviceToHost, S(stream)));
+    VSZ_CUDA(cudaStreamSynchronize(S(stream)));
+    uint32_t nc = ((uint32_t)h4[0] << 24) | ((uint32_t)h4[1] << 16) | ((uint32_t)h4[2] << 8) | h4[3];
+    if (nc == 0 || nc > (uint32_t)(2 * dict_size - 1) || 8 + tree_bytes_size(nc) > huff_bytes) return VSZ_ERR_CORRUPT;
+    VSZ_CUDA(cudaMemsetAsync(w.status, 0, sizeof(int), S(stream)));
+    // decode into w.code, then copy to the caller (w.code is sized for n)
+    int rc = decode_codes(d_huff, huff_bytes, nc, tree_bytes_size(nc), n, dict_size, nullptr, 0, 0, w, nullptr,
+                          (uint32_t)n, S(stream));
+    if (rc) return rc;
+    VSZ_CUDA(cudaMemcpyAsync(d_code, w.code, n * sizeof(uint16_t), cudaMemcpyDeviceToDevice, S(stream)));
+    int st = 0;
+    VSZ_CUDA(cudaMemcpyAsync(&st, w.status, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
+    VSZ_CUDA(cudaStreamSynchronize(S(stream)));
+    return st;
+}
+
+size_t vsz_dualquant_decompress_tmp_bytes(int ndim, const size_t dims[3]) {
+    if (!valid_dims(ndim, dims)) return 0;
+    Geometry g = make_geometry(ndim, dims);
+    uint32_t nxs = (g.d0 + 255) / 256;
+    size_t nsegd = g.nrows * nxs;
+    return 1024 + 4 * (nsegd + 64) + 8 * (nsegd + 64) + 8 * (scan_tmp_tiles(nsegd) + 2) + 1024;
+}
+
+vsz_status vsz_dualquant_decompress(int ndim, const size_t dims[3], int block_size, int dict_size,
+                                    const uint16_t* d_code, const float* d_outliers, uint64_t n_outlier,
+                                    const void* d_consts, float* d_out, void* d_tmp, size_t tmp_bytes, void* stream) {
+    if (!valid_dims(ndim, dims) || !valid_dict(dict_size) || !d_code || !d_consts || !d_out || !d_tmp)
+        return VSZ_ERR_INVALID;
+    if (!valid_bs(block_size)) return VSZ_ERR_UNSUPPORTED;
+    if (tmp_bytes < vsz_dualquant_decompress_tmp_bytes(ndim, dims)) return VSZ_ERR_CAPACITY;
+    Geometry g = make_geometry(ndim, dims);
+    uint32_t nxs = (g.d0 + 255) / 256;
+    size_t nsegd = g.nrows * nxs;
+    Bump b{reinterpret_cast<uint8_t*>(d_tmp), tmp_bytes};
+    int* status = b.take<int>(4);
+    uint32_t* counter = b.take<uint32_t>(4);
+    uint32_t* seg_zero = b.take<uint32_t>(nsegd + 1);
+    unsigned long long* seg_off = b.take<unsigned long long>(nsegd + 1);
+    unsigned long long* tstat = b.take<unsigned long long>(scan_tmp_tiles(nsegd) + 1);
+    VSZ_CUDA(cudaMemsetAsync(status, 0, sizeof(int), S(stream)));
+    VSZ_TRY(launch_count_zeros(d_code, g.d0, g.nrows, seg_zero, S(stream), num_sms()));
+    VSZ_TRY(launch_scan_u32(seg_zero, seg_off, nsegd, tstat, counter, nullptr, status, S(stream)));
+    DqDecArgs a{};
+    a.codes      = d_code;
+    a.outliers   = d_outliers;
+    a.n_outliers = n_outlier;
+    a.status     = status;
+    a.seg_off    = seg_off;
+    a.consts     = reinterpret_cast<const Consts*>(d_consts);
+    a.out        = d_out;
+    a.d0 = g.d0;
+    a.d1 = g.d1;
+    a.d2 = g.d2;
+    a.n  = g.n;
+    a.R  = dict_size / 2;
+    bool force_general = getenv("VSZ_FORCE_GENERAL_DECOMPRESS") != nullptr;
+    VSZ_TRY(launch_dq_decompress(a, ndim, block_size, force_general, S(stream), num_sms()));
+    int st = 0;
+    VSZ_CUDA(cudaMemcpyAsync(&st, status, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
+    VSZ_CUDA(cudaStreamSynchronize(S(stream)));
+    return st;
+}
+
+// ---- whole-field compress ------------------------------------------------------------------------
+
+vsz_status vsz_compress_bounds(const vsz_params* p, int ndim, const size_t dims[3], size_t* ws_bytes,
+                               size_t* archive_cap) {
+    VSZ_TRY(check_params(p, ndim, dims));
+    Geometry g = make_geometry(ndim, dims);
+    if (ws_bytes) *ws_bytes = layout_compress(g, p->dict_size, nullptr, 0).bytes;
+    if (archive_cap) *archive_cap = archive_capacity(g, p->dict_size);
+    return VSZ_OK;
+}
+
+vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], const float* d_in, void* d_ws,
+                        size_t ws_bytes, uint8_t* d_archive, size_t archive_cap, uint64_t* d_result, void* stream) {
+    VSZ_TRY(check_params(p, ndim, dims));
+    if (!d_in || !d_ws || !d_archive || !d_result) return VSZ_ERR_INVALID;
+    Geometry g   = make_geometry(ndim, dims);
+    CompressWs w = layout_compress(g, p->dict_size, reinterpret_cast<uint8_t*>(d_ws), ws_bytes);
+    if (w.bytes > ws_bytes) return VSZ_ERR_CAPACITY;
+    if (archive_cap < archive_capacity(g, p->dict_size)) return VSZ_ERR_CAPACITY;
+    cudaStream_t st = S(stream);
+    const int dict  = p->dict_size;
+    const size_t hdr = hdr_bytes(ndim);
+    VSZ_CUDA(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+    VSZ_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(unsigned long long) * dict, st));
+    VSZ_CUDA(cudaMemsetAsync(w.build_info, 0, 4 * sizeof(uint32_t), st));
+    VSZ_CUDA(cudaMemsetAsync(w.total_bits, 0, sizeof(unsigned long long), st));
+    VSZ_CUDA(cudaMemsetAsync(w.n_out, 0, sizeof(unsigned long long), st));
+    // 1. error-bound family (+ value range for r2r)
+    VSZ_TRY(launch_eb_setup(p->mode, p->eb, d_in, g.n, w.consts, w.mm, st, w.status));
+    // 2. dual-quant + histogram + outlier ranking
+    DqArgs a = make_dq_args(g, p->block_size, dict, d_in, w.consts, w.code, w.scratch, w.seg_count, w.hist);
+    VSZ_TRY(launch_dq_compress(a, ndim, p->block_size, st, num_sms()));
+    // 3. tree + codebook; the Huffman section starts right after the header (no padding values)
+    HuffBuildArgs hb{};
+    hb.hist = w.hist;
+    hb.dict = dict;
+    hb.cb_word = w.cb_word;
+    hb.cb_len = w.cb_len;
+    hb.out = d_archive + hdr;
+    hb.info = w.build_info;
+    hb.scratch = w.build_scratch;
+    hb.stack_offset = w.build_stack_off;
+    hb.heap_offset = w.build_heap_off;
+    hb.status = w.status;
+    VSZ_TRY(launch_huff_build(hb, st));
+    // 4. bitstream, placed after the tree bytes (an offset only the device knows)
+    HuffEncodeArgs he{};
+    he.codes = w.code;
+    he.n = g.n;
+    he.cb_word = w.cb_word;
+    he.cb_len = w.cb_len;
+    he.dict = dict;
+    he.out = d_archive;
+    he.out_off = DevOffset{hdr + 8, w.build_info + 1, nullptr};
+    he.total_bits = w.total_bits;
+    he.chunk_bits = w.chunk_bits;
+    he.tile_status = w.e_tile_status;
+    he.tail_flag = w.e_tail;
+    he.tile_counter = w.e_counter;
+    he.status = w.status;
+    he.build_info = w.build_info;
+    VSZ_TRY(launch_huff_encode(he, st, num_sms()));
+    // 5. outliers after the bitstream, in row-major order
+    GatherArgs ga{};
+    ga.seg_count = w.seg_count;
+    ga.scratch = w.scratch;
+    ga.nseg = g.nseg;
+    ga.out_bytes = d_archive;
+    ga.out_off = DevOffset{hdr + 8, w.build_info + 1, w.total_bits};
+    ga.total = w.n_out;
+    ga.tile_status = w.g_tile_status;
+    ga.tile_counter = w.g_counter;
+    ga.status = w.status;
+    VSZ_TRY(launch_outlier_gather(ga, st));
+    // 6. header, result record, trailer with the decode index
+    FinalizeArgs f{};
+    f.archive = d_archive;
+    f.ndim = ndim;
+    f.dims[0] = g.d0;
+    f.dims[1] = g.d1;
+    f.dims[2] = g.d2;
+    f.eb = p->eb;
+    f.mode = p->mode;
+    f.dict = dict;
+    f.bs = p->block_size;
+    f.hdr = hdr;
+    f.consts = w.consts;
+    f.build_info = w.build_info;
+    f.payload_bits = w.total_bits;
+    f.n_out = w.n_out;
+    f.status = w.status;
+    f.result = reinterpret_cast<unsigned long long*>(d_result);
+    f.chunk_bits = w.chunk_bits;
+    f.n_chunks = w.n_chunks;
+    int fg = (int)((w.n_chunks + 255) / 256);
+    if (fg < 1) fg = 1;
+    if (fg > num_sms() * 4) fg = num_sms() * 4;
+    k_finalize<<<fg, 256, 0, st>>>(f);
+    VSZ_CUDA(cudaGetLastError());
+    return VSZ_OK;
+}
+
+// ---- archive parsing (host) ---------------------------------------------------------------------
+
+vsz_status vsz_archive_parse(const uint8_t* h, size_t len, vsz_archive_desc* d) {
+    if (!h || !d) return VSZ_ERR_INVALID;
+    memset(d, 0, sizeof(*d));
+    if (len < 4) return VSZ_ERR_CORRUPT;
+    int32_t nd;
+    memcpy(&nd, h, 4);
+    if (nd < 1 || nd > 3) return VSZ_ERR_CORRUPT;
+    size_t hdr = hdr_bytes(nd);
+    if (len < hdr) return VSZ_ERR_CORRUPT;
+    d->ndim = nd;
+    d->dims[0] = d->dims[1] = d->dims[2] = 1;
+    for (int i = 0; i < nd; i++) {
+        int32_t v;
+        memcpy(&v, h + 4 * (1 + i), 4);
+        if (v <= 0) return VSZ_ERR_CORRUPT;
+        d->dims[i] = (uint64_t)v;
+    }
+    memcpy(&d->eb, h + 4 * (nd + 1), 8);
+    uint64_t lens[3];
+    memcpy(lens, h + 4 * (nd + 1) + 8, 24);
+    d->n_pad = lens[0];
+    d->huff_bytes = lens[1];
+    d->n_outlier = lens[2];
+    d->header_bytes = hdr;
+    if (d->n_pad > (1ull << 40) || d->huff_bytes > (1ull << 44) || d->n_outlier > (1ull << 40)) return VSZ_ERR_CORRUPT;
+    d->huff_offset = hdr + 4 * d->n_pad;
+    d->data_size = d->huff_offset + d->huff_bytes + 4 * d->n_outlier;
+    if (d->data_size > len || d->huff_bytes < 8) return VSZ_ERR_CORRUPT;
+    const uint8_t* hh = h + d->huff_offset;
+    uint32_t nc = ((uint32_t)hh[0] << 24) | ((uint32_t)hh[1] << 16) | ((uint32_t)hh[2] << 8) | hh[3];
+    if (nc == 0) return VSZ_ERR_CORRUPT;
+    d->node_count = nc;
+    d->tree_bytes = tree_bytes_size(nc);
+    if (8 + d->tree_bytes > d->huff_bytes) return VSZ_ERR_CORRUPT;
+    d->payload_offset = d->huff_offset + 8 + d->tree_bytes;
+    d->payload_bytes = d->huff_bytes - 8 - d->tree_bytes;
+    d->outlier_offset = d->huff_offset + d->huff_bytes;
+    // this library's trailer
+    if (len >= d->data_size + kTrailerFixed) {
+        const uint8_t* t = h + d->data_size;
+        uint32_t u32[4];
+        memcpy(u32, t, 16);
+        if (u32[0] == kTrailerMagic && u32[1] == kTrailerVersion && u32[2] == kTrailerFixed) {
+            d->chunk_syms = u32[3];
+            memcpy(&d->eb_final, t + 16, 8);
+            memcpy(&d->value_range, t + 24, 8);
+            int32_t i32[3];
+            memcpy(i32, t + 32, 12);
+            d->mode = i32[0];
+            d->dict_size = i32[1];
+            d->block_size = i32[2];
+            uint32_t pad;
+            memcpy(&pad, t + 44, 4);
+            memcpy(&d->n_chunks, t + 48, 8);
+            memcpy(&d->trailer_size, t + 56, 8);
+            uint64_t n = d->dims[0] * d->dims[1] * d->dims[2];
+            bool ok = d->chunk_syms == (uint32_t)kChunkSyms && d->n_chunks == (n + kChunkSyms - 1) / kChunkSyms &&
+                      pad >= kTrailerFixed && d->data_size + pad + 2 * d->n_chunks <= len &&
+                      ((d->data_size + pad) % 8) == 0 && valid_dict(d->dict_size) && valid_bs(d->block_size);
+            if (ok) {
+                d->has_trailer = 1;
+                d->index_offset = d->data_size + pad;
+            }
+        }
+    }
+    return VSZ_OK;
+}
+
+static int resolve_decode_params(const vsz_archive_desc* d, const vsz_decompress_opts* o, int* dict, int* bs,
+                                 double* ebf) {
+    if (d->has_trailer) {
+        *dict = d->dict_size;
+        *bs = d->block_size;
+        *ebf = d->eb_final;
+    } else {
+        if (!o) return VSZ_ERR_INVALID;
+        *dict = o->dict_size;
+        *bs = o->block_size;
+        *ebf = d->eb;
+        if (o->mode == VSZ_MODE_R2R) {
+            if (!(o->value_range > 0)) return VSZ_ERR_RANGE;
+            *ebf = d->eb * o->value_range;  // src/types.cc:58
+        }
+    }
+    if (!valid_dict(*dict)) return VSZ_ERR_INVALID;
+    if (!valid_bs(*bs)) return VSZ_ERR_UNSUPPORTED;
+    if (!(*ebf > 0)) return VSZ_ERR_INVALID;
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress_bounds(const vsz_archive_desc* d, const vsz_decompress_opts* o, size_t* ws_bytes) {
+    if (!d) return VSZ_ERR_INVALID;
+    int dict, bs;
+    double ebf;
+    VSZ_TRY(resolve_decode_params(d, o, &dict, &bs, &ebf));
+    size_t dims[3] = {d->dims[0], d->dims[1], d->dims[2]};
+    Geometry g = make_geometry(d->ndim, dims);
+    if (ws_bytes)
+        *ws_bytes = layout_decompress(g, dict, d->payload_bytes, d->n_outlier, d->has_trailer ? d->n_chunks : 0,
+                                      nullptr, 0).bytes;
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* o, const uint8_t* d_archive,
+                          void* d_ws, size_t ws_bytes, float* d_out, int* d_status, void* stream) {
+    if (!d || !d_archive || !d_ws || !d_out) return VSZ_ERR_INVALID;
+    int dict, bs;
+    double ebf;
+    VSZ_TRY(resolve_decode_params(d, o, &dict, &bs, &ebf));
+    if (d->n_pad != 0) return VSZ_ERR_UNSUPPORTED;  // padding modes (-p) are not built
+    size_t dims[3] = {d->dims[0], d->dims[1], d->dims[2]};
+    if (!valid_dims(d->ndim, dims)) return VSZ_ERR_CORRUPT;
+    Geometry g = make_geometry(d->ndim, dims);
+    if (d->node_count > (uint32_t)(2 * dict - 1)) return VSZ_ERR_CORRUPT;
+    DecompressWs w = layout_decompress(g, dict, d->payload_bytes, d->n_outlier, d->has_trailer ? d->n_chunks : 0,
+                                       reinterpret_cast<uint8_t*>(d_ws), ws_bytes);
+    if (w.bytes > ws_bytes) return VSZ_ERR_CAPACITY;
+    cudaStream_t st = S(stream);
+    uint32_t nxs = (g.d0 + 255) / 256;
+    size_t nsegd = g.nrows * nxs;
+    VSZ_CUDA(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+    VSZ_CUDA(cudaMemsetAsync(w.seg_zero, 0, 4 * nsegd, st));
+    VSZ_TRY(launch_eb_setup(VSZ_MODE_ABS, ebf, nullptr, 0, w.consts, w.mm, st, w.status));
+    const uint16_t* idx = d->has_trailer ? reinterpret_cast<const uint16_t*>(d_archive + d->index_offset) : nullptr;
+    VSZ_TRY(decode_codes(d_archive + d->huff_offset, d->huff_bytes, d->node_count, d->tree_bytes, g.n, dict, idx,
+                         d->has_trailer ? d->n_chunks : 0, d->chunk_syms, w, w.seg_zero, g.d0, st));
+    VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.scan_status, w.scan_counter, w.scan_total, w.status, st));
+    k_check_zeros<<<1, 1, 0, st>>>(w.scan_total, d->n_outlier, w.status);
+    if (d->n_outlier)
+        VSZ_CUDA(cudaMemcpyAsync(w.outliers, d_archive + d->outlier_offset, 4 * d->n_outlier, cudaMemcpyDeviceToDevice,
+                                 st));
+    DqDecArgs a{};
+    a.codes = w.code;
+    a.outliers = w.outliers;
+    a.n_outliers = d->n_outlier;
+    a.status = w.status;
+    a.seg_off = w.seg_off;
+    a.consts = w.consts;
+    a.out = d_out;
+    a.d0 = g.d0;
+    a.d1 = g.d1;
+    a.d2 = g.d2;
+    a.n = g.n;
+    a.R = dict / 2;
+    bool force_general = getenv("VSZ_FORCE_GENERAL_DECOMPRESS") != nullptr;
+    VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));
+    if (d_status) k_copy_status<<<1, 1, 0, st>>>(w.status, w.consts, d_status);
+    VSZ_CUDA(cudaGetLastError());
+    return VSZ_OK;
+}
+
+}  // extern "C"

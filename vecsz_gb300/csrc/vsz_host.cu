@@ -1,0 +1,375 @@
+// Host entry points of the C ABI: the reference's Compress / Decompress interface on host buffers
+// (src/vecsz_interface.hh:31-375), with device memory cached between calls, and the lossless pass
+// (src/lossless.hh) through the system zstd / zlib libraries loaded at run time.
+#include <dlfcn.h>
+
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "vsz_types.h"
+
+namespace {
+
+#define VSZ_TRY(x)                     \
+    do {                               \
+        int _rc = (x);                 \
+        if (_rc != VSZ_OK) return _rc; \
+    } while (0)
+#define VSZ_CUDA(x)                                  \
+    do {                                             \
+        if ((x) != cudaSuccess) return VSZ_ERR_CUDA; \
+    } while (0)
+
+// ---- cached device buffers, one set per device -----------------------------------------------
+struct DevBuf {
+    void* p    = nullptr;
+    size_t cap = 0;
+    int grow(size_t need) {
+        if (need <= cap) return VSZ_OK;
+        if (p) cudaFree(p);
+        p   = nullptr;
+        cap = 0;
+        size_t want = need + need / 8 + 4096;
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return VSZ_ERR_NOMEM;
+        }
+        cap = want;
+        return VSZ_OK;
+    }
+};
+
+struct HostCtx {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    DevBuf in, ws, archive, out, result;
+};
+
+HostCtx* ctx_for_device() {
+    static HostCtx ctxs[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    if (dev < 0 || dev >= 64) return nullptr;
+    return &ctxs[dev];
+}
+
+int ensure_stream(HostCtx* c) {
+    if (!c->stream) VSZ_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    return VSZ_OK;
+}
+
+// ---- lossless libraries --------------------------------------------------------------------
+struct Zstd {
+    bool tried = false, ok = false;
+    size_t (*compress)(void*, size_t, const void*, size_t, int) = nullptr;
+    size_t (*bound)(size_t) = nullptr;
+    unsigned (*is_error)(size_t) = nullptr;
+    size_t (*decompress)(void*, size_t, const void*, size_t) = nullptr;
+    unsigned long long (*content_size)(const void*, size_t) = nullptr;
+};
+struct Zlib {
+    bool tried = false, ok = false;
+    int (*compress2)(uint8_t*, unsigned long*, const uint8_t*, unsigned long, int) = nullptr;
+    unsigned long (*bound)(unsigned long) = nullptr;
+    int (*uncompress)(uint8_t*, unsigned long*, const uint8_t*, unsigned long) = nullptr;
+};
+
+std::mutex g_lib_mu;
+Zstd g_zstd;
+Zlib g_zlib;
+
+Zstd* zstd() {
+    std::lock_guard<std::mutex> lk(g_lib_mu);
+    if (!g_zstd.tried) {
+        g_zstd.tried = true;
+        void* h      = dlopen("libzstd.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!h) h = dlopen("libzstd.so", RTLD_NOW | RTLD_LOCAL);
+        if (h) {
+            g_zstd.compress     = (decltype(g_zstd.compress))dlsym(h, "ZSTD_compress");
+            g_zstd.bound        = (decltype(g_zstd.bound))dlsym(h, "ZSTD_compressBound");
+            g_zstd.is_error     = (decltype(g_zstd.is_error))dlsym(h, "ZSTD_isError");
+            g_zstd.decompress   = (decltype(g_zstd.decompress))dlsym(h, "ZSTD_decompress");
+            g_zstd.content_size = (decltype(g_zstd.content_size))dlsym(h, "ZSTD_getFrameContentSize");
+            g_zstd.ok = g_zstd.compress && g_zstd.bound && g_zstd.is_error && g_zstd.decompress && g_zstd.content_size;
+        }
+    }
+    return g_zstd.ok ? &g_zstd : nullptr;
+}
+
+Zlib* zlib() {
+    std::lock_guard<std::mutex> lk(g_lib_mu);
+    if (!g_zlib.tried) {
+        g_zlib.tried = true;
+        void* h      = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+        if (!h) h = dlopen("libz.so", RTLD_NOW | RTLD_LOCAL);
+        if (h) {
+            g_zlib.compress2  = (decltype(g_zlib.compress2))dlsym(h, "compress2");
+            g_zlib.bound      = (decltype(g_zlib.bound))dlsym(h, "compressBound");
+            g_zlib.uncompress = (decltype(g_zlib.uncompress))dlsym(h, "uncompress");
+            g_zlib.ok         = g_zlib.compress2 && g_zlib.bound && g_zlib.uncompress;
+        }
+    }
+    return g_zlib.ok ? &g_zlib : nullptr;
+}
+
+// zlib header check of isZlibFormat (src/lossless.hh:40-57)
+bool zlib_magic(const uint8_t* b, size_t len) {
+    if (len < 2) return false;
+    unsigned m1 = b[0], m2 = b[1];
+    if (m1 == 104 && (m2 == 5 || m2 == 129 || m2 == 222)) return true;
+    if (m1 == 120 && (m2 == 1 || m2 == 94 || m2 == 156 || m2 == 218)) return true;
+    return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+void vsz_free_host(void* p) { free(p); }
+
+int vsz_lossless_detect(const uint8_t* h, size_t len) {
+    if (!h || len < 2) return 0;
+    // ZSTD_getFrameContentSize != ZSTD_CONTENTSIZE_ERROR (src/lossless.hh:62-64); the magic
+    // number 0xFD2FB528 is what that check keys on.
+    if (len >= 4 && h[0] == 0x28 && h[1] == 0xB5 && h[2] == 0x2F && h[3] == 0xFD) return 1;
+    if (zlib_magic(h, len)) return 2;
+    return 0;
+}
+
+vsz_status vsz_lossless_compress(int which, const uint8_t* h_in, size_t len, uint8_t** h_out, size_t* out_len) {
+    if (!h_in || !h_out || !out_len) return VSZ_ERR_INVALID;
+    if (which == VSZ_LOSSLESS_ZSTD) {
+        Zstd* z = zstd();
+        if (!z) return VSZ_ERR_UNSUPPORTED;
+        size_t cap = z->bound(len);
+        uint8_t* o = (uint8_t*)malloc(cap ? cap : 1);
+        if (!o) return VSZ_ERR_NOMEM;
+        size_t r = z->compress(o, cap, h_in, len, 3);
+        if (z->is_error(r)) {
+            free(o);
+            return VSZ_ERR_CORRUPT;
+        }
+        *h_out   = o;
+        *out_len = r;
+        return VSZ_OK;
+    }
+    if (which == VSZ_LOSSLESS_GZIP) {
+        Zlib* z = zlib();
+        if (!z) return VSZ_ERR_UNSUPPORTED;
+        unsigned long cap = z->bound((unsigned long)len);
+        uint8_t* o        = (uint8_t*)malloc(cap ? cap : 1);
+        if (!o) return VSZ_ERR_NOMEM;
+        unsigned long ol = cap;
+        if (z->compress2(o, &ol, h_in, (unsigned long)len, 3) != 0) {
+            free(o);
+            return VSZ_ERR_CORRUPT;
+        }
+        *h_out   = o;
+        *out_len = ol;
+        return VSZ_OK;
+    }
+    return VSZ_ERR_INVALID;
+}
+
+vsz_status vsz_lossless_decompress(const uint8_t* h_in, size_t len, size_t target, uint8_t** h_out, size_t* out_len) {
+    if (!h_in || !h_out || !out_len) return VSZ_ERR_INVALID;
+    int kind   = vsz_lossless_detect(h_in, len);
+    uint8_t* o = (uint8_t*)malloc(target + 16);
+    if (!o) return VSZ_ERR_NOMEM;
+    if (kind == 1) {
+        Zstd* z = zstd();
+        if (!z) {
+            free(o);
+            return VSZ_ERR_UNSUPPORTED;
+        }
+        size_t r = z->decompress(o, target, h_in, len);
+        if (z->is_error(r)) {
+            free(o);
+            return VSZ_ERR_CORRUPT;
+        }
+        *out_len = r;
+    } else if (kind == 2) {
+        Zlib* z = zlib();
+        if (!z) {
+            free(o);
+            return VSZ_ERR_UNSUPPORTED;
+        }
+        unsigned long ol = (unsigned long)target;
+        if (z->uncompress(o, &ol, h_in, (unsigned long)len) != 0) {
+            free(o);
+            return VSZ_ERR_CORRUPT;
+        }
+        *out_len = ol;
+    } else {
+        free(o);
+        return VSZ_ERR_CORRUPT;
+    }
+    *h_out = o;
+    return VSZ_OK;
+}
+
+vsz_status vsz_compress_host_bound(const vsz_params* p, int ndim, const size_t dims[3], size_t* out_capacity) {
+    size_t ws = 0, cap = 0;
+    VSZ_TRY(vsz_compress_bounds(p, ndim, dims, &ws, &cap));
+    if (out_capacity) *out_capacity = cap;
+    return VSZ_OK;
+}
+
+vsz_status vsz_compress_host_into(const vsz_params* p, int ndim, const size_t dims[3], const float* h_in,
+                                  uint8_t* h_out, size_t out_capacity, size_t* out_bytes, size_t* data_size,
+                                  size_t* lossless_size, size_t* n_outlier) {
+    if (!h_in || !h_out) return VSZ_ERR_INVALID;
+    size_t ws = 0, cap = 0;
+    VSZ_TRY(vsz_compress_bounds(p, ndim, dims, &ws, &cap));
+    HostCtx* c = ctx_for_device();
+    if (!c) return VSZ_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lk(c->mu);
+    VSZ_TRY(ensure_stream(c));
+    size_t n = dims[0] * (ndim > 1 ? dims[1] : 1) * (ndim > 2 ? dims[2] : 1);
+    VSZ_TRY(c->in.grow(n * sizeof(float)));
+    VSZ_TRY(c->ws.grow(ws));
+    VSZ_TRY(c->archive.grow(cap));
+    VSZ_TRY(c->result.grow(64));
+    VSZ_CUDA(cudaMemcpyAsync(c->in.p, h_in, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    VSZ_TRY(vsz_compress(p, ndim, dims, (const float*)c->in.p, c->ws.p, c->ws.cap, (uint8_t*)c->archive.p,
+                         c->archive.cap, (uint64_t*)c->result.p, c->stream));
+    vsz_result r;
+    VSZ_CUDA(cudaMemcpyAsync(&r, c->result.p, sizeof(r), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaStreamSynchronize(c->stream));
+    if (r.status != VSZ_OK) return (vsz_status)r.status;
+    size_t total = r.data_size + r.trailer_size;
+    if (p->lossless == VSZ_LOSSLESS_NONE) {
+        if (total > out_capacity) return VSZ_ERR_CAPACITY;
+        VSZ_CUDA(cudaMemcpyAsync(h_out, c->archive.p, total, cudaMemcpyDeviceToHost, c->stream));
+        VSZ_CUDA(cudaStreamSynchronize(c->stream));
+        if (out_bytes) *out_bytes = total;
+        if (lossless_size) *lossless_size = 0;
+    } else {
+        std::vector<uint8_t> tmp(total);
+        VSZ_CUDA(cudaMemcpyAsync(tmp.data(), c->archive.p, total, cudaMemcpyDeviceToHost, c->stream));
+        VSZ_CUDA(cudaStreamSynchronize(c->stream));
+        uint8_t* frame = nullptr;
+        size_t flen    = 0;
+        VSZ_TRY(vsz_lossless_compress(p->lossless, tmp.data(), r.data_size, &frame, &flen));
+        if (flen + r.trailer_size > out_capacity) {
+            free(frame);
+            return VSZ_ERR_CAPACITY;
+        }
+        memcpy(h_out, frame, flen);
+        memcpy(h_out + flen, tmp.data() + r.data_size, r.trailer_size);
+        free(frame);
+        if (out_bytes) *out_bytes = flen + r.trailer_size;
+        if (lossless_size) *lossless_size = flen;
+    }
+    if (data_size) *data_size = r.data_size;
+    if (n_outlier) *n_outlier = r.n_outlier;
+    return VSZ_OK;
+}
+
+vsz_status vsz_compress_host(const vsz_params* p, int ndim, const size_t dims[3], const float* h_in, uint8_t** h_out,
+                             size_t* out_bytes, size_t* data_size, size_t* lossless_size, size_t* n_outlier) {
+    if (!h_out) return VSZ_ERR_INVALID;
+    size_t cap = 0;
+    VSZ_TRY(vsz_compress_host_bound(p, ndim, dims, &cap));
+    uint8_t* buf = (uint8_t*)malloc(cap);
+    if (!buf) return VSZ_ERR_NOMEM;
+    size_t ob = 0;
+    int rc    = vsz_compress_host_into(p, ndim, dims, h_in, buf, cap, &ob, data_size, lossless_size, n_outlier);
+    if (rc) {
+        free(buf);
+        return rc;
+    }
+    uint8_t* shrunk = (uint8_t*)realloc(buf, ob ? ob : 1);
+    *h_out          = shrunk ? shrunk : buf;
+    if (out_bytes) *out_bytes = ob;
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress_host_into(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
+                                    const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, size_t* n_out) {
+    if (!h_archive || !h_out) return VSZ_ERR_INVALID;
+    // 1. undo the lossless pass; the trailer (if any) follows the frame
+    std::vector<uint8_t> packed;
+    const uint8_t* block = h_archive;
+    size_t block_len     = len;
+    if (lossless_size > 0) {
+        if (lossless_size > len) return VSZ_ERR_CORRUPT;
+        uint8_t* raw = nullptr;
+        size_t rl    = 0;
+        VSZ_TRY(vsz_lossless_decompress(h_archive, lossless_size, data_size, &raw, &rl));
+        if (rl != data_size) {
+            free(raw);
+            return VSZ_ERR_CORRUPT;
+        }
+        packed.resize(data_size + (len - lossless_size));
+        memcpy(packed.data(), raw, data_size);
+        memcpy(packed.data() + data_size, h_archive + lossless_size, len - lossless_size);
+        free(raw);
+        block     = packed.data();
+        block_len = packed.size();
+    }
+    vsz_archive_desc d;
+    VSZ_TRY(vsz_archive_parse(block, block_len, &d));
+    if (data_size && d.data_size != data_size) return VSZ_ERR_CORRUPT;
+    size_t n = d.dims[0] * d.dims[1] * d.dims[2];
+    if (n > out_capacity) return VSZ_ERR_CAPACITY;
+    size_t ws = 0;
+    VSZ_TRY(vsz_decompress_bounds(&d, opts, &ws));
+    HostCtx* c = ctx_for_device();
+    if (!c) return VSZ_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lk(c->mu);
+    VSZ_TRY(ensure_stream(c));
+    size_t used = d.has_trailer ? (size_t)(d.index_offset + 2 * d.n_chunks) : (size_t)d.data_size;
+    VSZ_TRY(c->archive.grow(used + 64));
+    VSZ_TRY(c->ws.grow(ws));
+    VSZ_TRY(c->out.grow(n * sizeof(float)));
+    VSZ_TRY(c->result.grow(64));
+    VSZ_CUDA(cudaMemcpyAsync(c->archive.p, block, used, cudaMemcpyHostToDevice, c->stream));
+    VSZ_CUDA(cudaMemsetAsync((uint8_t*)c->archive.p + used, 0, 64, c->stream));
+    VSZ_TRY(vsz_decompress(&d, opts, (const uint8_t*)c->archive.p, c->ws.p, c->ws.cap, (float*)c->out.p,
+                           (int*)c->result.p, c->stream));
+    int st = 0;
+    VSZ_CUDA(cudaMemcpyAsync(&st, c->result.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaMemcpyAsync(h_out, c->out.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaStreamSynchronize(c->stream));
+    if (st != VSZ_OK) return st;
+    if (n_out) *n_out = n;
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress_host(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
+                               const vsz_decompress_opts* opts, float** h_out, size_t* n) {
+    if (!h_out) return VSZ_ERR_INVALID;
+    // size the output from the header (after the lossless pass if any)
+    size_t cap = 0;
+    if (lossless_size == 0) {
+        vsz_archive_desc d;
+        VSZ_TRY(vsz_archive_parse(h_archive, len, &d));
+        cap = d.dims[0] * d.dims[1] * d.dims[2];
+    } else {
+        uint8_t* raw = nullptr;
+        size_t rl    = 0;
+        VSZ_TRY(vsz_lossless_decompress(h_archive, lossless_size, data_size, &raw, &rl));
+        vsz_archive_desc d;
+        int rc = vsz_archive_parse(raw, rl, &d);
+        free(raw);
+        VSZ_TRY(rc);
+        cap = d.dims[0] * d.dims[1] * d.dims[2];
+    }
+    float* o = (float*)malloc(cap * sizeof(float) + 16);
+    if (!o) return VSZ_ERR_NOMEM;
+    int rc = vsz_decompress_host_into(h_archive, len, data_size, lossless_size, opts, o, cap, n);
+    if (rc) {
+        free(o);
+        return rc;
+    }
+    *h_out = o;
+    return VSZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+// Internal interface of the Huffman kernels (huffman.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "vsz_kernels.h"
+#include "vsz_types.h"
+
+namespace vsz {
+
+constexpr int kDecBits     = 12;   // primary decode table: 4096 entries
+constexpr int kChunkSyms   = 512;  // codewords per entry of this library's decode index
+constexpr int kSyncBits    = 8192; // chunk size (bits) of the self-synchronising decoder
+
+// Width of the serialized child indices (src/huffman.hh:425-502).
+__host__ __device__ inline int tree_index_width(uint32_t nc) { return nc <= 256 ? 1 : (nc <= 65536 ? 2 : 4); }
+// [u8 endian][L][R][C u32][t u8]
+__host__ __device__ inline size_t tree_bytes_size(uint32_t nc) {
+    int w = tree_index_width(nc);
+    return 1 + 2 * (size_t)w * nc + 4 * (size_t)nc + nc;
+}
+
+struct HuffBuildArgs {
+    const unsigned long long* hist;
+    int dict;
+    unsigned long long* cb_word;  // right-aligned codeword per symbol
+    uint8_t* cb_len;              // codeword length per symbol (0 = unused)
+    uint8_t* out;                 // [BE nc][BE dict][tree bytes], any alignment
+    uint32_t* info;               // [0] node count [1] tree bytes [2] max code length [3] nodes created
+    void* scratch;                // huff_build_scratch_bytes(dict)
+    size_t stack_offset, heap_offset;
+    int heap_in_smem;
+    int* status;
+};
+
+struct HuffEncodeArgs {
+    const uint16_t* codes;
+    size_t n;
+    const unsigned long long* cb_word;
+    const uint8_t* cb_len;
+    int dict;
+    uint8_t* out;                     // payload start = out + out_off.eval(), any alignment;
+    DevOffset out_off;                // bytes before the payload start are kept
+    unsigned long long* total_bits;
+    uint16_t* chunk_bits;             // bits per 512 codes (decode index), may be null
+    unsigned long long* tile_status;  // ntiles
+    uint32_t* tail_flag;              // ntiles
+    uint32_t* tile_counter;
+    int* status;
+    uint32_t ntiles;
+    int codes_aligned;
+    int cb_in_smem;
+    const uint32_t* build_info;       // optional: k_huff_build's info; max length > 64 is refused
+};
+
+struct HuffTableArgs {
+    const uint8_t* huff;  // [BE nc][BE dict][tree bytes]...
+    size_t huff_bytes;
+    int dict;
+    uint32_t max_nodes;
+    uint32_t* table;      // 1 << kDecBits entries
+    uint32_t* child;      // 2 * max_nodes
+    uint32_t* node_sym;   // max_nodes: 0x80000000 | symbol for leaves
+    uint32_t* parent;     // max_nodes (scratch)
+    uint32_t* info;       // [0] single-symbol tree flag [1] its symbol
+    int* status;
+};
+
+struct HuffDecodeArgs {
+    const uint8_t* payload;  // any alignment; 8 readable bytes past the end are required
+    unsigned long long payload_bits;
+    const uint32_t* table;
+    const uint32_t* child;
+    const uint32_t* node_sym;
+    const unsigned long long* start_bit;  // per chunk
+    const unsigned long long* out_begin;  // per chunk, or null: chunk * chunk_syms
+    const uint32_t* nsym;                 // per chunk, or null: chunk_syms
+    size_t nchunks;
+    uint32_t chunk_syms;
+    uint16_t* codes;
+    size_t n;
+    uint32_t* seg_zero;                   // zero codes per 256-wide row segment (may be null)
+    uint32_t d0, nxs;
+    uint32_t max_nodes;                   // node indices past this are a corrupt tree
+    int* status;
+};
+
+struct HuffSyncArgs {
+    const uint8_t* payload;
+    unsigned long long payload_bits;
+    const uint32_t* table;
+    const uint32_t* child;
+    const uint32_t* node_sym;
+    size_t nchunks;
+    uint32_t chunk_bits;
+    unsigned long long* start;   // nchunks
+    unsigned long long* exit_a;  // nchunks
+    uint32_t* count;             // nchunks
+    uint32_t max_nodes;
+    int* status;
+};
+
+int launch_huff_build(HuffBuildArgs a, cudaStream_t st);
+size_t huff_build_scratch_bytes(int dict, size_t* stack_offset, size_t* heap_offset);
+int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms);
+int launch_huff_table(HuffTableArgs a, cudaStream_t st);
+int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st);
+int launch_huff_const(uint16_t* codes, size_t n, const uint32_t* info, uint32_t* seg_zero, uint32_t d0, uint32_t nxs,
+                      const int* status, cudaStream_t st, int num_sms);
+int launch_huff_sync_init(HuffSyncArgs a, cudaStream_t st);
+int launch_huff_sync_round(HuffSyncArgs a, const unsigned long long* exit_in, unsigned long long* exit_out,
+                           int* changed, cudaStream_t st);
+int launch_scan_u16(const uint16_t* in, unsigned long long* out, size_t n, unsigned long long* tile_status,
+                    uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st);
+int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsigned long long* tile_status,
+                    uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st);
+size_t scan_tmp_tiles(size_t n);
+
+}  // namespace vsz

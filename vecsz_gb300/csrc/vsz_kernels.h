@@ -1,0 +1,114 @@
+// Internal launcher interface between the C-ABI layer (vsz_api.cu) and the kernel files.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "vsz_types.h"
+
+namespace vsz {
+
+struct Consts;
+
+// A byte offset known only on the device once earlier kernels ran (tree size, payload size):
+// base + *add_u32 + ceil(*add_bits / 8).
+struct DevOffset {
+    size_t base;
+    const uint32_t* add_u32;
+    const unsigned long long* add_bits;
+#ifdef __CUDACC__
+    __device__ __forceinline__ size_t eval() const {
+        size_t o = base;
+        if (add_u32) o += *add_u32;
+        if (add_bits) o += (size_t)((*add_bits + 7ull) >> 3);
+        return o;
+    }
+#endif
+};
+
+// ---- dual-quant compress ------------------------------------------------------------------
+struct DqArgs {
+    const float* x;
+    uint16_t* code;
+    float* scratch;              // outlier values, [segment][128]
+    uint8_t* seg_count;          // outliers per segment
+    unsigned long long* hist;    // dict entries, accumulated with atomics (caller zeroes)
+    const Consts* consts;
+    uint32_t d0, d1, d2;
+    uint32_t nxt;                // 128-wide x tiles per row
+    uint32_t nyg;                // groups of 8 rows
+    uint32_t nzb;                // Lorenzo blocks along z (3D) or 1
+    uint32_t xtail;              // first tail column: d0 & ~7 when d0 % 8 != 0, else d0
+    int R;                       // radius = dict / 2
+    int dict;
+    int smem_hist;               // 1: histogram privatised in shared memory
+    unsigned long long nunits;   // warp work units
+};
+
+struct GatherArgs {
+    const uint8_t* seg_count;
+    const float* scratch;
+    size_t nseg;
+    float* out_f32;              // aligned destination, or
+    uint8_t* out_bytes;          // byte-addressed destination at out_bytes + out_off.eval()
+    DevOffset out_off;
+    unsigned long long* total;   // number of outliers (written by the last tile)
+    unsigned long long* tile_status;
+    uint32_t* tile_counter;
+    int* status;
+    uint32_t ntiles;
+};
+
+// ---- dual-quant decompress ----------------------------------------------------------------
+struct DqDecArgs {
+    const uint16_t* codes;
+    const float* outliers;               // compact outlier values (aligned copy)
+    unsigned long long n_outliers;       // entries of `outliers`; a rank past it is VSZ_ERR_CORRUPT
+    int* status;
+    const unsigned long long* seg_off;   // exclusive zero-code offsets per 256-wide row segment
+    const Consts* consts;
+    float* out;
+    uint32_t d0, d1, d2;
+    size_t n;
+    int R;
+    uint32_t nxs;                        // 256-wide segments per row
+    uint32_t nyb;                        // Lorenzo blocks along y
+    uint32_t nbx;                        // Lorenzo blocks along x (general kernel)
+    unsigned long long nunits;
+};
+
+int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
+int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* seg_zero, cudaStream_t st,
+                       int num_sms);
+
+int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_consts, uint32_t* d_mm,
+                    cudaStream_t st, int* status_word = nullptr);
+int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms);
+int launch_outlier_gather(GatherArgs g, cudaStream_t st);
+size_t gather_tmp_bytes(size_t nseg);
+
+// Geometry helpers shared by compress and decompress.
+struct Geometry {
+    int ndim;
+    uint32_t d0, d1, d2;
+    size_t n;
+    uint32_t nxt;   // 128-wide tiles per row
+    size_t nrows;   // d1 * d2
+    size_t nseg;    // nrows * nxt
+};
+
+inline Geometry make_geometry(int ndim, const size_t* dims) {
+    Geometry g{};
+    g.ndim  = ndim;
+    g.d0    = (uint32_t)dims[0];
+    g.d1    = ndim > 1 ? (uint32_t)dims[1] : 1u;
+    g.d2    = ndim > 2 ? (uint32_t)dims[2] : 1u;
+    g.n     = (size_t)g.d0 * g.d1 * g.d2;
+    g.nxt   = (g.d0 + 127u) / 128u;
+    g.nrows = (size_t)g.d1 * g.d2;
+    g.nseg  = g.nrows * g.nxt;
+    return g;
+}
+
+}  // namespace vsz
