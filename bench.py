@@ -1,0 +1,461 @@
+#!/usr/bin/env python
+"""Headline benchmark: f32 compress + decompress throughput on one GB300.
+
+A step is one compress of the workload field (device-resident input) followed by one decompress of
+the archive it produced.  `value` is input bytes (4 N) per second of step time over all ranks;
+`compress_gbs` / `decompress_gbs` split it per direction.  `e2e` is the same round trip through the
+host C-ABI entry points (the reference's Compress / Decompress interface) with pinned host buffers,
+host<->device copies inside the timed region.
+
+Workload (default): 512^3 f32 Gaussian random field with a k^-11/3 power spectrum, exponentiated to
+a log-normal density spanning ~4 decades (NYX-like), r2r eb 1e-4, dict 1024 (radius 512), block 8.
+The field (537 MB) and its codes (268 MB) are larger than L2 (129 MB), so no L2 flush is needed.
+
+--impl reference times the reference's CPU algorithm (the C restatement in oracle/, OpenMP over all
+host cores, serial Huffman as in the reference) on a bounded slab of the same workload.
+
+Multi-GPU: the path does not shard across GPUs in this build ("replicas only"); under torchrun each
+rank compresses its own field of the same size (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "f32 compress/decompress GB/s on 1 GB300 (frac of HBM), batched vs plain, eb 1e-4"
+WORKLOADS = {
+    # name: (numpy shape (z, y, x), generator, eb, mode, dict, bs)
+    "nyx512": ((512, 512, 512), "grf", 1e-4, "r2r", 1024, 8),
+    "nyx256": ((256, 256, 256), "grf", 1e-4, "r2r", 1024, 8),
+    "cesm": ((1, 1800, 3600), "bump", 1e-4, "abs", 1024, 8),
+    "adversarial": ((256, 384, 384), "adv", 1e-6, "abs", 1024, 8),
+}
+WORKLOAD_DESC = {
+    "nyx512": "512^3 f32 GRF k^-11/3 log-normal (NYX-like), r2r eb 1e-4, dict 1024, block 8",
+    "nyx256": "256^3 f32 GRF k^-11/3 log-normal, r2r eb 1e-4, dict 1024, block 8",
+    "cesm": "1800x3600 f32 sum of 64 Gaussian bumps (CESM-like), abs eb 1e-4, dict 1024, block 8",
+    "adversarial": "256x384x384 f32 GRF + 5% Cauchy spikes + 8 steps, abs eb 1e-6, dict 1024, block 8",
+}
+# kernels this library launches per step (compress 7, decompress 8 with the indexed decoder)
+LAUNCHES_PER_STEP = 15
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="nyx512")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_field_torch(name, device="cuda", seed=0):
+    from vecsz_gb300 import fields
+    shape, gen, *_ = WORKLOADS[name]
+    nz, ny, nx = shape
+    if gen == "grf":
+        return fields.grf_3d_torch(nz, ny, nx, seed=seed, device=device)
+    if gen == "adv":
+        return fields.adversarial_3d_torch(nz, ny, nx, seed=seed, device=device)
+    return fields.bump_field_2d_torch(ny, nx, seed=seed, device=device)
+
+
+def ref_dims(name):
+    shape = WORKLOADS[name][0]
+    if shape[0] == 1:
+        return (shape[2], shape[1])
+    return (shape[2], shape[1], shape[0])
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+        except Exception:
+            pass
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the run; summarised over the timed window."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        win = [s for t, s in self.samples if t0 - 0.3 <= t <= t1 + 0.3] or [s for _, s in self.samples[-5:]]
+        if not win:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(s[1]) for s in win if num(s[1]) is not None]
+        mx = [num(s[2]) for s in win if num(s[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in win:
+            for name, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(win),
+                "power_w_max": max([num(s[3]) or 0 for s in win])}
+
+
+def stage_profile(V):
+    import ctypes as C
+    L = V.lib()
+    ms = (C.c_double * 32)()
+    cnt = (C.c_int * 32)()
+    names = (C.c_char_p * 32)()
+    n = L.vsz_profile_read(C.cast(ms, C.c_void_p), C.cast(cnt, C.c_void_p), C.cast(names, C.c_void_p), 32)
+    return {names[i].decode(): (ms[i], cnt[i]) for i in range(n) if cnt[i] > 0}
+
+
+def algorithmic_bytes(stage, n, res, desc):
+    """Bytes a stage must move per launch (reads + writes of its inputs and outputs)."""
+    nseg = desc["nseg128"]
+    nsegd = desc["nseg256"]
+    nout = res.n_outlier
+    payload = (res.payload_bits + 7) // 8
+    table = {
+        "eb_setup": 4 * n,                                       # min/max pass (r2r)
+        "dualquant": 4 * n + 2 * n + nseg + 4 * nout,            # field in; codes, counts, outliers out
+        "huff_encode": 2 * n + payload + 2 * ((n + 511) // 512),  # codes in; bitstream + index out
+        "outlier_gather": nseg + 8 * nout,
+        "huff_decode": payload + 2 * n + 4 * nsegd,              # bitstream in; codes, zero counts out
+        "lorenzo_decompress": 2 * n + 4 * n + 4 * nout + 8 * nsegd,  # codes + outliers in; field out
+    }
+    return table.get(stage)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import vecsz_gb300 as V
+    from vecsz_gb300 import _lib as L
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    shape, gen, eb, mode, dct, bs = WORKLOADS[args.workload]
+    dims = ref_dims(args.workload)
+    n = int(np.prod(shape))
+    x = make_field_torch(args.workload, seed=1000 + rank)
+    torch.cuda.synchronize()
+    codec = V.DeviceCodec(dims, eb=eb, mode=mode, dict_size=dct, block_size=bs)
+    stream = torch.cuda.Stream()
+    out = torch.empty_like(x)
+    with torch.cuda.stream(stream):
+        codec.compress(x, stream)
+    stream.synchronize()
+    archive = codec.archive_bytes()
+    res = codec.result_host()
+    codec.prepare_decompress(archive)
+
+    def step():
+        codec.compress(x, stream)
+        codec.decompress(codec.archive, out, stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    # correctness of what we time: deterministic archive, bounded error
+    assert codec.archive_bytes() == archive, "archive not deterministic"
+    assert codec.decompress_status() == 0
+    ebf = codec._desc.eb_final
+    err = (out.double() - x.double()).abs()
+    bound = ebf + 2.0 * torch.abs(x.double()) * 2.0 ** -23
+    verified = bool((err <= bound).all())
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.6)
+    L.lib().vsz_profile_reset()
+    L.lib().vsz_profile_enable(1)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        codec.compress(x, stream)
+        ev[i][1].record(stream)
+        codec.decompress(codec.archive, out, stream)
+        ev[i][2].record(stream)
+    stop.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    if world > 1:
+        dist.barrier()
+    L.lib().vsz_profile_enable(0)
+    total_ms = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    time.sleep(0.3)
+    clocks.stop()
+    comp_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    dec_ms = [b.elapsed_time(c) for _, b, c in ev]
+    prof = stage_profile(V)
+    peak, peak_src = measured_peaks()
+    nx_ = (dims[0] + 127) // 128
+    nrows = n // dims[0]
+    desc = {"nseg128": nrows * nx_, "nseg256": nrows * ((dims[0] + 255) // 256)}
+    dominant = max(prof.items(), key=lambda kv: kv[1][0])[0] if prof else None
+    roof = None
+    if dominant:
+        ms, cnt = prof[dominant]
+        per_launch_ms = ms / max(cnt, 1)
+        alg = algorithmic_bytes(dominant, n, res, desc)
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            try:
+                traffic = json.load(open(tpath)).get(args.workload, {}).get(dominant)
+            except Exception:
+                traffic = None
+        if alg:
+            ach = alg / (per_launch_ms * 1e-3) / 1e9
+            roof = {"bound": "hbm", "kernel": dominant, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(ach / peak, 4), "traffic": traffic, "algorithmic_bytes": int(alg),
+                    "ms_per_launch": round(per_launch_ms, 5), "peak_source": peak_src}
+    stages = {k: {"ms_per_launch": round(v[0] / max(v[1], 1), 5), "launches": v[1],
+                  "gbs": (round(algorithmic_bytes(k, n, res, desc) / (v[0] / max(v[1], 1) * 1e-3) / 1e9, 1)
+                          if algorithmic_bytes(k, n, res, desc) else None),
+                  "share": round(v[0] / max(sum(w[0] for w in prof.values()), 1e-9), 4)}
+              for k, v in prof.items()}
+    bytes_in = 4 * n
+    value = world * args.steps * bytes_in / (total_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_DESC[args.workload], "dims_xyz": list(dims), "eb": eb, "mode": mode,
+                   "dict_size": dct, "block_size": bs, "path": "plain (one field per launch sequence)",
+                   "l2": "inputs larger than L2 (field 4N bytes > 129 MB), no flush",
+                   "parallelism": f"replicas x{world}"},
+        "compress_gbs": round(bytes_in / (statistics.median(comp_ms) * 1e-3) / 1e9, 2),
+        "decompress_gbs": round(bytes_in / (statistics.median(dec_ms) * 1e-3) / 1e9, 2),
+        "compression_ratio": round(bytes_in / res.data_size, 3),
+        "archive_bytes": int(res.data_size), "index_trailer_bytes": int(res.trailer_size),
+        "n_outlier": int(res.n_outlier), "verified_error_bound": verified,
+        "roofline": roof, "stages": stages,
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+        "clocks": clocks.summary(t_wall0, t_wall1),
+    }
+    if not args.no_e2e:
+        line["e2e"] = run_e2e(V, x, dims, eb, mode, dct, bs, args.e2e_steps, bytes_in, world)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(x, dims, eb, mode, dct, bs)
+    if world > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(V, x, dims, eb, mode, dct, bs, steps, bytes_in, world):
+    """Round trip through vsz_compress_host_into / vsz_decompress_host_into with pinned buffers."""
+    import ctypes as C
+
+    import torch
+    from vecsz_gb300 import _lib as L
+    lib = L.lib()
+    n = x.numel()
+    h_in = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    h_in.copy_(x.view(-1).cpu())
+    p = V.make_params(eb, mode, dct, bs)
+    cap = C.c_size_t(0)
+    L.check(lib.vsz_compress_host_bound(C.byref(p), len(dims), L.dims_arg(dims), C.byref(cap)))
+    h_arch = torch.empty(cap.value, dtype=torch.uint8, pin_memory=True)
+    h_out = torch.empty(n, dtype=torch.float32, pin_memory=True)
+    opts = L.DecompressOpts(dct, bs, 1 if mode == "r2r" else 0, 0.0)
+    ob, ds, ls, no, nn = (C.c_size_t(0) for _ in range(5))
+
+    def one():
+        L.check(lib.vsz_compress_host_into(C.byref(p), len(dims), L.dims_arg(dims), C.c_void_p(h_in.data_ptr()),
+                                           C.c_void_p(h_arch.data_ptr()), cap.value, C.byref(ob), C.byref(ds),
+                                           C.byref(ls), C.byref(no)), "compress_host")
+        L.check(lib.vsz_decompress_host_into(C.c_void_p(h_arch.data_ptr()), ob.value, ds.value, ls.value,
+                                             C.byref(opts), C.c_void_p(h_out.data_ptr()), n, C.byref(nn)),
+                "decompress_host")
+
+    one()
+    one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    ok = bool(torch.equal(h_out.view(-1)[:1024], h_out.view(-1)[:1024]))
+    return {"value": round(world * bytes_in / dt / 1e9, 2), "unit": "GB/s",
+            "h2d_bytes_per_step": int(4 * n + ob.value), "d2h_bytes_per_step": int(ob.value + 4 * n),
+            "ms_per_step": round(dt * 1e3, 3), "steps": steps, "api": "vsz_compress_host_into + "
+            "vsz_decompress_host_into (pinned host buffers)", "ok": ok}
+
+
+def cpu_baseline(x, dims, eb, mode, dct, bs, max_bytes=None):
+    """The reference's algorithm on the host cores: C oracle, OpenMP dual-quant, serial Huffman."""
+    import oracle as O
+    xh = x.view(-1).cpu().numpy()
+    if max_bytes is not None and xh.nbytes > max_bytes:
+        # bounded sample: leading z-slab of the same field
+        plane = dims[0] * dims[1]
+        nz = max(1, max_bytes // (4 * plane))
+        xh = xh[: plane * nz]
+        dims = (dims[0], dims[1], nz) if len(dims) == 3 else dims
+    r2r = mode == "r2r"
+    tc = np.zeros(4)
+    td = np.zeros(3)
+    t0 = time.perf_counter()
+    archive, meta = O.compress(xh, dims, bs, dct, eb, r2r, timings=tc)
+    t1 = time.perf_counter()
+    O.decompress(archive, bs, dct, O.value_range(xh) if r2r else 0.0, timings=td)
+    t2 = time.perf_counter()
+    nbytes = xh.nbytes
+    return {"value": round(nbytes / (t2 - t0) / 1e9, 4), "unit": "GB/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"one compress + decompress round trip of {nbytes / 1e6:.0f} MB of the same field "
+                      f"(dims {list(dims)}) with the C oracle (OpenMP dual-quant, serial Huffman as the reference)",
+            "compress_gbs": round(nbytes / (t1 - t0) / 1e9, 4), "decompress_gbs": round(nbytes / (t2 - t1) / 1e9, 4),
+            "stage_s": {"value_range": round(tc[0], 4), "dualquant": round(tc[1], 4), "huffman_encode": round(tc[2], 4),
+                        "outlier_gather": round(tc[3], 4), "huffman_decode": round(td[0], 4),
+                        "outlier_scatter": round(td[1], 4), "reverse_dualquant": round(td[2], 4)},
+            "why_port": "the reference itself is x86 AVX code (src/dualquant.hh:6) and does not build on this "
+                        "aarch64 host; oracle/vsz_oracle.c restates it and is pinned to it"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+    shape, gen, eb, mode, dct, bs = WORKLOADS[args.workload]
+    dims = ref_dims(args.workload)
+    try:
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        x = make_field_torch(args.workload, device=dev, seed=1000)
+    except Exception:
+        from vecsz_gb300 import fields
+        nz, ny, nx = shape
+        x = None
+        xh = fields.grf_3d(nz, ny, nx, seed=1000) if gen == "grf" else fields.bump_field_2d(ny, nx, seed=1000)
+    xh = x.view(-1).cpu().numpy() if x is not None else xh.ravel()
+    # bounded step: a z-slab of ~64 MB of the same field (3D); the whole field for 2D workloads
+    if len(dims) == 3:
+        plane = dims[0] * dims[1]
+        nz = max(1, (64 << 20) // (4 * plane))
+        xs = xh[: plane * nz]
+        sdims = (dims[0], dims[1], nz)
+    else:
+        xs, sdims = xh, dims
+    r2r = mode == "r2r"
+    vr = O.value_range(xs) if r2r else 0.0
+
+    def step():
+        a, _ = O.compress(xs, sdims, bs, dct, eb, r2r)
+        O.decompress(a, bs, dct, vr)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = xs.nbytes / dt / 1e9
+    sample = (f"each step: one compress + decompress round trip of a {xs.nbytes / 1e6:.0f} MB slab "
+              f"(dims {list(sdims)}) of the workload field")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD_DESC[args.workload], "dims_xyz": list(dims), "eb": eb, "mode": mode,
+                       "dict_size": dct, "block_size": bs, "path": "reference CPU algorithm"},
+            "cpu_baseline": {"value": round(value, 4), "unit": "GB/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference = oracle/vsz_oracle.c, the pinned C restatement of vecSZ's AVX2+OpenMP path; the "
+                    "reference's own AVX sources (src/dualquant.hh:6) do not build on the aarch64 host"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.steps < 1:
+        raise SystemExit("--steps must be >= 1")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -226,6 +226,15 @@ vsz_status vsz_lossless_decompress(const uint8_t* h_in, size_t len, size_t targe
 /* 1 zstd frame, 2 zlib stream, 0 neither (is_lossless_compressed_data, src/lossless.hh:59-76). */
 int vsz_lossless_detect(const uint8_t* h_in, size_t len);
 
+/* Per-stage device timing: when enabled, the whole-field entry points record a CUDA event pair
+ * around each stage on the launching stream.  vsz_profile_read synchronises, returns the number of
+ * stages and fills ms[i] (milliseconds summed over all calls since the last reset), counts[i]
+ * (recorded launches) and names[i] (static strings).  No counterpart in the reference, which
+ * prints wall-clock stage times instead (src/vecsz_interface.hh:107-175). */
+void vsz_profile_enable(int on);
+void vsz_profile_reset(void);
+int vsz_profile_read(double* ms, int* counts, const char** names, int max_stages);
+
 #ifdef __cplusplus
 }
 #endif

@@ -662,23 +662,45 @@ int vso_huffman_encode(const int32_t* s, size_t n, int dict, uint8_t* out, size_
     tree_serialize(h, node_count, out + 8);
     uint8_t* pay = out + 8 + tsz;
     size_t pcap  = cap - 8 - tsz;
-    uint64_t bit = 0;
+    /* MSB-first bit writer with a 64-bit accumulator (same bytes as HuffmanEncode's byte loop) */
+    uint64_t bit = 0, acc = 0;
+    int nacc     = 0; /* bits pending in acc (left-aligned) */
+    size_t wpos  = 0;
     for (size_t i = 0; i < n; i++) {
         uint32_t sym = (uint32_t)s[i];
         int len      = h->cout[sym];
-        for (int b = 0; b < len; b++) {
-            uint64_t word = b < 64 ? h->code0[sym] : h->code1[sym];
-            int bb        = b < 64 ? b : b - 64;
-            int v         = (int)((word >> (63 - bb)) & 1u);
-            size_t byte   = (size_t)(bit >> 3);
-            if (byte >= pcap) {
-                tree_free(h);
-                return VSO_ERR_CAPACITY;
+        for (int part = 0; part < 2 && len > 0; part++) {
+            int take      = len > 64 ? 64 : len;
+            uint64_t word = part == 0 ? h->code0[sym] : h->code1[sym];
+            /* left-aligned `take` bits of word */
+            while (take > 0) {
+                int room = 64 - nacc;
+                int t    = take < room ? take : room;
+                uint64_t bits = word >> (64 - t);
+                acc |= (t == 64) ? bits : (bits << (64 - nacc - t));
+                nacc += t;
+                word = (t == 64) ? 0 : (word << t);
+                take -= t;
+                bit += (uint64_t)t;
+                while (nacc >= 8) {
+                    if (wpos >= pcap) {
+                        tree_free(h);
+                        return VSO_ERR_CAPACITY;
+                    }
+                    pay[wpos++] = (uint8_t)(acc >> 56);
+                    acc <<= 8;
+                    nacc -= 8;
+                }
             }
-            if ((bit & 7) == 0) pay[byte] = 0;
-            if (v) pay[byte] |= (uint8_t)(0x80u >> (bit & 7));
-            bit++;
+            len -= 64;
         }
+    }
+    if (nacc > 0) {
+        if (wpos >= pcap) {
+            tree_free(h);
+            return VSO_ERR_CAPACITY;
+        }
+        pay[wpos++] = (uint8_t)(acc >> 56);
     }
     *out_size = 8 + tsz + (size_t)((bit + 7) >> 3);
     tree_free(h);
@@ -711,23 +733,44 @@ int vso_huffman_decode(const uint8_t* in, size_t in_len, size_t n, int32_t* out)
         for (size_t k = 0; k < n; k++) out[k] = (int32_t)c;
         return VSO_OK;
     }
+    uint32_t* ch = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (size_t)nc);
+    int32_t* leaf = (int32_t*)malloc(sizeof(int32_t) * (size_t)nc);
+    if (!ch || !leaf) {
+        free(ch);
+        free(leaf);
+        return VSO_ERR_ARG;
+    }
+    for (uint32_t k = 0; k < nc; k++) {
+        ch[2 * k]     = get_index(Lb + (size_t)k * w, w);
+        ch[2 * k + 1] = get_index(Rb + (size_t)k * w, w);
+        uint32_t c;
+        memcpy(&c, Cb + 4 * (size_t)k, 4);
+        leaf[k] = (k != 0 && Tb[k]) ? (int32_t)c : -1;
+    }
     uint32_t node = 0;
     size_t count = 0, i = 0;
+    int rc = VSO_OK;
     while (count < n) {
-        if (i >= pbits) return VSO_ERR_CORRUPT;
+        if (i >= pbits) {
+            rc = VSO_ERR_CORRUPT;
+            break;
+        }
         int bitv      = (pay[i >> 3] >> (7 - (i & 7))) & 1;
-        uint32_t next = bitv ? get_index(Rb + (size_t)node * w, w) : get_index(Lb + (size_t)node * w, w);
-        if (next == 0 || next >= nc) return VSO_ERR_CORRUPT;
+        uint32_t next = ch[2 * node + (uint32_t)bitv];
+        if (next == 0 || next >= nc) {
+            rc = VSO_ERR_CORRUPT;
+            break;
+        }
         node = next;
         i++;
-        if (Tb[node]) {
-            uint32_t c;
-            memcpy(&c, Cb + 4 * (size_t)node, 4);
-            out[count++] = (int32_t)c;
+        if (leaf[node] >= 0) {
+            out[count++] = leaf[node];
             node         = 0;
         }
     }
-    return VSO_OK;
+    free(ch);
+    free(leaf);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------------------------ */

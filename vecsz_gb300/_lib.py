@@ -101,6 +101,9 @@ _PROTOS = {
     "vsz_lossless_compress": ([_i, _p, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_lossless_decompress": ([_p, _sz, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_lossless_detect": ([_p, _sz], _i),
+    "vsz_profile_enable": ([_i], None),
+    "vsz_profile_reset": ([], None),
+    "vsz_profile_read": ([_p, _p, _p, _i], _i),
 }
 
 

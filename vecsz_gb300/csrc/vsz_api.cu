@@ -9,6 +9,7 @@
 #include "vsz_device.cuh"
 #include "vsz_huffman.h"
 #include "vsz_kernels.h"
+#include "vsz_profile.h"
 
 using namespace vsz;
 
@@ -358,7 +359,10 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     ta.parent = w.parent;
     ta.info = w.tinfo;
     ta.status = w.status;
-    VSZ_TRY(launch_huff_table(ta, st));
+    {
+        StageTimer t(kStDecTable, st);
+        VSZ_TRY(launch_huff_table(ta, st));
+    }
     if (node_count == 1) {
         // one-symbol tree: constant output (src/huffman.hh:348-352)
         return launch_huff_const(w.code, n, w.tinfo, seg_zero, d0, nxs, w.status, st, num_sms());
@@ -377,13 +381,17 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     da.max_nodes = (uint32_t)(2 * dict - 1);
     da.status = w.status;
     if (chunk_bits) {
-        VSZ_TRY(launch_scan_u16(chunk_bits, w.chunk_start, n_index_chunks, w.scan_status, w.scan_counter, nullptr,
-                                w.status, st));
+        {
+            StageTimer t(kStDecScanIndex, st);
+            VSZ_TRY(launch_scan_u16(chunk_bits, w.chunk_start, n_index_chunks, w.scan_status, w.scan_counter, nullptr,
+                                    w.status, st));
+        }
         da.start_bit = w.chunk_start;
         da.out_begin = nullptr;
         da.nsym = nullptr;
         da.nchunks = n_index_chunks;
         da.chunk_syms = chunk_syms;
+        StageTimer t(kStHuffDecode, st);
         return launch_huff_decode(da, st);
     }
     // self-synchronising path
@@ -677,10 +685,16 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     VSZ_CUDA(cudaMemsetAsync(w.total_bits, 0, sizeof(unsigned long long), st));
     VSZ_CUDA(cudaMemsetAsync(w.n_out, 0, sizeof(unsigned long long), st));
     // 1. error-bound family (+ value range for r2r)
-    VSZ_TRY(launch_eb_setup(p->mode, p->eb, d_in, g.n, w.consts, w.mm, st, w.status));
+    {
+        StageTimer t(kStEbSetup, st);
+        VSZ_TRY(launch_eb_setup(p->mode, p->eb, d_in, g.n, w.consts, w.mm, st, w.status));
+    }
     // 2. dual-quant + histogram + outlier ranking
     DqArgs a = make_dq_args(g, p->block_size, dict, d_in, w.consts, w.code, w.scratch, w.seg_count, w.hist);
-    VSZ_TRY(launch_dq_compress(a, ndim, p->block_size, st, num_sms()));
+    {
+        StageTimer t(kStDualquant, st);
+        VSZ_TRY(launch_dq_compress(a, ndim, p->block_size, st, num_sms()));
+    }
     // 3. tree + codebook; the Huffman section starts right after the header (no padding values)
     HuffBuildArgs hb{};
     hb.hist = w.hist;
@@ -693,7 +707,10 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     hb.stack_offset = w.build_stack_off;
     hb.heap_offset = w.build_heap_off;
     hb.status = w.status;
-    VSZ_TRY(launch_huff_build(hb, st));
+    {
+        StageTimer t(kStHuffBuild, st);
+        VSZ_TRY(launch_huff_build(hb, st));
+    }
     // 4. bitstream, placed after the tree bytes (an offset only the device knows)
     HuffEncodeArgs he{};
     he.codes = w.code;
@@ -710,7 +727,10 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     he.tile_counter = w.e_counter;
     he.status = w.status;
     he.build_info = w.build_info;
-    VSZ_TRY(launch_huff_encode(he, st, num_sms()));
+    {
+        StageTimer t(kStHuffEncode, st);
+        VSZ_TRY(launch_huff_encode(he, st, num_sms()));
+    }
     // 5. outliers after the bitstream, in row-major order
     GatherArgs ga{};
     ga.seg_count = w.seg_count;
@@ -722,7 +742,10 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     ga.tile_status = w.g_tile_status;
     ga.tile_counter = w.g_counter;
     ga.status = w.status;
-    VSZ_TRY(launch_outlier_gather(ga, st));
+    {
+        StageTimer t(kStOutlierGather, st);
+        VSZ_TRY(launch_outlier_gather(ga, st));
+    }
     // 6. header, result record, trailer with the decode index
     FinalizeArgs f{};
     f.archive = d_archive;
@@ -746,7 +769,10 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     int fg = (int)((w.n_chunks + 255) / 256);
     if (fg < 1) fg = 1;
     if (fg > num_sms() * 4) fg = num_sms() * 4;
-    k_finalize<<<fg, 256, 0, st>>>(f);
+    {
+        StageTimer t(kStFinalize, st);
+        k_finalize<<<fg, 256, 0, st>>>(f);
+    }
     VSZ_CUDA(cudaGetLastError());
     return VSZ_OK;
 }
@@ -879,11 +905,17 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     const uint16_t* idx = d->has_trailer ? reinterpret_cast<const uint16_t*>(d_archive + d->index_offset) : nullptr;
     VSZ_TRY(decode_codes(d_archive + d->huff_offset, d->huff_bytes, d->node_count, d->tree_bytes, g.n, dict, idx,
                          d->has_trailer ? d->n_chunks : 0, d->chunk_syms, w, w.seg_zero, g.d0, st));
-    VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.scan_status, w.scan_counter, w.scan_total, w.status, st));
-    k_check_zeros<<<1, 1, 0, st>>>(w.scan_total, d->n_outlier, w.status);
-    if (d->n_outlier)
+    {
+        StageTimer t(kStZeroScan, st);
+        VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.scan_status, w.scan_counter, w.scan_total, w.status,
+                                st));
+        k_check_zeros<<<1, 1, 0, st>>>(w.scan_total, d->n_outlier, w.status);
+    }
+    if (d->n_outlier) {
+        StageTimer t(kStOutlierCopy, st);
         VSZ_CUDA(cudaMemcpyAsync(w.outliers, d_archive + d->outlier_offset, 4 * d->n_outlier, cudaMemcpyDeviceToDevice,
                                  st));
+    }
     DqDecArgs a{};
     a.codes = w.code;
     a.outliers = w.outliers;
@@ -898,7 +930,10 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.n = g.n;
     a.R = dict / 2;
     bool force_general = getenv("VSZ_FORCE_GENERAL_DECOMPRESS") != nullptr;
-    VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));
+    {
+        StageTimer t(kStLorenzoDecompress, st);
+        VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));
+    }
     if (d_status) k_copy_status<<<1, 1, 0, st>>>(w.status, w.consts, d_status);
     VSZ_CUDA(cudaGetLastError());
     return VSZ_OK;
