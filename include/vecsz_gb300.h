@@ -133,6 +133,18 @@ size_t vsz_outlier_gather_tmp_bytes(int ndim, const size_t dims[3]);
 vsz_status vsz_outlier_gather(int ndim, const size_t dims[3], const uint8_t* d_seg_count, const float* d_scratch,
                               float* d_out, uint64_t* d_count, void* d_tmp, size_t tmp_bytes, void* stream);
 
+/* The same gather for callers that cannot call cudaMalloc (a serving process whose device memory
+ * another allocator owns, a latency-critical loop that cannot take an allocation's implicit
+ * synchronisation, a plugin host that only hands over input and output buffers): it takes no
+ * workspace and allocates nothing.  No counterpart in the reference.  Its scratch is a static
+ * device array of about 512 KiB that every GPU loading this library holds until exit; fields with
+ * more than 2^28 row segments (vsz_outlier_segments) are rejected with VSZ_ERR_CAPACITY.  The first
+ * call on each device looks up the array's device address, so make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU (different streams,
+ * or different host threads) race and must be serialised by the caller. */
+vsz_status vsz_outlier_gather_noalloc(int ndim, const size_t dims[3], const uint8_t* d_seg_count,
+                                      const float* d_scratch, float* d_out, uint64_t* d_count, void* stream);
+
 /* Heap-tree Huffman codebook from a histogram, bit-identical to initHuffman + build_code +
  * convert_HuffTree_to_bytes_anyStates (src/huffman.hh:116-266, 374-502).
  * d_codebook: vsz_codebook_bytes(dict); d_huff_head: 8 + tree bytes, [BE nodeCount][BE dict][tree]

@@ -72,6 +72,7 @@ _PROTOS = {
     "vsz_dualquant": ([_i, C.POINTER(C.c_size_t), _i, _i, _p, _p, _p, _p, _p, _p, _p], _i),
     "vsz_outlier_gather_tmp_bytes": ([_i, C.POINTER(C.c_size_t)], _sz),
     "vsz_outlier_gather": ([_i, C.POINTER(C.c_size_t), _p, _p, _p, _p, _p, _sz, _p], _i),
+    "vsz_outlier_gather_noalloc": ([_i, C.POINTER(C.c_size_t), _p, _p, _p, _p, _p], _i),
     "vsz_codebook_bytes": ([_i], _sz),
     "vsz_huff_head_max": ([_i], _sz),
     "vsz_huffman_build_tmp_bytes": ([_i], _sz),

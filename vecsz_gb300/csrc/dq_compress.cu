@@ -17,6 +17,7 @@
 //   2D tail columns (d0 % 8 != 0): code 0, outlier 0.0 -- the reference skips those AVX chunks
 //   and never runs its scalar tail (src/dualquant.hh:490-495).
 #include <cstdint>
+#include <mutex>
 #include <type_traits>
 
 #include "vsz_device.cuh"
@@ -629,3 +630,75 @@ size_t gather_tmp_bytes(size_t nseg) {
 }
 
 }  // namespace vsz
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free outlier gather.
+//
+// Some callers of this library cannot call cudaMalloc: a serving process whose device memory is
+// wholly owned by another allocator or budget, a latency-critical loop that cannot afford the
+// implicit synchronisation and unpredictable latency of an allocation, or a plugin host that hands
+// a plugin only its input and output buffers.  vsz_outlier_gather_noalloc gives them the gather
+// without a caller workspace: its look-back scratch (a status word, a tile ticket and one status
+// entry per tile of 4096 row segments) lives in the file-scope array below, which every GPU that
+// loads this library holds until the process exits.
+// ------------------------------------------------------------------------------------------
+namespace vsz {
+
+constexpr size_t kNoAllocGatherMaxTiles   = 65536;                                  // tiles of 4096 segments
+constexpr size_t kNoAllocGatherMaxSegments = kNoAllocGatherMaxTiles * kGatherTile;  // 2^28 row segments
+constexpr size_t kNoAllocGatherBytes      = 256 + 8 * (kNoAllocGatherMaxTiles + 1);  // ~512 KiB
+
+static __device__ __align__(256) uint8_t g_noalloc_gather_scratch[kNoAllocGatherBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64];  // device address of g_noalloc_gather_scratch, per device
+}  // namespace
+
+// Set-up, once per device, with that device current: the array's name is only a host-side stand-in
+// in host code, so its device address comes from cudaGetSymbolAddress.
+static int noalloc_gather_scratch(uint8_t** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return VSZ_ERR_CUDA;
+    if (dev < 0 || dev >= 64) return VSZ_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p        = nullptr;
+        cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_gather_scratch);
+        if (rc != cudaSuccess || !p) return VSZ_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = reinterpret_cast<uint8_t*>(g_noalloc_ptr[dev]);
+    return VSZ_OK;
+}
+
+}  // namespace vsz
+
+extern "C" vsz_status vsz_outlier_gather_noalloc(int ndim, const size_t dims[3], const uint8_t* d_seg_count,
+                                                 const float* d_scratch, float* d_out, uint64_t* d_count,
+                                                 void* stream) {
+    using namespace vsz;
+    if (ndim < 1 || ndim > 3 || !dims || !d_seg_count || !d_scratch || !d_out || !d_count) return VSZ_ERR_INVALID;
+    for (int i = 0; i < ndim; i++)
+        if (dims[i] == 0 || dims[i] > 0x7fffffffu) return VSZ_ERR_INVALID;
+    Geometry g = make_geometry(ndim, dims);
+    if (g.nseg > kNoAllocGatherMaxSegments) return VSZ_ERR_CAPACITY;  // beyond the static scratch
+    uint8_t* base = nullptr;
+    int rc        = noalloc_gather_scratch(&base);
+    if (rc != VSZ_OK) return rc;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    GatherArgs ga{};
+    ga.status       = reinterpret_cast<int*>(base);
+    ga.tile_counter = reinterpret_cast<uint32_t*>(base + 4);
+    ga.tile_status  = reinterpret_cast<unsigned long long*>(base + 256);
+    ga.seg_count    = d_seg_count;
+    ga.scratch      = d_scratch;
+    ga.nseg         = g.nseg;
+    ga.out_f32      = d_out;
+    ga.total        = reinterpret_cast<unsigned long long*>(d_count);
+    // The array keeps the previous call's contents: clear the status word here; the launcher
+    // clears the tile ticket and the tile statuses it will use.
+    if (cudaMemsetAsync(ga.status, 0, sizeof(int), st) != cudaSuccess) return VSZ_ERR_CUDA;
+    return launch_outlier_gather(ga, st);
+}
+
