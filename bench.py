@@ -38,12 +38,14 @@ WORKLOADS = {
     # name: (numpy shape (z, y, x), generator, eb, mode, dict, bs)
     "nyx512": ((512, 512, 512), "grf", 1e-4, "r2r", 1024, 8),
     "nyx256": ((256, 256, 256), "grf", 1e-4, "r2r", 1024, 8),
+    "nyx512s": ((192, 512, 512), "grf", 1e-4, "r2r", 1024, 8),
     "cesm": ((1, 1800, 3600), "bump", 1e-4, "abs", 1024, 8),
     "adversarial": ((256, 384, 384), "adv", 1e-6, "abs", 1024, 8),
 }
 WORKLOAD_DESC = {
     "nyx512": "512^3 f32 GRF k^-11/3 log-normal (NYX-like), r2r eb 1e-4, dict 1024, block 8",
     "nyx256": "256^3 f32 GRF k^-11/3 log-normal, r2r eb 1e-4, dict 1024, block 8",
+    "nyx512s": "512x512x192 slab of the NYX-like field (ncu captures: > L2, ~1.5 GB on device)",
     "cesm": "1800x3600 f32 sum of 64 Gaussian bumps (CESM-like), abs eb 1e-4, dict 1024, block 8",
     "adversarial": "256x384x384 f32 GRF + 5% Cauchy spikes + 8 steps, abs eb 1e-6, dict 1024, block 8",
 }

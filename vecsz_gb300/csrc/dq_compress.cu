@@ -252,7 +252,7 @@ __device__ __forceinline__ void load_row(const DqArgs& a, const float* rowp, boo
 }
 
 template <int NDIM, int BS, bool VEC>
-__global__ void __launch_bounds__(256) k_dq_compress_23d(DqArgs a) {
+__global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
     extern __shared__ uint32_t s_hist_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
     const Consts c   = *a.consts;

@@ -24,134 +24,168 @@ namespace vsz {
 // ------------------------------------------------------------------------------------------
 
 constexpr int kKeyShift = 20;  // heap key = freq << 20 | node  (node < 2^20, freq < 2^44)
-
-struct DfsEntry {
-    uint32_t node;
-    int32_t parent;
-    uint32_t depth_side;  // depth << 1 | side
-    uint32_t pad;
-    unsigned long long code;
-};
+constexpr uint32_t kNodeMask = (1u << kKeyShift) - 1u;
 
 __device__ __forceinline__ unsigned long long kfreq(unsigned long long k) { return k >> kKeyShift; }
 
+// Working set of the tree build (shared memory when it fits, else the global scratch).
+struct BuildWs {
+    unsigned long long* heap;  // 2 dict + 8 (room for speculative reads below the heap end)
+    uint32_t* used;            // dict: symbol of leaf i
+    int32_t* lchild;           // dict: children of internal node k (node nused + k)
+    int32_t* rchild;
+    uint32_t* size;            // 2 dict: subtree sizes
+    uint32_t* pre;             // 2 dict: preorder index (pad_tree_* numbering)
+    unsigned long long* code;  // 2 dict: codeword, right-aligned
+    uint32_t* depth;           // 2 dict
+};
+
+__host__ __device__ inline size_t build_ws_bytes(int dict) {
+    size_t d = (size_t)dict;
+    return 8 * (2 * d + 8) + 4 * d + 8 * d + 4 * 2 * d * 2 + 8 * 2 * d + 4 * 2 * d + 256;
+}
+
+__device__ inline BuildWs carve_build_ws(uint8_t* p, int dict) {
+    size_t d = (size_t)dict;
+    BuildWs w;
+    w.heap   = reinterpret_cast<unsigned long long*>(p);
+    p += 8 * (2 * d + 8);
+    w.code   = reinterpret_cast<unsigned long long*>(p);
+    p += 8 * 2 * d;
+    w.used   = reinterpret_cast<uint32_t*>(p);
+    p += 4 * d;
+    w.lchild = reinterpret_cast<int32_t*>(p);
+    p += 4 * d;
+    w.rchild = reinterpret_cast<int32_t*>(p);
+    p += 4 * d;
+    w.size   = reinterpret_cast<uint32_t*>(p);
+    p += 4 * 2 * d;
+    w.pre    = reinterpret_cast<uint32_t*>(p);
+    p += 4 * 2 * d;
+    w.depth  = reinterpret_cast<uint32_t*>(p);
+    return w;
+}
+
 __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
-    extern __shared__ unsigned long long s_heap_dyn[];
+    extern __shared__ __align__(16) uint8_t s_build_dyn[];
     __shared__ uint32_t s_info[4];
     __shared__ int s_fail;
+    __shared__ uint32_t s_scan[33];
     if (*a.status != VSZ_OK) return;  // an earlier stage failed (uniform: one CTA)
     const int dict = a.dict;
-    uint8_t* base  = reinterpret_cast<uint8_t*>(a.scratch);
-    // global scratch layout (HuffBuildScratch::bytes)
-    uint32_t* used   = reinterpret_cast<uint32_t*>(base);                        // dict
-    int32_t* lchild  = reinterpret_cast<int32_t*>(used + dict);                  // dict (internal)
-    int32_t* rchild  = lchild + dict;                                            // dict
-    uint32_t* preL   = reinterpret_cast<uint32_t*>(rchild + dict);               // 2 dict
-    uint32_t* preR   = preL + 2 * dict;
-    uint32_t* preC   = preR + 2 * dict;
-    uint8_t* preT    = reinterpret_cast<uint8_t*>(preC + 2 * dict);              // 2 dict
-    DfsEntry* stack  = reinterpret_cast<DfsEntry*>(base + a.stack_offset);       // 2 dict
-    unsigned long long* heap = a.heap_in_smem ? s_heap_dyn : reinterpret_cast<unsigned long long*>(base + a.heap_offset);
-
+    BuildWs w      = carve_build_ws(a.ws_in_smem ? s_build_dyn : reinterpret_cast<uint8_t*>(a.scratch), dict);
+    if (threadIdx.x == 0) s_fail = 0;
+    for (int i = threadIdx.x; i < 2 * dict + 8; i += blockDim.x) w.heap[i] = 0ull;
     for (int i = threadIdx.x; i < dict; i += blockDim.x) {
         a.cb_word[i] = 0ull;
         a.cb_len[i]  = 0;
     }
-    for (int i = threadIdx.x; i < 2 * dict; i += blockDim.x) {
-        preL[i] = 0u;
-        preR[i] = 0u;
+    // ---- used symbols in symbol order (src/huffman.hh:248-254), block-wide compaction
+    const int per = (dict + blockDim.x - 1) / blockDim.x;
+    const int s0  = threadIdx.x * per;
+    uint32_t cnt  = 0;
+    for (int k = 0; k < per; k++) {
+        int sym = s0 + k;
+        if (sym < dict && a.hist[sym] != 0ull) cnt++;
     }
-    if (threadIdx.x == 0) s_fail = 0;
+    uint32_t tot;
+    uint32_t off = block_exclusive_scan<uint32_t>(cnt, s_scan, &tot);
+    for (int k = 0; k < per; k++) {
+        int sym = s0 + k;
+        if (sym < dict) {
+            unsigned long long f = a.hist[sym];
+            if (f != 0ull) {
+                w.used[off]   = (uint32_t)sym;
+                w.code[off++] = f;  // leaf frequencies, until the codewords are computed
+            }
+        }
+    }
     __syncthreads();
+    const int nused = (int)tot;
 
     if (threadIdx.x == 0) {
-        // leaves in symbol order (src/huffman.hh:248-254)
-        int nused = 0;
-        int qend  = 1;
-        for (int i = 0; i < dict; i++) {
-            unsigned long long f = a.hist[i];
-            if (f == 0) continue;
+        int qend = 1;
+        // leaves: qinsert(new_node(freq, i)) in symbol order (src/huffman.hh:169-177)
+        for (int i = 0; i < nused; i++) {
+            unsigned long long f = w.code[i];
             if (f >= (1ull << (64 - kKeyShift))) s_fail = VSZ_ERR_UNSUPPORTED;
-            used[nused] = (uint32_t)i;
-            unsigned long long key = (f << kKeyShift) | (unsigned long long)nused;
-            nused++;
-            int ii = qend++, j;  // qinsert
+            unsigned long long key = (f << kKeyShift) | (unsigned long long)i;
+            int ii = qend++, j;
             while ((j = ii >> 1)) {
-                if (kfreq(heap[j]) <= kfreq(key)) break;
-                heap[ii] = heap[j];
-                ii       = j;
+                unsigned long long pj = w.heap[j];
+                if (kfreq(pj) <= kfreq(key)) break;
+                w.heap[ii] = pj;
+                ii         = j;
             }
-            heap[ii] = key;
+            w.heap[ii] = key;
         }
         if (nused == 0) s_fail = VSZ_ERR_INVALID;
         int nnodes = nused;
-        // merge (src/huffman.hh:262): new_node(.., qremove(), qremove()) -- the first removal is
-        // the right child, the second the left (argument evaluation order of the reference build)
+        // merges (src/huffman.hh:262): the first qremove() is the RIGHT child, the second the LEFT
+        // (the reference build evaluates new_node's arguments right to left)
         while (!s_fail && qend > 2) {
             unsigned long long rem[2];
 #pragma unroll
-            for (int r = 0; r < 2; r++) {  // qremove
-                unsigned long long n = heap[1];
+            for (int r = 0; r < 2; r++) {
+                // qremove (src/huffman.hh:179-192): the hole sinks along the smaller child (ties:
+                // left) to the bottom, then takes the last element -- no sift-up.  The children of
+                // both candidates are loaded one level ahead.
+                const unsigned long long top = w.heap[1];
                 qend--;
-                int i = 1, l;
-                while ((l = i << 1) < qend) {
-                    ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(&heap[l]);
-                    unsigned long long best = pr.x;
-                    if (l + 1 < qend && kfreq(pr.y) < kfreq(pr.x)) {
-                        l++;
-                        best = pr.y;
-                    }
-                    heap[i] = best;
-                    i       = l;
+                const unsigned long long last = w.heap[qend];
+                int i = 1, l = 2;
+                ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(&w.heap[2]);
+                while (l < qend) {
+                    ulonglong2 ga = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l]);
+                    ulonglong2 gb = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l + 2]);
+                    const bool right = (l + 1 < qend) && (kfreq(pr.y) < kfreq(pr.x));
+                    w.heap[i] = right ? pr.y : pr.x;
+                    i         = right ? l + 1 : l;
+                    l         = 2 * i;
+                    pr        = right ? gb : ga;
                 }
-                heap[i] = heap[qend];
-                rem[r]  = n;
+                w.heap[i] = last;
+                rem[r]    = top;
             }
-            int node = nnodes++;
-            rchild[node - nused] = (int32_t)(rem[0] & ((1u << kKeyShift) - 1));
-            lchild[node - nused] = (int32_t)(rem[1] & ((1u << kKeyShift) - 1));
-            unsigned long long key = ((kfreq(rem[0]) + kfreq(rem[1])) << kKeyShift) | (unsigned long long)node;
+            const int k = nnodes - nused;
+            nnodes++;
+            w.rchild[k] = (int32_t)(rem[0] & kNodeMask);
+            w.lchild[k] = (int32_t)(rem[1] & kNodeMask);
+            unsigned long long key = ((kfreq(rem[0]) + kfreq(rem[1])) << kKeyShift) | (unsigned long long)(nused + k);
             int ii = qend++, j;
             while ((j = ii >> 1)) {
-                if (kfreq(heap[j]) <= kfreq(key)) break;
-                heap[ii] = heap[j];
-                ii       = j;
+                unsigned long long pj = w.heap[j];
+                if (kfreq(pj) <= kfreq(key)) break;
+                w.heap[ii] = pj;
+                ii         = j;
             }
-            heap[ii] = key;
+            w.heap[ii] = key;
         }
         uint32_t node_count = 0, max_len = 0;
         if (!s_fail) {
-            int root = (int)(heap[1] & ((1u << kKeyShift) - 1));
-            // preorder DFS: numbering of pad_tree_* (src/huffman.hh:374-423) and codewords of
-            // build_code (:200-227), left edge 0, right edge 1
-            int sp = 0;
-            stack[sp++] = DfsEntry{(uint32_t)root, -1, 0u, 0u, 0ull};
-            uint32_t counter = 0;
-            while (sp > 0) {
-                DfsEntry e   = stack[--sp];
-                uint32_t idx = counter++;
-                uint32_t depth = e.depth_side >> 1;
-                if (e.parent >= 0) {
-                    if (e.depth_side & 1u) preR[e.parent] = idx;
-                    else preL[e.parent] = idx;
-                }
-                if ((int)e.node < nused) {
-                    uint32_t sym = used[e.node];
-                    preC[idx]    = sym;
-                    preT[idx]    = 1;
-                    a.cb_len[sym]  = (uint8_t)(depth > 255 ? 255 : depth);
-                    a.cb_word[sym] = e.code;
-                    if (depth > max_len) max_len = depth;
-                } else {
-                    preC[idx] = 0;
-                    preT[idx] = 0;
-                    int k     = (int)e.node - nused;
-                    unsigned long long c2 = e.code << 1;
-                    stack[sp++] = DfsEntry{(uint32_t)rchild[k], (int32_t)idx, ((depth + 1) << 1) | 1u, 0u, c2 | 1ull};
-                    stack[sp++] = DfsEntry{(uint32_t)lchild[k], (int32_t)idx, ((depth + 1) << 1), 0u, c2};
-                }
+            const int nint = nnodes - nused;
+            // subtree sizes bottom-up (children are always created before their parent)
+            for (int i = 0; i < nused; i++) w.size[i] = 1u;
+            for (int k = 0; k < nint; k++) w.size[nused + k] = 1u + w.size[w.lchild[k]] + w.size[w.rchild[k]];
+            // root = the last node created (a one-leaf tree: the leaf); preorder numbering of
+            // pad_tree_* (src/huffman.hh:374-423) and codewords of build_code (:200-227) top-down
+            const int root = nnodes - 1;
+            w.pre[root]   = 0u;
+            w.code[root]  = 0ull;
+            w.depth[root] = 0u;
+            for (int k = nint - 1; k >= 0; k--) {
+                const int v = nused + k, l = w.lchild[k], r = w.rchild[k];
+                const uint32_t pv = w.pre[v], dv = w.depth[v] + 1u;
+                const unsigned long long cv = w.code[v] << 1;
+                w.pre[l]   = pv + 1u;
+                w.pre[r]   = pv + 1u + w.size[l];
+                w.code[l]  = cv;
+                w.code[r]  = cv | 1ull;
+                w.depth[l] = dv;
+                w.depth[r] = dv;
+                if (dv > max_len) max_len = dv;
             }
-            node_count = counter;
+            node_count = (uint32_t)nnodes;
         }
         s_info[0] = node_count;
         s_info[1] = (uint32_t)tree_bytes_size(node_count);
@@ -164,7 +198,8 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
         return;
     }
     const uint32_t nc = s_info[0];
-    const int w       = tree_index_width(nc);
+    const int nused_c = nused;
+    const int wdt     = tree_index_width(nc);
     // [BE nodeCount][BE dict][u8 0][L][R][C u32 LE][t]  (src/huffman.hh:649-653, 438-444)
     uint8_t* o = a.out;
     if (threadIdx.x == 0) {
@@ -180,20 +215,30 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
         o[8] = 0;
     }
     uint8_t* pL = o + 9;
-    uint8_t* pR = pL + (size_t)w * nc;
-    uint8_t* pC = pR + (size_t)w * nc;
+    uint8_t* pR = pL + (size_t)wdt * nc;
+    uint8_t* pC = pR + (size_t)wdt * nc;
     uint8_t* pT = pC + 4 * (size_t)nc;
-    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
-        uint32_t l = preL[i], r = preR[i], c = preC[i];
-        for (int b = 0; b < w; b++) {
-            pL[(size_t)i * w + b] = (uint8_t)(l >> (8 * b));
-            pR[(size_t)i * w + b] = (uint8_t)(r >> (8 * b));
+    for (uint32_t v = threadIdx.x; v < nc; v += blockDim.x) {
+        const uint32_t idx = w.pre[v];
+        const bool leaf    = (int)v < nused_c;
+        uint32_t l = 0, r = 0, c = 0;
+        if (leaf) {
+            c = w.used[v];
+            a.cb_len[c]  = (uint8_t)(w.depth[v] > 255u ? 255u : w.depth[v]);
+            a.cb_word[c] = w.code[v];
+        } else {
+            l = w.pre[w.lchild[v - nused_c]];
+            r = w.pre[w.rchild[v - nused_c]];
         }
-        pC[4 * (size_t)i + 0] = (uint8_t)c;
-        pC[4 * (size_t)i + 1] = (uint8_t)(c >> 8);
-        pC[4 * (size_t)i + 2] = (uint8_t)(c >> 16);
-        pC[4 * (size_t)i + 3] = (uint8_t)(c >> 24);
-        pT[i]                 = preT[i];
+        for (int b = 0; b < wdt; b++) {
+            pL[(size_t)idx * wdt + b] = (uint8_t)(l >> (8 * b));
+            pR[(size_t)idx * wdt + b] = (uint8_t)(r >> (8 * b));
+        }
+        pC[4 * (size_t)idx + 0] = (uint8_t)c;
+        pC[4 * (size_t)idx + 1] = (uint8_t)(c >> 8);
+        pC[4 * (size_t)idx + 2] = (uint8_t)(c >> 16);
+        pC[4 * (size_t)idx + 3] = (uint8_t)(c >> 24);
+        pT[idx]                 = leaf ? 1 : 0;
     }
     if (threadIdx.x < 4) a.info[threadIdx.x] = s_info[threadIdx.x];
 }
@@ -283,7 +328,7 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
         const unsigned long long gstart = base0 + B;  // tile's first bit on the global word grid
         const uint32_t r0     = (uint32_t)(gstart & 31u);
         const unsigned long long F = gstart >> 5;
-        const uint32_t nwords = (uint32_t)((r0 + tot + 31) >> 5);
+        const uint32_t nwords = tot ? (uint32_t)((r0 + tot + 31) >> 5) : 0u;
         for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) s_words[i] = 0u;
         __syncthreads();
         // ---- pack this thread's codewords into the word buffer; only a thread's first and last
@@ -325,41 +370,46 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
             if (nb > 0) atomicOr(&s_words[wi], (uint32_t)(acc >> 32));
         }
         __syncthreads();
-        // ---- store: interior words and the last word are plain stores; a first word shared with
-        // the previous tile is OR-ed in by thread 0 after that tile's last word has landed
-        const bool first_special = (r0 != 0) || (tile == 0 && base0 != 0);
+        // ---- store: words wholly inside the tile are plain stores; a partial first or last word
+        // (shared with the neighbouring tile, or with the tree bytes before the payload) is left to
+        // k_huff_encode_edges, which ORs the two halves -- no tile ever waits on another's store
+        const bool first_partial = (r0 != 0);
+        const bool last_partial  = ((r0 + tot) & 31ull) != 0;
         for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) {
-            if (i == 0 && first_special) continue;
+            if (i == 0 && first_partial) continue;
+            if (i == nwords - 1 && last_partial) continue;
             gw[F + i] = bswap32(s_words[i]);
         }
-        __threadfence();
-        __syncthreads();
         if (threadIdx.x == 0) {
-            if (first_special && nwords > 0) {
-                uint32_t v = bswap32(s_words[0]);
-                if (tile == 0) {
-                    // bytes before the payload start belong to the tree section: keep them
-                    uint32_t keep = (base0 == 0) ? 0u : ((1u << base0) - 1u);
-                    uint32_t old  = gw[F];
-                    gw[F]         = (old & keep) | v;
-                } else {
-                    long long spins = 0;
-                    while (atomicAdd(&a.tail_flag[tile - 1], 0u) == 0u) {
-                        if (++spins > kSpinLimit) {
-                            set_status(a.status, VSZ_ERR_TIMEOUT);
-                            break;
-                        }
-                    }
-                    atomicOr(&gw[F], v);
-                }
-            } else if (tile > 0 && nwords == 0) {
-                // empty tile (cannot happen for codes of length >= 1): keep the chain intact
-            }
-            __threadfence();
-            atomicExch(&a.tail_flag[tile], 1u);
+            const unsigned long long none = ~0ull;
+            a.edge_idx[2 * tile]      = (nwords && first_partial) ? F : none;
+            a.edge_bits[2 * tile]     = nwords ? bswap32(s_words[0]) : 0u;
+            a.edge_idx[2 * tile + 1]  = (nwords && last_partial) ? F + nwords - 1 : none;
+            a.edge_bits[2 * tile + 1] = nwords ? bswap32(s_words[nwords - 1]) : 0u;
         }
         __syncthreads();
     }
+}
+
+// Boundary words of the encoder tiles: tile t's partial first word is the same word as tile
+// t - 1's partial last word (a middle tile spans thousands of bits, so no word has a third
+// sharer); the payload's first word also holds the last bytes of the tree section, kept as is.
+__global__ void k_huff_encode_edges(HuffEncodeArgs a) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.ntiles || *a.status != VSZ_OK) return;
+    uint8_t* out         = a.out + a.out_off.eval();
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
+    uint32_t* gw         = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
+    const unsigned long long none = ~0ull;
+    const unsigned long long fi   = a.edge_idx[2 * t];
+    const unsigned long long li   = a.edge_idx[2 * t + 1];
+    if (fi != none) {
+        uint32_t v = a.edge_bits[2 * t];
+        if (t > 0 && a.edge_idx[2 * t - 1] == fi) v |= a.edge_bits[2 * t - 1];
+        if (fi == 0 && base0 != 0) v |= gw[0] & ((1u << base0) - 1u);  // tree bytes before the payload
+        gw[fi] = v;
+    }
+    if (t == a.ntiles - 1 && li != none && li != fi) gw[li] = a.edge_bits[2 * t + 1];
 }
 
 // ------------------------------------------------------------------------------------------
@@ -583,6 +633,83 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
     flush();
 }
 
+// Indexed decode with coalesced output: a warp decodes 32 consecutive chunks of 512 codewords
+// (one per lane) in rounds of 32 symbols staged in shared memory, then writes each lane's 32
+// symbols (64 contiguous bytes) as 16-byte stores.
+constexpr int kDecRound = 32;
+
+__global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
+    __shared__ uint32_t s_table[1 << kDecBits];
+    __shared__ __align__(16) uint16_t s_stage[8][32][kDecRound + 8];  // +8: keep rows 16-byte aligned
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    __syncthreads();
+    if (*a.status != VSZ_OK) return;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const size_t j      = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t jw0    = j - lane;  // first chunk of this warp
+    if (jw0 >= a.nchunks) return;
+    const bool active   = j < a.nchunks;
+    const unsigned long long out0 = (unsigned long long)j * kChunkSyms;
+    uint32_t cnt = 0;
+    if (active && out0 < a.n) cnt = (uint32_t)min((unsigned long long)kChunkSyms, a.n - out0);
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 3u) * 8u;
+    const uint32_t* gw   = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)3);
+    BitReader br;
+    if (cnt) br.init(gw, base0 + a.start_bit[j], base0 + a.payload_bits);
+    unsigned long long row = active ? out0 / a.d0 : 0;
+    uint32_t x             = active ? (uint32_t)(out0 - row * a.d0) : 0u;
+    uint32_t zeros         = 0;
+    auto flush = [&]() {
+        if (zeros && a.seg_zero) atomicAdd(&a.seg_zero[row * a.nxs + (x >> 8)], zeros);
+        zeros = 0;
+    };
+    bool bad = false;
+    for (uint32_t r0 = 0; r0 < (uint32_t)kChunkSyms; r0 += kDecRound) {
+        const uint32_t m = (cnt > r0) ? min((uint32_t)kDecRound, cnt - r0) : 0u;
+        for (uint32_t k = 0; k < m && !bad; k++) {
+            uint32_t sy = decode_one(br, s_table, a.child, a.node_sym, a.max_nodes);
+            if (sy == 0xffffffffu) {
+                bad = true;
+                break;
+            }
+            s_stage[warp][lane][k] = (uint16_t)sy;
+            zeros += (sy == 0);
+            x++;
+            if (x == a.d0) {
+                x--;
+                flush();
+                x = 0;
+                row++;
+            } else if ((x & 255u) == 0) {
+                x--;
+                flush();
+                x++;
+            }
+        }
+        __syncwarp();
+        // 32 rows x 4 pieces of 8 symbols; piece q*32 + lane
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t piece = q * 32 + lane, src = piece >> 2, part = piece & 3u;
+            const size_t jj      = jw0 + src;
+            const uint32_t cnt_s = __shfl_sync(0xffffffffu, cnt, src);
+            const uint32_t ms    = (cnt_s > r0) ? min((uint32_t)kDecRound, cnt_s - r0) : 0u;
+            const uint32_t p0    = part * 8;
+            if (jj < a.nchunks && p0 < ms) {
+                uint16_t* dst = a.codes + jj * kChunkSyms + r0 + p0;
+                if (p0 + 8 <= ms) {
+                    *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(&s_stage[warp][src][p0]);
+                } else {
+                    for (uint32_t e = p0; e < ms; e++) dst[e - p0] = s_stage[warp][src][e];
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (bad) set_status(a.status, VSZ_ERR_CORRUPT);
+    flush();
+}
+
 // Constant fill for a one-symbol tree (src/huffman.hh:348-352).
 __global__ void k_huff_const(uint16_t* codes, size_t n, const uint32_t* info, uint32_t* seg_zero, uint32_t d0, uint32_t nxs,
                              const int* status) {
@@ -712,29 +839,22 @@ __global__ void __launch_bounds__(256) k_scan_excl(const TIn* __restrict__ in, u
 // ------------------------------------------------------------------------------------------
 
 int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
-    size_t heap_bytes = ((size_t)a.dict + 2) * sizeof(unsigned long long);
-    size_t smem       = 0;
-    a.heap_in_smem    = heap_bytes <= 48 * 1024 ? 1 : 0;
-    if (a.heap_in_smem) smem = heap_bytes;
+    size_t bytes = build_ws_bytes(a.dict);
+    size_t smem  = 0;
+    a.ws_in_smem = bytes <= 200 * 1024 ? 1 : 0;
+    if (a.ws_in_smem) {
+        smem = bytes;
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_huff_build, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            attr = true;
+        }
+    }
     k_huff_build<<<1, 256, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
-size_t huff_build_scratch_bytes(int dict, size_t* stack_offset, size_t* heap_offset) {
-    size_t d   = (size_t)dict;
-    size_t off = 0;
-    off += 4 * d;          // used
-    off += 8 * d;          // lchild, rchild
-    off += 3 * 4 * 2 * d;  // preL, preR, preC
-    off += 2 * d;          // preT
-    off = (off + 15) & ~(size_t)15;
-    if (stack_offset) *stack_offset = off;
-    off += sizeof(DfsEntry) * 2 * d + 64;
-    off = (off + 15) & ~(size_t)15;
-    if (heap_offset) *heap_offset = off;
-    off += 8 * (d + 4);
-    return off;
-}
+size_t huff_build_scratch_bytes(int dict) { return build_ws_bytes(dict); }
 
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
     a.ntiles = (uint32_t)((a.n + kEncTile - 1) / kEncTile);
@@ -749,10 +869,10 @@ int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
         attr_set = true;
     }
     if (cudaMemsetAsync(a.tile_status, 0, 8 * (size_t)a.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
-    if (cudaMemsetAsync(a.tail_flag, 0, 4 * (size_t)a.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
     if (cudaMemsetAsync(a.tile_counter, 0, 4, st) != cudaSuccess) return VSZ_ERR_CUDA;
     int grid = (int)min((long long)a.ntiles, (long long)num_sms * 2);
     k_huff_encode<<<grid, kEncThreads, smem, st>>>(a);
+    k_huff_encode_edges<<<(a.ntiles + 255) / 256, 256, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
@@ -764,7 +884,10 @@ int launch_huff_table(HuffTableArgs a, cudaStream_t st) {
 int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
     if (a.nchunks == 0) return VSZ_OK;
     int grid = (int)((a.nchunks + 255) / 256);
-    k_huff_decode<<<grid, 256, 0, st>>>(a);
+    const bool indexed = !a.out_begin && !a.nsym && a.chunk_syms == (uint32_t)kChunkSyms &&
+                         (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0;
+    if (indexed) k_huff_decode_idx<<<grid, 256, 0, st>>>(a);
+    else k_huff_decode<<<grid, 256, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 

@@ -225,12 +225,12 @@ struct CompressWs {
     uint32_t* g_counter;
     unsigned long long* n_out;
     uint8_t* build_scratch;
-    size_t build_stack_off, build_heap_off;
     unsigned long long* cb_word;
     uint8_t* cb_len;
     uint32_t* build_info;
     unsigned long long* e_tile_status;
-    uint32_t* e_tail;
+    unsigned long long* e_edge_idx;
+    uint32_t* e_edge_bits;
     uint32_t* e_counter;
     unsigned long long* total_bits;
     uint16_t* chunk_bits;
@@ -252,17 +252,14 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     w.g_tile_status = b.take<unsigned long long>(gt);
     w.g_counter = b.take<uint32_t>(4);
     w.n_out     = b.take<unsigned long long>(1);
-    size_t so, ho;
-    size_t bsz  = huff_build_scratch_bytes(dict, &so, &ho);
-    w.build_scratch   = b.take<uint8_t>(bsz);
-    w.build_stack_off = so;
-    w.build_heap_off  = ho;
+    w.build_scratch = b.take<uint8_t>(huff_build_scratch_bytes(dict));
     w.cb_word    = b.take<unsigned long long>(dict);
     w.cb_len     = b.take<uint8_t>(dict);
     w.build_info = b.take<uint32_t>(4);
     size_t et    = (g.n + 4095) / 4096 + 1;
     w.e_tile_status = b.take<unsigned long long>(et);
-    w.e_tail     = b.take<uint32_t>(et);
+    w.e_edge_idx  = b.take<unsigned long long>(2 * et);
+    w.e_edge_bits = b.take<uint32_t>(2 * et);
     w.e_counter  = b.take<uint32_t>(4);
     w.total_bits = b.take<unsigned long long>(1);
     w.n_chunks   = (g.n + kChunkSyms - 1) / kChunkSyms;
@@ -527,7 +524,7 @@ vsz_status vsz_outlier_gather(int ndim, const size_t dims[3], const uint8_t* d_s
 
 size_t vsz_codebook_bytes(int dict_size) { return (size_t)dict_size * 9 + 64; }
 size_t vsz_huff_head_max(int dict_size) { return 8 + tree_bytes_size((uint32_t)(2 * dict_size - 1)); }
-size_t vsz_huffman_build_tmp_bytes(int dict_size) { return huff_build_scratch_bytes(dict_size, nullptr, nullptr) + 512; }
+size_t vsz_huffman_build_tmp_bytes(int dict_size) { return huff_build_scratch_bytes(dict_size) + 512; }
 
 vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_codebook, uint8_t* d_huff_head,
                              uint32_t* d_info, void* d_tmp, size_t tmp_bytes, void* stream) {
@@ -542,14 +539,13 @@ vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_code
     a.info    = d_info;
     a.status  = reinterpret_cast<int*>(d_tmp);
     a.scratch = reinterpret_cast<uint8_t*>(d_tmp) + 256;
-    huff_build_scratch_bytes(dict_size, &a.stack_offset, &a.heap_offset);
     VSZ_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), S(stream)));
     return launch_huff_build(a, S(stream));
 }
 
 size_t vsz_huffman_encode_tmp_bytes(size_t n) {
     size_t nt = (n + 4095) / 4096 + 1;
-    return 1024 + 12 * nt + 256;
+    return 1024 + 8 * nt + 16 * nt + 8 * nt + 1024;
 }
 
 vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_codebook, int dict_size,
@@ -563,7 +559,8 @@ vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_co
     a.tile_counter = b.take<uint32_t>(4);
     size_t nt      = (n + 4095) / 4096 + 1;
     a.tile_status  = b.take<unsigned long long>(nt);
-    a.tail_flag    = b.take<uint32_t>(nt);
+    a.edge_idx     = b.take<unsigned long long>(2 * nt);
+    a.edge_bits    = b.take<uint32_t>(2 * nt);
     a.codes        = d_code;
     a.n            = n;
     a.cb_word      = reinterpret_cast<const unsigned long long*>(d_codebook);
@@ -704,8 +701,6 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     hb.out = d_archive + hdr;
     hb.info = w.build_info;
     hb.scratch = w.build_scratch;
-    hb.stack_offset = w.build_stack_off;
-    hb.heap_offset = w.build_heap_off;
     hb.status = w.status;
     {
         StageTimer t(kStHuffBuild, st);
@@ -723,7 +718,8 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     he.total_bits = w.total_bits;
     he.chunk_bits = w.chunk_bits;
     he.tile_status = w.e_tile_status;
-    he.tail_flag = w.e_tail;
+    he.edge_idx = w.e_edge_idx;
+    he.edge_bits = w.e_edge_bits;
     he.tile_counter = w.e_counter;
     he.status = w.status;
     he.build_info = w.build_info;

@@ -29,9 +29,8 @@ struct HuffBuildArgs {
     uint8_t* cb_len;              // codeword length per symbol (0 = unused)
     uint8_t* out;                 // [BE nc][BE dict][tree bytes], any alignment
     uint32_t* info;               // [0] node count [1] tree bytes [2] max code length [3] nodes created
-    void* scratch;                // huff_build_scratch_bytes(dict)
-    size_t stack_offset, heap_offset;
-    int heap_in_smem;
+    void* scratch;                // huff_build_scratch_bytes(dict), used when shared memory is too small
+    int ws_in_smem;
     int* status;
 };
 
@@ -46,7 +45,8 @@ struct HuffEncodeArgs {
     unsigned long long* total_bits;
     uint16_t* chunk_bits;             // bits per 512 codes (decode index), may be null
     unsigned long long* tile_status;  // ntiles
-    uint32_t* tail_flag;              // ntiles
+    unsigned long long* edge_idx;     // 2 ntiles: word index of a tile's partial first / last word
+    uint32_t* edge_bits;              // 2 ntiles: its bits (stored byte order)
     uint32_t* tile_counter;
     int* status;
     uint32_t ntiles;
@@ -103,7 +103,7 @@ struct HuffSyncArgs {
 };
 
 int launch_huff_build(HuffBuildArgs a, cudaStream_t st);
-size_t huff_build_scratch_bytes(int dict, size_t* stack_offset, size_t* heap_offset);
+size_t huff_build_scratch_bytes(int dict);
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms);
 int launch_huff_table(HuffTableArgs a, cudaStream_t st);
 int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st);
