@@ -151,12 +151,14 @@ struct HistAcc {
     // other codes go to the block's shared-memory histogram.
     uint32_t c0 = 0, c1 = 0, c2 = 0;
     __device__ __forceinline__ void add(int code, int R, uint32_t* s_hist, int dict, unsigned long long* g_hist) {
-        int d = code - R;
-        if (d == 0) c1++;
-        else if (d == -1) c0++;
-        else if (d == 1) c2++;
-        else if (s_hist) atomicAdd(&s_hist[code], 1u);
-        else atomicAdd(&g_hist[code], 1ull);
+        const uint32_t d = (uint32_t)(code - R + 1);
+        c0 += (d == 0u);
+        c1 += (d == 1u);
+        c2 += (d == 2u);
+        if (d > 2u) {
+            if (s_hist) atomicAdd(&s_hist[code], 1u);
+            else atomicAdd(&g_hist[code], 1ull);
+        }
     }
     __device__ __forceinline__ void flush(int R, uint32_t* s_hist, int dict, unsigned long long* g_hist) {
         if (s_hist) {
@@ -195,19 +197,22 @@ __device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t x
     for (int j = 0; j < 4; j++)
         if (in[j]) h.add(code[j], a.R, s_hist, a.dict, a.hist);
     // Outlier ranking inside the row segment: element (lane, j) precedes (lane', j') iff
-    // 4 lane + j < 4 lane' + j'.
+    // 4 lane + j < 4 lane' + j'.  Most rows of a smooth field have none: one vote decides.
     bool o[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) o[j] = in[j] && code[j] == 0;
+    const size_t seg = row * a.nxt + xt;
+    if (!__any_sync(0xffffffffu, o[0] | o[1] | o[2] | o[3])) {
+        if (row_in && lane == 0) a.seg_count[seg] = 0;
+        return;
+    }
     unsigned m[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        o[j] = in[j] && code[j] == 0;
-        m[j] = __ballot_sync(0xffffffffu, o[j]);
-    }
+    for (int j = 0; j < 4; j++) m[j] = __ballot_sync(0xffffffffu, o[j]);
     if (!row_in) return;
     const unsigned lt = lanemask_lt();
     unsigned before   = __popc(m[0] & lt) + __popc(m[1] & lt) + __popc(m[2] & lt) + __popc(m[3] & lt);
     unsigned total    = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
-    size_t seg        = row * a.nxt + xt;
     if (lane == 0) a.seg_count[seg] = (uint8_t)total;
     if (total) {
         float* dst = a.scratch + seg * kSegX;
@@ -218,14 +223,14 @@ __device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t x
     }
 }
 
-template <int NDIM>
+template <int NDIM, bool TAIL>
 __device__ __forceinline__ float prequant_at(float v, uint32_t col, uint32_t xtail, float r_f, double r_d) {
-    if (NDIM == 3 && col >= xtail) return prequant_scalar(v, r_d);
+    if (NDIM == 3 && TAIL && col >= xtail) return prequant_scalar(v, r_d);
     return prequant_vec(v, r_f);
 }
 
 // Load and prequantize 4 consecutive columns [xb, xb+4) of one row; zero outside the field.
-template <int NDIM, bool VEC>
+template <int NDIM, bool VEC, bool TAIL>
 __device__ __forceinline__ void load_row(const DqArgs& a, const float* rowp, bool row_in, uint32_t xb, float r_f,
                                          double r_d, float S[4]) {
     float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -247,11 +252,11 @@ __device__ __forceinline__ void load_row(const DqArgs& a, const float* rowp, boo
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         bool in = row_in && (xb + j < a.d0);
-        S[j]    = in ? prequant_at<NDIM>(v[j], xb + j, a.xtail, r_f, r_d) : 0.0f;
+        S[j]    = in ? prequant_at<NDIM, TAIL>(v[j], xb + j, a.xtail, r_f, r_d) : 0.0f;
     }
 }
 
-template <int NDIM, int BS, bool VEC>
+template <int NDIM, int BS, bool VEC, bool TAIL>
 __global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
     extern __shared__ uint32_t s_hist_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
@@ -299,11 +304,11 @@ __global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
                 const uint32_t y = y0 + i;
                 const bool row_in = y < a.d1;
                 const float* rowp = a.x + ((size_t)z * a.d1 + y) * a.d0;
-                load_row<NDIM, VEC>(a, rowp, row_in, xb, r_f, r_d, S[i]);
+                load_row<NDIM, VEC, TAIL>(a, rowp, row_in, xb, r_f, r_d, S[i]);
             }
             if (yhalo) {
                 const float* rowp = a.x + ((size_t)z * a.d1 + (y0 - 1)) * a.d0;
-                load_row<NDIM, VEC>(a, rowp, true, xb, r_f, r_d, Sh);
+                load_row<NDIM, VEC, TAIL>(a, rowp, true, xb, r_f, r_d, Sh);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++) Sh[j] = 0.f;
@@ -329,7 +334,7 @@ __global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
                     const float X      = j ? S[i][j - 1] : SL[i];
                     const float Y      = i ? S[i - 1][j] : Sh[j];
                     const float XY     = i ? (j ? S[i - 1][j - 1] : SL[i - 1]) : (j ? Sh[j - 1] : ShL);
-                    const bool tail    = col >= a.xtail;
+                    const bool tail    = TAIL && col >= a.xtail;
                     float pred;
                     if (NDIM == 2) {
                         pred = __fadd_rn(X, __fsub_rn(Y, XY));  // W + (N - NW)
@@ -407,7 +412,7 @@ __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
 #pragma unroll
         for (int t = 0; t < U; t++) {
             const uint32_t xt = (uint32_t)(u * U + t);
-            load_row<1, VEC>(a, a.x, xt < a.nxt, xt * kTileX + lane * 4, r_f, 0.0, S[t]);
+            load_row<1, VEC, false>(a, a.x, xt < a.nxt, xt * kTileX + lane * 4, r_f, 0.0, S[t]);
         }
 #pragma unroll
         for (int t = 0; t < U; t++) {
@@ -569,8 +574,12 @@ int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_
 
 template <int NDIM, int BS>
 static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
-    if (vec) k_dq_compress_23d<NDIM, BS, true><<<grid, 256, smem, st>>>(a);
-    else k_dq_compress_23d<NDIM, BS, false><<<grid, 256, smem, st>>>(a);
+    // tail columns exist only when d0 % 8 != 0 (and then never with 16-byte rows)
+    const bool tail = (a.d0 % 8) != 0;
+    if (vec && !tail) k_dq_compress_23d<NDIM, BS, true, false><<<grid, 256, smem, st>>>(a);
+    else if (vec) k_dq_compress_23d<NDIM, BS, true, true><<<grid, 256, smem, st>>>(a);
+    else if (!tail) k_dq_compress_23d<NDIM, BS, false, false><<<grid, 256, smem, st>>>(a);
+    else k_dq_compress_23d<NDIM, BS, false, true><<<grid, 256, smem, st>>>(a);
 }
 
 template <int BS>

@@ -90,8 +90,25 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
                         if (lane >= (unsigned)o) incl += t;
                     }
                     (void)lt;
+                    unsigned long long seg_base;
+                    if (a.chunk_off) {
+                        // zeros before this row segment: the chunk's offset plus the zeros between the
+                        // chunk start and the segment start, counted by the warp (at most 511 codes)
+                        const unsigned long long q  = row * a.d0 + (unsigned long long)xs * kDSeg;
+                        const unsigned long long c0 = q & ~511ull;
+                        uint32_t zc = 0;
+                        const unsigned long long lo = c0 + (unsigned long long)lane * 16;
+#pragma unroll
+                        for (int t = 0; t < 16; t++)
+                            if (lo + t < q) zc += (a.codes[lo + t] == 0);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
+                        seg_base = a.chunk_off[q >> 9] + zc;
+                    } else {
+                        seg_base = a.seg_off[row * a.nxs + xs];
+                    }
                     if (zm) {
-                        unsigned long long base = a.seg_off[row * a.nxs + xs] + (incl - cnt);
+                        unsigned long long base = seg_base + (incl - cnt);
 #pragma unroll
                         for (int k = 0; k < 8; k++)
                             if (zm & (1u << k)) {

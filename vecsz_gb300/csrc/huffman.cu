@@ -66,14 +66,95 @@ __device__ inline BuildWs carve_build_ws(uint8_t* p, int dict) {
     return w;
 }
 
+// Heap key layouts: freq in the high bits, node in the low bits.  K32: 32 | 32 (histogram total
+// below 2^32, the usual case: the frequency is the high register, one 32-bit compare); otherwise
+// 44 | 20.  Only the frequency part is ever compared, as in the reference.
+template <bool K32>
+struct HeapKey {
+    static __device__ __forceinline__ unsigned long long fq(unsigned long long k) {
+        return K32 ? (unsigned long long)(uint32_t)(k >> 32) : (k >> kKeyShift);
+    }
+    static __device__ __forceinline__ unsigned long long make(unsigned long long f, uint32_t node) {
+        return K32 ? ((f << 32) | node) : ((f << kKeyShift) | node);
+    }
+    static __device__ __forceinline__ uint32_t node(unsigned long long k) {
+        return K32 ? (uint32_t)k : (uint32_t)(k & kNodeMask);
+    }
+};
+
+// The reference's heap, operation for operation (src/huffman.hh:169-192, 248-262).  Returns the
+// number of nodes created.
+template <bool K32>
+__device__ __forceinline__ int heap_replay(BuildWs& w, int nused, int* fail) {
+    using K  = HeapKey<K32>;
+    int qend = 1;
+    for (int i = 0; i < nused; i++) {  // leaves: qinsert(new_node(freq, i)) in symbol order
+        const unsigned long long key = K::make(w.code[i], (uint32_t)i);
+        const unsigned long long fk  = K::fq(key);
+        int ii = qend++, j;
+        while ((j = ii >> 1)) {
+            const unsigned long long pj = w.heap[j];
+            if (K::fq(pj) <= fk) break;
+            w.heap[ii] = pj;
+            ii         = j;
+        }
+        w.heap[ii] = key;
+    }
+    int nnodes = nused;
+    // merges: new_node(.., qremove(), qremove()) -- the first removal is the RIGHT child
+    while (qend > 2) {
+        unsigned long long rem[2];
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            // qremove: the hole sinks along the smaller child (ties: left) to the bottom, then takes
+            // the last element, without sifting it up.  Children of both candidates are loaded one
+            // level ahead.
+            const unsigned long long top = w.heap[1];
+            qend--;
+            const unsigned long long last = w.heap[qend];
+            int i = 1, l = 2;
+            ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(&w.heap[2]);
+            while (l < qend) {
+                const ulonglong2 ga = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l]);
+                const ulonglong2 gb = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l + 2]);
+                const bool right    = (l + 1 < qend) && (K::fq(pr.y) < K::fq(pr.x));
+                w.heap[i] = right ? pr.y : pr.x;
+                i         = right ? l + 1 : l;
+                l         = 2 * i;
+                pr        = right ? gb : ga;
+            }
+            w.heap[i] = last;
+            rem[r]    = top;
+        }
+        const int k = nnodes - nused;
+        nnodes++;
+        w.rchild[k] = (int32_t)K::node(rem[0]);
+        w.lchild[k] = (int32_t)K::node(rem[1]);
+        const unsigned long long key = K::make(K::fq(rem[0]) + K::fq(rem[1]), (uint32_t)(nused + k));
+        const unsigned long long fk  = K::fq(key);
+        int ii = qend++, j;
+        while ((j = ii >> 1)) {
+            const unsigned long long pj = w.heap[j];
+            if (K::fq(pj) <= fk) break;
+            w.heap[ii] = pj;
+            ii         = j;
+        }
+        w.heap[ii] = key;
+    }
+    (void)fail;
+    return nnodes;
+}
+
+template <bool IN_SMEM>
 __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
     extern __shared__ __align__(16) uint8_t s_build_dyn[];
     __shared__ uint32_t s_info[4];
     __shared__ int s_fail;
     __shared__ uint32_t s_scan[33];
+    __shared__ unsigned long long s_fsum[8];
     if (*a.status != VSZ_OK) return;  // an earlier stage failed (uniform: one CTA)
     const int dict = a.dict;
-    BuildWs w      = carve_build_ws(a.ws_in_smem ? s_build_dyn : reinterpret_cast<uint8_t*>(a.scratch), dict);
+    BuildWs w      = carve_build_ws(IN_SMEM ? s_build_dyn : reinterpret_cast<uint8_t*>(a.scratch), dict);
     if (threadIdx.x == 0) s_fail = 0;
     for (int i = threadIdx.x; i < 2 * dict + 8; i += blockDim.x) w.heap[i] = 0ull;
     for (int i = threadIdx.x; i < dict; i += blockDim.x) {
@@ -84,10 +165,18 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
     const int per = (dict + blockDim.x - 1) / blockDim.x;
     const int s0  = threadIdx.x * per;
     uint32_t cnt  = 0;
+    unsigned long long fsum = 0;
     for (int k = 0; k < per; k++) {
         int sym = s0 + k;
-        if (sym < dict && a.hist[sym] != 0ull) cnt++;
+        if (sym < dict) {
+            unsigned long long f = a.hist[sym];
+            cnt += (f != 0ull);
+            fsum += f;
+        }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fsum += __shfl_xor_sync(0xffffffffu, fsum, o);
+    if ((threadIdx.x & 31) == 0) s_fsum[threadIdx.x >> 5] = fsum;
     uint32_t tot;
     uint32_t off = block_exclusive_scan<uint32_t>(cnt, s_scan, &tot);
     for (int k = 0; k < per; k++) {
@@ -104,63 +193,13 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
     const int nused = (int)tot;
 
     if (threadIdx.x == 0) {
-        int qend = 1;
-        // leaves: qinsert(new_node(freq, i)) in symbol order (src/huffman.hh:169-177)
-        for (int i = 0; i < nused; i++) {
-            unsigned long long f = w.code[i];
-            if (f >= (1ull << (64 - kKeyShift))) s_fail = VSZ_ERR_UNSUPPORTED;
-            unsigned long long key = (f << kKeyShift) | (unsigned long long)i;
-            int ii = qend++, j;
-            while ((j = ii >> 1)) {
-                unsigned long long pj = w.heap[j];
-                if (kfreq(pj) <= kfreq(key)) break;
-                w.heap[ii] = pj;
-                ii         = j;
-            }
-            w.heap[ii] = key;
-        }
-        if (nused == 0) s_fail = VSZ_ERR_INVALID;
+        unsigned long long total = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) total += s_fsum[i];
         int nnodes = nused;
-        // merges (src/huffman.hh:262): the first qremove() is the RIGHT child, the second the LEFT
-        // (the reference build evaluates new_node's arguments right to left)
-        while (!s_fail && qend > 2) {
-            unsigned long long rem[2];
-#pragma unroll
-            for (int r = 0; r < 2; r++) {
-                // qremove (src/huffman.hh:179-192): the hole sinks along the smaller child (ties:
-                // left) to the bottom, then takes the last element -- no sift-up.  The children of
-                // both candidates are loaded one level ahead.
-                const unsigned long long top = w.heap[1];
-                qend--;
-                const unsigned long long last = w.heap[qend];
-                int i = 1, l = 2;
-                ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(&w.heap[2]);
-                while (l < qend) {
-                    ulonglong2 ga = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l]);
-                    ulonglong2 gb = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l + 2]);
-                    const bool right = (l + 1 < qend) && (kfreq(pr.y) < kfreq(pr.x));
-                    w.heap[i] = right ? pr.y : pr.x;
-                    i         = right ? l + 1 : l;
-                    l         = 2 * i;
-                    pr        = right ? gb : ga;
-                }
-                w.heap[i] = last;
-                rem[r]    = top;
-            }
-            const int k = nnodes - nused;
-            nnodes++;
-            w.rchild[k] = (int32_t)(rem[0] & kNodeMask);
-            w.lchild[k] = (int32_t)(rem[1] & kNodeMask);
-            unsigned long long key = ((kfreq(rem[0]) + kfreq(rem[1])) << kKeyShift) | (unsigned long long)(nused + k);
-            int ii = qend++, j;
-            while ((j = ii >> 1)) {
-                unsigned long long pj = w.heap[j];
-                if (kfreq(pj) <= kfreq(key)) break;
-                w.heap[ii] = pj;
-                ii         = j;
-            }
-            w.heap[ii] = key;
-        }
+        if (nused == 0) s_fail = VSZ_ERR_INVALID;
+        else if (total >= (1ull << (64 - kKeyShift))) s_fail = VSZ_ERR_UNSUPPORTED;
+        else if (total < (1ull << 32)) nnodes = heap_replay<true>(w, nused, &s_fail);
+        else nnodes = heap_replay<false>(w, nused, &s_fail);
         uint32_t node_count = 0, max_len = 0;
         if (!s_fail) {
             const int nint = nnodes - nused;
@@ -243,8 +282,16 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
     if (threadIdx.x < 4) a.info[threadIdx.x] = s_info[threadIdx.x];
 }
 
+int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsigned long long* tile_status,
+                    uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st);
+
 // ------------------------------------------------------------------------------------------
-// K3: encoder
+// K3: encoder, two passes over the codes with no cross-tile waiting:
+//   k_huff_count  bits per tile of 4096 codes (and per 512 codes: the decode index)
+//   k_scan_excl   exclusive scan of the tile totals -> each tile's first bit
+//   k_huff_pack   per tile: block scan of thread bit counts, codewords packed into a shared-memory
+//                 word buffer, interior words stored, partial boundary words left to
+//                 k_huff_encode_edges
 // ------------------------------------------------------------------------------------------
 
 constexpr int kEncThreads   = 256;
@@ -252,21 +299,71 @@ constexpr int kEncPerThread = 16;
 constexpr int kEncTile      = kEncThreads * kEncPerThread;  // 4096 codes
 constexpr int kEncMaxWords  = kEncTile * 64 / 32 + 4;       // codes are at most 64 bits
 
-__global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
+__device__ __forceinline__ void load_codes16(const HuffEncodeArgs& a, size_t c0, uint32_t sym[kEncPerThread]) {
+    if (c0 + kEncPerThread <= a.n && a.codes_aligned) {
+        const uint4* p = reinterpret_cast<const uint4*>(a.codes + c0);
+        uint4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+        uint32_t w8[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            sym[2 * k]     = w8[k] & 0xffffu;
+            sym[2 * k + 1] = w8[k] >> 16;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kEncPerThread; k++) sym[k] = (c0 + k < a.n) ? a.codes[c0 + k] : 0xffffffffu;
+    }
+}
+
+__global__ void __launch_bounds__(kEncThreads) k_huff_count(HuffEncodeArgs a) {
+    extern __shared__ uint8_t s_len_dyn[];
+    __shared__ uint32_t s_wsum[kEncThreads / 32];
+    if (*a.status != VSZ_OK) return;
+    if (a.build_info && (a.build_info[2] > 64u || a.build_info[0] == 0u)) {
+        if (threadIdx.x == 0 && blockIdx.x == 0)
+            set_status(a.status, a.build_info[0] ? VSZ_ERR_UNSUPPORTED : VSZ_ERR_INVALID);
+        return;
+    }
+    const uint8_t* cl = a.cb_len;
+    if (a.cb_in_smem) {
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_len_dyn[i] = a.cb_len[i];
+        __syncthreads();
+        cl = s_len_dyn;
+    }
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
+        const size_t c0 = (size_t)tile * kEncTile + (size_t)threadIdx.x * kEncPerThread;
+        uint32_t sym[kEncPerThread];
+        load_codes16(a, c0, sym);
+        uint32_t bits = 0;
+#pragma unroll
+        for (int k = 0; k < kEncPerThread; k++)
+            if (sym[k] != 0xffffffffu) bits += cl[sym[k]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) bits += __shfl_xor_sync(0xffffffffu, bits, o);
+        if (lane == 0) {
+            s_wsum[warp] = bits;
+            size_t chunk = (size_t)tile * (kEncTile / 512) + warp;
+            if (a.chunk_bits && chunk * 512 < a.n) a.chunk_bits[chunk] = (uint16_t)bits;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+#pragma unroll
+            for (int i = 0; i < kEncThreads / 32; i++) t += s_wsum[i];
+            a.tile_bits[tile] = t;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kEncThreads) k_huff_pack(HuffEncodeArgs a) {
     extern __shared__ uint8_t s_dyn[];
-    uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);                     // kEncMaxWords
+    uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);                                     // kEncMaxWords
     unsigned long long* s_cw = reinterpret_cast<unsigned long long*>(s_words + kEncMaxWords);  // dict (if cached)
     uint8_t* s_len = reinterpret_cast<uint8_t*>(s_cw + (a.cb_in_smem ? a.dict : 0));
     __shared__ unsigned long long s_scan[33];
-    __shared__ unsigned long long s_base;
-    __shared__ uint32_t s_tile;
-
     if (*a.status != VSZ_OK) return;  // set before this launch: uniform across the grid
-    if (a.build_info && (a.build_info[2] > 64u || a.build_info[0] == 0u)) {
-        // codewords longer than 64 bits (a tree deeper than any reachable in practice) or no tree
-        if (threadIdx.x == 0 && blockIdx.x == 0) set_status(a.status, a.build_info[0] ? VSZ_ERR_UNSUPPORTED : VSZ_ERR_INVALID);
-        return;
-    }
     const unsigned long long* cw = a.cb_word;
     const uint8_t* cl            = a.cb_len;
     if (a.cb_in_smem) {
@@ -281,64 +378,31 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
     uint8_t* out          = a.out + a.out_off.eval();
     const uint32_t base0  = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
     uint32_t* gw          = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
-    const unsigned lane   = threadIdx.x & 31u;
-    const unsigned warp   = threadIdx.x >> 5;
 
-    while (true) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(a.tile_counter, 1u);
-        __syncthreads();
-        const uint32_t tile = s_tile;
-        if (tile >= a.ntiles) break;
-        // ---- load 16 codes and their lengths
+    for (uint32_t tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
         const size_t c0 = (size_t)tile * kEncTile + (size_t)threadIdx.x * kEncPerThread;
         uint32_t sym[kEncPerThread];
-        if (c0 + kEncPerThread <= a.n && a.codes_aligned) {
-            const uint4* p = reinterpret_cast<const uint4*>(a.codes + c0);
-            uint4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
-            uint32_t w8[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                sym[2 * k]     = w8[k] & 0xffffu;
-                sym[2 * k + 1] = w8[k] >> 16;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < kEncPerThread; k++) sym[k] = (c0 + k < a.n) ? a.codes[c0 + k] : 0xffffffffu;
-        }
+        load_codes16(a, c0, sym);
         uint32_t bits = 0;
 #pragma unroll
         for (int k = 0; k < kEncPerThread; k++)
             if (sym[k] != 0xffffffffu) bits += cl[sym[k]];
-        // ---- per-warp totals feed the decode index (one entry per 512 codes)
-        uint32_t wsum = bits;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
-        if (lane == 0 && a.chunk_bits) {
-            size_t chunk = (size_t)tile * (kEncTile / 512) + warp;
-            if (chunk * 512 < a.n) a.chunk_bits[chunk] = (uint16_t)wsum;
-        }
         unsigned long long tot;
-        unsigned long long toff = block_exclusive_scan<unsigned long long>((unsigned long long)bits, s_scan, &tot);
-        if (threadIdx.x == 0) {
-            s_base = lookback_publish(a.tile_status, tile, tot, a.status);
-            if (tile == a.ntiles - 1) *a.total_bits = s_base + tot;
-        }
-        __syncthreads();
-        const unsigned long long B = s_base;
-        const unsigned long long gstart = base0 + B;  // tile's first bit on the global word grid
+        const unsigned long long toff = block_exclusive_scan<unsigned long long>((unsigned long long)bits, s_scan, &tot);
+        const unsigned long long gstart = base0 + a.tile_off[tile];  // tile's first bit on the word grid
         const uint32_t r0     = (uint32_t)(gstart & 31u);
         const unsigned long long F = gstart >> 5;
         const uint32_t nwords = tot ? (uint32_t)((r0 + tot + 31) >> 5) : 0u;
         for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) s_words[i] = 0u;
         __syncthreads();
-        // ---- pack this thread's codewords into the word buffer; only a thread's first and last
-        // word can be shared with its neighbours, so only those use atomics
+        // pack this thread's codewords; only a thread's first and last word can be shared with its
+        // neighbours, so only those use shared-memory atomics
         {
-            unsigned long long pos = r0 + toff;
-            uint32_t wi   = (uint32_t)(pos >> 5);
-            uint32_t nb   = (uint32_t)(pos & 31u);  // bits already taken in the current word
-            bool first    = true;
-            unsigned long long acc = 0;             // MSB-aligned pending bits of word wi..
+            const unsigned long long pos = r0 + toff;
+            uint32_t wi = (uint32_t)(pos >> 5);
+            uint32_t nb = (uint32_t)(pos & 31u);  // bits already taken in the current word
+            bool first  = true;
+            unsigned long long acc = 0;            // MSB-aligned pending bits of word wi
             auto emit = [&](uint32_t word) {
                 if (first && (pos & 31u)) atomicOr(&s_words[wi], word);
                 else s_words[wi] = word;
@@ -358,8 +422,8 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
 #pragma unroll
             for (int k = 0; k < kEncPerThread; k++) {
                 if (sym[k] == 0xffffffffu) continue;
-                uint32_t len          = cl[sym[k]];
-                unsigned long long v  = cw[sym[k]];
+                const uint32_t len         = cl[sym[k]];
+                const unsigned long long v = cw[sym[k]];
                 if (len > 32) {
                     append(v >> 32, len - 32);
                     append(v & 0xffffffffull, 32);
@@ -370,9 +434,9 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_encode(HuffEncodeArgs a) {
             if (nb > 0) atomicOr(&s_words[wi], (uint32_t)(acc >> 32));
         }
         __syncthreads();
-        // ---- store: words wholly inside the tile are plain stores; a partial first or last word
-        // (shared with the neighbouring tile, or with the tree bytes before the payload) is left to
-        // k_huff_encode_edges, which ORs the two halves -- no tile ever waits on another's store
+        // store: words wholly inside the tile are plain stores; a partial first or last word (shared
+        // with the neighbouring tile, or with the tree bytes before the payload) is left to
+        // k_huff_encode_edges, which ORs the two halves
         const bool first_partial = (r0 != 0);
         const bool last_partial  = ((r0 + tot) & 31ull) != 0;
         for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) {
@@ -635,7 +699,10 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 
 // Indexed decode with coalesced output: a warp decodes 32 consecutive chunks of 512 codewords
 // (one per lane) in rounds of 32 symbols staged in shared memory, then writes each lane's 32
-// symbols (64 contiguous bytes) as 16-byte stores.
+// symbols (64 contiguous bytes) as 16-byte stores.  The index gives every chunk's first bit and
+// length, so the inner loop has no bounds test: a chunk must consume exactly its indexed length
+// (checked at the end), and reads stop 64 bits past it whatever the bits say.  Zero codes are
+// counted per chunk (outlier ranks for the reverse Lorenzo kernel).
 constexpr int kDecRound = 32;
 
 __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
@@ -654,37 +721,81 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
     if (active && out0 < a.n) cnt = (uint32_t)min((unsigned long long)kChunkSyms, a.n - out0);
     const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 3u) * 8u;
     const uint32_t* gw   = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)3);
-    BitReader br;
-    if (cnt) br.init(gw, base0 + a.start_bit[j], base0 + a.payload_bits);
-    unsigned long long row = active ? out0 / a.d0 : 0;
-    uint32_t x             = active ? (uint32_t)(out0 - row * a.d0) : 0u;
-    uint32_t zeros         = 0;
-    auto flush = [&]() {
-        if (zeros && a.seg_zero) atomicAdd(&a.seg_zero[row * a.nxs + (x >> 8)], zeros);
-        zeros = 0;
-    };
     bool bad = false;
+    unsigned long long pos = 0, end = 0;
+    unsigned long long buf = 0;
+    int nbits = 0;
+    if (cnt) {
+        const unsigned long long sb = a.start_bit[j], cb = a.chunk_len[j];
+        if (sb + cb > a.payload_bits) bad = true;
+        pos = base0 + sb;
+        end = pos + cb;
+        if (!bad) {
+            const unsigned long long wi = pos >> 5;
+            const uint32_t off          = (uint32_t)(pos & 31u);
+            buf   = ((((unsigned long long)bswap32(__ldg(&gw[wi]))) << 32) | bswap32(__ldg(&gw[wi + 1]))) << off;
+            nbits = 64 - (int)off;
+        }
+    }
+    uint32_t zeros = 0;
     for (uint32_t r0 = 0; r0 < (uint32_t)kChunkSyms; r0 += kDecRound) {
-        const uint32_t m = (cnt > r0) ? min((uint32_t)kDecRound, cnt - r0) : 0u;
-        for (uint32_t k = 0; k < m && !bad; k++) {
-            uint32_t sy = decode_one(br, s_table, a.child, a.node_sym, a.max_nodes);
-            if (sy == 0xffffffffu) {
-                bad = true;
-                break;
+        const uint32_t m = (cnt > r0 && !bad) ? min((uint32_t)kDecRound, cnt - r0) : 0u;
+        for (uint32_t k = 0; k < m; k++) {
+            if (nbits <= 32) {
+                const unsigned long long nxt = pos + (unsigned long long)nbits;  // word aligned
+                if (nxt > end + 64) {
+                    bad = true;
+                    break;
+                }
+                buf |= ((unsigned long long)bswap32(__ldg(&gw[nxt >> 5]))) << (32 - nbits);
+                nbits += 32;
             }
+            const uint32_t e = s_table[(uint32_t)(buf >> (64 - kDecBits))];
+            uint32_t len     = e & 0xffu;
+            uint32_t sy;
+            if (len) {
+                sy = e >> 8;
+            } else {
+                // codeword longer than the table: walk the tree bit by bit from the table's node,
+                // refilling as it goes (codewords may be up to 64 bits)
+                uint32_t node = e >> 8;
+                sy            = 0xffffffffu;
+                if (node == 0 || node >= a.max_nodes) {
+                    bad = true;
+                    break;
+                }
+                buf <<= kDecBits;
+                nbits -= kDecBits;
+                pos += kDecBits;
+                for (int guard = 0; guard < 64; guard++) {
+                    if (nbits <= 32) {
+                        const unsigned long long nxt = pos + (unsigned long long)nbits;
+                        if (nxt > end + 64) break;
+                        buf |= ((unsigned long long)bswap32(__ldg(&gw[nxt >> 5]))) << (32 - nbits);
+                        nbits += 32;
+                    }
+                    node = __ldg(&a.child[2 * (size_t)node + (uint32_t)(buf >> 63)]);
+                    buf <<= 1;
+                    nbits--;
+                    pos++;
+                    if (node == 0 || node >= a.max_nodes) break;
+                    const uint32_t ns = __ldg(&a.node_sym[node]);
+                    if (ns & 0x80000000u) {
+                        sy = ns & 0xffffu;
+                        break;
+                    }
+                }
+                if (sy == 0xffffffffu) {
+                    bad = true;
+                    break;
+                }
+                len = 0;  // already consumed
+            }
+            buf <<= len;
+            nbits -= (int)len;
+            pos += len;
             s_stage[warp][lane][k] = (uint16_t)sy;
-            zeros += (sy == 0);
-            x++;
-            if (x == a.d0) {
-                x--;
-                flush();
-                x = 0;
-                row++;
-            } else if ((x & 255u) == 0) {
-                x--;
-                flush();
-                x++;
-            }
+            zeros += (sy == 0u);
         }
         __syncwarp();
         // 32 rows x 4 pieces of 8 symbols; piece q*32 + lane
@@ -700,14 +811,15 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
                 if (p0 + 8 <= ms) {
                     *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(&s_stage[warp][src][p0]);
                 } else {
-                    for (uint32_t e = p0; e < ms; e++) dst[e - p0] = s_stage[warp][src][e];
+                    for (uint32_t e2 = p0; e2 < ms; e2++) dst[e2 - p0] = s_stage[warp][src][e2];
                 }
             }
         }
         __syncwarp();
     }
+    if (cnt && !bad && pos != end) bad = true;  // the chunk must fill exactly its indexed length
     if (bad) set_status(a.status, VSZ_ERR_CORRUPT);
-    flush();
+    if (active && a.chunk_zero) a.chunk_zero[j] = zeros;
 }
 
 // Constant fill for a one-symbol tree (src/huffman.hh:348-352).
@@ -840,17 +952,17 @@ __global__ void __launch_bounds__(256) k_scan_excl(const TIn* __restrict__ in, u
 
 int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
     size_t bytes = build_ws_bytes(a.dict);
-    size_t smem  = 0;
     a.ws_in_smem = bytes <= 200 * 1024 ? 1 : 0;
     if (a.ws_in_smem) {
-        smem = bytes;
         static bool attr = false;
         if (!attr) {
-            cudaFuncSetAttribute(k_huff_build, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(k_huff_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             attr = true;
         }
+        k_huff_build<true><<<1, 256, bytes, st>>>(a);
+    } else {
+        k_huff_build<false><<<1, 256, 0, st>>>(a);
     }
-    k_huff_build<<<1, 256, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
@@ -865,13 +977,17 @@ int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
     size_t smem     = kEncMaxWords * 4 + (a.cb_in_smem ? cb_bytes : 0) + 16;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_huff_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024 + 64 * 1024 + 1024);
+        cudaFuncSetAttribute(k_huff_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024 + 64 * 1024 + 1024);
+        cudaFuncSetAttribute(k_huff_count, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024 + 1024);
         attr_set = true;
     }
-    if (cudaMemsetAsync(a.tile_status, 0, 8 * (size_t)a.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
-    if (cudaMemsetAsync(a.tile_counter, 0, 4, st) != cudaSuccess) return VSZ_ERR_CUDA;
-    int grid = (int)min((long long)a.ntiles, (long long)num_sms * 2);
-    k_huff_encode<<<grid, kEncThreads, smem, st>>>(a);
+    int grid = (int)min((long long)a.ntiles, (long long)num_sms * 8);
+    k_huff_count<<<grid, kEncThreads, a.cb_in_smem ? (size_t)a.dict : 0, st>>>(a);
+    int rc = launch_scan_u32(a.tile_bits, a.tile_off, a.ntiles, a.tile_status, a.tile_counter, a.total_bits,
+                             a.status, st);
+    if (rc) return rc;
+    int pgrid = (int)min((long long)a.ntiles, (long long)num_sms * 3);
+    k_huff_pack<<<pgrid, kEncThreads, smem, st>>>(a);
     k_huff_encode_edges<<<(a.ntiles + 255) / 256, 256, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }

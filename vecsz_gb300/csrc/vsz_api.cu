@@ -229,6 +229,8 @@ struct CompressWs {
     uint8_t* cb_len;
     uint32_t* build_info;
     unsigned long long* e_tile_status;
+    uint32_t* e_tile_bits;
+    unsigned long long* e_tile_off;
     unsigned long long* e_edge_idx;
     uint32_t* e_edge_bits;
     uint32_t* e_counter;
@@ -258,6 +260,8 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     w.build_info = b.take<uint32_t>(4);
     size_t et    = (g.n + 4095) / 4096 + 1;
     w.e_tile_status = b.take<unsigned long long>(et);
+    w.e_tile_bits   = b.take<uint32_t>(et);
+    w.e_tile_off    = b.take<unsigned long long>(et);
     w.e_edge_idx  = b.take<unsigned long long>(2 * et);
     w.e_edge_bits = b.take<uint32_t>(2 * et);
     w.e_counter  = b.take<uint32_t>(4);
@@ -286,6 +290,8 @@ struct DecompressWs {
     uint16_t* code;
     uint32_t* seg_zero;
     unsigned long long* seg_off;
+    uint32_t* chunk_zero;
+    unsigned long long* chunk_off;
     unsigned long long* scan_status;
     uint32_t* scan_counter;
     unsigned long long* scan_total;
@@ -318,6 +324,8 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
     size_t nsegd = g.nrows * nxs;
     w.seg_zero = b.take<uint32_t>(nsegd + 1);
     w.seg_off  = b.take<unsigned long long>(nsegd + 1);
+    w.chunk_zero = b.take<uint32_t>(n_index_chunks + 1);
+    w.chunk_off  = b.take<unsigned long long>(n_index_chunks + 1);
     size_t nsync = (payload_bytes * 8 + kSyncBits - 1) / kSyncBits + 1;
     size_t scan_n = nsegd;
     if (n_index_chunks > scan_n) scan_n = n_index_chunks;
@@ -384,6 +392,8 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
                                     w.status, st));
         }
         da.start_bit = w.chunk_start;
+        da.chunk_len = chunk_bits;
+        da.chunk_zero = w.chunk_zero;
         da.out_begin = nullptr;
         da.nsym = nullptr;
         da.nchunks = n_index_chunks;
@@ -545,7 +555,7 @@ vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_code
 
 size_t vsz_huffman_encode_tmp_bytes(size_t n) {
     size_t nt = (n + 4095) / 4096 + 1;
-    return 1024 + 8 * nt + 16 * nt + 8 * nt + 1024;
+    return 2048 + 8 * nt + 4 * nt + 8 * nt + 16 * nt + 8 * nt + 2048;
 }
 
 vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_codebook, int dict_size,
@@ -559,6 +569,8 @@ vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_co
     a.tile_counter = b.take<uint32_t>(4);
     size_t nt      = (n + 4095) / 4096 + 1;
     a.tile_status  = b.take<unsigned long long>(nt);
+    a.tile_bits    = b.take<uint32_t>(nt);
+    a.tile_off     = b.take<unsigned long long>(nt);
     a.edge_idx     = b.take<unsigned long long>(2 * nt);
     a.edge_bits    = b.take<uint32_t>(2 * nt);
     a.codes        = d_code;
@@ -718,6 +730,8 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     he.total_bits = w.total_bits;
     he.chunk_bits = w.chunk_bits;
     he.tile_status = w.e_tile_status;
+    he.tile_bits = w.e_tile_bits;
+    he.tile_off = w.e_tile_off;
     he.edge_idx = w.e_edge_idx;
     he.edge_bits = w.e_edge_bits;
     he.tile_counter = w.e_counter;
@@ -900,11 +914,20 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     VSZ_TRY(launch_eb_setup(VSZ_MODE_ABS, ebf, nullptr, 0, w.consts, w.mm, st, w.status));
     const uint16_t* idx = d->has_trailer ? reinterpret_cast<const uint16_t*>(d_archive + d->index_offset) : nullptr;
     VSZ_TRY(decode_codes(d_archive + d->huff_offset, d->huff_bytes, d->node_count, d->tree_bytes, g.n, dict, idx,
-                         d->has_trailer ? d->n_chunks : 0, d->chunk_syms, w, w.seg_zero, g.d0, st));
+                         d->has_trailer ? d->n_chunks : 0, d->chunk_syms, w, idx ? nullptr : w.seg_zero, g.d0, st));
+    // outlier ranks: per 512-code chunk from the indexed decoder (block size 8), else per 256-wide
+    // row segment
+    const bool chunk_rank = idx != nullptr && bs == 8 && d->node_count > 1;
     {
         StageTimer t(kStZeroScan, st);
-        VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.scan_status, w.scan_counter, w.scan_total, w.status,
-                                st));
+        if (chunk_rank) {
+            VSZ_TRY(launch_scan_u32(w.chunk_zero, w.chunk_off, d->n_chunks, w.scan_status, w.scan_counter,
+                                    w.scan_total, w.status, st));
+        } else {
+            if (idx) VSZ_TRY(launch_count_zeros(w.code, g.d0, g.nrows, w.seg_zero, st, num_sms()));
+            VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.scan_status, w.scan_counter, w.scan_total,
+                                    w.status, st));
+        }
         k_check_zeros<<<1, 1, 0, st>>>(w.scan_total, d->n_outlier, w.status);
     }
     if (d->n_outlier) {
@@ -918,6 +941,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.n_outliers = d->n_outlier;
     a.status = w.status;
     a.seg_off = w.seg_off;
+    a.chunk_off = chunk_rank ? w.chunk_off : nullptr;
     a.consts = w.consts;
     a.out = d_out;
     a.d0 = g.d0;

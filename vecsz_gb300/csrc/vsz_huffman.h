@@ -44,7 +44,9 @@ struct HuffEncodeArgs {
     DevOffset out_off;                // bytes before the payload start are kept
     unsigned long long* total_bits;
     uint16_t* chunk_bits;             // bits per 512 codes (decode index), may be null
-    unsigned long long* tile_status;  // ntiles
+    unsigned long long* tile_status;  // scan scratch (ntiles / 4096 + 1)
+    uint32_t* tile_bits;              // ntiles: bits per tile of 4096 codes
+    unsigned long long* tile_off;     // ntiles: first bit of each tile
     unsigned long long* edge_idx;     // 2 ntiles: word index of a tile's partial first / last word
     uint32_t* edge_bits;              // 2 ntiles: its bits (stored byte order)
     uint32_t* tile_counter;
@@ -75,6 +77,8 @@ struct HuffDecodeArgs {
     const uint32_t* child;
     const uint32_t* node_sym;
     const unsigned long long* start_bit;  // per chunk
+    const uint16_t* chunk_len;            // indexed path: bits of each chunk
+    uint32_t* chunk_zero;                 // indexed path: zero codes per chunk (may be null)
     const unsigned long long* out_begin;  // per chunk, or null: chunk * chunk_syms
     const uint32_t* nsym;                 // per chunk, or null: chunk_syms
     size_t nchunks;

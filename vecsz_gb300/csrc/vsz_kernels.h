@@ -66,7 +66,8 @@ struct DqDecArgs {
     const float* outliers;               // compact outlier values (aligned copy)
     unsigned long long n_outliers;       // entries of `outliers`; a rank past it is VSZ_ERR_CORRUPT
     int* status;
-    const unsigned long long* seg_off;   // exclusive zero-code offsets per 256-wide row segment
+    const unsigned long long* seg_off;   // exclusive zero-code offsets per 256-wide row segment, or
+    const unsigned long long* chunk_off; // exclusive zero-code offsets per 512-code chunk (block 8)
     const Consts* consts;
     float* out;
     uint32_t d0, d1, d2;
