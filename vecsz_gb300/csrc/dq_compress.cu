@@ -20,6 +20,7 @@
 #include <mutex>
 #include <type_traits>
 
+#include "scan.cuh"
 #include "vsz_device.cuh"
 #include "vsz_kernels.h"
 
@@ -454,35 +455,6 @@ constexpr int kGatherThreads = 256;
 constexpr int kGatherPerThread = 16;
 constexpr int kGatherTile = kGatherThreads * kGatherPerThread;  // segments per tile
 
-__device__ unsigned long long lookback(unsigned long long* tile_status, uint32_t tile, unsigned long long agg,
-                                       int* status) {
-    constexpr unsigned long long FA = 1ull << 62, FP = 2ull << 62, VM = (1ull << 62) - 1;
-    if (tile == 0) {
-        st_release_u64(&tile_status[0], FP | agg);
-        return 0;
-    }
-    st_release_u64(&tile_status[tile], FA | agg);
-    unsigned long long excl = 0;
-    long long spins         = 0;
-    int t                   = (int)tile - 1;
-    while (t >= 0) {
-        unsigned long long s = ld_acquire_u64(&tile_status[t]);
-        unsigned long long f = s & (3ull << 62);
-        if (f == 0) {
-            if (++spins > kSpinLimit) {
-                set_status(status, VSZ_ERR_TIMEOUT);
-                break;
-            }
-            continue;
-        }
-        excl += s & VM;
-        if (f == FP) break;
-        t--;
-    }
-    st_release_u64(&tile_status[tile], FP | (excl + agg));
-    return excl;
-}
-
 __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g) {
     if (*g.status != VSZ_OK) return;  // set before this launch, so uniform across the grid
     __shared__ uint32_t s_off[kGatherTile];
@@ -495,11 +467,21 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
     const size_t seg0   = (size_t)tile * kGatherTile + (size_t)threadIdx.x * kGatherPerThread;
     uint32_t cnt[kGatherPerThread];
     uint32_t sum = 0;
+    if (seg0 + kGatherPerThread <= g.nseg && (reinterpret_cast<uintptr_t>(g.seg_count) & 15u) == 0) {
+        const uint4 v = *reinterpret_cast<const uint4*>(g.seg_count + seg0);
+        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int k = 0; k < kGatherPerThread; k++) {
-        size_t s = seg0 + k;
-        cnt[k]   = (s < g.nseg) ? g.seg_count[s] : 0u;
-        sum += cnt[k];
+        for (int k = 0; k < kGatherPerThread; k++) {
+            cnt[k] = (w4[k >> 2] >> (8 * (k & 3))) & 0xffu;
+            sum += cnt[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kGatherPerThread; k++) {
+            size_t s = seg0 + k;
+            cnt[k]   = (s < g.nseg) ? g.seg_count[s] : 0u;
+            sum += cnt[k];
+        }
     }
     // block exclusive scan of per-thread sums
     const unsigned lane = lane_id(), w = threadIdx.x >> 5;
@@ -511,15 +493,20 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
     }
     if (lane == 31) s_warp[w] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
         uint32_t run = 0;
-        for (int i = 0; i < kGatherThreads / 32; i++) {
-            uint32_t v = s_warp[i];
-            s_warp[i]  = run;
-            run += v;
+        for (int i = 0; i < kGatherThreads / 32; i++) run += s_warp[i];
+        const unsigned long long b = lookback_publish_warp(g.tile_status, tile, run, g.status);
+        if (threadIdx.x == 0) {
+            uint32_t r2 = 0;
+            for (int i = 0; i < kGatherThreads / 32; i++) {
+                uint32_t v = s_warp[i];
+                s_warp[i]  = r2;
+                r2 += v;
+            }
+            s_base = b;
+            if (tile == g.ntiles - 1) *g.total = b + run;
         }
-        s_base = lookback(g.tile_status, tile, run, g.status);
-        if (tile == g.ntiles - 1) *g.total = s_base + run;
     }
     __syncthreads();
     uint32_t run = incl - sum + s_warp[w];

@@ -27,15 +27,32 @@ constexpr int kDSeg = 256;  // decompress row segment (one warp of 8-wide blocks
 // 32 consecutive blocks (one 256-wide row segment), so code loads (16 B) and value stores (32 B)
 // of a row are contiguous across the warp.
 // ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    const int n       = valid ? 16 : 0;  // 0: zero-fill without reading
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 template <int NDIM, bool VEC>
-__global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
+__global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
+    // dynamic shared memory (b8_smem_bytes): per warp, two planes of codes [buffer][row][lane] of
+    // 16 bytes (8 codes) filled by cp.async (VEC), then the previous plane of every lane's block
+    // [row][column][lane] (3D; lane-minor, so conflict-free)
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    typedef uint4 CodesT[2][8][32];
+    typedef float PrevT[8][8][32];
+    CodesT* s_codes = reinterpret_cast<CodesT*>(s_dq_dyn);
+    PrevT* s_prev   = reinterpret_cast<PrevT*>(s_dq_dyn + (VEC ? 4 * sizeof(CodesT) : 0));
     const Consts c = *a.consts;
     if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
     const int R           = a.R;
     const unsigned lane   = lane_id();
+    const unsigned wib    = threadIdx.x >> 5;  // warp in block (4 warps)
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const unsigned lt = lanemask_lt();
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + wib;
 
     for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
         const uint32_t xs = (uint32_t)(u % a.nxs);
@@ -46,14 +63,36 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
         const uint32_t y0 = yb * 8, z0 = zb * 8;
         const int ny = (NDIM >= 2) ? (int)min(8u, a.d1 - y0) : 1;
         const int nz = (NDIM == 3) ? (int)min(8u, a.d2 - z0) : 1;
+        const bool col_in = x0 < a.d0;  // VEC: d0 % 8 == 0, so all 8 columns or none
 
-        float P[8][8];
+        auto issue_plane = [&](int zz, int buf) {
 #pragma unroll
-        for (int i = 0; i < 8; i++)
+            for (int y = 0; y < 8; y++) {
+                const bool ok         = col_in && y < ny;
+                const size_t row      = ((size_t)(z0 + zz) * a.d1 + (y0 + (ok ? y : 0)));
+                const uint16_t* gsrc  = a.codes + row * a.d0 + (ok ? x0 : 0);
+                cp_async16(&s_codes[wib][buf][y][lane], gsrc, ok);
+            }
+            cp_async_commit();
+        };
+        if (VEC) issue_plane(0, 0);
+
+        if (NDIM == 3) {
 #pragma unroll
-            for (int k = 0; k < 8; k++) P[i][k] = 0.f;
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int k = 0; k < 8; k++) s_prev[wib][i][k][lane] = 0.f;
+        }
 
         for (int zz = 0; zz < nz; zz++) {
+            if (VEC) {
+                if (zz + 1 < nz) {
+                    issue_plane(zz + 1, (zz + 1) & 1);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+            }
             float Cm[8];
 #pragma unroll
             for (int k = 0; k < 8; k++) Cm[k] = 0.f;
@@ -61,27 +100,26 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
             for (int y = 0; y < 8; y++) {
                 const bool row_in = y < ny;
                 const size_t row  = ((size_t)(z0 + zz) * a.d1 + (y0 + y));
-                // ---- codes of my 8 columns
-                uint32_t cd[8];
-                bool in[8];
-#pragma unroll
-                for (int k = 0; k < 8; k++) in[k] = row_in && (x0 + k < a.d0);
-                const uint16_t* crow = a.codes + row * a.d0;
-                if (VEC && in[0]) {
-                    uint4 v = __ldcs(reinterpret_cast<const uint4*>(crow + x0));
-                    cd[0] = v.x & 0xffffu; cd[1] = v.x >> 16; cd[2] = v.y & 0xffffu; cd[3] = v.y >> 16;
-                    cd[4] = v.z & 0xffffu; cd[5] = v.z >> 16; cd[6] = v.w & 0xffffu; cd[7] = v.w >> 16;
+                // ---- codes of my 8 columns (packed, 2 per word)
+                const bool all_in = row_in && (x0 + 7 < a.d0);
+                uint4 cv;
+                if (VEC) {
+                    cv = s_codes[wib][zz & 1][y][lane];
                 } else {
+                    const uint16_t* crow = a.codes + row * a.d0;
+                    uint32_t t[8];
 #pragma unroll
-                    for (int k = 0; k < 8; k++) cd[k] = in[k] ? (uint32_t)crow[x0 + k] : (uint32_t)R;
+                    for (int k = 0; k < 8; k++) t[k] = (row_in && x0 + k < a.d0) ? (uint32_t)crow[x0 + k] : (uint32_t)R;
+                    cv = make_uint4(t[0] | (t[1] << 16), t[2] | (t[3] << 16), t[4] | (t[5] << 16), t[6] | (t[7] << 16));
                 }
+                const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                auto code_at = [&](int k) -> uint32_t { return (cw[k >> 1] >> (16 * (k & 1))) & 0xffffu; };
+                auto in_at   = [&](int k) -> bool { return all_in || (row_in && x0 + (uint32_t)k < a.d0); };
                 // ---- outliers of this row segment, ranked in row-major order
                 uint32_t zm = 0;
 #pragma unroll
-                for (int k = 0; k < 8; k++) zm |= (in[k] && cd[k] == 0u) ? (1u << k) : 0u;
-                float ov[8];
-#pragma unroll
-                for (int k = 0; k < 8; k++) ov[k] = 0.f;
+                for (int k = 0; k < 8; k++) zm |= (in_at(k) && code_at(k) == 0u) ? (1u << k) : 0u;
+                unsigned long long obase = 0;
                 if (__any_sync(0xffffffffu, zm != 0u)) {
                     uint32_t cnt = __popc(zm), incl = cnt;
 #pragma unroll
@@ -89,7 +127,6 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
                         uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
                         if (lane >= (unsigned)o) incl += t;
                     }
-                    (void)lt;
                     unsigned long long seg_base;
                     if (a.chunk_off) {
                         // zeros before this row segment: the chunk's offset plus the zeros between the
@@ -107,19 +144,12 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
                     } else {
                         seg_base = a.seg_off[row * a.nxs + xs];
                     }
-                    if (zm) {
-                        unsigned long long base = seg_base + (incl - cnt);
-#pragma unroll
-                        for (int k = 0; k < 8; k++)
-                            if (zm & (1u << k)) {
-                                unsigned long long oi = base + __popc(zm & ((1u << k) - 1u));
-                                if (oi < a.n_outliers) ov[k] = a.outliers[oi];
-                                else set_status(a.status, VSZ_ERR_CORRUPT);
-                            }
-                    }
+                    obase = seg_base + (incl - cnt);
                 }
-                // ---- reverse Lorenzo along the row (registers only)
+                // ---- reverse Lorenzo along the row, dequantize, store
                 float C[8];
+                float pZ = 0.f, pYZ = 0.f;
+                float* orow = a.out + row * a.d0;
 #pragma unroll
                 for (int k = 0; k < 8; k++) {
                     float pred;
@@ -131,36 +161,49 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
                         const float XY = (y && k) ? Cm[k - 1] : 0.f;
                         pred           = __fsub_rn(__fadd_rn(Y, X), XY);  // (N + W) - NW
                     } else {
-                        const float XYZ = (y && k) ? P[y - 1][k - 1] : 0.f;
+                        // previous plane: this row (z-1, y) and the row above (z-1, y-1), rolled along x
+                        const float Z   = s_prev[wib][y][k][lane];
+                        const float YZ  = y ? s_prev[wib][y - 1][k][lane] : 0.f;
+                        const float XYZ = (y && k) ? pYZ : 0.f;
+                        const float XZ  = k ? pZ : 0.f;
+                        pZ              = Z;
+                        pYZ             = YZ;
                         const float XY  = (y && k) ? Cm[k - 1] : 0.f;
-                        const float XZ  = k ? P[y][k - 1] : 0.f;
-                        const float YZ  = y ? P[y - 1][k] : 0.f;
                         const float X   = k ? C[k - 1] : 0.f;
                         const float Y   = y ? Cm[k] : 0.f;
-                        const float Z   = P[y][k];
                         pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
                     }
-                    const float delta = (float)((int)cd[k] - R);
-                    float s           = (cd[k] == 0u) ? ov[k] : __fadd_rn(pred, delta);
-                    C[k]              = in[k] ? s : 0.f;
+                    const uint32_t cd = code_at(k);
+                    float s;
+                    if (cd == 0u) {
+                        s = 0.f;
+                        if (zm & (1u << k)) {
+                            const unsigned long long oi = obase + __popc(zm & ((1u << k) - 1u));
+                            if (oi < a.n_outliers) s = a.outliers[oi];
+                            else set_status(a.status, VSZ_ERR_CORRUPT);
+                        }
+                    } else {
+                        s = __fadd_rn(pred, (float)((int)cd - R));
+                    }
+                    C[k] = in_at(k) ? s : 0.f;
                 }
-                // ---- dequantize and store
-                float xo[8];
 #pragma unroll
-                for (int k = 0; k < 8; k++) xo[k] = dequant(C[k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
-                float* orow = a.out + row * a.d0;
-                if (VEC && in[0]) {
-                    __stcs(reinterpret_cast<float4*>(orow + x0), make_float4(xo[0], xo[1], xo[2], xo[3]));
-                    __stcs(reinterpret_cast<float4*>(orow + x0 + 4), make_float4(xo[4], xo[5], xo[6], xo[7]));
-                } else {
+                for (int h = 0; h < 2; h++) {
+                    float xo[4];
 #pragma unroll
-                    for (int k = 0; k < 8; k++)
-                        if (in[k]) orow[x0 + k] = xo[k];
+                    for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                    if (VEC && all_in) {
+                        __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            if (in_at(4 * h + k)) orow[x0 + 4 * h + k] = xo[k];
+                    }
                 }
                 if (NDIM == 3) {
-                    if (y > 0) {
+                    if (y > 0) {  // row y-1 of this plane is no longer needed as "plane z-1"
 #pragma unroll
-                        for (int k = 0; k < 8; k++) P[y - 1][k] = Cm[k];
+                        for (int k = 0; k < 8; k++) s_prev[wib][y - 1][k][lane] = Cm[k];
                     }
                 }
 #pragma unroll
@@ -169,7 +212,7 @@ __global__ void __launch_bounds__(128) k_dq_decompress_b8(DqDecArgs a) {
             }
             if (NDIM == 3) {
 #pragma unroll
-                for (int k = 0; k < 8; k++) P[7][k] = Cm[k];
+                for (int k = 0; k < 8; k++) s_prev[wib][7][k][lane] = Cm[k];
             }
         }
     }
@@ -346,9 +389,14 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
         long long cap  = (long long)num_sms * 16;
         int grid = (int)(want < cap ? want : cap);
         if (grid < 1) grid = 1;
-        if (ndim == 3) vec ? k_dq_decompress_b8<3, true><<<grid, 128, 0, st>>>(a) : k_dq_decompress_b8<3, false><<<grid, 128, 0, st>>>(a);
-        else if (ndim == 2) vec ? k_dq_decompress_b8<2, true><<<grid, 128, 0, st>>>(a) : k_dq_decompress_b8<2, false><<<grid, 128, 0, st>>>(a);
-        else vec ? k_dq_decompress_b8<1, true><<<grid, 128, 0, st>>>(a) : k_dq_decompress_b8<1, false><<<grid, 128, 0, st>>>(a);
+        auto go = [&](auto kern, int nd) {
+            const size_t smem = (vec ? 4 * 2 * 8 * 32 * 16 : 0) + (nd == 3 ? 4 * 8 * 8 * 32 * 4 : 0);
+            if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<grid, 128, smem, st>>>(a);
+        };
+        if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);
+        else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true>, 2) : go(k_dq_decompress_b8<2, false>, 2);
+        else vec ? go(k_dq_decompress_b8<1, true>, 1) : go(k_dq_decompress_b8<1, false>, 1);
         return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
     }
     a.nxs = (a.d0 + kDSeg - 1) / kDSeg;

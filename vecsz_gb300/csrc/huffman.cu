@@ -532,6 +532,7 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
             a.child[2 * (size_t)i]     = l;
             a.child[2 * (size_t)i + 1] = r;
         } else {
+            if (a.walk) a.walk[i] = 0u;
             a.child[2 * (size_t)i]     = 0;
             a.child[2 * (size_t)i + 1] = 0;
         }
@@ -540,6 +541,19 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
     if (s_bad) {
         if (threadIdx.x == 0) set_status(a.status, VSZ_ERR_CORRUPT);
         return;
+    }
+    // packed children for the shared-memory walk: 15-bit fields (dict <= 16384, nc < 32768)
+    if (a.walk && nc < 32768u && a.dict <= 16384) {
+        for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
+            const bool leaf = (a.node_sym[i] & 0x80000000u) != 0;
+            if (leaf) continue;
+            const uint32_t l = a.child[2 * (size_t)i], r = a.child[2 * (size_t)i + 1];
+            auto enc = [&](uint32_t c) -> uint32_t {
+                const uint32_t ns = a.node_sym[c];
+                return (ns & 0x80000000u) ? (0x8000u | (ns & 0x7fffu)) : c;
+            };
+            a.walk[i] = enc(l) | (enc(r) << 16);
+        }
     }
     if (root_leaf) {
         if (threadIdx.x == 0) {
@@ -705,10 +719,14 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 // counted per chunk (outlier ranks for the reverse Lorenzo kernel).
 constexpr int kDecRound = 32;
 
+template <bool WALK_SMEM>
 __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
     __shared__ uint32_t s_table[1 << kDecBits];
     __shared__ __align__(16) uint16_t s_stage[8][32][kDecRound + 8];  // +8: keep rows 16-byte aligned
+    extern __shared__ uint32_t s_walk[];                               // WALK_SMEM: a.nodes entries
     for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    if (WALK_SMEM)
+        for (uint32_t i = threadIdx.x; i < a.nodes; i += blockDim.x) s_walk[i] = a.walk[i];
     __syncthreads();
     if (*a.status != VSZ_OK) return;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -774,15 +792,26 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
                         buf |= ((unsigned long long)bswap32(__ldg(&gw[nxt >> 5]))) << (32 - nbits);
                         nbits += 32;
                     }
-                    node = __ldg(&a.child[2 * (size_t)node + (uint32_t)(buf >> 63)]);
+                    const uint32_t bit = (uint32_t)(buf >> 63);
                     buf <<= 1;
                     nbits--;
                     pos++;
-                    if (node == 0 || node >= a.max_nodes) break;
-                    const uint32_t ns = __ldg(&a.node_sym[node]);
-                    if (ns & 0x80000000u) {
-                        sy = ns & 0xffffu;
-                        break;
+                    if (WALK_SMEM) {
+                        const uint32_t ent = (s_walk[node] >> (16 * bit)) & 0xffffu;
+                        if (ent & 0x8000u) {
+                            sy = ent & 0x7fffu;
+                            break;
+                        }
+                        node = ent;
+                        if (node == 0 || node >= a.nodes) break;
+                    } else {
+                        node = __ldg(&a.child[2 * (size_t)node + bit]);
+                        if (node == 0 || node >= a.max_nodes) break;
+                        const uint32_t ns = __ldg(&a.node_sym[node]);
+                        if (ns & 0x80000000u) {
+                            sy = ns & 0xffffu;
+                            break;
+                        }
                     }
                 }
                 if (sy == 0xffffffffu) {
@@ -933,9 +962,12 @@ __global__ void __launch_bounds__(256) k_scan_excl(const TIn* __restrict__ in, u
     }
     unsigned long long tot;
     unsigned long long ex = block_exclusive_scan<unsigned long long>(sum, s_scan, &tot);
-    if (threadIdx.x == 0) {
-        s_base = lookback_publish(tile_status, tile, tot, status);
-        if ((size_t)(tile + 1) * 256 * PER >= n && total) *total = s_base + tot;
+    if (threadIdx.x < 32) {
+        const unsigned long long b = lookback_publish_warp(tile_status, tile, tot, status);
+        if (threadIdx.x == 0) {
+            s_base = b;
+            if ((size_t)(tile + 1) * 256 * PER >= n && total) *total = b + tot;
+        }
     }
     __syncthreads();
     unsigned long long run = s_base + ex;
@@ -1001,9 +1033,22 @@ int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
     if (a.nchunks == 0) return VSZ_OK;
     int grid = (int)((a.nchunks + 255) / 256);
     const bool indexed = !a.out_begin && !a.nsym && a.chunk_syms == (uint32_t)kChunkSyms &&
-                         (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0;
-    if (indexed) k_huff_decode_idx<<<grid, 256, 0, st>>>(a);
-    else k_huff_decode<<<grid, 256, 0, st>>>(a);
+                         (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0 && a.chunk_len;
+    if (indexed) {
+        if (a.walk_smem) {
+            size_t smem = (size_t)a.nodes * 4;
+            static bool attr = false;
+            if (!attr) {
+                cudaFuncSetAttribute(k_huff_decode_idx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 140 * 1024);
+                attr = true;
+            }
+            k_huff_decode_idx<true><<<grid, 256, smem, st>>>(a);
+        } else {
+            k_huff_decode_idx<false><<<grid, 256, 0, st>>>(a);
+        }
+    } else {
+        k_huff_decode<<<grid, 256, 0, st>>>(a);
+    }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 

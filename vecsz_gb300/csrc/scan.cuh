@@ -42,6 +42,47 @@ __device__ __forceinline__ unsigned long long lookback_publish(unsigned long lon
     return excl;
 }
 
+// Warp-parallel variant: called by all 32 lanes of ONE warp of the tile.  Each step inspects the
+// 32 nearest predecessors at once and stops at the nearest one that published its inclusive
+// prefix, so the walk is short even when many predecessors only published aggregates.
+// Returns the exclusive prefix in every lane.
+__device__ __forceinline__ unsigned long long lookback_publish_warp(unsigned long long* tile_status, uint32_t tile,
+                                                                    unsigned long long agg, int* status) {
+    const unsigned lane = threadIdx.x & 31u;
+    if (tile == 0) {
+        if (lane == 0) st_release_u64(&tile_status[0], kFlagPre | agg);
+        return 0;
+    }
+    if (lane == 0) st_release_u64(&tile_status[tile], kFlagAgg | agg);
+    unsigned long long excl = 0;
+    long long base          = (long long)tile - 1;
+    long long spins         = 0;
+    while (true) {
+        const long long idx   = base - (long long)lane;
+        unsigned long long sv = (idx >= 0) ? ld_acquire_u64(&tile_status[idx]) : kFlagPre;  // before tile 0: 0
+        const unsigned long long f = sv & (3ull << 62);
+        const unsigned pmask = __ballot_sync(0xffffffffu, f == kFlagPre);
+        const unsigned zmask = __ballot_sync(0xffffffffu, f == 0);
+        const int first_p    = pmask ? (__ffs(pmask) - 1) : 32;
+        const unsigned need  = (first_p >= 31) ? 0xffffffffu : ((2u << first_p) - 1u);
+        if (zmask & need) {
+            if (++spins > kSpinLimit) {  // a predecessor never published: give up, report
+                if (lane == 0) set_status(status, VSZ_ERR_TIMEOUT);
+                break;
+            }
+            continue;
+        }
+        unsigned long long v = ((int)lane <= first_p) ? (sv & kValMask) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        excl += v;
+        if (first_p < 32) break;
+        base -= 32;
+    }
+    if (lane == 0) st_release_u64(&tile_status[tile], kFlagPre | (excl + agg));
+    return excl;
+}
+
 // Block-wide exclusive scan of one value per thread (blockDim.x <= 1024, multiple of 32).
 // Returns the exclusive prefix; *total receives the block sum.  Uses `warp_sums` (33 entries).
 template <typename T>

@@ -286,6 +286,7 @@ struct DecompressWs {
     uint32_t* child;
     uint32_t* node_sym;
     uint32_t* parent;
+    uint32_t* walk;
     uint32_t* tinfo;
     uint16_t* code;
     uint32_t* seg_zero;
@@ -318,6 +319,7 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
     w.child    = b.take<uint32_t>(2 * (size_t)maxn);
     w.node_sym = b.take<uint32_t>(maxn);
     w.parent   = b.take<uint32_t>(maxn);
+    w.walk     = b.take<uint32_t>(maxn);
     w.tinfo    = b.take<uint32_t>(4);
     w.code     = b.take<uint16_t>(g.n + 8);
     uint32_t nxs = (g.d0 + 255) / 256;
@@ -362,6 +364,7 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     ta.child = w.child;
     ta.node_sym = w.node_sym;
     ta.parent = w.parent;
+    ta.walk = w.walk;
     ta.info = w.tinfo;
     ta.status = w.status;
     {
@@ -384,6 +387,9 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     da.d0 = d0;
     da.nxs = nxs;
     da.max_nodes = (uint32_t)(2 * dict - 1);
+    da.walk = w.walk;
+    da.nodes = node_count;
+    da.walk_smem = (dict <= 16384 && node_count < 32768u) ? 1 : 0;
     da.status = w.status;
     if (chunk_bits) {
         {

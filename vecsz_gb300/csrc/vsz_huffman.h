@@ -66,6 +66,8 @@ struct HuffTableArgs {
     uint32_t* child;      // 2 * max_nodes
     uint32_t* node_sym;   // max_nodes: 0x80000000 | symbol for leaves
     uint32_t* parent;     // max_nodes (scratch)
+    uint32_t* walk;       // max_nodes: both children of an internal node, 16 bits each:
+                          // 0x8000 | symbol for a leaf, else the node index (dict <= 16384)
     uint32_t* info;       // [0] single-symbol tree flag [1] its symbol
     int* status;
 };
@@ -76,6 +78,9 @@ struct HuffDecodeArgs {
     const uint32_t* table;
     const uint32_t* child;
     const uint32_t* node_sym;
+    const uint32_t* walk;                 // packed children (k_huff_table), when walk_smem
+    int walk_smem;                        // 1: dict <= 16384, the walk array is copied to shared memory
+    uint32_t nodes;                       // node count of the tree
     const unsigned long long* start_bit;  // per chunk
     const uint16_t* chunk_len;            // indexed path: bits of each chunk
     uint32_t* chunk_zero;                 // indexed path: zero codes per chunk (may be null)
