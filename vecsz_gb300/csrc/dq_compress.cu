@@ -458,6 +458,7 @@ constexpr int kGatherTile = kGatherThreads * kGatherPerThread;  // segments per 
 __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g) {
     if (*g.status != VSZ_OK) return;  // set before this launch, so uniform across the grid
     __shared__ uint32_t s_off[kGatherTile];
+    __shared__ uint8_t s_cnt[kGatherTile];
     __shared__ uint32_t s_warp[kGatherThreads / 32];
     __shared__ unsigned long long s_base;
     __shared__ uint32_t s_tile;
@@ -513,17 +514,24 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
 #pragma unroll
     for (int k = 0; k < kGatherPerThread; k++) {
         s_off[threadIdx.x * kGatherPerThread + k] = run;
+        s_cnt[threadIdx.x * kGatherPerThread + k] = (uint8_t)cnt[k];
         run += cnt[k];
     }
     __syncthreads();
     const unsigned long long base = s_base;
     uint8_t* out_bytes = g.out_bytes ? g.out_bytes + g.out_off.eval() : nullptr;
-    // warp-cooperative copies, one segment at a time
-    for (int k = w; k < kGatherTile; k += kGatherThreads / 32) {
-        size_t s = (size_t)tile * kGatherTile + k;
-        if (s >= g.nseg) break;
-        uint32_t n = g.seg_count[s];
-        if (n == 0) continue;
+    // warp-cooperative copies of the non-empty segments: each warp scans 32 segment counts at a
+    // time from shared memory and visits only those with outliers
+    const size_t tseg0 = (size_t)tile * kGatherTile;
+    for (int k0 = w * 32; k0 < kGatherTile; k0 += kGatherThreads) {
+        const int kk = k0 + (int)lane;
+        const bool has = (tseg0 + kk < g.nseg) && s_cnt[kk] != 0;
+        unsigned nz = __ballot_sync(0xffffffffu, has);
+        while (nz) {
+        const int k = k0 + __ffs(nz) - 1;
+        nz &= nz - 1;
+        const size_t s = tseg0 + k;
+        const uint32_t n = s_cnt[k];
         const float* src          = g.scratch + s * kSegX;
         unsigned long long dst0   = base + s_off[k];
         for (uint32_t i = lane; i < n; i += 32) {
@@ -538,6 +546,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
                 d[2]       = (uint8_t)(b >> 16);
                 d[3]       = (uint8_t)(b >> 24);
             }
+        }
         }
     }
 }
