@@ -155,6 +155,25 @@ size_t vsz_huffman_build_tmp_bytes(int dict_size);
 vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_codebook, uint8_t* d_huff_head,
                              uint32_t* d_info, void* d_tmp, size_t tmp_bytes, void* stream);
 
+/* The same codebook and tree built on the calling host thread from a host histogram (host
+ * pointers only): what vsz_compress runs inside its stream-ordered host step.  h_codebook:
+ * [cb_word dict x u64][cb_len dict x u8]; h_huff_head: vsz_huff_head_max(dict) bytes.  Returns
+ * VSZ_ERR_INVALID when no symbol occurs.  No counterpart in the reference (whose build is host
+ * code inside Compress, src/vecsz_interface.hh:121-123). */
+vsz_status vsz_huffman_build_host(const uint64_t* h_hist, int dict_size, void* h_codebook, uint8_t* h_huff_head,
+                                  uint32_t h_info[4]);
+
+/* Where vsz_compress builds the Huffman tree.  VSZ_TREE_HOST (the default): the histogram is
+ * copied to pinned host memory, a host function enqueued on the same stream builds the tree, and
+ * async copies bring the codebook and tree back -- stream-ordered, no synchronisation of the
+ * calling thread.  Streams under graph capture always use the device builder.  VSZ_TREE_DEVICE: the
+ * one-CTA device builder (vsz_huffman_build).  The environment variable VSZ_TREE_BUILD=device
+ * selects the device builder at load.  Process-wide; returns the previous setting (a negative
+ * argument only queries). */
+#define VSZ_TREE_DEVICE 1
+#define VSZ_TREE_HOST 2
+int vsz_set_tree_builder(int which);
+
 /* Bit packing of codes with a codebook: the payload of HuffmanEncode (src/huffman.hh:268-341),
  * MSB-first codewords, ceil(bits / 8) bytes, written at d_payload (any alignment; the bytes of its
  * first 32-bit word before d_payload are preserved; 4 writable bytes past the end are needed).

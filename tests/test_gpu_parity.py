@@ -186,3 +186,49 @@ def test_zero_range_r2r_is_an_error(cuda):
     with pytest.raises(V.VszError) as e:
         V.compress(x, (1000,), 1e-3, "r2r", 1024, 8)
     assert e.value.status == 7
+
+
+@pytest.fixture
+def device_tree_builder():
+    from vecsz_gb300 import _lib as L
+    prev = L.lib().vsz_set_tree_builder(L.TREE_DEVICE)
+    yield
+    L.lib().vsz_set_tree_builder(prev)
+
+
+@pytest.mark.parametrize("seed", range(0, 24, 3))
+def test_device_tree_builder_matches_oracle(cuda, device_tree_builder, seed):
+    """vsz_compress with the one-CTA device tree builder (the host builder is the default)."""
+    dims, bs, dct, eb, r2r, x = _random_case(seed)
+    if r2r and O.value_range(x) == 0:
+        r2r = False
+    a_or, meta = O.compress(x, dims, bs, dct, eb, r2r)
+    c = V.compress(x, dims, eb, "r2r" if r2r else "abs", dct, bs)
+    assert c.data[: c.data_size] == a_or and c.n_outlier == meta["n_outlier"]
+
+
+def test_compress_replayed_from_cuda_graph(cuda):
+    """vsz_compress captured in a CUDA graph (the device tree builder is used under capture) and
+    replayed on new input matches the oracle for that input."""
+    torch = cuda
+    dims = (64, 48, 40)
+    xa = fields.grf_3d(40, 48, 64, seed=21).ravel()
+    xb = (fields.grf_3d(40, 48, 64, seed=22).ravel() * 3.0).astype(np.float32)
+    codec = V.DeviceCodec(dims, eb=1e-4, mode="r2r", dict_size=1024, block_size=8)
+    xd = dev(cuda, xa)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        codec.compress(xd)  # eager first call: one-time kernel attributes are set outside capture
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        codec.compress(xd)
+    for x in (xb, xa):
+        xd.copy_(torch.from_numpy(x))
+        g.replay()
+        torch.cuda.synchronize()
+        a_or, meta = O.compress(x, dims, 8, 1024, 1e-4, True)
+        r = codec.result_host()
+        assert r.data_size == len(a_or) and r.n_outlier == meta["n_outlier"]
+        assert codec.archive_bytes()[: r.data_size] == a_or

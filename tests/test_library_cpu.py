@@ -124,3 +124,69 @@ def test_lossless_roundtrip(which):
                                        C.byref(bl)) == 0
     assert C.string_at(back.value, bl.value) == a.tobytes()
     lib.vsz_free_host(back)
+
+
+def _host_build(hist, dict_size):
+    hist = np.ascontiguousarray(hist, np.uint64)
+    cb = np.zeros(9 * dict_size, np.uint8)
+    head = np.zeros(V.lib().vsz_huff_head_max(dict_size), np.uint8)
+    info = np.zeros(4, np.uint32)
+    rc = V.lib().vsz_huffman_build_host(hist.ctypes.data, dict_size, cb.ctypes.data, head.ctypes.data,
+                                        info.ctypes.data)
+    return rc, cb[:8 * dict_size].view(np.uint64), cb[8 * dict_size:], head, info
+
+
+def _hist_cases():
+    rng = np.random.default_rng(11)
+    yield "zipf", 1024, np.minimum(rng.zipf(1.3, 1024), 5000).astype(np.uint64) * (rng.random(1024) < 0.7)
+    yield "ties", 256, np.full(256, 7, np.uint64)                     # every comparison a tie
+    yield "two_level_ties", 512, np.where(np.arange(512) % 3 == 0, 4, 2).astype(np.uint64)
+    yield "single", 1024, np.eye(1, 1024, 513, dtype=np.uint64)[0] * 99
+    yield "pair", 2, np.array([5, 1], np.uint64)
+    yield "wide_w2", 4096, rng.integers(0, 40, 4096).astype(np.uint64)        # 256 < nodes <= 65536
+    yield "wide_w4", 65536, rng.integers(1, 3, 65536).astype(np.uint64)       # nodes > 65536: 4-byte indices
+    yield "peaked", 1024, np.concatenate([np.zeros(500), [3, 90, 100000, 80, 2], np.zeros(519)]).astype(np.uint64)
+
+
+@pytest.mark.parametrize("case", list(_hist_cases()), ids=lambda c: c[0])
+def test_host_tree_build_matches_oracle(case):
+    """The host tree builder used inside vsz_compress gives the reference's tree and codebook."""
+    _, dict_size, hist = case
+    rc, words, lens, head, info = _host_build(hist, dict_size)
+    assert rc == L.VSZ_OK
+    o_lens, o_w0, _, o_nc = O.huffman_codebook(hist, dict_size)
+    np.testing.assert_array_equal(lens, o_lens)
+    assert int(info[0]) == o_nc and int(info[2]) == int(o_lens.max())
+    short = (o_lens > 0) & (o_lens <= 64)
+    want = o_w0[short] >> (64 - o_lens[short].astype(np.uint64))
+    np.testing.assert_array_equal(words[short], want)
+    # serialised tree: the oracle's encode_withTree section head for codes with this histogram
+    codes = np.repeat(np.arange(dict_size, dtype=np.int32), hist.astype(np.int64))
+    sec = np.frombuffer(O.huffman_encode(codes, dict_size), np.uint8)
+    n_head = 8 + int(info[1])
+    assert head[:n_head].tobytes() == sec[:n_head].tobytes()
+
+
+def test_host_tree_build_deep_and_empty():
+    # Fibonacci frequencies give a path-shaped tree with codes longer than 64 bits: lengths and
+    # node count still match; the encoder refuses max length > 64 (info[2])
+    fib = [1, 1]
+    while len(fib) < 90:
+        fib.append(fib[-1] + fib[-2])
+    hist = np.zeros(128, np.uint64)
+    hist[:90] = np.array(fib, np.uint64)
+    rc, _, lens, _, info = _host_build(hist, 128)
+    o_lens, _, _, o_nc = O.huffman_codebook(hist, 128)
+    assert rc == L.VSZ_OK and int(info[0]) == o_nc and int(info[2]) > 64
+    np.testing.assert_array_equal(lens, o_lens)
+    rc, *_ , info = _host_build(np.zeros(64, np.uint64), 64)
+    assert rc == L.VSZ_ERR_INVALID and not info.any()
+
+
+def test_tree_builder_switch():
+    lib = V.lib()
+    prev = lib.vsz_set_tree_builder(-1)
+    assert prev in (L.TREE_DEVICE, L.TREE_HOST)
+    assert lib.vsz_set_tree_builder(L.TREE_DEVICE) == prev
+    assert lib.vsz_set_tree_builder(-1) == L.TREE_DEVICE
+    lib.vsz_set_tree_builder(prev)

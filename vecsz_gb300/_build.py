@@ -1,6 +1,6 @@
-"""Builds libvecsz_gb300.so (every CUDA translation unit of vecsz_gb300/csrc) for sm_103a.
+"""Builds libvecsz_gb300.so (every translation unit of vecsz_gb300/csrc) for sm_103a.
 
-nvcc compiles the .cu files in parallel into vecsz_gb300/_build/, then links the shared library
+nvcc compiles the .cu and .cpp files in parallel into vecsz_gb300/_build/, then links the shared library
 into vecsz_gb300/_lib/.  Rebuilds only when a source or header is newer than the library.
 """
 from __future__ import annotations
@@ -41,7 +41,8 @@ def cuda_lib_dir(nv: str) -> str:
 
 
 def sources() -> list[str]:
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    # .cu: device code and the C ABI; .cpp: host-only code (nvcc hands it to the host compiler)
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _stale() -> bool:
@@ -61,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(OBJ, os.path.basename(src).replace(".cu", ".o"))
+        obj = os.path.join(OBJ, os.path.splitext(os.path.basename(src))[0] + ".o")
         cmd = [nv, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -22,6 +22,9 @@ VSZ_ERR_NO_DEVICE = 9
 
 MODE_ABS = 0
 MODE_R2R = 1
+
+TREE_DEVICE = 1
+TREE_HOST = 2
 LOSSLESS_NONE = 0
 LOSSLESS_ZSTD = 1
 LOSSLESS_GZIP = 2
@@ -77,6 +80,8 @@ _PROTOS = {
     "vsz_huff_head_max": ([_i], _sz),
     "vsz_huffman_build_tmp_bytes": ([_i], _sz),
     "vsz_huffman_build": ([_p, _i, _p, _p, _p, _p, _sz, _p], _i),
+    "vsz_huffman_build_host": ([_p, _i, _p, _p, _p], _i),
+    "vsz_set_tree_builder": ([_i], _i),
     "vsz_huffman_encode_tmp_bytes": ([_sz], _sz),
     "vsz_huffman_encode": ([_p, _sz, _p, _i, _p, _p, _p, _p, _sz, _p], _i),
     "vsz_huffman_decode_tmp_bytes": ([_sz, _sz, _i], _sz),

@@ -558,8 +558,10 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
 int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_consts, uint32_t* d_mm,
                     cudaStream_t st, int* status_word) {
     if (mode == VSZ_MODE_R2R) {
-        uint32_t init[2] = {0u, 0xffffffffu};
-        if (cudaMemcpyAsync(d_mm, init, sizeof(init), cudaMemcpyHostToDevice, st) != cudaSuccess) return VSZ_ERR_CUDA;
+        // {0, 0xffffffff} by memsets: a copy from a host array would, under stream capture, bake
+        // that host address into the graph
+        if (cudaMemsetAsync(d_mm, 0, 4, st) != cudaSuccess || cudaMemsetAsync(d_mm + 1, 0xff, 4, st) != cudaSuccess)
+            return VSZ_ERR_CUDA;
         size_t nb = (n + 1023) / 1024; int blocks = (int)(nb < (size_t)(152 * 8) ? nb : (size_t)(152 * 8));
         if (blocks < 1) blocks = 1;
         k_minmax<<<blocks, 256, 0, st>>>(d_in, n, d_mm);

@@ -365,11 +365,8 @@ static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
         k_dq_decompress_gen<1, BS><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(a);
     } else {
         size_t smem = (size_t)G * 2 * BS * BS * sizeof(float);
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_dq_decompress_gen<NDIM, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            attr = true;
-        }
+        static std::atomic<unsigned long long> attr{0};
+        smem_limit_once(k_dq_decompress_gen<NDIM, BS>, (int)smem, attr);
         unsigned grid = (unsigned)((a.nunits + G - 1) / G);
         k_dq_decompress_gen<NDIM, BS><<<grid, G * BS, smem, st>>>(a);
     }
@@ -389,9 +386,10 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
         long long cap  = (long long)num_sms * 16;
         int grid = (int)(want < cap ? want : cap);
         if (grid < 1) grid = 1;
+        static std::atomic<unsigned long long> attr[6];
         auto go = [&](auto kern, int nd) {
             const size_t smem = (vec ? 4 * 2 * 8 * 32 * 16 : 0) + (nd == 3 ? 4 * 8 * 8 * 32 * 4 : 0);
-            if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[(nd - 1) * 2 + (vec ? 1 : 0)]);
             kern<<<grid, 128, smem, st>>>(a);
         };
         if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);

@@ -30,7 +30,7 @@ __device__ __forceinline__ unsigned long long kfreq(unsigned long long k) { retu
 
 // Working set of the tree build (shared memory when it fits, else the global scratch).
 struct BuildWs {
-    unsigned long long* heap;  // 4 dict + 16 (room for speculative reads below the heap end)
+    unsigned long long* heap;  // 2 dict + 8 (room for speculative reads below the heap end)
     uint32_t* used;            // dict: symbol of leaf i
     int32_t* lchild;           // dict: children of internal node k (node nused + k)
     int32_t* rchild;
@@ -40,17 +40,16 @@ struct BuildWs {
     uint32_t* depth;           // 2 dict
 };
 
-// heap: 4 dict + 16 entries, so reads two levels below the last element stay inside it
 __host__ __device__ inline size_t build_ws_bytes(int dict) {
     size_t d = (size_t)dict;
-    return 8 * (4 * d + 16) + 4 * d + 8 * d + 4 * 2 * d * 2 + 8 * 2 * d + 4 * 2 * d + 256;
+    return 8 * (2 * d + 8) + 4 * d + 8 * d + 4 * 2 * d * 2 + 8 * 2 * d + 4 * 2 * d + 256;
 }
 
 __device__ inline BuildWs carve_build_ws(uint8_t* p, int dict) {
     size_t d = (size_t)dict;
     BuildWs w;
     w.heap   = reinterpret_cast<unsigned long long*>(p);
-    p += 8 * (4 * d + 16);
+    p += 8 * (2 * d + 8);
     w.code   = reinterpret_cast<unsigned long long*>(p);
     p += 8 * 2 * d;
     w.used   = reinterpret_cast<uint32_t*>(p);
@@ -113,24 +112,16 @@ __device__ __forceinline__ int heap_replay(BuildWs& w, int nused, int* fail) {
             const unsigned long long top = w.heap[1];
             qend--;
             const unsigned long long last = w.heap[qend];
-            // two levels ahead: pr = children of the hole, ga/gb = children of either child,
-            // then the four grandchild pairs are fetched while this level's compare resolves
             int i = 1, l = 2;
             ulonglong2 pr = *reinterpret_cast<const ulonglong2*>(&w.heap[2]);
-            ulonglong2 ga = *reinterpret_cast<const ulonglong2*>(&w.heap[4]);
-            ulonglong2 gb = *reinterpret_cast<const ulonglong2*>(&w.heap[6]);
             while (l < qend) {
-                const ulonglong2 g0 = *reinterpret_cast<const ulonglong2*>(&w.heap[4 * l]);
-                const ulonglong2 g1 = *reinterpret_cast<const ulonglong2*>(&w.heap[4 * l + 2]);
-                const ulonglong2 g2 = *reinterpret_cast<const ulonglong2*>(&w.heap[4 * l + 4]);
-                const ulonglong2 g3 = *reinterpret_cast<const ulonglong2*>(&w.heap[4 * l + 6]);
+                const ulonglong2 ga = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l]);
+                const ulonglong2 gb = *reinterpret_cast<const ulonglong2*>(&w.heap[2 * l + 2]);
                 const bool right    = (l + 1 < qend) && (K::fq(pr.y) < K::fq(pr.x));
                 w.heap[i] = right ? pr.y : pr.x;
                 i         = right ? l + 1 : l;
                 l         = 2 * i;
                 pr        = right ? gb : ga;
-                ga        = right ? g2 : g0;
-                gb        = right ? g3 : g1;
             }
             w.heap[i] = last;
             rem[r]    = top;
@@ -165,7 +156,7 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
     const int dict = a.dict;
     BuildWs w      = carve_build_ws(IN_SMEM ? s_build_dyn : reinterpret_cast<uint8_t*>(a.scratch), dict);
     if (threadIdx.x == 0) s_fail = 0;
-    for (int i = threadIdx.x; i < 4 * dict + 16; i += blockDim.x) w.heap[i] = 0ull;
+    for (int i = threadIdx.x; i < 2 * dict + 8; i += blockDim.x) w.heap[i] = 0ull;
     for (int i = threadIdx.x; i < dict; i += blockDim.x) {
         a.cb_word[i] = 0ull;
         a.cb_len[i]  = 0;
@@ -991,15 +982,16 @@ __global__ void __launch_bounds__(256) k_scan_excl(const TIn* __restrict__ in, u
 // launchers
 // ------------------------------------------------------------------------------------------
 
+void huff_build_prepare() {
+    static std::atomic<unsigned long long> attr{0};
+    smem_limit_once(k_huff_build<true>, 220 * 1024, attr);
+}
+
 int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
     size_t bytes = build_ws_bytes(a.dict);
     a.ws_in_smem = bytes <= 220 * 1024 ? 1 : 0;
     if (a.ws_in_smem) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_huff_build<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-            attr = true;
-        }
+        huff_build_prepare();
         k_huff_build<true><<<1, 256, bytes, st>>>(a);
     } else {
         k_huff_build<false><<<1, 256, 0, st>>>(a);
@@ -1016,12 +1008,9 @@ int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
     size_t cb_bytes = (size_t)a.dict * 9;
     a.cb_in_smem    = cb_bytes <= 64 * 1024 ? 1 : 0;
     size_t smem     = kEncMaxWords * 4 + (a.cb_in_smem ? cb_bytes : 0) + 16;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_huff_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024 + 64 * 1024 + 1024);
-        cudaFuncSetAttribute(k_huff_count, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024 + 1024);
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_pack{0}, attr_count{0};
+    smem_limit_once(k_huff_pack, 48 * 1024 + 64 * 1024 + 1024, attr_pack);
+    smem_limit_once(k_huff_count, 64 * 1024 + 1024, attr_count);
     int grid = (int)min((long long)a.ntiles, (long long)num_sms * 8);
     k_huff_count<<<grid, kEncThreads, a.cb_in_smem ? (size_t)a.dict : 0, st>>>(a);
     int rc = launch_scan_u32(a.tile_bits, a.tile_off, a.ntiles, a.tile_status, a.tile_counter, a.total_bits,
@@ -1046,11 +1035,8 @@ int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
     if (indexed) {
         if (a.walk_smem) {
             size_t smem = (size_t)a.nodes * 4;
-            static bool attr = false;
-            if (!attr) {
-                cudaFuncSetAttribute(k_huff_decode_idx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 140 * 1024);
-                attr = true;
-            }
+            static std::atomic<unsigned long long> attr{0};
+            smem_limit_once(k_huff_decode_idx<true>, 140 * 1024, attr);
             k_huff_decode_idx<true><<<grid, 256, smem, st>>>(a);
         } else {
             k_huff_decode_idx<false><<<grid, 256, 0, st>>>(a);

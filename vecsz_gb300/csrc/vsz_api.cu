@@ -1,11 +1,14 @@
 // C ABI of the library (include/vecsz_gb300.h): argument checks, workspace layout and the
 // stream-ordered compress / decompress pipelines built from the kernels in dq_*.cu and huffman.cu.
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
+#include "host_tree.h"
 #include "vsz_device.cuh"
 #include "vsz_huffman.h"
 #include "vsz_kernels.h"
@@ -225,6 +228,7 @@ struct CompressWs {
     uint32_t* g_counter;
     unsigned long long* n_out;
     uint8_t* build_scratch;
+    uint8_t* cb_block;
     unsigned long long* cb_word;
     uint8_t* cb_len;
     uint32_t* build_info;
@@ -239,6 +243,10 @@ struct CompressWs {
     size_t n_chunks;
     size_t bytes;
 };
+
+inline size_t codebook_block_bytes(int dict) { return 9 * (size_t)dict + 16; }
+// [BE nc][BE dict] + the largest serialised tree a dictionary can give
+inline size_t tree_head_max(int dict) { return 8 + tree_bytes_size((uint32_t)(2 * dict - 1)); }
 
 CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t cap) {
     Bump b{base, cap};
@@ -255,9 +263,13 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     w.g_counter = b.take<uint32_t>(4);
     w.n_out     = b.take<unsigned long long>(1);
     w.build_scratch = b.take<uint8_t>(huff_build_scratch_bytes(dict));
-    w.cb_word    = b.take<unsigned long long>(dict);
-    w.cb_len     = b.take<uint8_t>(dict);
-    w.build_info = b.take<uint32_t>(4);
+    // codebook block [cb_word dict x u64][info 4 x u32][cb_len dict x u8]: one copy from the host
+    // tree builder's staging fills it
+    uint8_t* cb  = b.take<uint8_t>(codebook_block_bytes(dict));
+    w.cb_block   = cb;
+    w.cb_word    = reinterpret_cast<unsigned long long*>(cb);
+    w.build_info = cb ? reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict) : nullptr;
+    w.cb_len     = cb ? cb + 8 * (size_t)dict + 16 : nullptr;
     size_t et    = (g.n + 4095) / 4096 + 1;
     w.e_tile_status = b.take<unsigned long long>(et);
     w.e_tile_bits   = b.take<uint32_t>(et);
@@ -450,6 +462,116 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     return launch_huff_decode(da, st);
 }
 
+// ---- Huffman tree on the host, stream-ordered ---------------------------------------------------
+// The tree build replays the reference's binary heap one operation at a time: ~20k dependent,
+// branchy steps on a few KB for a 1024-symbol dictionary.  One GPU thread runs that chain at
+// shared-memory latency; a host core runs it from L1, several times faster.  The step stays in
+// stream order: the histogram comes down by an async copy, a host function on the stream builds
+// the tree into pinned staging, and two async copies put the codebook into the workspace and the
+// serialised tree into the archive.  Nothing returns to the caller's thread and nothing
+// synchronises.  Under stream capture (a CUDA graph) the device builder k_huff_build is used.
+
+std::atomic<int> g_tree_builder{-1};
+
+int tree_builder() {
+    int v = g_tree_builder.load(std::memory_order_relaxed);
+    if (v < 0) {
+        v               = VSZ_TREE_HOST;
+        const char* env = getenv("VSZ_TREE_BUILD");
+        if (env && !strcmp(env, "device")) v = VSZ_TREE_DEVICE;
+        g_tree_builder.store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
+// One pinned staging area: [hist dict x u64][codebook block][tree head].  A slot is reused once the
+// event recorded after its last upload has completed.
+struct TreeSlot {
+    int device    = -1;
+    int dict_cap  = 0;
+    int dict      = 0;
+    bool reserved = false;
+    uint8_t* pinned = nullptr;
+    cudaEvent_t done = nullptr;
+    size_t hist_off = 0, cb_off = 0, head_off = 0;
+};
+
+std::mutex g_slot_mu;
+std::vector<TreeSlot*> g_slots;
+
+void host_tree_callback(void* p) {
+    TreeSlot* s    = static_cast<TreeSlot*>(p);
+    const int dict = s->dict;
+    uint8_t* cb    = s->pinned + s->cb_off;
+    host_huffman_build(reinterpret_cast<const uint64_t*>(s->pinned + s->hist_off), dict,
+                       reinterpret_cast<uint64_t*>(cb), cb + 8 * (size_t)dict + 16,
+                       reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict), s->pinned + s->head_off);
+}
+
+TreeSlot* acquire_tree_slot(int dict) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> g(g_slot_mu);
+    for (TreeSlot* s : g_slots) {
+        if (s->reserved || s->device != dev || s->dict_cap < dict) continue;
+        if (cudaEventQuery(s->done) != cudaSuccess) continue;  // an upload from it is still queued
+        s->reserved = true;
+        return s;
+    }
+    TreeSlot* s   = new TreeSlot();
+    s->device     = dev;
+    s->dict_cap   = dict;
+    s->hist_off   = 0;
+    s->cb_off     = (8 * (size_t)dict + 255) & ~(size_t)255;
+    s->head_off   = (s->cb_off + codebook_block_bytes(dict) + 255) & ~(size_t)255;
+    size_t bytes  = s->head_off + tree_head_max(dict);
+    if (cudaHostAlloc(reinterpret_cast<void**>(&s->pinned), bytes, cudaHostAllocDefault) != cudaSuccess) {
+        delete s;
+        return nullptr;
+    }
+    if (cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaFreeHost(s->pinned);
+        delete s;
+        return nullptr;
+    }
+    s->reserved = true;
+    g_slots.push_back(s);
+    return s;
+}
+
+void release_tree_slot(TreeSlot* s) {
+    std::lock_guard<std::mutex> g(g_slot_mu);
+    s->reserved = false;
+}
+
+// Enqueue the host build: hist (device) -> codebook block (device workspace) and
+// [BE nc][BE dict][tree] at huff_out (device archive; up to tree_head_max(dict) bytes are written,
+// the bytes past the tree are overwritten by the encoder that follows).
+int enqueue_host_tree(const unsigned long long* hist, int dict, uint8_t* cb_block, uint8_t* huff_out,
+                      cudaStream_t st) {
+    TreeSlot* s = acquire_tree_slot(dict);
+    if (!s) return VSZ_ERR_CUDA;
+    s->dict = dict;
+    int rc  = VSZ_OK;
+    if (cudaMemcpyAsync(s->pinned + s->hist_off, hist, 8 * (size_t)dict, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaLaunchHostFunc(st, host_tree_callback, s) != cudaSuccess ||
+        cudaMemcpyAsync(cb_block, s->pinned + s->cb_off, codebook_block_bytes(dict), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(huff_out, s->pinned + s->head_off, tree_head_max(dict), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess)
+        rc = VSZ_ERR_CUDA;
+    // recorded even after a failed enqueue, so the slot is not reused while anything queued reads it
+    if (cudaEventRecord(s->done, st) != cudaSuccess) rc = VSZ_ERR_CUDA;
+    release_tree_slot(s);
+    return rc;
+}
+
+bool stream_capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return true;
+    return cs != cudaStreamCaptureStatusNone;
+}
+
 }  // namespace
 
 // =================================================================================================
@@ -541,6 +663,21 @@ vsz_status vsz_outlier_gather(int ndim, const size_t dims[3], const uint8_t* d_s
 size_t vsz_codebook_bytes(int dict_size) { return (size_t)dict_size * 9 + 64; }
 size_t vsz_huff_head_max(int dict_size) { return 8 + tree_bytes_size((uint32_t)(2 * dict_size - 1)); }
 size_t vsz_huffman_build_tmp_bytes(int dict_size) { return huff_build_scratch_bytes(dict_size) + 512; }
+
+vsz_status vsz_huffman_build_host(const uint64_t* h_hist, int dict_size, void* h_codebook, uint8_t* h_huff_head,
+                                  uint32_t h_info[4]) {
+    if (!valid_dict(dict_size) || !h_hist || !h_codebook || !h_huff_head || !h_info) return VSZ_ERR_INVALID;
+    uint8_t* cb = static_cast<uint8_t*>(h_codebook);
+    int rc = host_huffman_build(h_hist, dict_size, reinterpret_cast<uint64_t*>(cb), cb + 8 * (size_t)dict_size,
+                                h_info, h_huff_head);
+    return rc ? VSZ_ERR_INVALID : VSZ_OK;
+}
+
+int vsz_set_tree_builder(int which) {
+    int prev = tree_builder();
+    if (which == VSZ_TREE_DEVICE || which == VSZ_TREE_HOST) g_tree_builder.store(which);
+    return prev;
+}
 
 vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_codebook, uint8_t* d_huff_head,
                              uint32_t* d_info, void* d_tmp, size_t tmp_bytes, void* stream) {
@@ -722,7 +859,11 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     hb.status = w.status;
     {
         StageTimer t(kStHuffBuild, st);
-        VSZ_TRY(launch_huff_build(hb, st));
+        if (tree_builder() == VSZ_TREE_HOST && !stream_capturing(st)) {
+            huff_build_prepare();  // a later captured call takes the device builder
+            VSZ_TRY(enqueue_host_tree(w.hist, dict, w.cb_block, d_archive + hdr, st));
+        } else
+            VSZ_TRY(launch_huff_build(hb, st));
     }
     // 4. bitstream, placed after the tree bytes (an offset only the device knows)
     HuffEncodeArgs he{};

@@ -6,6 +6,7 @@
 // no contraction or reassociation can change a single bit of a quant code or a reconstruction.
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -22,6 +23,19 @@ constexpr int kSegX = kTileX;
 // Bounded spin for every cross-CTA wait (decoupled look-back): after this many polls the kernel
 // records VSZ_ERR_TIMEOUT in the status word and gives up instead of hanging the GPU.
 constexpr long long kSpinLimit = 1ll << 22;
+
+// Raises a kernel's dynamic shared-memory limit on the current device once per (kernel, device):
+// the attribute is per device, and the host call stays out of later launches.  The bit is set
+// only after the attribute is, so a racing thread at worst sets it twice.
+template <class K>
+inline void smem_limit_once(K kern, int bytes, std::atomic<unsigned long long>& done) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done.fetch_or(bit, std::memory_order_release);
+}
 
 // ------------------------------------------------------------------------------------------
 // Constants derived from the error bound, resident in device memory so that r2r fields can

@@ -112,6 +112,7 @@ struct HuffSyncArgs {
 };
 
 int launch_huff_build(HuffBuildArgs a, cudaStream_t st);
+void huff_build_prepare();  // one-time kernel attributes of launch_huff_build (call outside capture)
 size_t huff_build_scratch_bytes(int dict);
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms);
 int launch_huff_table(HuffTableArgs a, cudaStream_t st);

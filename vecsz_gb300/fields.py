@@ -48,7 +48,7 @@ def _grf_spectrum_np(shape, rng, slope=-11.0 / 6.0):
 
 def grf_3d(nz: int, ny: int, nx: int, seed: int = 0, decades: float = 4.0) -> np.ndarray:
     rng = np.random.default_rng(seed)
-    g = np.fft.irfftn(_grf_spectrum_np((nz, ny, nx), rng), s=(nz, ny, nx))
+    g = np.fft.irfftn(_grf_spectrum_np((nz, ny, nx), rng), s=(nz, ny, nx), axes=(0, 1, 2))
     g = (g - g.mean()) / g.std()
     a = decades * math.log(10.0) / (g.max() - g.min())
     return np.exp(a * g).astype(np.float32)
