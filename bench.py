@@ -49,8 +49,6 @@ WORKLOAD_DESC = {
     "cesm": "1800x3600 f32 sum of 64 Gaussian bumps (CESM-like), abs eb 1e-4, dict 1024, block 8",
     "adversarial": "256x384x384 f32 GRF + 5% Cauchy spikes + 8 steps, abs eb 1e-6, dict 1024, block 8",
 }
-# kernels this library launches per step (compress 7, decompress 8 with the indexed decoder)
-LAUNCHES_PER_STEP = 15
 
 
 def parse_args():
@@ -63,6 +61,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-stage-profile", action="store_true",
+                    help="no per-stage CUDA events in the timed loop (no roofline / stages)")
     return ap.parse_args()
 
 
@@ -235,12 +235,13 @@ def run_ours(args):
     clocks.start()
     time.sleep(0.6)
     L.lib().vsz_profile_reset()
-    L.lib().vsz_profile_enable(1)
+    L.lib().vsz_profile_enable(0 if args.no_stage_profile else 1)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
+    launches0 = L.lib().vsz_launch_count()
     t_wall0 = time.time()
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
@@ -255,6 +256,7 @@ def run_ours(args):
     stream.synchronize()
     torch.cuda.synchronize()
     t_wall1 = time.time()
+    launches = L.lib().vsz_launch_count() - launches0
     if world > 1:
         dist.barrier()
     L.lib().vsz_profile_enable(0)
@@ -311,7 +313,7 @@ def run_ours(args):
         "archive_bytes": int(res.data_size), "index_trailer_bytes": int(res.trailer_size),
         "n_outlier": int(res.n_outlier), "verified_error_bound": verified,
         "roofline": roof, "stages": stages,
-        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+        "gpu_launches": int(launches),
         "clocks": clocks.summary(t_wall0, t_wall1),
     }
     if not args.no_e2e:

@@ -266,6 +266,10 @@ void vsz_profile_enable(int on);
 void vsz_profile_reset(void);
 int vsz_profile_read(double* ms, int* counts, const char** names, int max_stages);
 
+/* Kernels this library has launched in this process, all entry points and devices together (a
+ * relaxed atomic count taken at each launch).  No counterpart in the reference. */
+uint64_t vsz_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -232,3 +232,27 @@ def test_compress_replayed_from_cuda_graph(cuda):
         r = codec.result_host()
         assert r.data_size == len(a_or) and r.n_outlier == meta["n_outlier"]
         assert codec.archive_bytes()[: r.data_size] == a_or
+
+
+def test_long_codewords_match_oracle(cuda):
+    """Codewords past the 12-bit primary table: 13..20 bits resolve through the secondary
+    table, longer ones walk the tree.  1D field with 2 eb = 1 whose Lorenzo differences d have
+    P(|d| = k) ~ 2^-k, so code lengths reach the mid 20s; archive, indexed decode and
+    self-synchronising decode all checked against the oracle."""
+    rng = np.random.default_rng(77)
+    n = 1 << 22
+    k = np.minimum(rng.geometric(0.5, n) - 1, 40)
+    d = k * rng.choice(np.array([-1, 1]), n)
+    s = np.cumsum(d).astype(np.int64)
+    s -= int(np.round(s.mean()))
+    x = np.clip(s, -30000, 30000).astype(np.float32)
+    a_or, meta = O.compress(x, (n,), 8, 65536, 0.5, False)
+    lens, *_ = O.huffman_codebook(np.bincount(O.dualquant(x, (n,), 8, 65536, 0.5)[0], minlength=65536).astype(np.uint64),
+                                  65536)
+    assert lens.max() > 20  # both the secondary table and the walk are exercised
+    c = V.compress(x, (n,), 0.5, "abs", 65536, 8)
+    assert c.data[: c.data_size] == a_or
+    y_or = O.decompress(a_or, 8, 65536)
+    np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y_or.view(np.uint32))  # indexed
+    y = V.decompress(a_or, len(a_or), 0, 65536, 8)                                          # self-sync
+    np.testing.assert_array_equal(y.view(np.uint32), y_or.view(np.uint32))

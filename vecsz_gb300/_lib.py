@@ -82,6 +82,7 @@ _PROTOS = {
     "vsz_huffman_build": ([_p, _i, _p, _p, _p, _p, _sz, _p], _i),
     "vsz_huffman_build_host": ([_p, _i, _p, _p, _p], _i),
     "vsz_set_tree_builder": ([_i], _i),
+    "vsz_launch_count": ([], C.c_uint64),
     "vsz_huffman_encode_tmp_bytes": ([_sz], _sz),
     "vsz_huffman_encode": ([_p, _sz, _p, _i, _p, _p, _p, _p, _sz, _p], _i),
     "vsz_huffman_decode_tmp_bytes": ([_sz, _sz, _i], _sz),

@@ -565,8 +565,10 @@ int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_
         size_t nb = (n + 1023) / 1024; int blocks = (int)(nb < (size_t)(152 * 8) ? nb : (size_t)(152 * 8));
         if (blocks < 1) blocks = 1;
         k_minmax<<<blocks, 256, 0, st>>>(d_in, n, d_mm);
+        count_launch();
     }
     k_consts<<<1, 32, 0, st>>>(mode, eb, d_mm, d_in, d_consts, status_word);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
@@ -578,12 +580,14 @@ static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStr
     else if (vec) k_dq_compress_23d<NDIM, BS, true, true><<<grid, 256, smem, st>>>(a);
     else if (!tail) k_dq_compress_23d<NDIM, BS, false, false><<<grid, 256, smem, st>>>(a);
     else k_dq_compress_23d<NDIM, BS, false, true><<<grid, 256, smem, st>>>(a);
+    count_launch();
 }
 
 template <int BS>
 static void launch_1d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
     if (vec) k_dq_compress_1d<BS, true><<<grid, 256, smem, st>>>(a);
     else k_dq_compress_1d<BS, false><<<grid, 256, smem, st>>>(a);
+    count_launch();
 }
 
 template <int NDIM>
@@ -628,6 +632,7 @@ int launch_outlier_gather(GatherArgs g, cudaStream_t st) {
     if (cudaMemsetAsync(g.tile_status, 0, sizeof(unsigned long long) * g.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
     if (cudaMemsetAsync(g.tile_counter, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
     k_outlier_gather<<<g.ntiles, kGatherThreads, 0, st>>>(g);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 

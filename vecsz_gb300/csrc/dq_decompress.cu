@@ -23,32 +23,28 @@ constexpr int kDSeg = 256;  // decompress row segment (one warp of 8-wide blocks
 
 // ------------------------------------------------------------------------------------------
 // Fast path, block size 8: one lane reconstructs one whole Lorenzo block (8 x by 8 y, plane by
-// plane in z) in registers -- the x, y and z recurrences never leave the thread.  A warp covers
-// 32 consecutive blocks (one 256-wide row segment), so code loads (16 B) and value stores (32 B)
-// of a row are contiguous across the warp.
+// plane in z) -- the x, y and z recurrences never leave the thread.  A warp covers 32 consecutive
+// blocks (one 256-wide row segment), so code loads (16 B) and value stores (32 B) of a row are
+// contiguous across the warp.  Codes are prefetched one row ahead into registers; the previous
+// plane of every lane's block lives in shared memory [row][column][lane] (lane-minor, so
+// conflict-free).  Rows are processed in a rolled loop (8 columns unrolled): the body stays small
+// enough for the instruction cache (two rows per iteration measured fastest).
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
-    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
-    const int n       = valid ? 16 : 0;  // 0: zero-fill without reading
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(n) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Any zero 16-bit half in a word (exact: a borrow out of the low half needs the low half zero).
+__device__ __forceinline__ uint32_t zero_halves(uint32_t w) { return (w - 0x00010001u) & ~w & 0x80008000u; }
 
 template <int NDIM, bool VEC>
 __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
-    // dynamic shared memory (b8_smem_bytes): per warp, two planes of codes [buffer][row][lane] of
-    // 16 bytes (8 codes) filled by cp.async (VEC), then the previous plane of every lane's block
-    // [row][column][lane] (3D; lane-minor, so conflict-free)
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
-    typedef uint4 CodesT[2][8][32];
     typedef float PrevT[8][8][32];
-    CodesT* s_codes = reinterpret_cast<CodesT*>(s_dq_dyn);
-    PrevT* s_prev   = reinterpret_cast<PrevT*>(s_dq_dyn + (VEC ? 4 * sizeof(CodesT) : 0));
+    PrevT* s_prev  = reinterpret_cast<PrevT*>(s_dq_dyn);  // 3D only
     const Consts c = *a.consts;
     if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
     const int R           = a.R;
+    // (float)(code - R) exactly: 2^23 + code as float bits, minus 2^23 + R (both exact, R < 2^16)
+    const float rbias     = 8388608.0f + (float)R;
+    const uint32_t rpair  = (uint32_t)R | ((uint32_t)R << 16);
     const unsigned lane   = lane_id();
     const unsigned wib    = threadIdx.x >> 5;  // warp in block (4 warps)
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
@@ -65,17 +61,14 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
         const int nz = (NDIM == 3) ? (int)min(8u, a.d2 - z0) : 1;
         const bool col_in = x0 < a.d0;  // VEC: d0 % 8 == 0, so all 8 columns or none
 
-        auto issue_plane = [&](int zz, int buf) {
-#pragma unroll
-            for (int y = 0; y < 8; y++) {
-                const bool ok         = col_in && y < ny;
-                const size_t row      = ((size_t)(z0 + zz) * a.d1 + (y0 + (ok ? y : 0)));
-                const uint16_t* gsrc  = a.codes + row * a.d0 + (ok ? x0 : 0);
-                cp_async16(&s_codes[wib][buf][y][lane], gsrc, ok);
-            }
-            cp_async_commit();
+        // VEC: the 8 codes of this lane's columns in one 16-byte load; rows outside the field
+        // read as R (no zero codes, so they never enter the outlier path)
+        auto load_row = [&](int zz, int y) -> uint4 {
+            if (!(col_in && y < ny && zz < nz)) return make_uint4(rpair, rpair, rpair, rpair);
+            const size_t row = (size_t)(z0 + zz) * a.d1 + (y0 + y);
+            return __ldcs(reinterpret_cast<const uint4*>(a.codes + row * a.d0 + x0));
         };
-        if (VEC) issue_plane(0, 0);
+        uint4 cv_next = VEC ? load_row(0, 0) : make_uint4(0u, 0u, 0u, 0u);
 
         if (NDIM == 3) {
 #pragma unroll
@@ -85,26 +78,18 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
         }
 
         for (int zz = 0; zz < nz; zz++) {
-            if (VEC) {
-                if (zz + 1 < nz) {
-                    issue_plane(zz + 1, (zz + 1) & 1);
-                    cp_async_wait<1>();
-                } else {
-                    cp_async_wait<0>();
-                }
-            }
-            float Cm[8];
+            float Cm[8];  // row y - 1 of this plane (zeros above the block)
 #pragma unroll
             for (int k = 0; k < 8; k++) Cm[k] = 0.f;
-#pragma unroll
+#pragma unroll 2
             for (int y = 0; y < 8; y++) {
                 const bool row_in = y < ny;
                 const size_t row  = ((size_t)(z0 + zz) * a.d1 + (y0 + y));
-                // ---- codes of my 8 columns (packed, 2 per word)
                 const bool all_in = row_in && (x0 + 7 < a.d0);
                 uint4 cv;
                 if (VEC) {
-                    cv = s_codes[wib][zz & 1][y][lane];
+                    cv      = cv_next;
+                    cv_next = (y < 7) ? load_row(zz, y + 1) : load_row(zz + 1, 0);
                 } else {
                     const uint16_t* crow = a.codes + row * a.d0;
                     uint32_t t[8];
@@ -117,8 +102,10 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                 auto in_at   = [&](int k) -> bool { return all_in || (row_in && x0 + (uint32_t)k < a.d0); };
                 // ---- outliers of this row segment, ranked in row-major order
                 uint32_t zm = 0;
+                if (zero_halves(cv.x) | zero_halves(cv.y) | zero_halves(cv.z) | zero_halves(cv.w)) {
 #pragma unroll
-                for (int k = 0; k < 8; k++) zm |= (in_at(k) && code_at(k) == 0u) ? (1u << k) : 0u;
+                    for (int k = 0; k < 8; k++) zm |= (in_at(k) && code_at(k) == 0u) ? (1u << k) : 0u;
+                }
                 unsigned long long obase = 0;
                 if (__any_sync(0xffffffffu, zm != 0u)) {
                     uint32_t cnt = __popc(zm), incl = cnt;
@@ -146,47 +133,50 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                     }
                     obase = seg_base + (incl - cnt);
                 }
-                // ---- reverse Lorenzo along the row, dequantize, store
+                // ---- reverse Lorenzo along the row; an element with code 0 takes its outlier
                 float C[8];
-                float pZ = 0.f, pYZ = 0.f;
-                float* orow = a.out + row * a.d0;
+                auto row_pass = [&](auto with_outliers) {
+                    float pZ = 0.f, pYZ = 0.f;
+                    const int ym1 = y ? y - 1 : 0;
 #pragma unroll
-                for (int k = 0; k < 8; k++) {
-                    float pred;
-                    if (NDIM == 1) {
-                        pred = k ? C[k - 1] : 0.f;
-                    } else if (NDIM == 2) {
-                        const float X  = k ? C[k - 1] : 0.f;
-                        const float Y  = y ? Cm[k] : 0.f;
-                        const float XY = (y && k) ? Cm[k - 1] : 0.f;
-                        pred           = __fsub_rn(__fadd_rn(Y, X), XY);  // (N + W) - NW
-                    } else {
-                        // previous plane: this row (z-1, y) and the row above (z-1, y-1), rolled along x
-                        const float Z   = s_prev[wib][y][k][lane];
-                        const float YZ  = y ? s_prev[wib][y - 1][k][lane] : 0.f;
-                        const float XYZ = (y && k) ? pYZ : 0.f;
-                        const float XZ  = k ? pZ : 0.f;
-                        pZ              = Z;
-                        pYZ             = YZ;
-                        const float XY  = (y && k) ? Cm[k - 1] : 0.f;
-                        const float X   = k ? C[k - 1] : 0.f;
-                        const float Y   = y ? Cm[k] : 0.f;
-                        pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
-                    }
-                    const uint32_t cd = code_at(k);
-                    float s;
-                    if (cd == 0u) {
-                        s = 0.f;
-                        if (zm & (1u << k)) {
-                            const unsigned long long oi = obase + __popc(zm & ((1u << k) - 1u));
-                            if (oi < a.n_outliers) s = a.outliers[oi];
-                            else set_status(a.status, VSZ_ERR_CORRUPT);
+                    for (int k = 0; k < 8; k++) {
+                        float pred;
+                        if (NDIM == 1) {
+                            pred = k ? C[k - 1] : 0.f;
+                        } else if (NDIM == 2) {
+                            const float X  = k ? C[k - 1] : 0.f;
+                            const float XY = k ? Cm[k - 1] : 0.f;
+                            pred           = __fsub_rn(__fadd_rn(Cm[k], X), XY);  // (N + W) - NW
+                        } else {
+                            // previous plane: this row (z-1, y) and the row above (z-1, y-1), rolled along x
+                            const float Z   = s_prev[wib][y][k][lane];
+                            const float yz  = s_prev[wib][ym1][k][lane];
+                            const float YZ  = y ? yz : 0.f;
+                            const float XYZ = k ? pYZ : 0.f;
+                            const float XZ  = k ? pZ : 0.f;
+                            pZ              = Z;
+                            pYZ             = YZ;
+                            const float XY  = k ? Cm[k - 1] : 0.f;
+                            const float X   = k ? C[k - 1] : 0.f;
+                            pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Cm[k]),
+                                             Z);
                         }
-                    } else {
-                        s = __fadd_rn(pred, (float)((int)cd - R));
+                        const uint32_t cd = code_at(k);
+                        float s = __fadd_rn(pred, __fsub_rn(__uint_as_float(0x4B000000u | cd), rbias));
+                        if (decltype(with_outliers)::value) {
+                            if (zm & (1u << k)) {
+                                const unsigned long long oi = obase + __popc(zm & ((1u << k) - 1u));
+                                s = 0.f;
+                                if (oi < a.n_outliers) s = a.outliers[oi];
+                                else set_status(a.status, VSZ_ERR_CORRUPT);
+                            }
+                        }
+                        C[k] = in_at(k) ? s : 0.f;
                     }
-                    C[k] = in_at(k) ? s : 0.f;
-                }
+                };
+                if (zm) row_pass(std::true_type{});
+                else row_pass(std::false_type{});
+                float* orow = a.out + row * a.d0;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     float xo[4];
@@ -200,11 +190,9 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                             if (in_at(4 * h + k)) orow[x0 + 4 * h + k] = xo[k];
                     }
                 }
-                if (NDIM == 3) {
-                    if (y > 0) {  // row y-1 of this plane is no longer needed as "plane z-1"
+                if (NDIM == 3 && y > 0) {  // row y-1 of this plane is no longer needed as "plane z-1"
 #pragma unroll
-                        for (int k = 0; k < 8; k++) s_prev[wib][y - 1][k][lane] = Cm[k];
-                    }
+                    for (int k = 0; k < 8; k++) s_prev[wib][y - 1][k][lane] = Cm[k];
                 }
 #pragma unroll
                 for (int k = 0; k < 8; k++) Cm[k] = C[k];
@@ -354,6 +342,7 @@ int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_
     long long want = (long long)((nseg + 7) / 8), cap = (long long)num_sms * 16;
     int grid = (int)(want < cap ? want : cap);
     k_count_zeros<<<grid, 256, 0, st>>>(codes, d0, nrows, nxs, seg_zero);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
@@ -363,12 +352,14 @@ static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
     if (NDIM == 1) {
         size_t nblk = (a.d0 + BS - 1) / BS;
         k_dq_decompress_gen<1, BS><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(a);
+        count_launch();
     } else {
         size_t smem = (size_t)G * 2 * BS * BS * sizeof(float);
         static std::atomic<unsigned long long> attr{0};
         smem_limit_once(k_dq_decompress_gen<NDIM, BS>, (int)smem, attr);
         unsigned grid = (unsigned)((a.nunits + G - 1) / G);
         k_dq_decompress_gen<NDIM, BS><<<grid, G * BS, smem, st>>>(a);
+        count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
@@ -388,9 +379,10 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
         if (grid < 1) grid = 1;
         static std::atomic<unsigned long long> attr[6];
         auto go = [&](auto kern, int nd) {
-            const size_t smem = (vec ? 4 * 2 * 8 * 32 * 16 : 0) + (nd == 3 ? 4 * 8 * 8 * 32 * 4 : 0);
+            const size_t smem = (nd == 3) ? 4 * 8 * 8 * 32 * 4 : 0;  // previous plane per warp
             if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[(nd - 1) * 2 + (vec ? 1 : 0)]);
             kern<<<grid, 128, smem, st>>>(a);
+            count_launch();
         };
         if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);
         else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true>, 2) : go(k_dq_decompress_b8<2, false>, 2);

@@ -490,6 +490,8 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
     const uint8_t* h = a.huff;
     __shared__ uint32_t s_nc;
     __shared__ int s_bad;
+    __shared__ uint32_t s_w2[1 << kDecBits];  // secondary table width per primary prefix
+    __shared__ uint32_t s_scan[33];
     if (threadIdx.x == 0) {
         s_nc  = ((uint32_t)h[0] << 24) | ((uint32_t)h[1] << 16) | ((uint32_t)h[2] << 8) | (uint32_t)h[3];
         s_bad = 0;
@@ -562,26 +564,27 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
         }
         return;
     }
-    // depth and code of every node by walking up to the root (depth bounded by nc)
-    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
-        uint32_t depth = 0, cur = i;
-        unsigned long long code = 0;
-        bool ok = true;
+    // depth and code of every node by walking up to the root (depth bounded by 64)
+    auto depth_code = [&](uint32_t i, uint32_t& depth, unsigned long long& code) -> bool {
+        uint32_t cur = i;
+        depth        = 0;
+        code         = 0;
         while (cur != 0) {
-            uint32_t p = parent[cur];
-            if (p == 0xffffffffu || depth >= 64) {
-                ok = false;
-                break;
-            }
+            const uint32_t p = parent[cur];
+            if (p == 0xffffffffu || depth >= 64) return false;  // unreachable, or longer than 64 bits
             code |= (unsigned long long)(p & 1u) << depth;
             depth++;
             cur = p >> 1;
         }
-        if (!ok) {
-            // unreachable node or a code longer than 64 bits: only the walk can reach it
-            if (depth >= 64 && parent[i] != 0xffffffffu) continue;
-            continue;
-        }
+        return true;
+    };
+    // pass 1: primary entries; width of the secondary table below every depth-kDecBits prefix
+    for (uint32_t i = threadIdx.x; i < (1u << kDecBits); i += blockDim.x) s_w2[i] = 0u;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
+        uint32_t depth;
+        unsigned long long code;
+        if (!depth_code(i, depth, code)) continue;  // only the walk can reach it
         bool leaf = (a.node_sym[i] & 0x80000000u) != 0;
         if (leaf && depth >= 1 && depth <= (uint32_t)kDecBits) {
             uint32_t lo = (uint32_t)(code << (kDecBits - depth));
@@ -589,7 +592,57 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
             uint32_t e  = ((a.node_sym[i] & 0xffffu) << 8) | depth;
             for (uint32_t t = lo; t < hi; t++) a.table[t] = e;
         } else if (!leaf && depth == (uint32_t)kDecBits) {
-            a.table[(uint32_t)code] = (i << 8);  // len 0: continue bit by bit from node i
+            a.table[(uint32_t)code] = (i << 8);  // walk from node i (until a secondary table replaces it)
+        } else if (leaf && depth > (uint32_t)kDecBits) {
+            const uint32_t r = depth - kDecBits;
+            atomicMax(&s_w2[(uint32_t)(code >> r)], r < (uint32_t)kDec2Max ? r : (uint32_t)kDec2Max);
+        }
+    }
+    __syncthreads();
+    // offsets of the secondary tables (exclusive scan of 2^w2, kDecBits-bit prefixes in order)
+    constexpr int kPer = (1 << kDecBits) / 1024;
+    uint32_t sizes[kPer], mine = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const uint32_t w2 = s_w2[threadIdx.x * kPer + k];
+        sizes[k]          = w2 ? (1u << w2) : 0u;
+        mine += sizes[k];
+    }
+    uint32_t total;
+    uint32_t off = block_exclusive_scan<uint32_t>(mine, s_scan, &total);
+    const bool fits = total <= table2_capacity(a.max_nodes);  // always, by the capacity's construction
+    if (fits) {
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const uint32_t pfx = threadIdx.x * kPer + k, w2 = s_w2[pfx];
+            if (w2) a.table[pfx] = (off << 12) | (w2 << 8) | 0x80u;
+            off += sizes[k];
+        }
+        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) a.table2[i] = 0u;  // not a codeword
+    }
+    __syncthreads();
+    // pass 2: secondary entries -- leaves within w2 bits of their prefix, and walk entries for the
+    // internal nodes w2 bits down (codewords longer than kDecBits + kDec2Max)
+    if (fits) {
+        for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
+            uint32_t depth;
+            unsigned long long code;
+            if (!depth_code(i, depth, code) || depth <= (uint32_t)kDecBits) continue;
+            const uint32_t r   = depth - kDecBits;
+            const uint32_t pfx = (uint32_t)(code >> r);
+            const uint32_t e   = a.table[pfx];
+            if (!(e & 0x80u)) continue;
+            const uint32_t w2 = (e >> 8) & 0xfu, base = e >> 12;
+            if (r > w2) continue;
+            const uint32_t rel = (uint32_t)(code & ((1ull << r) - 1ull));
+            const bool leaf    = (a.node_sym[i] & 0x80000000u) != 0;
+            if (leaf) {
+                const uint32_t lo = base + (rel << (w2 - r)), hi = lo + (1u << (w2 - r));
+                const uint32_t v  = ((a.node_sym[i] & 0xffffu) << 8) | depth;
+                for (uint32_t t = lo; t < hi; t++) a.table2[t] = v;
+            } else if (r == w2) {
+                a.table2[base + rel] = (i << 8);
+            }
         }
     }
     if (threadIdx.x == 0) {
@@ -637,20 +690,32 @@ struct BitReader {
 };
 
 // Decode one symbol; returns 0xffffffff on a malformed walk or on running past the payload.
-__device__ __forceinline__ uint32_t decode_one(BitReader& br, const uint32_t* table, const uint32_t* child,
-                                               const uint32_t* node_sym, uint32_t max_nodes) {
-    br.refill();
+__device__ __forceinline__ uint32_t decode_one(BitReader& br, const uint32_t* table, const uint32_t* table2,
+                                               const uint32_t* child, const uint32_t* node_sym, uint32_t max_nodes) {
+    br.refill();  // > 32 valid bits: enough for both table levels
     uint32_t e   = table[br.peek(kDecBits)];
-    uint32_t len = e & 0xffu;
+    uint32_t len = e & 0x7fu;
     if (len) {
         if (br.pos + len > br.limit) return 0xffffffffu;
         br.skip((int)len);
         return e >> 8;
     }
-    uint32_t node = e >> 8;
+    uint32_t node = e >> 8, used = kDecBits;
+    if (e & 0x80u) {
+        const uint32_t w2 = (e >> 8) & 0xfu;
+        const uint32_t e2 = __ldg(&table2[(e >> 12) + (br.peek(kDecBits + (int)w2) & ((1u << w2) - 1u))]);
+        len               = e2 & 0xffu;
+        if (len) {
+            if (br.pos + len > br.limit) return 0xffffffffu;
+            br.skip((int)len);
+            return e2 >> 8;
+        }
+        node = e2 >> 8;
+        used = kDecBits + w2;
+    }
     if (node == 0 || node >= max_nodes) return 0xffffffffu;  // prefix not in the tree
-    if (br.pos + kDecBits > br.limit) return 0xffffffffu;
-    br.skip(kDecBits);
+    if (br.pos + used > br.limit) return 0xffffffffu;
+    br.skip((int)used);
     for (int guard = 0; guard < 4096; guard++) {
         br.refill();
         if (br.pos + 1 > br.limit) return 0xffffffffu;
@@ -689,7 +754,7 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
     };
     uint16_t* out = a.codes + out0;
     for (unsigned long long k = 0; k < cnt; k++) {
-        uint32_t s = decode_one(br, s_table, a.child, a.node_sym, a.max_nodes);
+        uint32_t s = decode_one(br, s_table, a.table2, a.child, a.node_sym, a.max_nodes);
         if (s == 0xffffffffu) {
             set_status(a.status, VSZ_ERR_CORRUPT);
             return;
@@ -717,12 +782,14 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 // length, so the inner loop has no bounds test: a chunk must consume exactly its indexed length
 // (checked at the end), and reads stop 64 bits past it whatever the bits say.  Zero codes are
 // counted per chunk (outlier ranks for the reverse Lorenzo kernel).
-constexpr int kDecRound = 32;
+constexpr int kDecRound = 16;                 // codes per lane staged before the coalesced store
+constexpr int kDecParts = kDecRound / 8;      // 16-byte pieces per staged row
 
 template <bool WALK_SMEM>
 __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
     __shared__ uint32_t s_table[1 << kDecBits];
     __shared__ __align__(16) uint16_t s_stage[8][32][kDecRound + 8];  // +8: keep rows 16-byte aligned
+    __shared__ __align__(16) uint4 s_ring[8][4][32];                   // per lane: 4 blocks of its stream
     extern __shared__ uint32_t s_walk[];                               // WALK_SMEM: a.nodes entries
     for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
     if (WALK_SMEM)
@@ -737,8 +804,41 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
     const unsigned long long out0 = (unsigned long long)j * kChunkSyms;
     uint32_t cnt = 0;
     if (active && out0 < a.n) cnt = (uint32_t)min((unsigned long long)kChunkSyms, a.n - out0);
-    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 3u) * 8u;
-    const uint32_t* gw   = reinterpret_cast<const uint32_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)3);
+    // Bits come through a per-lane ring of four 16-byte blocks in shared memory, filled by
+    // cp.async three blocks (~380 bits, ~60 codewords) ahead of use: the 32 lanes of a warp read
+    // 32 separate streams, which thrash L1 when fetched word by word.  Positions are bits from the
+    // 16-byte aligned base; bytes past the readable end are zero-filled by the copy.
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 15u) * 8u;
+    const uint8_t* g16   = reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)15);
+    // readable bytes from g16: the payload plus the 8 bytes past its end that callers provide
+    const unsigned long long readable = base0 / 8u + (a.payload_bits + 7) / 8 + 8;
+    uint4* ring = &s_ring[warp][0][lane];  // slot k at ring[32 k]
+    auto fetch = [&](unsigned long long b) {  // block b into slot b % 4, one commit group
+        const unsigned long long off = b * 16;
+        const uint32_t nb = off >= readable ? 0u : (uint32_t)min(16ull, readable - off);
+        cp_async16_zfill(ring + 32 * (uint32_t)(b & 3), g16 + (nb ? off : 0), nb);
+        cp_async_commit();
+    };
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    int nq = 0;
+    unsigned long long blk = 0;  // next block to take from the ring
+    // blocks blk, blk + 1, blk + 2 are in flight here; slot (blk + 3) % 4 was read one block ago
+    auto next_block = [&]() {
+        cp_async_wait<2>();
+        q = ring[32 * (uint32_t)(blk & 3)];
+        fetch(blk + 3);
+        blk++;
+        nq = 4;
+    };
+    auto pop = [&]() -> uint32_t {
+        if (nq == 0) next_block();
+        const uint32_t w = q.x;
+        q.x = q.y;
+        q.y = q.z;
+        q.z = q.w;
+        nq--;
+        return bswap32(w);
+    };
     bool bad = false;
     unsigned long long pos = 0, end = 0;
     unsigned long long buf = 0;
@@ -751,7 +851,14 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
         if (!bad) {
             const unsigned long long wi = pos >> 5;
             const uint32_t off          = (uint32_t)(pos & 31u);
-            buf   = ((((unsigned long long)bswap32(__ldg(&gw[wi]))) << 32) | bswap32(__ldg(&gw[wi + 1]))) << off;
+            blk = wi >> 2;
+            fetch(blk);
+            fetch(blk + 1);
+            fetch(blk + 2);
+            for (uint32_t k = 0; k < (uint32_t)(wi & 3u); k++) pop();
+            const uint32_t w0 = pop();
+            const uint32_t w1 = pop();
+            buf   = ((((unsigned long long)w0) << 32) | w1) << off;
             nbits = 64 - (int)off;
         }
     }
@@ -765,31 +872,44 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
                     bad = true;
                     break;
                 }
-                buf |= ((unsigned long long)bswap32(__ldg(&gw[nxt >> 5]))) << (32 - nbits);
+                buf |= ((unsigned long long)pop()) << (32 - nbits);
                 nbits += 32;
             }
             const uint32_t e = s_table[(uint32_t)(buf >> (64 - kDecBits))];
-            uint32_t len     = e & 0xffu;
-            uint32_t sy;
-            if (len) {
-                sy = e >> 8;
-            } else {
-                // codeword longer than the table: walk the tree bit by bit from the table's node,
-                // refilling as it goes (codewords may be up to 64 bits)
-                uint32_t node = e >> 8;
-                sy            = 0xffffffffu;
+            uint32_t len     = e & 0x7fu;
+            uint32_t sy      = e >> 8;
+            uint32_t node = 0, used = 0;
+            if (!len) {
+                // a longer codeword: the secondary table (next w2 bits) resolves it, or gives the
+                // node to walk from (nbits > 32 covers both lookups)
+                node = e >> 8;
+                used = kDecBits;
+                if (e & 0x80u) {
+                    const uint32_t w2 = (e >> 8) & 0xfu;
+                    const uint32_t e2 =
+                        __ldg(&a.table2[(e >> 12) + ((uint32_t)(buf >> (64 - kDecBits - w2)) & ((1u << w2) - 1u))]);
+                    len  = e2 & 0xffu;
+                    sy   = e2 >> 8;
+                    node = e2 >> 8;
+                    used = kDecBits + w2;
+                }
+            }
+            if (!len) {
+                // codeword longer than both tables: walk the tree bit by bit, refilling as it goes
+                // (codewords may be up to 64 bits)
+                sy = 0xffffffffu;
                 if (node == 0 || node >= a.max_nodes) {
                     bad = true;
                     break;
                 }
-                buf <<= kDecBits;
-                nbits -= kDecBits;
-                pos += kDecBits;
+                buf <<= used;
+                nbits -= (int)used;
+                pos += used;
                 for (int guard = 0; guard < 64; guard++) {
                     if (nbits <= 32) {
                         const unsigned long long nxt = pos + (unsigned long long)nbits;
                         if (nxt > end + 64) break;
-                        buf |= ((unsigned long long)bswap32(__ldg(&gw[nxt >> 5]))) << (32 - nbits);
+                        buf |= ((unsigned long long)pop()) << (32 - nbits);
                         nbits += 32;
                     }
                     const uint32_t bit = (uint32_t)(buf >> 63);
@@ -827,10 +947,10 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
             zeros += (sy == 0u);
         }
         __syncwarp();
-        // 32 rows x 4 pieces of 8 symbols; piece q*32 + lane
+        // 32 rows x kDecParts pieces of 8 symbols; piece pq * 32 + lane
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const uint32_t piece = q * 32 + lane, src = piece >> 2, part = piece & 3u;
+        for (int pq = 0; pq < kDecParts; pq++) {
+            const uint32_t piece = pq * 32 + lane, src = piece / kDecParts, part = piece % kDecParts;
             const size_t jj      = jw0 + src;
             const uint32_t cnt_s = __shfl_sync(0xffffffffu, cnt, src);
             const uint32_t ms    = (cnt_s > r0) ? min((uint32_t)kDecRound, cnt_s - r0) : 0u;
@@ -846,6 +966,7 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
         }
         __syncwarp();
     }
+    cp_async_wait<0>();  // no copy into this CTA's shared memory may outlive it
     if (cnt && !bad && pos != end) bad = true;  // the chunk must fill exactly its indexed length
     if (bad) set_status(a.status, VSZ_ERR_CORRUPT);
     if (active && a.chunk_zero) a.chunk_zero[j] = zeros;
@@ -883,7 +1004,7 @@ __device__ void sync_decode_chunk(const HuffSyncArgs& a, const uint32_t* table, 
     br.init(gw, base0 + start, base0 + a.payload_bits);
     uint32_t cnt = 0;
     while (br.pos - base0 < end && br.pos - base0 < a.payload_bits) {
-        uint32_t s = decode_one(br, table, a.child, a.node_sym, a.max_nodes);
+        uint32_t s = decode_one(br, table, a.table2, a.child, a.node_sym, a.max_nodes);
         if (s == 0xffffffffu) break;  // padding at the stream end, or a wrong (unsynchronised) start
         cnt++;
     }
@@ -993,8 +1114,10 @@ int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
     if (a.ws_in_smem) {
         huff_build_prepare();
         k_huff_build<true><<<1, 256, bytes, st>>>(a);
+        count_launch();
     } else {
         k_huff_build<false><<<1, 256, 0, st>>>(a);
+        count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
@@ -1013,17 +1136,21 @@ int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
     smem_limit_once(k_huff_count, 64 * 1024 + 1024, attr_count);
     int grid = (int)min((long long)a.ntiles, (long long)num_sms * 8);
     k_huff_count<<<grid, kEncThreads, a.cb_in_smem ? (size_t)a.dict : 0, st>>>(a);
+    count_launch();
     int rc = launch_scan_u32(a.tile_bits, a.tile_off, a.ntiles, a.tile_status, a.tile_counter, a.total_bits,
                              a.status, st);
     if (rc) return rc;
     int pgrid = (int)min((long long)a.ntiles, (long long)num_sms * 3);
     k_huff_pack<<<pgrid, kEncThreads, smem, st>>>(a);
+    count_launch();
     k_huff_encode_edges<<<(a.ntiles + 255) / 256, 256, 0, st>>>(a);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
 int launch_huff_table(HuffTableArgs a, cudaStream_t st) {
     k_huff_table<<<1, 1024, 0, st>>>(a);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
@@ -1038,11 +1165,14 @@ int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
             static std::atomic<unsigned long long> attr{0};
             smem_limit_once(k_huff_decode_idx<true>, 140 * 1024, attr);
             k_huff_decode_idx<true><<<grid, 256, smem, st>>>(a);
+            count_launch();
         } else {
             k_huff_decode_idx<false><<<grid, 256, 0, st>>>(a);
+            count_launch();
         }
     } else {
         k_huff_decode<<<grid, 256, 0, st>>>(a);
+        count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
@@ -1052,18 +1182,21 @@ int launch_huff_const(uint16_t* codes, size_t n, const uint32_t* info, uint32_t*
     int grid = (int)min((long long)((n + 255) / 256), (long long)num_sms * 8);
     if (grid < 1) grid = 1;
     k_huff_const<<<grid, 256, 0, st>>>(codes, n, info, seg_zero, d0, nxs, status);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
 int launch_huff_sync_init(HuffSyncArgs a, cudaStream_t st) {
     if (a.nchunks == 0) return VSZ_OK;
     k_huff_sync_init<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
 int launch_huff_sync_round(HuffSyncArgs a, const unsigned long long* exit_in, unsigned long long* exit_out, int* changed,
                            cudaStream_t st) {
     k_huff_sync_round<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a, exit_in, exit_out, changed);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
@@ -1078,6 +1211,7 @@ int launch_scan_excl_t(const TIn* in, unsigned long long* out, size_t n, unsigne
     if (cudaMemsetAsync(tile_status, 0, 8 * ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
     if (cudaMemsetAsync(tile_counter, 0, 4, st) != cudaSuccess) return VSZ_ERR_CUDA;
     k_scan_excl<TIn><<<(unsigned)ntiles, 256, 0, st>>>(in, out, n, tile_status, tile_counter, total, status);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 

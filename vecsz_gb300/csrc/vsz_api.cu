@@ -295,6 +295,7 @@ struct DecompressWs {
     uint32_t* mm;
     int* status;
     uint32_t* table;
+    uint32_t* table2;
     uint32_t* child;
     uint32_t* node_sym;
     uint32_t* parent;
@@ -328,6 +329,7 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
     w.mm       = b.take<uint32_t>(4);
     w.status   = b.take<int>(4);
     w.table    = b.take<uint32_t>(1u << kDecBits);
+    w.table2   = b.take<uint32_t>(table2_capacity(maxn));
     w.child    = b.take<uint32_t>(2 * (size_t)maxn);
     w.node_sym = b.take<uint32_t>(maxn);
     w.parent   = b.take<uint32_t>(maxn);
@@ -377,6 +379,7 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     ta.node_sym = w.node_sym;
     ta.parent = w.parent;
     ta.walk = w.walk;
+    ta.table2 = w.table2;
     ta.info = w.tinfo;
     ta.status = w.status;
     {
@@ -391,6 +394,7 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     da.payload = payload;
     da.payload_bits = pbits;
     da.table = w.table;
+    da.table2 = w.table2;
     da.child = w.child;
     da.node_sym = w.node_sym;
     da.codes = w.code;
@@ -424,6 +428,7 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     sa.payload = payload;
     sa.payload_bits = pbits;
     sa.table = w.table;
+    sa.table2 = w.table2;
     sa.child = w.child;
     sa.node_sym = w.node_sym;
     sa.nchunks = (size_t)((pbits + kSyncBits - 1) / kSyncBits);
@@ -929,6 +934,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     {
         StageTimer t(kStFinalize, st);
         k_finalize<<<fg, 256, 0, st>>>(f);
+        count_launch();
     }
     VSZ_CUDA(cudaGetLastError());
     return VSZ_OK;
@@ -1076,6 +1082,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
                                     w.status, st));
         }
         k_check_zeros<<<1, 1, 0, st>>>(w.scan_total, d->n_outlier, w.status);
+        count_launch();
     }
     if (d->n_outlier) {
         StageTimer t(kStOutlierCopy, st);
@@ -1101,7 +1108,10 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));
     }
-    if (d_status) k_copy_status<<<1, 1, 0, st>>>(w.status, w.consts, d_status);
+    if (d_status) {
+        k_copy_status<<<1, 1, 0, st>>>(w.status, w.consts, d_status);
+        count_launch();
+    }
     VSZ_CUDA(cudaGetLastError());
     return VSZ_OK;
 }

@@ -24,6 +24,10 @@ constexpr int kSegX = kTileX;
 // records VSZ_ERR_TIMEOUT in the status word and gives up instead of hanging the GPU.
 constexpr long long kSpinLimit = 1ll << 22;
 
+// Counts one kernel launch of this library (read through vsz_launch_count); called after every
+// <<<>>> launch.
+void count_launch();
+
 // Raises a kernel's dynamic shared-memory limit on the current device once per (kernel, device):
 // the attribute is per device, and the host call stays out of later launches.  The bit is set
 // only after the attribute is, so a racing thread at worst sets it twice.
@@ -116,6 +120,17 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
 }
+
+// 16-byte asynchronous global -> shared copy (cp.async.cg); only the first src_bytes (0..16)
+// are read, the rest of the 16 bytes is zero-filled.  Both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16_zfill(void* smem, const void* gmem, uint32_t src_bytes) {
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// Wait until at most N of this thread's committed groups are still in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Big-endian byte order of a 32-bit word (the bitstream is MSB-first bytes).
 __device__ __forceinline__ uint32_t bswap32(uint32_t v) { return __byte_perm(v, 0, 0x0123); }

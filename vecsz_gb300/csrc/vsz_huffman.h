@@ -11,6 +11,19 @@
 namespace vsz {
 
 constexpr int kDecBits     = 12;   // primary decode table: 4096 entries
+constexpr int kDec2Max     = 8;    // widest secondary table: codewords of up to 20 bits in two lookups
+
+// Decode table entries (k_huff_table).  Primary table, indexed by the next kDecBits bits:
+//   (sym << 8) | len           len in 1..kDecBits: a whole codeword
+//   (off << 12) | (w2 << 8) | 0x80   a longer codeword: index table2[off + next w2 bits]
+//   (node << 8)                walk the tree bit by bit from `node` after kDecBits bits
+// Secondary table2 entries: (sym << 8) | total length, or (node << 8) to walk from `node` after
+// kDecBits + w2 bits (codewords longer than kDecBits + kDec2Max).  A zero entry is not a codeword.
+// Capacity: every secondary table hangs off a distinct internal node at depth kDecBits.
+__host__ __device__ inline size_t table2_capacity(uint32_t max_nodes) {
+    const uint32_t p = max_nodes < (1u << kDecBits) ? max_nodes : (1u << kDecBits);
+    return (size_t)p << kDec2Max;
+}
 constexpr int kChunkSyms   = 512;  // codewords per entry of this library's decode index
 constexpr int kSyncBits    = 8192; // chunk size (bits) of the self-synchronising decoder
 
@@ -68,6 +81,7 @@ struct HuffTableArgs {
     uint32_t* parent;     // max_nodes (scratch)
     uint32_t* walk;       // max_nodes: both children of an internal node, 16 bits each:
                           // 0x8000 | symbol for a leaf, else the node index (dict <= 16384)
+    uint32_t* table2;     // table2_capacity(max_nodes) secondary entries
     uint32_t* info;       // [0] single-symbol tree flag [1] its symbol
     int* status;
 };
@@ -76,6 +90,7 @@ struct HuffDecodeArgs {
     const uint8_t* payload;  // any alignment; 8 readable bytes past the end are required
     unsigned long long payload_bits;
     const uint32_t* table;
+    const uint32_t* table2;
     const uint32_t* child;
     const uint32_t* node_sym;
     const uint32_t* walk;                 // packed children (k_huff_table), when walk_smem
@@ -100,6 +115,7 @@ struct HuffSyncArgs {
     const uint8_t* payload;
     unsigned long long payload_bits;
     const uint32_t* table;
+    const uint32_t* table2;
     const uint32_t* child;
     const uint32_t* node_sym;
     size_t nchunks;

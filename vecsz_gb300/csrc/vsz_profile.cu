@@ -1,5 +1,7 @@
 // Per-stage CUDA-event timing (see vsz_profile.h).  Event pairs are kept until vsz_profile_read,
 // which synchronises on them and accumulates elapsed times.
+#include <atomic>
+#include <cstdint>
 #include <mutex>
 #include <vector>
 
@@ -24,6 +26,11 @@ const char* g_names[kStCount] = {"eb_setup",        "dualquant",     "huff_build
 }  // namespace
 
 bool profile_on() { return g_on; }
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 StageTimer::StageTimer(int s, cudaStream_t stream) : stage(s), st(stream) {
     if (!g_on) return;
@@ -51,6 +58,8 @@ StageTimer::~StageTimer() {
 extern "C" {
 
 void vsz_profile_enable(int on) { vsz::g_on = on != 0; }
+
+uint64_t vsz_launch_count(void) { return vsz::g_launches.load(std::memory_order_relaxed); }
 
 void vsz_profile_reset(void) {
     std::lock_guard<std::mutex> lk(vsz::g_mu);
