@@ -286,83 +286,88 @@ int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsig
                     uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st);
 
 // ------------------------------------------------------------------------------------------
-// K3: encoder, two passes over the codes with no cross-tile waiting:
-//   k_huff_count  bits per tile of 4096 codes (and per 512 codes: the decode index)
-//   k_scan_excl   exclusive scan of the tile totals -> each tile's first bit
-//   k_huff_pack   per tile: block scan of thread bit counts, codewords packed into a shared-memory
-//                 word buffer, interior words stored, partial boundary words left to
-//                 k_huff_encode_edges
+// K3: encoder, two passes over the codes with no cross-warp waiting.  The unit is a chunk of 512
+// codes -- one warp, 16 codes per lane -- the same chunk the decode index records:
+//   k_huff_count  bits per chunk (chunk_bits, also the archive's decode index)
+//   k_scan_excl   exclusive scan of chunk_bits -> each chunk's first bit, total bits
+//   k_huff_pack   per chunk: warp scan of lane bit counts, codewords packed into the warp's
+//                 shared-memory word buffer, interior words stored, the partial first and last
+//                 words left to k_huff_encode_edges.  No block-wide barriers; the next chunk's
+//                 codes are loaded while the current one is packed.
 // ------------------------------------------------------------------------------------------
 
 constexpr int kEncThreads   = 256;
 constexpr int kEncPerThread = 16;
-constexpr int kEncTile      = kEncThreads * kEncPerThread;  // 4096 codes
-constexpr int kEncMaxWords  = kEncTile * 64 / 32 + 4;       // codes are at most 64 bits
+constexpr int kEncChunk     = 32 * kEncPerThread;        // 512 codes per warp chunk (= kChunkSyms)
+constexpr int kEncWarpWords = kEncChunk * 64 / 32 + 4;   // codes are at most 64 bits
+static_assert(kEncChunk == kChunkSyms, "the encoder chunk is the decode index chunk");
 
-__device__ __forceinline__ void load_codes16(const HuffEncodeArgs& a, size_t c0, uint32_t sym[kEncPerThread]) {
-    if (c0 + kEncPerThread <= a.n && a.codes_aligned) {
+// Raw 16 codes of one lane (two 16-byte loads when aligned and whole) and how many are valid.
+struct Codes16 {
+    uint4 v0, v1;
+    uint32_t nvalid;
+};
+
+__device__ __forceinline__ Codes16 load_codes16(const HuffEncodeArgs& a, size_t c0) {
+    Codes16 r;
+    r.nvalid = c0 >= a.n ? 0u : (uint32_t)min((size_t)kEncPerThread, a.n - c0);
+    if (r.nvalid == (uint32_t)kEncPerThread && a.codes_aligned) {
         const uint4* p = reinterpret_cast<const uint4*>(a.codes + c0);
-        uint4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
-        uint32_t w8[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            sym[2 * k]     = w8[k] & 0xffffu;
-            sym[2 * k + 1] = w8[k] >> 16;
-        }
+        r.v0 = __ldcs(p);
+        r.v1 = __ldcs(p + 1);
     } else {
+        uint32_t t[kEncPerThread];
 #pragma unroll
-        for (int k = 0; k < kEncPerThread; k++) sym[k] = (c0 + k < a.n) ? a.codes[c0 + k] : 0xffffffffu;
+        for (int k = 0; k < kEncPerThread; k++) t[k] = ((uint32_t)k < r.nvalid) ? a.codes[c0 + k] : 0u;
+        r.v0 = make_uint4(t[0] | (t[1] << 16), t[2] | (t[3] << 16), t[4] | (t[5] << 16), t[6] | (t[7] << 16));
+        r.v1 = make_uint4(t[8] | (t[9] << 16), t[10] | (t[11] << 16), t[12] | (t[13] << 16), t[14] | (t[15] << 16));
     }
+    return r;
+}
+
+__device__ __forceinline__ uint32_t code_k(const Codes16& c, int k) {
+    const uint32_t w8[8] = {c.v0.x, c.v0.y, c.v0.z, c.v0.w, c.v1.x, c.v1.y, c.v1.z, c.v1.w};
+    return (w8[k >> 1] >> (16 * (k & 1))) & 0xffffu;
+}
+
+// Refuses a tree the encoder cannot pack (no tree, or codewords longer than 64 bits).
+__device__ __forceinline__ bool encode_tree_ok(const HuffEncodeArgs& a) {
+    if (a.build_info && (a.build_info[2] > 64u || a.build_info[0] == 0u)) {
+        if (threadIdx.x == 0 && blockIdx.x == 0)
+            set_status(a.status, a.build_info[0] ? VSZ_ERR_UNSUPPORTED : VSZ_ERR_INVALID);
+        return false;
+    }
+    return true;
 }
 
 __global__ void __launch_bounds__(kEncThreads) k_huff_count(HuffEncodeArgs a) {
     extern __shared__ uint8_t s_len_dyn[];
-    __shared__ uint32_t s_wsum[kEncThreads / 32];
-    if (*a.status != VSZ_OK) return;
-    if (a.build_info && (a.build_info[2] > 64u || a.build_info[0] == 0u)) {
-        if (threadIdx.x == 0 && blockIdx.x == 0)
-            set_status(a.status, a.build_info[0] ? VSZ_ERR_UNSUPPORTED : VSZ_ERR_INVALID);
-        return;
-    }
+    if (*a.status != VSZ_OK || !encode_tree_ok(a)) return;
     const uint8_t* cl = a.cb_len;
     if (a.cb_in_smem) {
         for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_len_dyn[i] = a.cb_len[i];
         __syncthreads();
         cl = s_len_dyn;
     }
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (uint32_t tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const size_t c0 = (size_t)tile * kEncTile + (size_t)threadIdx.x * kEncPerThread;
-        uint32_t sym[kEncPerThread];
-        load_codes16(a, c0, sym);
-        uint32_t bits = 0;
+    const unsigned lane = threadIdx.x & 31u;
+    const size_t warps  = (size_t)gridDim.x * (kEncThreads / 32);
+    for (size_t c = blockIdx.x * (size_t)(kEncThreads / 32) + (threadIdx.x >> 5); c < a.nchunks; c += warps) {
+        const Codes16 cc = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
+        uint32_t bits    = 0;
 #pragma unroll
         for (int k = 0; k < kEncPerThread; k++)
-            if (sym[k] != 0xffffffffu) bits += cl[sym[k]];
+            if ((uint32_t)k < cc.nvalid) bits += cl[code_k(cc, k)];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) bits += __shfl_xor_sync(0xffffffffu, bits, o);
-        if (lane == 0) {
-            s_wsum[warp] = bits;
-            size_t chunk = (size_t)tile * (kEncTile / 512) + warp;
-            if (a.chunk_bits && chunk * 512 < a.n) a.chunk_bits[chunk] = (uint16_t)bits;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t t = 0;
-#pragma unroll
-            for (int i = 0; i < kEncThreads / 32; i++) t += s_wsum[i];
-            a.tile_bits[tile] = t;
-        }
-        __syncthreads();
+        if (lane == 0) a.chunk_bits[c] = (uint16_t)bits;  // <= 512 x 64
     }
 }
 
-__global__ void __launch_bounds__(kEncThreads) k_huff_pack(HuffEncodeArgs a) {
+__global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) {
     extern __shared__ uint8_t s_dyn[];
-    uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);                                     // kEncMaxWords
-    unsigned long long* s_cw = reinterpret_cast<unsigned long long*>(s_words + kEncMaxWords);  // dict (if cached)
+    uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);                                     // 8 x kEncWarpWords
+    unsigned long long* s_cw = reinterpret_cast<unsigned long long*>(s_words + 8 * kEncWarpWords);  // dict (if cached)
     uint8_t* s_len = reinterpret_cast<uint8_t*>(s_cw + (a.cb_in_smem ? a.dict : 0));
-    __shared__ unsigned long long s_scan[33];
     if (*a.status != VSZ_OK) return;  // set before this launch: uniform across the grid
     const unsigned long long* cw = a.cb_word;
     const uint8_t* cl            = a.cb_len;
@@ -373,46 +378,57 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_pack(HuffEncodeArgs a) {
         }
         cw = s_cw;
         cl = s_len;
+        __syncthreads();
     }
-    __syncthreads();
+    const unsigned lane   = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t* sw          = s_words + warp * kEncWarpWords;
     uint8_t* out          = a.out + a.out_off.eval();
     const uint32_t base0  = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
     uint32_t* gw          = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
-
-    for (uint32_t tile = blockIdx.x; tile < a.ntiles; tile += gridDim.x) {
-        const size_t c0 = (size_t)tile * kEncTile + (size_t)threadIdx.x * kEncPerThread;
-        uint32_t sym[kEncPerThread];
-        load_codes16(a, c0, sym);
-        uint32_t bits = 0;
+    const size_t warps    = (size_t)gridDim.x * (kEncThreads / 32);
+    size_t c              = blockIdx.x * (size_t)(kEncThreads / 32) + warp;
+    Codes16 nxt           = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
+    for (; c < a.nchunks; c += warps) {
+        const Codes16 cc = nxt;
+        if (c + warps < a.nchunks) nxt = load_codes16(a, (c + warps) * kEncChunk + lane * kEncPerThread);
+        uint32_t sym[kEncPerThread], len[kEncPerThread], bits = 0;
 #pragma unroll
-        for (int k = 0; k < kEncPerThread; k++)
-            if (sym[k] != 0xffffffffu) bits += cl[sym[k]];
-        unsigned long long tot;
-        const unsigned long long toff = block_exclusive_scan<unsigned long long>((unsigned long long)bits, s_scan, &tot);
-        const unsigned long long gstart = base0 + a.tile_off[tile];  // tile's first bit on the word grid
-        const uint32_t r0     = (uint32_t)(gstart & 31u);
-        const unsigned long long F = gstart >> 5;
-        const uint32_t nwords = tot ? (uint32_t)((r0 + tot + 31) >> 5) : 0u;
-        for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) s_words[i] = 0u;
-        __syncthreads();
-        // pack this thread's codewords; only a thread's first and last word can be shared with its
+        for (int k = 0; k < kEncPerThread; k++) {
+            sym[k] = code_k(cc, k);
+            len[k] = ((uint32_t)k < cc.nvalid) ? (uint32_t)cl[sym[k]] : 0u;
+            bits += len[k];
+        }
+        uint32_t incl = bits;  // warp inclusive scan of lane bit counts
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (unsigned)o) incl += t;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        const unsigned long long gstart = base0 + a.chunk_off[c];  // chunk's first bit on the word grid
+        const uint32_t r0               = (uint32_t)(gstart & 31u);
+        const unsigned long long F      = gstart >> 5;
+        const uint32_t nwords           = tot ? (r0 + tot + 31) >> 5 : 0u;
+        for (uint32_t i = lane; i < nwords; i += 32) sw[i] = 0u;
+        __syncwarp();
+        // pack this lane's codewords; only a lane's first and last word can be shared with its
         // neighbours, so only those use shared-memory atomics
         {
-            const unsigned long long pos = r0 + toff;
-            uint32_t wi = (uint32_t)(pos >> 5);
-            uint32_t nb = (uint32_t)(pos & 31u);  // bits already taken in the current word
-            bool first  = true;
-            unsigned long long acc = 0;            // MSB-aligned pending bits of word wi
+            const uint32_t pos = r0 + incl - bits;
+            uint32_t wi        = pos >> 5;
+            uint32_t nb        = pos & 31u;  // bits already taken in the current word
+            bool first         = true;
+            unsigned long long acc = 0;       // MSB-aligned pending bits of word wi
             auto emit = [&](uint32_t word) {
-                if (first && (pos & 31u)) atomicOr(&s_words[wi], word);
-                else s_words[wi] = word;
+                if (first && (pos & 31u)) atomicOr(&sw[wi], word);
+                else sw[wi] = word;
                 first = false;
                 wi++;
             };
-            auto append = [&](unsigned long long v, uint32_t len) {  // len <= 32
-                if (len == 0) return;
-                acc |= v << (64 - nb - len);
-                nb += len;
+            auto append = [&](unsigned long long v, uint32_t l) {  // l <= 32
+                if (l == 0) return;
+                acc |= v << (64 - nb - l);
+                nb += l;
                 if (nb >= 32) {
                     emit((uint32_t)(acc >> 32));
                     acc <<= 32;
@@ -421,46 +437,44 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_pack(HuffEncodeArgs a) {
             };
 #pragma unroll
             for (int k = 0; k < kEncPerThread; k++) {
-                if (sym[k] == 0xffffffffu) continue;
-                const uint32_t len         = cl[sym[k]];
+                if (len[k] == 0) continue;
                 const unsigned long long v = cw[sym[k]];
-                if (len > 32) {
-                    append(v >> 32, len - 32);
+                if (len[k] > 32) {
+                    append(v >> 32, len[k] - 32);
                     append(v & 0xffffffffull, 32);
                 } else {
-                    append(v, len);
+                    append(v, len[k]);
                 }
             }
-            if (nb > 0) atomicOr(&s_words[wi], (uint32_t)(acc >> 32));
+            if (nb > 0) atomicOr(&sw[wi], (uint32_t)(acc >> 32));
         }
-        __syncthreads();
-        // store: words wholly inside the tile are plain stores; a partial first or last word (shared
-        // with the neighbouring tile, or with the tree bytes before the payload) is left to
-        // k_huff_encode_edges, which ORs the two halves
+        __syncwarp();
+        // interior words are plain stores; a partial first or last word (shared with the
+        // neighbouring chunk, or with the tree bytes before the payload) goes to the edge records
         const bool first_partial = (r0 != 0);
-        const bool last_partial  = ((r0 + tot) & 31ull) != 0;
-        for (uint32_t i = threadIdx.x; i < nwords; i += blockDim.x) {
+        const bool last_partial  = ((r0 + tot) & 31u) != 0;
+        for (uint32_t i = lane; i < nwords; i += 32) {
             if (i == 0 && first_partial) continue;
             if (i == nwords - 1 && last_partial) continue;
-            gw[F + i] = bswap32(s_words[i]);
+            gw[F + i] = bswap32(sw[i]);
         }
-        if (threadIdx.x == 0) {
+        if (lane == 0) {
             const unsigned long long none = ~0ull;
-            a.edge_idx[2 * tile]      = (nwords && first_partial) ? F : none;
-            a.edge_bits[2 * tile]     = nwords ? bswap32(s_words[0]) : 0u;
-            a.edge_idx[2 * tile + 1]  = (nwords && last_partial) ? F + nwords - 1 : none;
-            a.edge_bits[2 * tile + 1] = nwords ? bswap32(s_words[nwords - 1]) : 0u;
+            a.edge_idx[2 * c]      = (nwords && first_partial) ? F : none;
+            a.edge_bits[2 * c]     = nwords ? bswap32(sw[0]) : 0u;
+            a.edge_idx[2 * c + 1]  = (nwords && last_partial) ? F + nwords - 1 : none;
+            a.edge_bits[2 * c + 1] = nwords ? bswap32(sw[nwords - 1]) : 0u;
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
-// Boundary words of the encoder tiles: tile t's partial first word is the same word as tile
-// t - 1's partial last word (a middle tile spans thousands of bits, so no word has a third
-// sharer); the payload's first word also holds the last bytes of the tree section, kept as is.
+// Boundary words of the chunks: chunk t's partial first word is the same word as chunk t - 1's
+// partial last word (a chunk of 512 codewords of >= 1 bit spans >= 512 bits, so no word has a
+// third sharer); the payload's first word also holds the last bytes of the tree section, kept as is.
 __global__ void k_huff_encode_edges(HuffEncodeArgs a) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.ntiles || *a.status != VSZ_OK) return;
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= a.nchunks || *a.status != VSZ_OK) return;
     uint8_t* out         = a.out + a.out_off.eval();
     const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
     uint32_t* gw         = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
@@ -473,7 +487,7 @@ __global__ void k_huff_encode_edges(HuffEncodeArgs a) {
         if (fi == 0 && base0 != 0) v |= gw[0] & ((1u << base0) - 1u);  // tree bytes before the payload
         gw[fi] = v;
     }
-    if (t == a.ntiles - 1 && li != none && li != fi) gw[li] = a.edge_bits[2 * t + 1];
+    if (t == a.nchunks - 1 && li != none && li != fi) gw[li] = a.edge_bits[2 * t + 1];
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1125,25 +1139,26 @@ int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
 size_t huff_build_scratch_bytes(int dict) { return build_ws_bytes(dict); }
 
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
-    a.ntiles = (uint32_t)((a.n + kEncTile - 1) / kEncTile);
-    if (a.ntiles == 0) return cudaMemsetAsync(a.total_bits, 0, 8, st) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+    a.nchunks = (a.n + kEncChunk - 1) / kEncChunk;
+    if (a.nchunks == 0) return cudaMemsetAsync(a.total_bits, 0, 8, st) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
     a.codes_aligned = (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0;
     size_t cb_bytes = (size_t)a.dict * 9;
     a.cb_in_smem    = cb_bytes <= 64 * 1024 ? 1 : 0;
-    size_t smem     = kEncMaxWords * 4 + (a.cb_in_smem ? cb_bytes : 0) + 16;
+    size_t smem     = (size_t)8 * kEncWarpWords * 4 + (a.cb_in_smem ? cb_bytes : 0) + 16;
     static std::atomic<unsigned long long> attr_pack{0}, attr_count{0};
-    smem_limit_once(k_huff_pack, 48 * 1024 + 64 * 1024 + 1024, attr_pack);
+    smem_limit_once(k_huff_pack, 8 * kEncWarpWords * 4 + 64 * 1024 + 1024, attr_pack);
     smem_limit_once(k_huff_count, 64 * 1024 + 1024, attr_count);
-    int grid = (int)min((long long)a.ntiles, (long long)num_sms * 8);
+    const long long blocks = (long long)((a.nchunks + 7) / 8);
+    int grid = (int)min(blocks, (long long)num_sms * 8);
     k_huff_count<<<grid, kEncThreads, a.cb_in_smem ? (size_t)a.dict : 0, st>>>(a);
     count_launch();
-    int rc = launch_scan_u32(a.tile_bits, a.tile_off, a.ntiles, a.tile_status, a.tile_counter, a.total_bits,
+    int rc = launch_scan_u16(a.chunk_bits, a.chunk_off, a.nchunks, a.scan_status, a.scan_counter, a.total_bits,
                              a.status, st);
     if (rc) return rc;
-    int pgrid = (int)min((long long)a.ntiles, (long long)num_sms * 3);
+    int pgrid = (int)min(blocks, (long long)num_sms * 4);
     k_huff_pack<<<pgrid, kEncThreads, smem, st>>>(a);
     count_launch();
-    k_huff_encode_edges<<<(a.ntiles + 255) / 256, 256, 0, st>>>(a);
+    k_huff_encode_edges<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a);
     count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }

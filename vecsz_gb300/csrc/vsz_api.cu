@@ -232,9 +232,8 @@ struct CompressWs {
     unsigned long long* cb_word;
     uint8_t* cb_len;
     uint32_t* build_info;
-    unsigned long long* e_tile_status;
-    uint32_t* e_tile_bits;
-    unsigned long long* e_tile_off;
+    unsigned long long* e_chunk_off;
+    unsigned long long* e_scan_status;
     unsigned long long* e_edge_idx;
     uint32_t* e_edge_bits;
     uint32_t* e_counter;
@@ -270,15 +269,13 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     w.cb_word    = reinterpret_cast<unsigned long long*>(cb);
     w.build_info = cb ? reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict) : nullptr;
     w.cb_len     = cb ? cb + 8 * (size_t)dict + 16 : nullptr;
-    size_t et    = (g.n + 4095) / 4096 + 1;
-    w.e_tile_status = b.take<unsigned long long>(et);
-    w.e_tile_bits   = b.take<uint32_t>(et);
-    w.e_tile_off    = b.take<unsigned long long>(et);
-    w.e_edge_idx  = b.take<unsigned long long>(2 * et);
-    w.e_edge_bits = b.take<uint32_t>(2 * et);
+    w.n_chunks   = (g.n + kChunkSyms - 1) / kChunkSyms;
+    w.e_chunk_off   = b.take<unsigned long long>(w.n_chunks + 1);
+    w.e_scan_status = b.take<unsigned long long>(scan_tmp_tiles(w.n_chunks) + 1);
+    w.e_edge_idx  = b.take<unsigned long long>(2 * w.n_chunks + 2);
+    w.e_edge_bits = b.take<uint32_t>(2 * w.n_chunks + 2);
     w.e_counter  = b.take<uint32_t>(4);
     w.total_bits = b.take<unsigned long long>(1);
-    w.n_chunks   = (g.n + kChunkSyms - 1) / kChunkSyms;
     w.chunk_bits = b.take<uint16_t>(w.n_chunks + 8);
     w.bytes      = b.off + 256;
     return w;
@@ -702,8 +699,16 @@ vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_code
 }
 
 size_t vsz_huffman_encode_tmp_bytes(size_t n) {
-    size_t nt = (n + 4095) / 4096 + 1;
-    return 2048 + 8 * nt + 4 * nt + 8 * nt + 16 * nt + 8 * nt + 2048;
+    const size_t nc = (n + kChunkSyms - 1) / kChunkSyms;
+    Bump b{nullptr, 0};
+    b.take<int>(4);
+    b.take<uint32_t>(4);
+    b.take<unsigned long long>(scan_tmp_tiles(nc) + 1);
+    b.take<unsigned long long>(nc + 1);
+    b.take<unsigned long long>(2 * nc + 2);
+    b.take<uint32_t>(2 * nc + 2);
+    b.take<uint16_t>(nc + 8);
+    return b.off + 256;
 }
 
 vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_codebook, int dict_size,
@@ -713,14 +718,14 @@ vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_co
     if (tmp_bytes < vsz_huffman_encode_tmp_bytes(n)) return VSZ_ERR_CAPACITY;
     Bump b{reinterpret_cast<uint8_t*>(d_tmp), tmp_bytes};
     HuffEncodeArgs a{};
+    const size_t nc = (n + kChunkSyms - 1) / kChunkSyms;
     a.status       = b.take<int>(4);
-    a.tile_counter = b.take<uint32_t>(4);
-    size_t nt      = (n + 4095) / 4096 + 1;
-    a.tile_status  = b.take<unsigned long long>(nt);
-    a.tile_bits    = b.take<uint32_t>(nt);
-    a.tile_off     = b.take<unsigned long long>(nt);
-    a.edge_idx     = b.take<unsigned long long>(2 * nt);
-    a.edge_bits    = b.take<uint32_t>(2 * nt);
+    a.scan_counter = b.take<uint32_t>(4);
+    a.scan_status  = b.take<unsigned long long>(scan_tmp_tiles(nc) + 1);
+    a.chunk_off    = b.take<unsigned long long>(nc + 1);
+    a.edge_idx     = b.take<unsigned long long>(2 * nc + 2);
+    a.edge_bits    = b.take<uint32_t>(2 * nc + 2);
+    uint16_t* own_chunk_bits = b.take<uint16_t>(nc + 8);  // when the caller wants no index
     a.codes        = d_code;
     a.n            = n;
     a.cb_word      = reinterpret_cast<const unsigned long long*>(d_codebook);
@@ -728,7 +733,7 @@ vsz_status vsz_huffman_encode(const uint16_t* d_code, size_t n, const void* d_co
     a.dict         = dict_size;
     a.out          = d_payload;
     a.total_bits   = reinterpret_cast<unsigned long long*>(d_bits);
-    a.chunk_bits   = d_chunk_bits;
+    a.chunk_bits   = d_chunk_bits ? d_chunk_bits : own_chunk_bits;
     VSZ_CUDA(cudaMemsetAsync(a.status, 0, sizeof(int), S(stream)));
     return launch_huff_encode(a, S(stream), num_sms());
 }
@@ -881,12 +886,11 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     he.out_off = DevOffset{hdr + 8, w.build_info + 1, nullptr};
     he.total_bits = w.total_bits;
     he.chunk_bits = w.chunk_bits;
-    he.tile_status = w.e_tile_status;
-    he.tile_bits = w.e_tile_bits;
-    he.tile_off = w.e_tile_off;
+    he.chunk_off = w.e_chunk_off;
+    he.scan_status = w.e_scan_status;
+    he.scan_counter = w.e_counter;
     he.edge_idx = w.e_edge_idx;
     he.edge_bits = w.e_edge_bits;
-    he.tile_counter = w.e_counter;
     he.status = w.status;
     he.build_info = w.build_info;
     {

@@ -56,18 +56,17 @@ struct HuffEncodeArgs {
     uint8_t* out;                     // payload start = out + out_off.eval(), any alignment;
     DevOffset out_off;                // bytes before the payload start are kept
     unsigned long long* total_bits;
-    uint16_t* chunk_bits;             // bits per 512 codes (decode index), may be null
-    unsigned long long* tile_status;  // scan scratch (ntiles / 4096 + 1)
-    uint32_t* tile_bits;              // ntiles: bits per tile of 4096 codes
-    unsigned long long* tile_off;     // ntiles: first bit of each tile
-    unsigned long long* edge_idx;     // 2 ntiles: word index of a tile's partial first / last word
-    uint32_t* edge_bits;              // 2 ntiles: its bits (stored byte order)
-    uint32_t* tile_counter;
+    uint16_t* chunk_bits;             // nchunks: bits per 512 codes (scan input; the decode index)
+    unsigned long long* chunk_off;    // nchunks: first bit of each chunk
+    unsigned long long* scan_status;  // scan scratch: scan_tmp_tiles(nchunks) + 1
+    uint32_t* scan_counter;
+    unsigned long long* edge_idx;     // 2 nchunks: word index of a chunk's partial first / last word
+    uint32_t* edge_bits;              // 2 nchunks: its bits (stored byte order)
     int* status;
-    uint32_t ntiles;
+    size_t nchunks;
     int codes_aligned;
     int cb_in_smem;
-    const uint32_t* build_info;       // optional: k_huff_build's info; max length > 64 is refused
+    const uint32_t* build_info;       // optional: the tree's info; max length > 64 is refused
 };
 
 struct HuffTableArgs {
