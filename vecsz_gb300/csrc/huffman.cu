@@ -506,6 +506,7 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
     __shared__ int s_bad;
     __shared__ uint32_t s_w2[1 << kDecBits];  // secondary table width per primary prefix
     __shared__ uint32_t s_scan[33];
+    __shared__ uint32_t s_maxlen;             // longest codeword (255: some leaf deeper than 64)
     if (threadIdx.x == 0) {
         s_nc  = ((uint32_t)h[0] << 24) | ((uint32_t)h[1] << 16) | ((uint32_t)h[2] << 8) | (uint32_t)h[3];
         s_bad = 0;
@@ -575,6 +576,7 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
         if (threadIdx.x == 0) {
             a.info[0] = 1;  // single-symbol tree: constant output, no bits
             a.info[1] = a.node_sym[0] & 0xffffu;
+            a.info[2] = 0;
         }
         return;
     }
@@ -594,12 +596,17 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
     };
     // pass 1: primary entries; width of the secondary table below every depth-kDecBits prefix
     for (uint32_t i = threadIdx.x; i < (1u << kDecBits); i += blockDim.x) s_w2[i] = 0u;
+    if (threadIdx.x == 0) s_maxlen = 0u;
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) {
         uint32_t depth;
         unsigned long long code;
-        if (!depth_code(i, depth, code)) continue;  // only the walk can reach it
         bool leaf = (a.node_sym[i] & 0x80000000u) != 0;
+        if (!depth_code(i, depth, code)) {  // only the walk can reach it
+            if (leaf) atomicMax(&s_maxlen, 255u);
+            continue;
+        }
+        if (leaf) atomicMax(&s_maxlen, depth);
         if (leaf && depth >= 1 && depth <= (uint32_t)kDecBits) {
             uint32_t lo = (uint32_t)(code << (kDecBits - depth));
             uint32_t hi = lo + (1u << (kDecBits - depth));
@@ -662,6 +669,7 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
     if (threadIdx.x == 0) {
         a.info[0] = 0;
         a.info[1] = 0;
+        a.info[2] = s_maxlen;
     }
 }
 
@@ -796,6 +804,152 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 // length, so the inner loop has no bounds test: a chunk must consume exactly its indexed length
 // (checked at the end), and reads stop 64 bits past it whatever the bits say.  Zero codes are
 // counted per chunk (outlier ranks for the reverse Lorenzo kernel).
+// ------------------------------------------------------------------------------------------
+// K4b': indexed decoder for trees whose codewords are at most kWinMaxLen (32) bits -- the table
+// builder records the longest one.  Lane j decodes chunk j (512 codewords from its indexed start
+// bit).  The lane holds a 96-bit window of its stream in three registers (w0 w1 w2, bit offset
+// `off` into w0) and decodes kWinRound codewords per round; a codeword moves the window by at
+// most one word, so the move and the ring read are predicated, not branched.  Words come from a
+// per-lane ring of kWinRing 16-byte blocks in shared memory that cp.async keeps filled ahead of
+// the window: one round reads at most kWinRound * 32 bits = 8 words, and the blocks holding them
+// have landed at the round's start.  The warp diverges only on codewords
+// longer than the primary table.  Decoded codes are packed in registers and stored 16 bytes per
+// lane per round.
+// ------------------------------------------------------------------------------------------
+constexpr int kWinMaxLen = 32;
+constexpr int kWinRound  = 8;
+constexpr int kWinRing   = 8;  // blocks of 16 bytes per lane
+
+__global__ void __launch_bounds__(256, 4) k_huff_decode_win(HuffDecodeArgs a) {
+    __shared__ uint32_t s_table[1 << kDecBits];
+    __shared__ __align__(16) uint4 s_ring[8][kWinRing][32];
+    if (!a.tree_info || a.tree_info[2] > (uint32_t)kWinMaxLen) return;  // uniform: k_huff_decode_idx's trees
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    __syncthreads();
+    if (*a.status != VSZ_OK) return;  // no block barrier below
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const size_t j      = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (j - lane >= a.nchunks) return;
+    const unsigned long long out0 = (unsigned long long)j * kChunkSyms;
+    uint32_t cnt = 0;
+    if (j < a.nchunks && out0 < a.n) cnt = (uint32_t)min((unsigned long long)kChunkSyms, a.n - out0);
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(a.payload) & 15u) * 8u;
+    const uint8_t* g16   = reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)15);
+    // readable bytes from g16: the payload plus the 8 bytes past its end that callers provide
+    const unsigned long long readable = base0 / 8u + (a.payload_bits + 7) / 8 + 8;
+    uint4* ring           = &s_ring[warp][0][lane];
+    const uint32_t* ringw = reinterpret_cast<const uint32_t*>(ring);  // word k of slot s: ringw[128 s + k]
+    auto fetch = [&](unsigned long long b) {  // block b into slot b % kWinRing, one commit group
+        const unsigned long long o = b * 16;
+        const uint32_t nb = o >= readable ? 0u : (uint32_t)min(16ull, readable - o);
+        cp_async16_zfill(ring + 32 * (uint32_t)(b % kWinRing), g16 + (nb ? o : 0), nb);
+        cp_async_commit();
+    };
+    auto ring_word = [&](unsigned long long w) -> uint32_t {
+        return bswap32(ringw[128u * ((uint32_t)(w >> 2) % kWinRing) + ((uint32_t)w & 3u)]);
+    };
+    bool bad = false;
+    unsigned long long cb = 0, wn = 0, breq = 0;
+    uint32_t off = 0;
+    if (cnt) {
+        const unsigned long long sb = a.start_bit[j];
+        cb = a.chunk_len[j];
+        if (sb + cb > a.payload_bits) bad = true;
+        const unsigned long long pos0 = base0 + sb;
+        off  = (uint32_t)(pos0 & 31u);
+        wn   = pos0 >> 5;  // next word to enter the window
+        breq = wn >> 2;
+    }
+    const bool live = cnt && !bad;
+    // blocks [wn / 4, wn / 4 + kWinRing - 1) stay requested: the slot a fetch overwrites held a
+    // block whose words entered the window at least one block earlier; with kWinRing / 2 groups
+    // allowed in flight, blocks wn / 4 .. + 2 (at least 9 words from wn) have landed
+    if (live)
+        for (int k = 0; k < kWinRing - 1; k++) fetch(breq++);
+    cp_async_wait<kWinRing / 2>();
+    uint32_t w0 = 0, w1 = 0, w2 = 0;
+    if (live) {
+        w0 = ring_word(wn);
+        w1 = ring_word(wn + 1);
+        w2 = ring_word(wn + 2);
+        wn += 3;
+    }
+    uint32_t used = 0, zeros = 0;
+    uint16_t* dst = a.codes + out0;
+    for (uint32_t r0 = 0; r0 < (uint32_t)kChunkSyms; r0 += kWinRound) {
+        const uint32_t m = (live && cnt > r0) ? min((uint32_t)kWinRound, cnt - r0) : 0u;
+        if (m) {
+            const unsigned long long bneed = (wn >> 2) + kWinRing - 1;
+            while (breq < bneed) fetch(breq++);
+        }
+        cp_async_wait<kWinRing / 2>();
+        uint32_t pk[kWinRound / 2] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int k = 0; k < kWinRound; k++) {
+            if ((uint32_t)k < m) {
+                const uint32_t win = __funnelshift_l(w1, w0, off);  // 32 bits from the current position
+                const uint32_t e   = s_table[win >> (32 - kDecBits)];
+                uint32_t len       = e & 0x7fu;
+                uint32_t sy        = e >> 8;
+                if (!len) {
+                    uint32_t node = e >> 8, usedb = kDecBits;
+                    if (e & 0x80u) {
+                        const uint32_t w2b = (e >> 8) & 0xfu;
+                        const uint32_t e2 =
+                            __ldg(&a.table2[(e >> 12) + ((win >> (32 - kDecBits - w2b)) & ((1u << w2b) - 1u))]);
+                        len   = e2 & 0xffu;
+                        sy    = e2 >> 8;
+                        node  = e2 >> 8;
+                        usedb = kDecBits + w2b;
+                    }
+                    if (!len) {
+                        // longer than both tables: walk the tree over a 64-bit view of the window
+                        unsigned long long v = ((((unsigned long long)w0) << 32) | w1) << off;
+                        if (off) v |= (unsigned long long)w2 >> (32 - off);
+                        sy = 0xffffffffu;
+                        if (node != 0 && node < a.max_nodes) {
+                            for (uint32_t d = usedb; d < (uint32_t)kWinMaxLen; d++) {
+                                node = __ldg(&a.child[2 * (size_t)node + (uint32_t)((v >> (63 - d)) & 1ull)]);
+                                if (node == 0 || node >= a.max_nodes) break;
+                                const uint32_t ns = __ldg(&a.node_sym[node]);
+                                if (ns & 0x80000000u) {
+                                    sy  = ns & 0xffffu;
+                                    len = d + 1;
+                                    break;
+                                }
+                            }
+                        }
+                        if (sy == 0xffffffffu) {
+                            bad = true;
+                            sy  = 0;
+                            len = 0;
+                        }
+                    }
+                }
+                pk[k >> 1] |= (sy & 0xffffu) << (16 * (k & 1));
+                zeros += (sy == 0u);
+                used += len;
+                off += len;
+                if (off >= 32u) {  // at most one word per codeword (len <= 32)
+                    off -= 32u;
+                    w0 = w1;
+                    w1 = w2;
+                    w2 = ring_word(wn);
+                    wn++;
+                }
+            }
+        }
+        if (m == (uint32_t)kWinRound) {
+            *reinterpret_cast<uint4*>(dst + r0) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        } else {
+            for (uint32_t k = 0; k < m; k++) dst[r0 + k] = (uint16_t)(pk[k >> 1] >> (16 * (k & 1)));
+        }
+    }
+    cp_async_wait<0>();  // no copy into this CTA's shared memory may outlive it
+    if (cnt && (bad || used != cb)) set_status(a.status, VSZ_ERR_CORRUPT);  // must fill exactly its length
+    if (j < a.nchunks && a.chunk_zero) a.chunk_zero[j] = zeros;
+}
+
 constexpr int kDecRound = 16;                 // codes per lane staged before the coalesced store
 constexpr int kDecParts = kDecRound / 8;      // 16-byte pieces per staged row
 
@@ -810,6 +964,7 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
         for (uint32_t i = threadIdx.x; i < a.nodes; i += blockDim.x) s_walk[i] = a.walk[i];
     __syncthreads();
     if (*a.status != VSZ_OK) return;
+    if (a.tree_info && a.tree_info[2] <= (uint32_t)kWinMaxLen) return;  // k_huff_decode_win's trees
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const size_t j      = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const size_t jw0    = j - lane;  // first chunk of this warp
@@ -1175,6 +1330,10 @@ int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
     const bool indexed = !a.out_begin && !a.nsym && a.chunk_syms == (uint32_t)kChunkSyms &&
                          (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0 && a.chunk_len;
     if (indexed) {
+        if (a.tree_info) {
+            k_huff_decode_win<<<grid, 256, 0, st>>>(a);
+            count_launch();
+        }
         if (a.walk_smem) {
             size_t smem = (size_t)a.nodes * 4;
             static std::atomic<unsigned long long> attr{0};

@@ -403,6 +403,7 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     da.walk = w.walk;
     da.nodes = node_count;
     da.walk_smem = (dict <= 16384 && node_count < 32768u) ? 1 : 0;
+    da.tree_info = w.tinfo;
     da.status = w.status;
     if (chunk_bits) {
         {

@@ -81,7 +81,7 @@ struct HuffTableArgs {
     uint32_t* walk;       // max_nodes: both children of an internal node, 16 bits each:
                           // 0x8000 | symbol for a leaf, else the node index (dict <= 16384)
     uint32_t* table2;     // table2_capacity(max_nodes) secondary entries
-    uint32_t* info;       // [0] single-symbol tree flag [1] its symbol
+    uint32_t* info;       // [0] single-symbol tree flag [1] its symbol [2] longest codeword (255: > 64)
     int* status;
 };
 
@@ -107,6 +107,7 @@ struct HuffDecodeArgs {
     uint32_t* seg_zero;                   // zero codes per 256-wide row segment (may be null)
     uint32_t d0, nxs;
     uint32_t max_nodes;                   // node indices past this are a corrupt tree
+    const uint32_t* tree_info;            // k_huff_table's info ([2] longest codeword), or null
     int* status;
 };
 
