@@ -256,3 +256,24 @@ def test_long_codewords_match_oracle(cuda):
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y_or.view(np.uint32))  # indexed
     y = V.decompress(a_or, len(a_or), 0, 65536, 8)                                          # self-sync
     np.testing.assert_array_equal(y.view(np.uint32), y_or.view(np.uint32))
+
+
+@pytest.mark.parametrize("seed", [0, 4, 9, 14, 19])
+def test_general_kernels_match_oracle(cuda, monkeypatch, seed):
+    """The general indexed Huffman decoder (taken by trees with codewords over 32 bits) and the
+    general reverse-Lorenzo kernel, forced on fields the fast kernels would otherwise take."""
+    monkeypatch.setenv("VSZ_DECODE_NO_WINDOW", "1")
+    monkeypatch.setenv("VSZ_FORCE_GENERAL_DECOMPRESS", "1")
+    dims, bs, dct, eb, r2r, x = _random_case(seed)
+    if r2r and O.value_range(x) == 0:
+        r2r = False
+    a_or, _ = O.compress(x, dims, bs, dct, eb, r2r)
+    c = V.compress(x, dims, eb, "r2r" if r2r else "abs", dct, bs)
+    assert c.data[: c.data_size] == a_or
+    y_or = O.decompress(a_or, bs, dct, O.value_range(x) if r2r else 0.0)
+    np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y_or.view(np.uint32))
+
+
+def test_long_codewords_general_decoder(cuda, monkeypatch):
+    monkeypatch.setenv("VSZ_DECODE_NO_WINDOW", "1")
+    test_long_codewords_match_oracle(cuda)

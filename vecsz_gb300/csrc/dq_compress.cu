@@ -230,50 +230,65 @@ __device__ __forceinline__ float prequant_at(float v, uint32_t col, uint32_t xta
     return prequant_vec(v, r_f);
 }
 
-// Load and prequantize 4 consecutive columns [xb, xb+4) of one row; zero outside the field.
-template <int NDIM, bool VEC, bool TAIL>
-__device__ __forceinline__ void load_row(const DqArgs& a, const float* rowp, bool row_in, uint32_t xb, float r_f,
-                                         double r_d, float S[4]) {
-    float v[4] = {0.f, 0.f, 0.f, 0.f};
-    if (row_in) {
-        if (VEC) {
-            if (xb < a.d0) {
-                float4 t = __ldcs(reinterpret_cast<const float4*>(rowp + xb));
-                v[0] = t.x;
-                v[1] = t.y;
-                v[2] = t.z;
-                v[3] = t.w;
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-                if (xb + j < a.d0) v[j] = __ldcs(rowp + xb + j);
-        }
+// Raw values of 4 consecutive columns [xb, xb+4) of one row (zeros outside the field).
+template <bool VEC>
+__device__ __forceinline__ float4 load_raw(const DqArgs& a, size_t row, bool row_in, uint32_t xb) {
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!row_in) return v;
+    const float* rowp = a.x + row * a.d0;
+    if (VEC) {
+        if (xb < a.d0) v = __ldcs(reinterpret_cast<const float4*>(rowp + xb));
+    } else {
+        if (xb < a.d0) v.x = __ldcs(rowp + xb);
+        if (xb + 1 < a.d0) v.y = __ldcs(rowp + xb + 1);
+        if (xb + 2 < a.d0) v.z = __ldcs(rowp + xb + 2);
+        if (xb + 3 < a.d0) v.w = __ldcs(rowp + xb + 3);
     }
+    return v;
+}
+
+// Prequantized values of a raw row; zero outside the field.
+template <int NDIM, bool TAIL>
+__device__ __forceinline__ void prequant_row(const DqArgs& a, float4 v, bool row_in, uint32_t xb, float r_f, double r_d,
+                                             float S[4]) {
+    const float t[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        bool in = row_in && (xb + j < a.d0);
-        S[j]    = in ? prequant_at<NDIM, TAIL>(v[j], xb + j, a.xtail, r_f, r_d) : 0.0f;
+        const bool in = row_in && (xb + j < a.d0);
+        S[j]          = in ? prequant_at<NDIM, TAIL>(t[j], xb + j, a.xtail, r_f, r_d) : 0.0f;
     }
 }
 
+// 2D / 3D.  Work unit = one warp tile: 128 consecutive x (4 per lane) by 8 rows (y) by one
+// Lorenzo block of planes (z).  Rows are processed one at a time (the next row's values are
+// loaded while the current one is coded); a lane keeps in registers only its 4 values of the
+// current row and of the row above, in this plane and in the previous one.  The previous plane's
+// 8 rows live in shared memory [row][column][lane] (conflict-free), each row overwritten by the
+// current plane's once it has been used.  x - 1 neighbours come from the lane to the left.
 template <int NDIM, int BS, bool VEC, bool TAIL>
-__global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
-    extern __shared__ uint32_t s_hist_dyn[];
-    uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
+__global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
+    typedef float PrevRows[8][4][32];
+    PrevRows* s_prev = reinterpret_cast<PrevRows*>(s_dyn + (a.smem_hist ? ((a.dict + 3) & ~3) : 0));
     const Consts c   = *a.consts;
     if (c.status != VSZ_OK) return;  // uniform across the grid
     if (s_hist) {
         for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
         __syncthreads();
     }
-    const float r_f   = c.r_f;
-    const double r_d  = c.r_d;
-    const float Rf    = (float)a.R;
+    const float r_f     = c.r_f;
+    const double r_d    = c.r_d;
+    const float Rf      = (float)a.R;
     const unsigned lane = lane_id();
+    const unsigned wib  = threadIdx.x >> 5;
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + wib;
     const bool xbound = ((lane * 4) % BS) == 0;  // my first column starts a Lorenzo block
+    auto left = [&](float v) {                   // x - 1 neighbour of my first column
+        const float t = __shfl_up_sync(0xffffffffu, v, 1);
+        return xbound ? 0.f : t;
+    };
     HistAcc h;
 
     for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
@@ -287,63 +302,58 @@ __global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
         const uint32_t z0 = (NDIM == 3) ? zb * BS : 0;
         const int nz      = (NDIM == 3) ? (int)min((uint32_t)BS, a.d2 - z0) : 1;
 
-        float P[8][4], Ph[4], PL[8], PhL = 0.f;  // previous plane (3D): rows, halo row, x - 1 column
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            PL[i] = 0.f;
-#pragma unroll
-            for (int j = 0; j < 4; j++) P[i][j] = 0.f;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++) Ph[j] = 0.f;
-
+        float Ph[4] = {0.f, 0.f, 0.f, 0.f}, PhL = 0.f;  // previous plane's halo row (y0 - 1)
+        float4 nxt = load_raw<VEC>(a, (size_t)z0 * a.d1 + y0, y0 < a.d1, xb);
         for (int zz = 0; zz < nz; zz++) {
             const uint32_t z = z0 + zz;
-            float S[8][4], Sh[4], SL[8], ShL;
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                const uint32_t y = y0 + i;
-                const bool row_in = y < a.d1;
-                const float* rowp = a.x + ((size_t)z * a.d1 + y) * a.d0;
-                load_row<NDIM, VEC, TAIL>(a, rowp, row_in, xb, r_f, r_d, S[i]);
-            }
+            const bool zp    = zz > 0;  // a previous plane inside the block
+            float Sp[4] = {0.f, 0.f, 0.f, 0.f}, SpL = 0.f;  // row above, this plane (halo row at i = 0)
             if (yhalo) {
-                const float* rowp = a.x + ((size_t)z * a.d1 + (y0 - 1)) * a.d0;
-                load_row<NDIM, VEC, TAIL>(a, rowp, true, xb, r_f, r_d, Sh);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 4; j++) Sh[j] = 0.f;
+                prequant_row<NDIM, TAIL>(a, load_raw<VEC>(a, (size_t)z * a.d1 + (y0 - 1), true, xb), true, xb, r_f,
+                                         r_d, Sp);
+                SpL = left(Sp[3]);
             }
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                SL[i] = __shfl_up_sync(0xffffffffu, S[i][3], 1);
-                if (xbound) SL[i] = 0.f;
-            }
-            ShL = __shfl_up_sync(0xffffffffu, Sh[3], 1);
-            if (xbound) ShL = 0.f;
-
-#pragma unroll
+            const float ShNext[4] = {Sp[0], Sp[1], Sp[2], Sp[3]};
+            const float ShNextL   = SpL;
+            float Pp[4] = {Ph[0], Ph[1], Ph[2], Ph[3]}, PpL = PhL;  // row above, previous plane
+#pragma unroll 2
             for (int i = 0; i < 8; i++) {
                 const uint32_t y  = y0 + i;
                 const bool row_in = y < a.d1;
+                const float4 raw  = nxt;
+                {  // the next row of this plane, or the first row of the next plane
+                    const bool last_row = (i == 7);
+                    const uint32_t zn = last_row ? z + 1 : z, yn = last_row ? y0 : y + 1;
+                    const bool more = !last_row || zz + 1 < nz;
+                    nxt = more ? load_raw<VEC>(a, (size_t)zn * a.d1 + yn, yn < a.d1, xb) : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                float S[4];
+                prequant_row<NDIM, TAIL>(a, raw, row_in, xb, r_f, r_d, S);
+                const float SL = left(S[3]);
+                float Pc[4] = {0.f, 0.f, 0.f, 0.f}, PcL = 0.f;  // this row, previous plane
+                if (NDIM == 3) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) Pc[j] = zp ? s_prev[wib][i][j][lane] : 0.f;
+                    PcL = left(Pc[3]);
+                }
                 int code[4];
                 float outv[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const uint32_t col = xb + j;
-                    const float cur    = S[i][j];
-                    const float X      = j ? S[i][j - 1] : SL[i];
-                    const float Y      = i ? S[i - 1][j] : Sh[j];
-                    const float XY     = i ? (j ? S[i - 1][j - 1] : SL[i - 1]) : (j ? Sh[j - 1] : ShL);
+                    const float cur    = S[j];
+                    const float X      = j ? S[j - 1] : SL;
+                    const float Y      = Sp[j];
+                    const float XY     = j ? Sp[j - 1] : SpL;
                     const bool tail    = TAIL && col >= a.xtail;
                     float pred;
                     if (NDIM == 2) {
                         pred = __fadd_rn(X, __fsub_rn(Y, XY));  // W + (N - NW)
                     } else {
-                        const float Z   = P[i][j];
-                        const float XZ  = j ? P[i][j - 1] : PL[i];
-                        const float YZ  = i ? P[i - 1][j] : Ph[j];
-                        const float XYZ = i ? (j ? P[i - 1][j - 1] : PL[i - 1]) : (j ? Ph[j - 1] : PhL);
+                        const float Z   = Pc[j];
+                        const float XZ  = j ? Pc[j - 1] : PcL;
+                        const float YZ  = Pp[j];
+                        const float XYZ = j ? Pp[j - 1] : PpL;
                         if (!tail) {
                             float dist1 = __fadd_rn(X, __fadd_rn(Y, Z));
                             float dist2 = __fadd_rn(XY, __fadd_rn(XZ, YZ));
@@ -353,28 +363,31 @@ __global__ void __launch_bounds__(256, 2) k_dq_compress_23d(DqArgs a) {
                                              Z);
                         }
                     }
-                    const float e  = __fsub_rn(cur, pred);
-                    const bool q   = fabsf(e) < Rf;
-                    code[j]        = q ? (int)__fadd_rn(e, Rf) : 0;
-                    outv[j]        = cur;
+                    const float e = __fsub_rn(cur, pred);
+                    const bool q  = fabsf(e) < Rf;
+                    code[j]       = q ? (int)__fadd_rn(e, Rf) : 0;
+                    outv[j]       = cur;
                     if (NDIM == 2 && tail) {
                         code[j] = 0;
                         outv[j] = 0.0f;
                     }
                 }
                 emit_row<VEC>(a, (size_t)z * a.d1 + y, xb, xt, row_in, code, outv, h, s_hist);
-            }
-            if (NDIM == 3) {
+                if (NDIM == 3) {
 #pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    PL[i] = SL[i];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) P[i][j] = S[i][j];
+                    for (int j = 0; j < 4; j++) s_prev[wib][i][j][lane] = S[j];  // row i of plane z
                 }
 #pragma unroll
-                for (int j = 0; j < 4; j++) Ph[j] = Sh[j];
-                PhL = ShL;
+                for (int j = 0; j < 4; j++) {
+                    Sp[j] = S[j];
+                    Pp[j] = Pc[j];
+                }
+                SpL = SL;
+                PpL = PcL;
             }
+#pragma unroll
+            for (int j = 0; j < 4; j++) Ph[j] = ShNext[j];
+            PhL = ShNextL;
         }
     }
     h.flush(a.R, s_hist, a.dict, a.hist);
@@ -413,7 +426,8 @@ __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
 #pragma unroll
         for (int t = 0; t < U; t++) {
             const uint32_t xt = (uint32_t)(u * U + t);
-            load_row<1, VEC, false>(a, a.x, xt < a.nxt, xt * kTileX + lane * 4, r_f, 0.0, S[t]);
+            const uint32_t xb = xt * kTileX + lane * 4;
+            prequant_row<1, false>(a, load_raw<VEC>(a, 0, xt < a.nxt, xb), xt < a.nxt, xb, r_f, 0.0, S[t]);
         }
 #pragma unroll
         for (int t = 0; t < U; t++) {
@@ -576,10 +590,18 @@ template <int NDIM, int BS>
 static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
     // tail columns exist only when d0 % 8 != 0 (and then never with 16-byte rows)
     const bool tail = (a.d0 % 8) != 0;
-    if (vec && !tail) k_dq_compress_23d<NDIM, BS, true, false><<<grid, 256, smem, st>>>(a);
-    else if (vec) k_dq_compress_23d<NDIM, BS, true, true><<<grid, 256, smem, st>>>(a);
-    else if (!tail) k_dq_compress_23d<NDIM, BS, false, false><<<grid, 256, smem, st>>>(a);
-    else k_dq_compress_23d<NDIM, BS, false, true><<<grid, 256, smem, st>>>(a);
+    // dynamic shared memory: [histogram, padded to 16 bytes][3D: previous plane, 8 warps x 4 KB]
+    if (a.smem_hist) smem = (size_t)((a.dict + 3) & ~3) * sizeof(uint32_t);
+    if (NDIM == 3) smem += 8 * 8 * 4 * 32 * sizeof(float);
+    static std::atomic<unsigned long long> attr[4];
+    auto go = [&](auto kern, int which) {
+        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[which]);
+        kern<<<grid, 256, smem, st>>>(a);
+    };
+    if (vec && !tail) go(k_dq_compress_23d<NDIM, BS, true, false>, 0);
+    else if (vec) go(k_dq_compress_23d<NDIM, BS, true, true>, 1);
+    else if (!tail) go(k_dq_compress_23d<NDIM, BS, false, false>, 2);
+    else go(k_dq_compress_23d<NDIM, BS, false, true>, 3);
     count_launch();
 }
 
@@ -614,7 +636,7 @@ int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms)
     if (a.nunits == 0) return VSZ_OK;
     size_t smem = a.smem_hist ? (size_t)a.dict * sizeof(uint32_t) : 0;
     long long want = (long long)((a.nunits + 7) / 8);
-    long long cap = (long long)num_sms * 8; int grid = (int)(want < cap ? want : cap);
+    long long cap = (long long)num_sms * 16; int grid = (int)(want < cap ? want : cap);
     if (grid < 1) grid = 1;
     int rc;
     if (ndim == 1) rc = dispatch_bs<1>(a, bs, vec, grid, smem, st);

@@ -403,7 +403,9 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
     da.walk = w.walk;
     da.nodes = node_count;
     da.walk_smem = (dict <= 16384 && node_count < 32768u) ? 1 : 0;
-    da.tree_info = w.tinfo;
+    // the window decoder takes trees whose codewords are at most 32 bits; VSZ_DECODE_NO_WINDOW
+    // sends every tree to the general indexed decoder (tests of that path)
+    da.tree_info = getenv("VSZ_DECODE_NO_WINDOW") ? nullptr : w.tinfo;
     da.status = w.status;
     if (chunk_bits) {
         {
@@ -1075,7 +1077,11 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
                          d->has_trailer ? d->n_chunks : 0, d->chunk_syms, w, idx ? nullptr : w.seg_zero, g.d0, st));
     // outlier ranks: per 512-code chunk from the indexed decoder (block size 8), else per 256-wide
     // row segment
-    const bool chunk_rank = idx != nullptr && bs == 8 && d->node_count > 1;
+    // VSZ_FORCE_GENERAL_DECOMPRESS: the general reverse-Lorenzo kernel for every block size (tests
+    // of that path); it ranks outliers by row segment only
+    const bool force_general = getenv("VSZ_FORCE_GENERAL_DECOMPRESS") != nullptr;
+    // the block-8 kernel ranks outliers from the decoder's per-chunk zero counts directly
+    const bool chunk_rank = idx != nullptr && bs == 8 && d->node_count > 1 && !force_general;
     {
         StageTimer t(kStZeroScan, st);
         if (chunk_rank) {
@@ -1108,7 +1114,6 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.d2 = g.d2;
     a.n = g.n;
     a.R = dict / 2;
-    bool force_general = getenv("VSZ_FORCE_GENERAL_DECOMPRESS") != nullptr;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));
