@@ -174,18 +174,20 @@ def stage_profile(V):
 
 
 def algorithmic_bytes(stage, n, res, desc):
-    """Bytes a stage must move per launch (reads + writes of its inputs and outputs)."""
+    """Bytes a stage must move per launch: reads + writes of its inputs and outputs (n elements,
+    nch = 512-code chunks of the decode index, nseg = 128-wide row segments of the gather)."""
     nseg = desc["nseg128"]
-    nsegd = desc["nseg256"]
+    nch = (n + 511) // 512
     nout = res.n_outlier
     payload = (res.payload_bits + 7) // 8
     table = {
-        "eb_setup": 4 * n,                                       # min/max pass (r2r)
-        "dualquant": 4 * n + 2 * n + nseg + 4 * nout,            # field in; codes, counts, outliers out
-        "huff_encode": 2 * n + payload + 2 * ((n + 511) // 512),  # codes in; bitstream + index out
+        "eb_setup": 4 * n,                                         # min/max pass (r2r)
+        "dualquant": 4 * n + 2 * n + nseg + 4 * nout,              # field in; codes, counts, outliers out
+        "huff_count": 2 * n + 2 * nch + 2 * nch + 8 * nch,         # codes in; chunk bits; their scan
+        "huff_pack": 2 * n + 8 * nch + payload + 24 * nch,         # codes, offsets in; bitstream, edges out
         "outlier_gather": nseg + 8 * nout,
-        "huff_decode": payload + 2 * n + 4 * nsegd,              # bitstream in; codes, zero counts out
-        "lorenzo_decompress": 2 * n + 4 * n + 4 * nout + 8 * nsegd,  # codes + outliers in; field out
+        "huff_decode": payload + 10 * nch + 2 * n + 4 * nch,       # bitstream, index in; codes, zero counts out
+        "lorenzo_decompress": 2 * n + 4 * nout + 8 * nch + 4 * n,  # codes, outliers, ranks in; field out
     }
     return table.get(stage)
 

@@ -16,6 +16,7 @@
 #include "scan.cuh"
 #include "vsz_device.cuh"
 #include "vsz_huffman.h"
+#include "vsz_profile.h"
 
 namespace vsz {
 
@@ -1304,17 +1305,23 @@ int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
     smem_limit_once(k_huff_pack, 8 * kEncWarpWords * 4 + 64 * 1024 + 1024, attr_pack);
     smem_limit_once(k_huff_count, 64 * 1024 + 1024, attr_count);
     const long long blocks = (long long)((a.nchunks + 7) / 8);
-    int grid = (int)min(blocks, (long long)num_sms * 8);
-    k_huff_count<<<grid, kEncThreads, a.cb_in_smem ? (size_t)a.dict : 0, st>>>(a);
-    count_launch();
-    int rc = launch_scan_u16(a.chunk_bits, a.chunk_off, a.nchunks, a.scan_status, a.scan_counter, a.total_bits,
-                             a.status, st);
-    if (rc) return rc;
-    int pgrid = (int)min(blocks, (long long)num_sms * 4);
-    k_huff_pack<<<pgrid, kEncThreads, smem, st>>>(a);
-    count_launch();
-    k_huff_encode_edges<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a);
-    count_launch();
+    {
+        StageTimer t(kStHuffCount, st);
+        int grid = (int)min(blocks, (long long)num_sms * 8);
+        k_huff_count<<<grid, kEncThreads, a.cb_in_smem ? (size_t)a.dict : 0, st>>>(a);
+        count_launch();
+        int rc = launch_scan_u16(a.chunk_bits, a.chunk_off, a.nchunks, a.scan_status, a.scan_counter, a.total_bits,
+                                 a.status, st);
+        if (rc) return rc;
+    }
+    {
+        StageTimer t(kStHuffPack, st);
+        int pgrid = (int)min(blocks, (long long)num_sms * 4);
+        k_huff_pack<<<pgrid, kEncThreads, smem, st>>>(a);
+        count_launch();
+        k_huff_encode_edges<<<(unsigned)((a.nchunks + 255) / 256), 256, 0, st>>>(a);
+        count_launch();
+    }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 

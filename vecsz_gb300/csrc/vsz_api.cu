@@ -896,10 +896,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     he.edge_bits = w.e_edge_bits;
     he.status = w.status;
     he.build_info = w.build_info;
-    {
-        StageTimer t(kStHuffEncode, st);
-        VSZ_TRY(launch_huff_encode(he, st, num_sms()));
-    }
+    VSZ_TRY(launch_huff_encode(he, st, num_sms()));  // stages huff_count, huff_pack
     // 5. outliers after the bitstream, in row-major order
     GatherArgs ga{};
     ga.seg_count = w.seg_count;

@@ -20,9 +20,10 @@ struct Pair {
 std::vector<Pair> g_pairs;
 double g_ms[kStCount];
 int g_cnt[kStCount];
-const char* g_names[kStCount] = {"eb_setup",        "dualquant",     "huff_build", "huff_encode",
-                                 "outlier_gather",  "finalize",      "dec_table",  "dec_index_scan",
-                                 "huff_decode",     "zero_scan",     "outlier_copy", "lorenzo_decompress"};
+const char* g_names[kStCount] = {"eb_setup",       "dualquant",   "huff_build",     "huff_count",
+                                 "huff_pack",      "outlier_gather", "finalize",    "dec_table",
+                                 "dec_index_scan", "huff_decode",  "zero_scan",      "outlier_copy",
+                                 "lorenzo_decompress"};
 }  // namespace
 
 bool profile_on() { return g_on; }

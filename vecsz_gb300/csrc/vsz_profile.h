@@ -8,7 +8,8 @@ enum Stage {
     kStEbSetup = 0,
     kStDualquant,
     kStHuffBuild,
-    kStHuffEncode,
+    kStHuffCount,
+    kStHuffPack,
     kStOutlierGather,
     kStFinalize,
     kStDecTable,
