@@ -212,6 +212,34 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
                         size_t ws_bytes, uint8_t* d_archive, size_t archive_capacity, uint64_t* d_result,
                         void* stream);
 
+/* ---- many fields at once -------------------------------------------------------------------
+ * A batch of fields of any shapes, dimensionalities, error bounds and dictionary sizes is
+ * compressed in a handful of launches: each stage is one launch (one per kernel class for the
+ * dual-quant stage) over a device-side table of per-field arguments and a list of block-wide
+ * tasks, and the Huffman trees are built on the device, one CTA per field.  Every field's archive
+ * and result are byte-identical to vsz_compress of that field alone.  No counterpart in the
+ * reference, which compresses one field per process.
+ *
+ * vsz_batch_create lays out the caller's workspace (vsz_batch_workspace_bytes), resolves every
+ * pointer and uploads the tables once (synchronous; it allocates the tables).  vsz_batch_compress
+ * then only enqueues device work on `stream` -- memsets and launches, no host synchronisation and no
+ * allocation -- so it may be captured in a CUDA graph and replayed; each replay recompresses the
+ * current contents of the fields' input buffers.  d_results: 8 u64 (vsz_result) per field. */
+typedef struct vsz_batch_field {
+    const float* d_in;     /* device field */
+    int ndim;
+    size_t dims[3];
+    vsz_params params;     /* lossless is ignored: the batch writes packed blocks */
+    uint8_t* d_archive;    /* device output of at least vsz_compress_bounds' archive capacity */
+    size_t archive_capacity;
+} vsz_batch_field;
+typedef struct vsz_batch vsz_batch;
+vsz_status vsz_batch_workspace_bytes(const vsz_batch_field* fields, int nfields, size_t* ws_bytes);
+vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_ws, size_t ws_bytes,
+                            uint64_t* d_results, vsz_batch** batch);
+vsz_status vsz_batch_compress(vsz_batch* batch, void* stream);
+void vsz_batch_destroy(vsz_batch* batch);
+
 /* Parse a packed block (+ optional trailer) held in host memory. */
 vsz_status vsz_archive_parse(const uint8_t* h_archive, size_t len, vsz_archive_desc* desc);
 vsz_status vsz_decompress_bounds(const vsz_archive_desc* desc, const vsz_decompress_opts* opts, size_t* ws_bytes);

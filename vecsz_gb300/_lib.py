@@ -43,6 +43,11 @@ class Params(C.Structure):
                 ("lossless", C.c_int)]
 
 
+class BatchField(C.Structure):
+    _fields_ = [("d_in", C.c_void_p), ("ndim", C.c_int), ("dims", C.c_size_t * 3), ("params", Params),
+                ("d_archive", C.c_void_p), ("archive_capacity", C.c_size_t)]
+
+
 class Result(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("data_size", "trailer_size", "n_outlier", "huff_bytes", "payload_bits",
                                           "status", "max_code_len", "node_count")]
@@ -83,6 +88,10 @@ _PROTOS = {
     "vsz_huffman_build_host": ([_p, _i, _p, _p, _p], _i),
     "vsz_set_tree_builder": ([_i], _i),
     "vsz_launch_count": ([], C.c_uint64),
+    "vsz_batch_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t)], _i),
+    "vsz_batch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
+    "vsz_batch_compress": ([_p, _p], _i),
+    "vsz_batch_destroy": ([_p], None),
     "vsz_huffman_encode_tmp_bytes": ([_sz], _sz),
     "vsz_huffman_encode": ([_p, _sz, _p, _i, _p, _p, _p, _p, _sz, _p], _i),
     "vsz_huffman_decode_tmp_bytes": ([_sz, _sz, _i], _sz),

@@ -166,6 +166,69 @@ class DeviceCodec:
         return int(self._dstatus.item())
 
 
+class BatchCompressor:
+    """Many device fields compressed in one launch sequence (vsz_batch_*).
+
+    fields: list of dicts {"x": CUDA float32 tensor, "dims": dims, "eb", "mode", "dict_size",
+    "block_size"}.  The archives land in per-field uint8 tensors (self.archives[i]); compress()
+    may be called repeatedly (or captured in a CUDA graph) and recompresses the current inputs."""
+
+    def __init__(self, fields, device="cuda"):
+        torch = _torch()
+        from ._lib import BatchField
+        self.n = len(fields)
+        self.fields = fields
+        arr = (BatchField * self.n)()
+        self.archives = []
+        for i, f in enumerate(fields):
+            dims = tuple(int(v) for v in f["dims"])
+            p = make_params(f.get("eb", 1e-4), f.get("mode", "abs"), f.get("dict_size", 1024), f.get("block_size", 8))
+            ws, cap = C.c_size_t(0), C.c_size_t(0)
+            check(lib().vsz_compress_bounds(C.byref(p), len(dims), dims_arg(dims), C.byref(ws), C.byref(cap)),
+                  "compress_bounds")
+            a = torch.zeros(cap.value + 64, dtype=torch.uint8, device=device)
+            self.archives.append(a)
+            arr[i].d_in = _ptr(f["x"]).value
+            arr[i].ndim = len(dims)
+            arr[i].dims = dims_arg(dims)
+            arr[i].params = p
+            arr[i].d_archive = _ptr(a).value
+            arr[i].archive_capacity = cap.value
+        self._arr = arr
+        ws = C.c_size_t(0)
+        check(lib().vsz_batch_workspace_bytes(arr, self.n, C.byref(ws)), "batch_workspace_bytes")
+        self.ws = torch.empty(ws.value, dtype=torch.uint8, device=device)
+        self.results = torch.zeros(8 * self.n, dtype=torch.int64, device=device)
+        h = C.c_void_p(0)
+        check(lib().vsz_batch_create(arr, self.n, _ptr(self.ws), self.ws.numel(), _ptr(self.results), C.byref(h)),
+              "batch_create")
+        self._h = h
+
+    def compress(self, stream=None) -> None:
+        check(lib().vsz_batch_compress(self._h, _stream_ptr(stream)), "batch_compress")
+
+    def result(self, i) -> Result:
+        r = self.results[8 * i: 8 * i + 8].cpu().numpy().view(np.uint64)
+        return Result(*[int(v) for v in r])
+
+    def archive_bytes(self, i) -> bytes:
+        r = self.result(i)
+        if r.status != 0:
+            raise VszError(int(r.status), f"batch field {i}")
+        return self.archives[i][: r.data_size + r.trailer_size].cpu().numpy().tobytes()
+
+    def close(self) -> None:
+        if self._h:
+            lib().vsz_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------------------------------------
 # Stage-level calls on torch CUDA tensors (one per reference routine)
 # ------------------------------------------------------------------------------------------------

@@ -92,9 +92,8 @@ __global__ void __launch_bounds__(256) k_minmax(const float* __restrict__ x, siz
 // Error-bound constants (one thread).  For r2r: range = (double)((float)max - (float)min), with
 // std::max_element's rule that a NaN first element wins; a zero range is VSZ_ERR_RANGE, as the
 // reference exits there (src/types.cc:49-56).
-__global__ void k_consts(int mode, double eb, const uint32_t* __restrict__ mm, const float* __restrict__ x,
-                         Consts* __restrict__ c, int* status_word) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void consts_of(int mode, double eb, const uint32_t* __restrict__ mm,
+                                          const float* __restrict__ x, Consts* __restrict__ c, int* status_word) {
     double ebf   = eb;
     double range = 0.0;
     int status   = VSZ_OK;
@@ -129,6 +128,12 @@ __global__ void k_consts(int mode, double eb, const uint32_t* __restrict__ mm, c
     c->dq_fast = normal(ch) && (cl == 0.0f || normal(cl));
     c->status  = status;
     if (status != VSZ_OK && status_word) set_status(status_word, status);
+}
+
+__global__ void k_consts(int mode, double eb, const uint32_t* __restrict__ mm, const float* __restrict__ x,
+                         Consts* __restrict__ c, int* status_word) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    consts_of(mode, eb, mm, x, c, status_word);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -265,33 +270,37 @@ __device__ __forceinline__ void prequant_row(const DqArgs& a, float4 v, bool row
 // current row and of the row above, in this plane and in the previous one.  The previous plane's
 // 8 rows live in shared memory [row][column][lane] (conflict-free), each row overwritten by the
 // current plane's once it has been used.  x - 1 neighbours come from the lane to the left.
-template <int NDIM, int BS, bool VEC, bool TAIL>
-__global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
-    extern __shared__ __align__(16) uint32_t s_dyn[];
-    uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
-    typedef float PrevRows[8][4][32];
-    PrevRows* s_prev = reinterpret_cast<PrevRows*>(s_dyn + (a.smem_hist ? ((a.dict + 3) & ~3) : 0));
-    const Consts c   = *a.consts;
-    if (c.status != VSZ_OK) return;  // uniform across the grid
+typedef float PrevRows[8][4][32];
+
+// The histogram share of a block: the threads' private hot-code counters into shared memory, then
+// shared memory into the field's histogram.
+__device__ __forceinline__ void hist_flush_block(const DqArgs& a, uint32_t* s_hist, HistAcc& h) {
+    h.flush(a.R, s_hist, a.dict, a.hist);
     if (s_hist) {
-        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
         __syncthreads();
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
+            uint32_t v = s_hist[i];
+            if (v) atomicAdd(&a.hist[i], (unsigned long long)v);
+        }
     }
+}
+
+// Warp units u0, u0 + ustep, ... < u1 of one field.
+template <int NDIM, int BS, bool VEC, bool TAIL>
+__device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, unsigned long long u0,
+                                           unsigned long long u1, unsigned long long ustep, uint32_t* s_hist,
+                                           PrevRows* s_prev, HistAcc& h) {
     const float r_f     = c.r_f;
     const double r_d    = c.r_d;
     const float Rf      = (float)a.R;
     const unsigned lane = lane_id();
     const unsigned wib  = threadIdx.x >> 5;
-    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + wib;
-    const bool xbound = ((lane * 4) % BS) == 0;  // my first column starts a Lorenzo block
-    auto left = [&](float v) {                   // x - 1 neighbour of my first column
+    const bool xbound   = ((lane * 4) % BS) == 0;  // my first column starts a Lorenzo block
+    auto left = [&](float v) {                     // x - 1 neighbour of my first column
         const float t = __shfl_up_sync(0xffffffffu, v, 1);
         return xbound ? 0.f : t;
     };
-    HistAcc h;
-
-    for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
+    for (unsigned long long u = u0; u < u1; u += ustep) {
         const uint32_t xt = (uint32_t)(u % a.nxt);
         const unsigned long long r = u / a.nxt;
         const uint32_t yg = (uint32_t)(r % a.nyg);
@@ -390,13 +399,48 @@ __global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
             PhL = ShNextL;
         }
     }
-    h.flush(a.R, s_hist, a.dict, a.hist);
+}
+
+template <int NDIM, int BS, bool VEC, bool TAIL>
+__global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
+    PrevRows* s_prev = reinterpret_cast<PrevRows*>(s_dyn + (a.smem_hist ? ((a.dict + 3) & ~3) : 0));
+    const Consts c   = *a.consts;
+    if (c.status != VSZ_OK) return;  // uniform across the grid
     if (s_hist) {
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
         __syncthreads();
-        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
-            uint32_t v = s_hist[i];
-            if (v) atomicAdd(&a.hist[i], (unsigned long long)v);
+    }
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    HistAcc h;
+    dq23_units<NDIM, BS, VEC, TAIL>(a, c, warp0, a.nunits, warps_total, s_hist, s_prev, h);
+    hist_flush_block(a, s_hist, h);
+}
+
+// Many fields in one launch: block-wide tasks (one field, a range of its warp units) taken in
+// grid-stride order.  hist_words = shared-memory histogram words reserved before the planes.
+template <int NDIM, int BS, bool VEC, bool TAIL>
+__global__ void __launch_bounds__(256, 3)
+    k_dq_compress_23d_batch(const DqArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks,
+                            uint32_t hist_words) {
+    extern __shared__ __align__(16) uint32_t s_dyn[];
+    PrevRows* s_prev = reinterpret_cast<PrevRows*>(s_dyn + hist_words);
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk = tasks[t];
+        const DqArgs& a    = args[tk.field];  // read-only table: loads stay cached
+        const Consts c     = *a.consts;
+        if (c.status != VSZ_OK) continue;  // uniform: the whole block is on this task
+        uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
+        if (s_hist) {
+            for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
+            __syncthreads();
         }
+        HistAcc h;
+        dq23_units<NDIM, BS, VEC, TAIL>(a, c, tk.u0 + (threadIdx.x >> 5), tk.u1, blockDim.x >> 5, s_hist, s_prev, h);
+        hist_flush_block(a, s_hist, h);
+        __syncthreads();  // the next task reuses shared memory
     }
 }
 
@@ -404,24 +448,14 @@ __global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
 // the left or, at a tile start, from the previous tile's last lane.  Blocks start on multiples of
 // block_size (which divide 128), so tile starts are block starts.
 template <int BS, bool VEC>
-__global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
-    extern __shared__ uint32_t s_hist_dyn[];
-    uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
-    const Consts c   = *a.consts;
-    if (c.status != VSZ_OK) return;
-    if (s_hist) {
-        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
-        __syncthreads();
-    }
+__device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, unsigned long long u0, unsigned long long u1,
+                                           unsigned long long ustep, uint32_t* s_hist, HistAcc& h) {
     const float r_f     = c.r_f;
     const float Rf      = (float)a.R;
     const unsigned lane = lane_id();
-    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const bool xbound = ((lane * 4) % BS) == 0;
-    constexpr int U   = 4;
-    HistAcc h;
-    for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
+    const bool xbound   = ((lane * 4) % BS) == 0;
+    constexpr int U     = 4;
+    for (unsigned long long u = u0; u < u1; u += ustep) {
         float S[U][4];
 #pragma unroll
         for (int t = 0; t < U; t++) {
@@ -448,13 +482,43 @@ __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
             emit_row<VEC>(a, 0, xb, xt, xt < a.nxt, code, outv, h, s_hist);
         }
     }
-    h.flush(a.R, s_hist, a.dict, a.hist);
+}
+
+template <int BS, bool VEC>
+__global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
+    extern __shared__ uint32_t s_hist_dyn[];
+    uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
+    const Consts c   = *a.consts;
+    if (c.status != VSZ_OK) return;
     if (s_hist) {
+        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
         __syncthreads();
-        for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
-            uint32_t v = s_hist[i];
-            if (v) atomicAdd(&a.hist[i], (unsigned long long)v);
+    }
+    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    HistAcc h;
+    dq1d_units<BS, VEC>(a, c, warp0, a.nunits, warps_total, s_hist, h);
+    hist_flush_block(a, s_hist, h);
+}
+
+template <int BS, bool VEC>
+__global__ void __launch_bounds__(256)
+    k_dq_compress_1d_batch(const DqArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ uint32_t s_hist_dyn[];
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk = tasks[t];
+        const DqArgs& a    = args[tk.field];
+        const Consts c     = *a.consts;
+        if (c.status != VSZ_OK) continue;
+        uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
+        if (s_hist) {
+            for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_hist[i] = 0u;
+            __syncthreads();
         }
+        HistAcc h;
+        dq1d_units<BS, VEC>(a, c, tk.u0 + (threadIdx.x >> 5), tk.u1, blockDim.x >> 5, s_hist, h);
+        hist_flush_block(a, s_hist, h);
+        __syncthreads();
     }
 }
 
@@ -469,15 +533,21 @@ constexpr int kGatherThreads = 256;
 constexpr int kGatherPerThread = 16;
 constexpr int kGatherTile = kGatherThreads * kGatherPerThread;  // segments per tile
 
-__global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g) {
-    if (*g.status != VSZ_OK) return;  // set before this launch, so uniform across the grid
+// One tile of 4096 row segments of one field: the next ticket of the field's look-back.  The
+// status is read once per block, so the early exit is uniform.
+__device__ __forceinline__ void gather_tile(const GatherArgs& g) {
     __shared__ uint32_t s_off[kGatherTile];
     __shared__ uint8_t s_cnt[kGatherTile];
     __shared__ uint32_t s_warp[kGatherThreads / 32];
     __shared__ unsigned long long s_base;
     __shared__ uint32_t s_tile;
-    if (threadIdx.x == 0) s_tile = atomicAdd(g.tile_counter, 1u);
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        s_ok = (*g.status == VSZ_OK);
+        if (s_ok) s_tile = atomicAdd(g.tile_counter, 1u);
+    }
     __syncthreads();
+    if (!s_ok) return;
     const uint32_t tile = s_tile;
     const size_t seg0   = (size_t)tile * kGatherTile + (size_t)threadIdx.x * kGatherPerThread;
     uint32_t cnt[kGatherPerThread];
@@ -563,6 +633,77 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
         }
         }
     }
+}
+
+__global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g) { gather_tile(g); }
+
+// Many fields: one task per tile of each field (tasks[t].field; the field's tickets keep its tiles
+// in look-back order, and the holder of every earlier ticket is already running).
+__global__ void __launch_bounds__(kGatherThreads)
+    k_outlier_gather_batch(const GatherArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const GatherArgs g = args[tasks[t].field];
+        gather_tile(g);
+        __syncthreads();  // the next task reuses shared memory
+    }
+}
+
+// Many fields: min/max over element ranges (tasks[t] = field, [u0, u1) elements, u0 a multiple of 4).
+__global__ void __launch_bounds__(256)
+    k_minmax_batch(const MinmaxField* __restrict__ f, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    __shared__ uint32_t smax[8], smin[8];
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk = tasks[t];
+        const float* x     = f[tk.field].x;
+        uint32_t kmax = 0u, kmin = 0xffffffffu;
+        const bool aligned = ((reinterpret_cast<uintptr_t>(x) & 15u) == 0);
+        const unsigned long long q0 = aligned ? tk.u0 / 4 : 0, q1 = aligned ? tk.u1 / 4 : 0;
+        const float4* x4 = reinterpret_cast<const float4*>(x);
+        for (unsigned long long i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
+            const float4 v   = __ldcs(&x4[i]);
+            const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (e[j] == e[j]) {
+                    kmax = max(kmax, f2key(e[j]));
+                    kmin = min(kmin, f2key(e[j]));
+                }
+        }
+        for (unsigned long long i = (aligned ? q1 * 4 : tk.u0) + threadIdx.x; i < tk.u1; i += blockDim.x) {
+            const float v = x[i];
+            if (v == v) {
+                kmax = max(kmax, f2key(v));
+                kmin = min(kmin, f2key(v));
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+            kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            smax[threadIdx.x >> 5] = kmax;
+            smin[threadIdx.x >> 5] = kmin;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
+                kmax = max(kmax, smax[i]);
+                kmin = min(kmin, smin[i]);
+            }
+            atomicMax(&f[tk.field].mm[0], kmax);
+            atomicMin(&f[tk.field].mm[1], kmin);
+        }
+        __syncthreads();
+    }
+}
+
+// Many fields: error-bound constants, one thread per field.
+__global__ void k_consts_batch(const ConstsField* __restrict__ f, uint32_t nfields) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nfields) return;
+    const ConstsField c = f[i];
+    consts_of(c.mode, c.eb, c.mm, c.x, c.consts, c.status);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -654,6 +795,77 @@ int launch_outlier_gather(GatherArgs g, cudaStream_t st) {
     if (cudaMemsetAsync(g.tile_status, 0, sizeof(unsigned long long) * g.ntiles, st) != cudaSuccess) return VSZ_ERR_CUDA;
     if (cudaMemsetAsync(g.tile_counter, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
     k_outlier_gather<<<g.ntiles, kGatherThreads, 0, st>>>(g);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_minmax_batch(const MinmaxField* f, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st, int num_sms) {
+    if (ntasks == 0) return VSZ_OK;
+    const uint32_t grid = ntasks < (uint32_t)num_sms * 8 ? ntasks : (uint32_t)num_sms * 8;
+    k_minmax_batch<<<grid, 256, 0, st>>>(f, tasks, ntasks);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_consts_batch(const ConstsField* f, uint32_t nfields, cudaStream_t st) {
+    if (nfields == 0) return VSZ_OK;
+    k_consts_batch<<<(nfields + 127) / 128, 128, 0, st>>>(f, nfields);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, int bs, bool vec,
+                             bool tail, uint32_t hist_words, cudaStream_t st, int num_sms) {
+    if (ntasks == 0) return VSZ_OK;
+    size_t smem = (size_t)hist_words * sizeof(uint32_t);
+    if (ndim == 3) smem += sizeof(PrevRows) * 8;
+    const uint32_t cap = (uint32_t)num_sms * (ndim == 1 ? 8u : 3u);
+    const uint32_t grid = ntasks < cap ? ntasks : cap;
+    int rc = VSZ_OK;
+    auto go23 = [&](auto kern, std::atomic<unsigned long long>& attr) {
+        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr);
+        kern<<<grid, 256, smem, st>>>(args, tasks, ntasks, hist_words);
+    };
+    auto go1 = [&](auto kern, std::atomic<unsigned long long>& attr) {
+        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr);
+        kern<<<grid, 256, smem, st>>>(args, tasks, ntasks);
+    };
+    auto pick = [&](auto nd_c, auto bs_c) {
+        constexpr int ND = decltype(nd_c)::value, B = decltype(bs_c)::value;
+        static std::atomic<unsigned long long> attr[4];
+        if constexpr (ND == 1) {
+            if (vec) go1(k_dq_compress_1d_batch<B, true>, attr[0]);
+            else go1(k_dq_compress_1d_batch<B, false>, attr[1]);
+        } else {
+            if (vec && !tail) go23(k_dq_compress_23d_batch<ND, B, true, false>, attr[0]);
+            else if (vec) go23(k_dq_compress_23d_batch<ND, B, true, true>, attr[1]);
+            else if (!tail) go23(k_dq_compress_23d_batch<ND, B, false, false>, attr[2]);
+            else go23(k_dq_compress_23d_batch<ND, B, false, true>, attr[3]);
+        }
+    };
+    auto by_bs = [&](auto nd_c) {
+        switch (bs) {
+            case 8: pick(nd_c, std::integral_constant<int, 8>{}); break;
+            case 16: pick(nd_c, std::integral_constant<int, 16>{}); break;
+            case 32: pick(nd_c, std::integral_constant<int, 32>{}); break;
+            case 64: pick(nd_c, std::integral_constant<int, 64>{}); break;
+            default: rc = VSZ_ERR_UNSUPPORTED;
+        }
+    };
+    if (ndim == 1) by_bs(std::integral_constant<int, 1>{});
+    else if (ndim == 2) by_bs(std::integral_constant<int, 2>{});
+    else by_bs(std::integral_constant<int, 3>{});
+    if (rc) return rc;
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_outlier_gather_batch(const GatherArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
+                                int num_sms) {
+    if (ntasks == 0) return VSZ_OK;
+    const uint32_t cap  = (uint32_t)num_sms * 4;
+    const uint32_t grid = ntasks < cap ? ntasks : cap;
+    k_outlier_gather_batch<<<grid, kGatherThreads, 0, st>>>(args, tasks, ntasks);
     count_launch();
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }

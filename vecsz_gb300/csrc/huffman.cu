@@ -147,8 +147,7 @@ __device__ __forceinline__ int heap_replay(BuildWs& w, int nused, int* fail) {
 }
 
 template <bool IN_SMEM>
-__global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
-    extern __shared__ __align__(16) uint8_t s_build_dyn[];
+__device__ __forceinline__ void build_field(const HuffBuildArgs& a, uint8_t* s_build_dyn) {
     __shared__ uint32_t s_info[4];
     __shared__ int s_fail;
     __shared__ uint32_t s_scan[33];
@@ -283,6 +282,22 @@ __global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
     if (threadIdx.x < 4) a.info[threadIdx.x] = s_info[threadIdx.x];
 }
 
+template <bool IN_SMEM>
+__global__ void __launch_bounds__(256) k_huff_build(HuffBuildArgs a) {
+    extern __shared__ __align__(16) uint8_t s_build_dyn[];
+    build_field<IN_SMEM>(a, s_build_dyn);
+}
+
+// Many fields: one CTA per field (grid-stride).
+template <bool IN_SMEM>
+__global__ void __launch_bounds__(256) k_huff_build_batch(const HuffBuildArgs* __restrict__ args, uint32_t nfields) {
+    extern __shared__ __align__(16) uint8_t s_build_dyn[];
+    for (uint32_t f = blockIdx.x; f < nfields; f += gridDim.x) {
+        build_field<IN_SMEM>(args[f], s_build_dyn);
+        __syncthreads();
+    }
+}
+
 int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsigned long long* tile_status,
                     uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st);
 
@@ -341,9 +356,9 @@ __device__ __forceinline__ bool encode_tree_ok(const HuffEncodeArgs& a) {
     return true;
 }
 
-__global__ void __launch_bounds__(kEncThreads) k_huff_count(HuffEncodeArgs a) {
-    extern __shared__ uint8_t s_len_dyn[];
-    if (*a.status != VSZ_OK || !encode_tree_ok(a)) return;
+// Bits of chunks c, c + cstep, ... < c1 of one field (one warp per chunk).
+__device__ __forceinline__ void count_chunks(const HuffEncodeArgs& a, size_t c, size_t c1, size_t cstep,
+                                             uint8_t* s_len_dyn) {
     const uint8_t* cl = a.cb_len;
     if (a.cb_in_smem) {
         for (int i = threadIdx.x; i < a.dict; i += blockDim.x) s_len_dyn[i] = a.cb_len[i];
@@ -351,8 +366,7 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_count(HuffEncodeArgs a) {
         cl = s_len_dyn;
     }
     const unsigned lane = threadIdx.x & 31u;
-    const size_t warps  = (size_t)gridDim.x * (kEncThreads / 32);
-    for (size_t c = blockIdx.x * (size_t)(kEncThreads / 32) + (threadIdx.x >> 5); c < a.nchunks; c += warps) {
+    for (; c < c1; c += cstep) {
         const Codes16 cc = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
         uint32_t bits    = 0;
 #pragma unroll
@@ -364,12 +378,33 @@ __global__ void __launch_bounds__(kEncThreads) k_huff_count(HuffEncodeArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) {
-    extern __shared__ uint8_t s_dyn[];
+__global__ void __launch_bounds__(kEncThreads) k_huff_count(HuffEncodeArgs a) {
+    extern __shared__ uint8_t s_len_dyn[];
+    if (*a.status != VSZ_OK || !encode_tree_ok(a)) return;
+    count_chunks(a, blockIdx.x * (size_t)(kEncThreads / 32) + (threadIdx.x >> 5), a.nchunks,
+                 (size_t)gridDim.x * (kEncThreads / 32), s_len_dyn);
+}
+
+// Many fields: tasks of (field, chunk range).
+__global__ void __launch_bounds__(kEncThreads)
+    k_huff_count_batch(const HuffEncodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ uint8_t s_len_dyn[];
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk       = tasks[t];
+        const HuffEncodeArgs& a  = args[tk.field];
+        if (*a.status != VSZ_OK || !encode_tree_ok(a)) continue;  // same answer for the whole block
+        count_chunks(a, tk.u0 + (threadIdx.x >> 5), tk.u1, kEncThreads / 32, s_len_dyn);
+        __syncthreads();
+    }
+}
+
+// Chunks c, c + cstep, ... < c1 of one field (one warp per chunk); the next chunk's codes are
+// loaded while the current one is packed.
+__device__ __forceinline__ void pack_chunks(const HuffEncodeArgs& a, size_t c, size_t c1, size_t cstep,
+                                            uint8_t* s_dyn) {
     uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);                                     // 8 x kEncWarpWords
     unsigned long long* s_cw = reinterpret_cast<unsigned long long*>(s_words + 8 * kEncWarpWords);  // dict (if cached)
     uint8_t* s_len = reinterpret_cast<uint8_t*>(s_cw + (a.cb_in_smem ? a.dict : 0));
-    if (*a.status != VSZ_OK) return;  // set before this launch: uniform across the grid
     const unsigned long long* cw = a.cb_word;
     const uint8_t* cl            = a.cb_len;
     if (a.cb_in_smem) {
@@ -386,12 +421,12 @@ __global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) 
     uint8_t* out          = a.out + a.out_off.eval();
     const uint32_t base0  = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
     uint32_t* gw          = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
-    const size_t warps    = (size_t)gridDim.x * (kEncThreads / 32);
-    size_t c              = blockIdx.x * (size_t)(kEncThreads / 32) + warp;
-    Codes16 nxt           = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
-    for (; c < a.nchunks; c += warps) {
+    // a batch scans all fields' chunks at once: offsets are relative to the field's first chunk
+    const unsigned long long off0 = a.chunk_off[0];
+    Codes16 nxt                   = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
+    for (; c < c1; c += cstep) {
         const Codes16 cc = nxt;
-        if (c + warps < a.nchunks) nxt = load_codes16(a, (c + warps) * kEncChunk + lane * kEncPerThread);
+        if (c + cstep < c1) nxt = load_codes16(a, (c + cstep) * kEncChunk + lane * kEncPerThread);
         uint32_t sym[kEncPerThread], len[kEncPerThread], bits = 0;
 #pragma unroll
         for (int k = 0; k < kEncPerThread; k++) {
@@ -406,7 +441,7 @@ __global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) 
             if (lane >= (unsigned)o) incl += t;
         }
         const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-        const unsigned long long gstart = base0 + a.chunk_off[c];  // chunk's first bit on the word grid
+        const unsigned long long gstart = base0 + (a.chunk_off[c] - off0);  // chunk's first bit on the word grid
         const uint32_t r0               = (uint32_t)(gstart & 31u);
         const unsigned long long F      = gstart >> 5;
         const uint32_t nwords           = tot ? (r0 + tot + 31) >> 5 : 0u;
@@ -470,12 +505,29 @@ __global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) 
     }
 }
 
+__global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) {
+    extern __shared__ uint8_t s_dyn[];
+    if (*a.status != VSZ_OK) return;  // set before this launch: uniform across the grid
+    pack_chunks(a, blockIdx.x * (size_t)(kEncThreads / 32) + (threadIdx.x >> 5), a.nchunks,
+                (size_t)gridDim.x * (kEncThreads / 32), s_dyn);
+}
+
+__global__ void __launch_bounds__(kEncThreads, 4)
+    k_huff_pack_batch(const HuffEncodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ uint8_t s_dyn[];
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk      = tasks[t];
+        const HuffEncodeArgs& a = args[tk.field];
+        if (*a.status != VSZ_OK) continue;  // no kernel of this launch writes it
+        pack_chunks(a, tk.u0 + (threadIdx.x >> 5), tk.u1, kEncThreads / 32, s_dyn);
+        __syncthreads();
+    }
+}
+
 // Boundary words of the chunks: chunk t's partial first word is the same word as chunk t - 1's
 // partial last word (a chunk of 512 codewords of >= 1 bit spans >= 512 bits, so no word has a
 // third sharer); the payload's first word also holds the last bytes of the tree section, kept as is.
-__global__ void k_huff_encode_edges(HuffEncodeArgs a) {
-    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (t >= a.nchunks || *a.status != VSZ_OK) return;
+__device__ __forceinline__ void edge_fix(const HuffEncodeArgs& a, size_t t) {
     uint8_t* out         = a.out + a.out_off.eval();
     const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
     uint32_t* gw         = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
@@ -489,6 +541,33 @@ __global__ void k_huff_encode_edges(HuffEncodeArgs a) {
         gw[fi] = v;
     }
     if (t == a.nchunks - 1 && li != none && li != fi) gw[li] = a.edge_bits[2 * t + 1];
+}
+
+__global__ void k_huff_encode_edges(HuffEncodeArgs a) {
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= a.nchunks || *a.status != VSZ_OK) return;
+    edge_fix(a, t);
+}
+
+__global__ void k_huff_encode_edges_batch(const HuffEncodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks,
+                                          uint32_t ntasks) {
+    for (uint32_t k = blockIdx.x; k < ntasks; k += gridDim.x) {
+        const BatchTask tk      = tasks[k];
+        const HuffEncodeArgs& a = args[tk.field];
+        if (*a.status != VSZ_OK) continue;
+        for (size_t t = tk.u0 + threadIdx.x; t < tk.u1; t += blockDim.x) edge_fix(a, t);
+    }
+}
+
+// Many fields: each field's payload length from the scan of all fields' chunk bits (chunk_off has
+// an entry past the field's last chunk: the next field's first, or the scan total); a failed scan
+// fails every field.
+__global__ void k_field_bits(const HuffEncodeArgs* __restrict__ args, uint32_t nfields, const int* scan_status) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nfields) return;
+    const HuffEncodeArgs& a = args[f];
+    if (*scan_status != VSZ_OK) set_status(a.status, *scan_status);
+    *a.total_bits = a.nchunks ? a.chunk_off[a.nchunks] - a.chunk_off[0] : 0ull;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1293,6 +1372,62 @@ int launch_huff_build(HuffBuildArgs a, cudaStream_t st) {
 }
 
 size_t huff_build_scratch_bytes(int dict) { return build_ws_bytes(dict); }
+
+bool huff_build_in_smem(int dict) { return build_ws_bytes(dict) <= 220 * 1024; }
+
+int launch_huff_build_batch(const HuffBuildArgs* args, uint32_t nfields, bool in_smem, int dict_max, cudaStream_t st,
+                            int num_sms) {
+    if (nfields == 0) return VSZ_OK;
+    const uint32_t grid = nfields < (uint32_t)num_sms * 8 ? nfields : (uint32_t)num_sms * 8;
+    if (in_smem) {
+        static std::atomic<unsigned long long> attr{0};
+        smem_limit_once(k_huff_build_batch<true>, 220 * 1024, attr);
+        k_huff_build_batch<true><<<grid, 256, build_ws_bytes(dict_max), st>>>(args, nfields);
+    } else {
+        k_huff_build_batch<false><<<grid, 256, 0, st>>>(args, nfields);
+    }
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_encode_batch(const HuffEncodeArgs* args, uint32_t nfields, const BatchTask* tasks, uint32_t ntasks,
+                             int cb_dict_max, uint16_t* all_bits, unsigned long long* all_off, size_t total_chunks,
+                             unsigned long long* scan_status, uint32_t* scan_counter, int* batch_status,
+                             cudaStream_t st, int num_sms) {
+    if (ntasks == 0) return VSZ_OK;
+    const size_t cb_bytes = (size_t)cb_dict_max * 9;  // fields with cb_in_smem: codebook cached per task
+    const size_t smem     = (size_t)8 * kEncWarpWords * 4 + cb_bytes + 16;
+    static std::atomic<unsigned long long> attr_pack{0}, attr_count{0};
+    smem_limit_once(k_huff_pack_batch, 8 * kEncWarpWords * 4 + 64 * 1024 + 1024, attr_pack);
+    smem_limit_once(k_huff_count_batch, 64 * 1024 + 1024, attr_count);
+    {
+        StageTimer t(kStHuffCount, st);
+        const uint32_t grid = ntasks < (uint32_t)num_sms * 8 ? ntasks : (uint32_t)num_sms * 8;
+        k_huff_count_batch<<<grid, kEncThreads, (size_t)cb_dict_max, st>>>(args, tasks, ntasks);
+        count_launch();
+        int rc = launch_scan_u16(all_bits, all_off, total_chunks, scan_status, scan_counter, all_off + total_chunks,
+                                 batch_status, st);
+        if (rc) return rc;
+        k_field_bits<<<(nfields + 127) / 128, 128, 0, st>>>(args, nfields, batch_status);
+        count_launch();
+    }
+    {
+        StageTimer t(kStHuffPack, st);
+        const uint32_t grid = ntasks < (uint32_t)num_sms * 4 ? ntasks : (uint32_t)num_sms * 4;
+        k_huff_pack_batch<<<grid, kEncThreads, smem, st>>>(args, tasks, ntasks);
+        count_launch();
+        k_huff_encode_edges_batch<<<grid, 256, 0, st>>>(args, tasks, ntasks);
+        count_launch();
+    }
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+// Per-field encoder flags a batch table needs (launch_huff_encode sets them for one field).
+void huff_encode_prepare(HuffEncodeArgs& a) {
+    a.nchunks       = (a.n + kEncChunk - 1) / kEncChunk;
+    a.codes_aligned = (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0;
+    a.cb_in_smem    = (size_t)a.dict * 9 <= 64 * 1024 ? 1 : 0;
+}
 
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms) {
     a.nchunks = (a.n + kEncChunk - 1) / kEncChunk;

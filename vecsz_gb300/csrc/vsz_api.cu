@@ -8,6 +8,7 @@
 #include <mutex>
 #include <vector>
 
+#include "api_common.cuh"
 #include "host_tree.h"
 #include "vsz_device.cuh"
 #include "vsz_huffman.h"
@@ -15,42 +16,12 @@
 #include "vsz_profile.h"
 
 using namespace vsz;
+using namespace vsz::api;
 
 static_assert(sizeof(Consts) <= VSZ_CONSTS_BYTES, "Consts must fit VSZ_CONSTS_BYTES");
 
-namespace {
-
-constexpr uint32_t kTrailerMagic   = 0x545A5356u;  // "VSZT"
-constexpr uint32_t kTrailerVersion = 1;
-constexpr uint32_t kTrailerFixed   = 64;
-
-#define VSZ_TRY(x)                        \
-    do {                                  \
-        int _rc = (x);                    \
-        if (_rc != VSZ_OK) return _rc;    \
-    } while (0)
-#define VSZ_CUDA(x)                                    \
-    do {                                               \
-        if ((x) != cudaSuccess) return VSZ_ERR_CUDA;   \
-    } while (0)
-
-// Bump allocator over a caller workspace; with base == nullptr it only measures.
-struct Bump {
-    uint8_t* base;
-    size_t cap;
-    size_t off = 0;
-    template <class T>
-    T* take(size_t count, size_t align = 256) {
-        off  = (off + align - 1) & ~(align - 1);
-        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
-        off += count * sizeof(T);
-        return p;
-    }
-    bool fits() const { return off <= cap; }
-};
-
+namespace vsz {
 int g_sms[64];
-
 int num_sms() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
@@ -61,149 +32,11 @@ int num_sms() {
     }
     return g_sms[dev];
 }
+}  // namespace vsz
 
-inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+namespace {
 
-bool valid_dims(int ndim, const size_t* dims) {
-    if (ndim < 1 || ndim > 3 || !dims) return false;
-    size_t n = 1;
-    for (int i = 0; i < ndim; i++) {
-        if (dims[i] == 0 || dims[i] > 0x7fffffffu) return false;  // the archive stores i32 dims
-        n *= dims[i];
-        if (n > (1ull << 36)) return false;
-    }
-    return true;
-}
-
-bool valid_dict(int dict) { return dict >= 2 && dict <= 65536 && (dict % 2) == 0; }
-bool valid_bs(int bs) { return bs == 8 || bs == 16 || bs == 32 || bs == 64; }
-
-int check_params(const vsz_params* p, int ndim, const size_t* dims) {
-    if (!p || !valid_dims(ndim, dims)) return VSZ_ERR_INVALID;
-    if (!(p->eb > 0.0) || p->eb != p->eb || p->eb > 1e300) return VSZ_ERR_INVALID;
-    if (p->mode != VSZ_MODE_ABS && p->mode != VSZ_MODE_R2R) return VSZ_ERR_INVALID;
-    if (!valid_dict(p->dict_size)) return VSZ_ERR_INVALID;
-    if (p->block_size <= 0) return VSZ_ERR_INVALID;
-    if (!valid_bs(p->block_size)) return VSZ_ERR_UNSUPPORTED;
-    return VSZ_OK;
-}
-
-size_t hdr_bytes(int ndim) { return 4 * (size_t)(ndim + 1) + 8 + 24; }
-
-DqArgs make_dq_args(const Geometry& g, int bs, int dict, const float* x, const Consts* c, uint16_t* code,
-                    float* scratch, uint8_t* seg_count, unsigned long long* hist) {
-    DqArgs a{};
-    a.x = x;
-    a.code = code;
-    a.scratch = scratch;
-    a.seg_count = seg_count;
-    a.hist = hist;
-    a.consts = c;
-    a.d0 = g.d0;
-    a.d1 = g.d1;
-    a.d2 = g.d2;
-    a.nxt = g.nxt;
-    a.nyg = (g.d1 + 7) / 8;
-    a.nzb = (g.ndim == 3) ? (g.d2 + bs - 1) / bs : 1;
-    a.xtail = (g.d0 % 8) ? (g.d0 & ~7u) : g.d0;
-    a.R = dict / 2;
-    a.dict = dict;
-    a.smem_hist = dict <= 16384 ? 1 : 0;
-    if (g.ndim == 1) a.nunits = (g.nxt + 3) / 4;  // 4 tiles per unit
-    else a.nunits = (unsigned long long)g.nxt * a.nyg * a.nzb;
-    return a;
-}
-
-// ---- archive finalization --------------------------------------------------------------------
-
-struct FinalizeArgs {
-    uint8_t* archive;
-    int ndim;
-    uint32_t dims[3];
-    double eb;  // user eb (header field)
-    int mode, dict, bs;
-    size_t hdr;
-    const Consts* consts;
-    const uint32_t* build_info;             // node count, tree bytes, max len
-    const unsigned long long* payload_bits;
-    const unsigned long long* n_out;
-    const int* status;
-    unsigned long long* result;             // vsz_result
-    const uint16_t* chunk_bits;
-    unsigned long long n_chunks;
-};
-
-__device__ __forceinline__ void put_bytes(uint8_t* d, const void* src, int n) {
-    const uint8_t* s = reinterpret_cast<const uint8_t*>(src);
-    for (int i = 0; i < n; i++) d[i] = s[i];
-}
-
-__device__ __forceinline__ size_t trailer_index_pad(size_t data_size) {
-    size_t start = data_size + kTrailerFixed;
-    return ((start + 7) & ~(size_t)7) - data_size;
-}
-
-// Header, result record and trailer (one thread), then the index copy (whole grid).
-__global__ void k_finalize(FinalizeArgs f) {
-    const unsigned long long bits = *f.payload_bits;
-    const unsigned long long nout = *f.n_out;
-    const uint32_t tree           = f.build_info[1];
-    const size_t huff_bytes       = 8 + (size_t)tree + (size_t)((bits + 7) >> 3);
-    const size_t data_size        = f.hdr + huff_bytes + 4 * (size_t)nout;
-    const size_t pad              = trailer_index_pad(data_size);
-    const size_t trailer          = ((pad + 2 * (size_t)f.n_chunks) + 7) & ~(size_t)7;
-    uint8_t* t                    = f.archive + data_size;
-    const int st                  = f.consts->status != VSZ_OK ? f.consts->status : *f.status;
-    if (st != VSZ_OK) {
-        // sizes from failed stages are not meaningful: report the status, write no archive bytes
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            for (int i = 0; i < 8; i++) f.result[i] = 0;
-            f.result[5] = (unsigned long long)st;
-        }
-        return;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int32_t nd = f.ndim;
-        put_bytes(f.archive, &nd, 4);
-        for (int i = 0; i < f.ndim; i++) {
-            int32_t d = (int32_t)f.dims[i];
-            put_bytes(f.archive + 4 * (1 + i), &d, 4);
-        }
-        put_bytes(f.archive + 4 * (f.ndim + 1), &f.eb, 8);
-        unsigned long long lens[3] = {0ull, (unsigned long long)huff_bytes, nout};
-        put_bytes(f.archive + 4 * (f.ndim + 1) + 8, lens, 24);
-        // trailer fixed part
-        uint32_t u32[4] = {kTrailerMagic, kTrailerVersion, kTrailerFixed, (uint32_t)kChunkSyms};
-        put_bytes(t, u32, 16);
-        double ebf = f.consts->eb_final, vr = f.consts->range;
-        put_bytes(t + 16, &ebf, 8);
-        put_bytes(t + 24, &vr, 8);
-        int32_t i32[3] = {f.mode, f.dict, f.bs};
-        put_bytes(t + 32, i32, 12);
-        uint32_t padu = (uint32_t)pad;
-        put_bytes(t + 44, &padu, 4);
-        unsigned long long nch = f.n_chunks, tsz = trailer;
-        put_bytes(t + 48, &nch, 8);
-        put_bytes(t + 56, &tsz, 8);
-        for (size_t i = kTrailerFixed; i < pad; i++) t[i] = 0;
-        unsigned long long* r = f.result;
-        r[0] = data_size;
-        r[1] = trailer;
-        r[2] = nout;
-        r[3] = huff_bytes;
-        r[4] = bits;
-        r[5] = (unsigned long long)st;
-        r[6] = f.build_info[2];
-        r[7] = f.build_info[0];
-    }
-    uint16_t* idx = reinterpret_cast<uint16_t*>(t + pad);
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < f.n_chunks; i += (size_t)gridDim.x * blockDim.x)
-        idx[i] = f.chunk_bits[i];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        size_t used = pad + 2 * (size_t)f.n_chunks;
-        for (size_t i = used; i < trailer; i++) t[i] = 0;
-    }
-}
+__global__ void k_finalize(FinalizeArgs f) { finalize_field(f, blockIdx.x, gridDim.x); }
 
 __global__ void k_check_zeros(const unsigned long long* total_zeros, unsigned long long n_out, int* status) {
     if (*total_zeros != n_out) set_status(status, VSZ_ERR_CORRUPT);
@@ -243,10 +76,6 @@ struct CompressWs {
     size_t bytes;
 };
 
-inline size_t codebook_block_bytes(int dict) { return 9 * (size_t)dict + 16; }
-// [BE nc][BE dict] + the largest serialised tree a dictionary can give
-inline size_t tree_head_max(int dict) { return 8 + tree_bytes_size((uint32_t)(2 * dict - 1)); }
-
 CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t cap) {
     Bump b{base, cap};
     CompressWs w{};
@@ -281,11 +110,6 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     return w;
 }
 
-size_t archive_capacity(const Geometry& g, int dict) {
-    size_t tree_max = tree_bytes_size((uint32_t)(2 * dict - 1));
-    size_t n_chunks = (g.n + kChunkSyms - 1) / kChunkSyms;
-    return hdr_bytes(g.ndim) + 8 + tree_max + 8 * g.n + 4 * g.n + kTrailerFixed + 8 + 2 * n_chunks + 64;
-}
 
 struct DecompressWs {
     Consts* consts;

@@ -128,6 +128,18 @@ struct HuffSyncArgs {
 };
 
 int launch_huff_build(HuffBuildArgs a, cudaStream_t st);
+// Batches: one CTA per field; in_smem for every field when huff_build_in_smem(dict) (the others
+// need HuffBuildArgs::scratch).  Encode: tasks of (field, 512-code chunk range); all fields' chunk
+// bits are scanned at once (all_bits / all_off hold total_chunks + 1 entries, the fields' ranges
+// in field order; each field's chunk_bits / chunk_off point into them).
+bool huff_build_in_smem(int dict);
+int launch_huff_build_batch(const HuffBuildArgs* args, uint32_t nfields, bool in_smem, int dict_max, cudaStream_t st,
+                            int num_sms);
+int launch_huff_encode_batch(const HuffEncodeArgs* args, uint32_t nfields, const BatchTask* tasks, uint32_t ntasks,
+                             int cb_dict_max, uint16_t* all_bits, unsigned long long* all_off, size_t total_chunks,
+                             unsigned long long* scan_status, uint32_t* scan_counter, int* batch_status,
+                             cudaStream_t st, int num_sms);
+void huff_encode_prepare(HuffEncodeArgs& a);
 void huff_build_prepare();  // one-time kernel attributes of launch_huff_build (call outside capture)
 size_t huff_build_scratch_bytes(int dict);
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms);

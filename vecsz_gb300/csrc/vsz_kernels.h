@@ -27,6 +27,30 @@ struct DevOffset {
 #endif
 };
 
+// ---- many fields in one launch -------------------------------------------------------------
+// A block-wide unit of work: one field of a batch and a range [u0, u1) of that field's work units
+// (warp tiles, 512-code chunks, elements or look-back tiles, by stage).  Tasks are built on the
+// host, where every field's geometry is known.
+struct BatchTask {
+    unsigned long long u0, u1;
+    uint32_t field;
+    uint32_t pad;
+};
+
+struct MinmaxField {
+    const float* x;
+    uint32_t* mm;  // {max key, min key}, initialised to {0, 0xffffffff}
+};
+
+struct ConstsField {
+    int mode;
+    double eb;
+    const uint32_t* mm;
+    const float* x;
+    Consts* consts;
+    int* status;
+};
+
 // ---- dual-quant compress ------------------------------------------------------------------
 struct DqArgs {
     const float* x;
@@ -87,6 +111,16 @@ int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_
                     cudaStream_t st, int* status_word = nullptr);
 int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms);
 int launch_outlier_gather(GatherArgs g, cudaStream_t st);
+
+// Batched launchers (device arrays of per-field arguments and of tasks).  A dual-quant batch
+// holds fields of one kernel class: ndim, block size, vec (d0 % 4 == 0 and aligned), tail
+// (d0 % 8 != 0); hist_words = shared-memory histogram words (0 when no field uses one).
+int launch_minmax_batch(const MinmaxField* f, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st, int num_sms);
+int launch_consts_batch(const ConstsField* f, uint32_t nfields, cudaStream_t st);
+int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, int bs, bool vec,
+                             bool tail, uint32_t hist_words, cudaStream_t st, int num_sms);
+int launch_outlier_gather_batch(const GatherArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
+                                int num_sms);
 size_t gather_tmp_bytes(size_t nseg);
 
 // Geometry helpers shared by compress and decompress.
