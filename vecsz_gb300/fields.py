@@ -133,3 +133,93 @@ def adversarial_3d_torch(nz, ny, nx, seed=0, device="cuda"):
         x = torch.linspace(-0.5, 0.5, nx, device=device, dtype=torch.float64)[None, None, :]
         f += ((nrm[0] * z + nrm[1] * y + nrm[2] * x) > off).double() * amp
     return f.float().contiguous()
+
+
+# ------------------------------------------------------------------------------------------------
+# Mixed field sets for the batched path: 1D/2D/3D at 20/40/40 %, element counts log-uniform in
+# [16K, 16M] factored into random aspect ratios, each field the k^-11/3 random field or the smooth
+# bump field, with its own r2r error bound log-uniform in [1e-5, 1e-2].
+# ------------------------------------------------------------------------------------------------
+
+def _factor(n: int, nd: int, rng) -> tuple:
+    """dims (x fastest) of about n elements with random aspect ratios."""
+    if nd == 1:
+        return (n,)
+    if nd == 2:
+        u = rng.uniform(0.25, 0.75)
+        d0 = max(1, int(round(n ** u)))
+        return (d0, max(1, int(round(n / d0))))
+    w = rng.uniform(0.5, 1.5, 3)
+    w = w / w.sum()
+    d0 = max(1, int(round(n ** w[0])))
+    d1 = max(1, int(round(n ** w[1])))
+    return (d0, d1, max(1, int(round(n / (d0 * d1)))))
+
+
+def batch_field_specs(n_fields: int = 1000, seed: int = 0, n_min: int = 1 << 14, n_max: int = 1 << 24) -> list:
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_fields):
+        nd = int(rng.choice([1, 2, 3], p=[0.2, 0.4, 0.4]))
+        n = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        dims = _factor(n, nd, rng)
+        kind = "bump" if (nd == 2 and rng.random() < 0.5) else "grf"
+        specs.append({"ndim": nd, "dims": dims, "kind": kind, "eb": float(10 ** rng.uniform(-5, -2)),
+                      "seed": seed * 100003 + i})
+    return specs
+
+
+def grf_torch(shape, seed=0, decades=4.0, device="cuda"):
+    """k^-11/3 random field of any dimensionality (numpy-order shape), exponentiated to span
+    `decades` decades."""
+    import torch
+    gen = torch.Generator(device=device).manual_seed(seed)
+    shape = tuple(int(v) for v in shape)
+    ks = []
+    for ax, m in enumerate(shape):
+        f = torch.fft.rfftfreq(m, device=device) if ax == len(shape) - 1 else torch.fft.fftfreq(m, device=device)
+        view = [1] * len(shape)
+        view[ax] = -1
+        ks.append(f.view(view) ** 2)
+    k2 = ks[0]
+    for t in ks[1:]:
+        k2 = k2 + t
+    k = torch.sqrt(k2)
+    k.view(-1)[0] = 1.0
+    amp = k ** (-11.0 / 6.0)
+    amp.view(-1)[0] = 0.0
+    spec = torch.complex(amp * torch.randn(amp.shape, generator=gen, device=device),
+                         amp * torch.randn(amp.shape, generator=gen, device=device))
+    g = torch.fft.irfftn(spec, s=shape)
+    del spec, amp, k
+    sd = g.std()
+    g = (g - g.mean()) / (sd if float(sd) > 0 else 1.0)
+    span = float(g.max() - g.min())
+    a = decades * math.log(10.0) / (span if span > 0 else 1.0)
+    return torch.exp(a * g).float().contiguous()
+
+
+def bump_field_2d_torch32(ny, nx, seed=0, nbumps=64, device="cuda"):
+    """bump_field_2d in float32 on the device (for large mixed sets)."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    cy = (torch.rand(nbumps, generator=g) * ny).tolist()
+    cx = (torch.rand(nbumps, generator=g) * nx).tolist()
+    sig = (20 + torch.rand(nbumps, generator=g) * 380).tolist()
+    amp = torch.randn(nbumps, generator=g).tolist()
+    yy = torch.arange(ny, dtype=torch.float32, device=device)[:, None]
+    xx = torch.arange(nx, dtype=torch.float32, device=device)[None, :]
+    f = torch.zeros((ny, nx), dtype=torch.float32, device=device)
+    for i in range(nbumps):
+        f += amp[i] * torch.exp(-((yy - cy[i]) ** 2 + (xx - cx[i]) ** 2) / (2 * sig[i] ** 2))
+    f += torch.rand((ny, nx), generator=torch.Generator(device=device).manual_seed(seed), device=device) * 1e-5
+    lo, hi = f.min(), f.max()
+    return ((f - lo) / (hi - lo if float(hi - lo) > 0 else 1.0)).contiguous()
+
+
+def batch_field_torch(spec, device="cuda"):
+    dims = spec["dims"]
+    shape = tuple(reversed(dims))
+    if spec["kind"] == "bump":
+        return bump_field_2d_torch32(shape[0], shape[1], seed=spec["seed"], device=device).reshape(-1)
+    return grf_torch(shape, seed=spec["seed"], device=device).reshape(-1)
