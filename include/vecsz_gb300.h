@@ -240,6 +240,45 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
 vsz_status vsz_batch_compress(vsz_batch* batch, void* stream);
 void vsz_batch_destroy(vsz_batch* batch);
 
+/* ---- request server ---------------------------------------------------------------------------
+ * Continuous admission of compress / decompress requests under a device-memory budget, their work
+ * overlapping on the device.  Requests queue in arrival order; a dispatcher thread admits the head
+ * request as soon as one of `slots` streams is free and its workspace and output fit in the budget
+ * (one device arena of budget_bytes, allocated at creation; admission never calls cudaMalloc).
+ * The workspace returns to the arena when the request completes; the output (compress: the archive,
+ * trimmed to its real size; decompress: the field) stays until vsz_server_release.  Results are
+ * the same as vsz_compress / vsz_decompress of the request alone.  Decompress requests carry the
+ * parsed archive (vsz_archive_parse); archives without this library's index synchronise their
+ * slot's stream, which holds the dispatcher meanwhile.  No counterpart in the reference. */
+#define VSZ_REQ_COMPRESS 0
+#define VSZ_REQ_DECOMPRESS 1
+typedef struct vsz_request {
+    int kind;                  /* VSZ_REQ_COMPRESS | VSZ_REQ_DECOMPRESS */
+    const void* d_in;          /* compress: device field; decompress: device archive (16 readable bytes past it) */
+    int ndim;                  /* compress */
+    size_t dims[3];            /* compress */
+    vsz_params params;         /* compress (lossless ignored) */
+    vsz_archive_desc desc;     /* decompress */
+    vsz_decompress_opts opts;  /* decompress */
+} vsz_request;
+typedef struct vsz_completion {
+    int status;                /* VSZ_OK or why the request failed */
+    void* d_out;               /* device output inside the server's arena, valid until released */
+    size_t out_bytes;          /* compress: packed block + trailer; decompress: 4 N */
+    double t_submit, t_start, t_done;  /* host steady-clock seconds: queued, admitted, completed */
+    uint64_t result[8];        /* compress: vsz_result */
+} vsz_completion;
+typedef struct vsz_server vsz_server;
+vsz_status vsz_server_create(size_t budget_bytes, int slots, vsz_server** server);
+/* Non-blocking; VSZ_ERR_CAPACITY when the request could never fit in the budget. */
+vsz_status vsz_server_submit(vsz_server* server, const vsz_request* request, uint64_t* ticket);
+/* Blocks until the request completed (VSZ_ERR_TIMEOUT after timeout_s). */
+vsz_status vsz_server_wait(vsz_server* server, uint64_t ticket, double timeout_s, vsz_completion* done);
+vsz_status vsz_server_release(vsz_server* server, uint64_t ticket);
+vsz_status vsz_server_stats(vsz_server* server, uint64_t* completed, uint64_t* input_bytes_completed,
+                            size_t* arena_bytes_in_use, int* queued);
+void vsz_server_destroy(vsz_server* server);
+
 /* Parse a packed block (+ optional trailer) held in host memory. */
 vsz_status vsz_archive_parse(const uint8_t* h_archive, size_t len, vsz_archive_desc* desc);
 vsz_status vsz_decompress_bounds(const vsz_archive_desc* desc, const vsz_decompress_opts* opts, size_t* ws_bytes);

@@ -4,8 +4,8 @@ The compute path is libvecsz_gb300.so (hand-written CUDA kernels behind a C ABI,
 include/vecsz_gb300.h); this package binds it with ctypes.  There is no CPU fallback.
 """
 from ._lib import VszError, lib, library_path  # noqa: F401
-from .api import (BatchCompressor, Compressed, DeviceCodec, compress, decompress, make_params,  # noqa: F401
-                  parse_archive, read_sz_file)
+from .api import (BatchCompressor, Compressed, DeviceCodec, Server, compress, decompress,  # noqa: F401
+                  make_params, parse_archive, read_sz_file)
 
-__all__ = ["VszError", "lib", "library_path", "BatchCompressor", "Compressed", "DeviceCodec", "compress",
-           "decompress", "make_params", "parse_archive", "read_sz_file"]
+__all__ = ["VszError", "lib", "library_path", "BatchCompressor", "Compressed", "DeviceCodec", "Server",
+           "compress", "decompress", "make_params", "parse_archive", "read_sz_file"]

@@ -68,6 +68,19 @@ class DecompressOpts(C.Structure):
     _fields_ = [("dict_size", C.c_int), ("block_size", C.c_int), ("mode", C.c_int), ("value_range", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("d_in", C.c_void_p), ("ndim", C.c_int), ("dims", C.c_size_t * 3),
+                ("params", Params), ("desc", ArchiveDesc), ("opts", DecompressOpts)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("status", C.c_int), ("d_out", C.c_void_p), ("out_bytes", C.c_size_t), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double), ("result", C.c_uint64 * 8)]
+
+
+REQ_COMPRESS = 0
+REQ_DECOMPRESS = 1
+
 _LIB = None
 
 _p, _sz, _i, _d, _u64p, _u32p = C.c_void_p, C.c_size_t, C.c_int, C.c_double, C.c_void_p, C.c_void_p
@@ -92,6 +105,13 @@ _PROTOS = {
     "vsz_batch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
     "vsz_batch_compress": ([_p, _p], _i),
     "vsz_batch_destroy": ([_p], None),
+    "vsz_server_create": ([_sz, _i, C.POINTER(C.c_void_p)], _i),
+    "vsz_server_submit": ([_p, _p, C.POINTER(C.c_uint64)], _i),
+    "vsz_server_wait": ([_p, C.c_uint64, _d, _p], _i),
+    "vsz_server_release": ([_p, C.c_uint64], _i),
+    "vsz_server_stats": ([_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_size_t),
+                          C.POINTER(C.c_int)], _i),
+    "vsz_server_destroy": ([_p], None),
     "vsz_huffman_encode_tmp_bytes": ([_sz], _sz),
     "vsz_huffman_encode": ([_p, _sz, _p, _i, _p, _p, _p, _p, _sz, _p], _i),
     "vsz_huffman_decode_tmp_bytes": ([_sz, _sz, _i], _sz),

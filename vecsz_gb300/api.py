@@ -229,6 +229,94 @@ class BatchCompressor:
             pass
 
 
+class _CudaArray:
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def _device_view(ptr, nbytes, dtype="uint8"):
+    """A torch tensor over raw device memory owned by the library (no copy)."""
+    torch = _torch()
+    if dtype == "float32":
+        return torch.as_tensor(_CudaArray(ptr, nbytes // 4, "<f4"), device="cuda")
+    return torch.as_tensor(_CudaArray(ptr, nbytes, "|u1"), device="cuda")
+
+
+class Server:
+    """Request server (vsz_server_*): compress / decompress requests admitted under a device-memory
+    budget as stream slots and memory free up, their work overlapping on the device.
+
+    submit_compress / submit_decompress return a ticket; wait(ticket) returns the Completion (its
+    d_out points into the server's arena); output_tensor copies the output out; release frees it."""
+
+    def __init__(self, budget_bytes, slots=8):
+        h = C.c_void_p(0)
+        check(lib().vsz_server_create(int(budget_bytes), int(slots), C.byref(h)), "server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit_compress(self, d_in, dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8) -> int:
+        from ._lib import REQ_COMPRESS, Request
+        dims = tuple(int(v) for v in dims)
+        r = Request()
+        r.kind = REQ_COMPRESS
+        r.d_in = _ptr(d_in).value
+        r.ndim = len(dims)
+        r.dims = dims_arg(dims)
+        r.params = make_params(eb, mode, dict_size, block_size)
+        t = C.c_uint64(0)
+        check(lib().vsz_server_submit(self._h, C.byref(r), C.byref(t)), "server_submit")
+        self._keep[t.value] = d_in
+        return t.value
+
+    def submit_decompress(self, d_archive, desc, opts) -> int:
+        from ._lib import REQ_DECOMPRESS, Request
+        r = Request()
+        r.kind = REQ_DECOMPRESS
+        r.d_in = _ptr(d_archive).value
+        r.desc = desc
+        r.opts = opts
+        t = C.c_uint64(0)
+        check(lib().vsz_server_submit(self._h, C.byref(r), C.byref(t)), "server_submit")
+        self._keep[t.value] = d_archive
+        return t.value
+
+    def wait(self, ticket, timeout_s=60.0):
+        from ._lib import Completion
+        c = Completion()
+        check(lib().vsz_server_wait(self._h, C.c_uint64(ticket), float(timeout_s), C.byref(c)), "server_wait")
+        return c
+
+    def output_view(self, c, dtype="uint8"):
+        """Zero-copy torch view of a completion's device output (valid until release)."""
+        return _device_view(c.d_out, c.out_bytes, dtype)
+
+    def output_bytes(self, c) -> bytes:
+        return self.output_view(c).cpu().numpy().tobytes() if c.out_bytes else b""
+
+    def release(self, ticket) -> None:
+        check(lib().vsz_server_release(self._h, C.c_uint64(ticket)), "server_release")
+        self._keep.pop(ticket, None)
+
+    def stats(self):
+        d, b, u, q = C.c_uint64(0), C.c_uint64(0), C.c_size_t(0), C.c_int(0)
+        check(lib().vsz_server_stats(self._h, C.byref(d), C.byref(b), C.byref(u), C.byref(q)), "server_stats")
+        return {"completed": d.value, "input_bytes_completed": b.value, "arena_bytes_in_use": u.value,
+                "queued": q.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib().vsz_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ------------------------------------------------------------------------------------------------
 # Stage-level calls on torch CUDA tensors (one per reference routine)
 # ------------------------------------------------------------------------------------------------
