@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -63,6 +64,8 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain mixed field set")
     ap.add_argument("--batch-fields", type=int, default=1000)
+    ap.add_argument("--no-serving", action="store_true", help="skip the request-server stream")
+    ap.add_argument("--serving-seconds", type=float, default=8.0)
     ap.add_argument("--no-stage-profile", action="store_true",
                     help="no per-stage CUDA events in the timed loop (no roofline / stages)")
     return ap.parse_args()
@@ -324,6 +327,8 @@ def run_ours(args):
         line["e2e"] = run_e2e(V, x, dims, eb, mode, dct, bs, args.e2e_steps, bytes_in, world)
     if not args.no_batch:
         line["batched"] = run_batch(V, args.batch_fields, 1000 + rank, reps=3)
+    if not args.no_serving:
+        line["serving"] = run_serving(V, args.serving_seconds, 2000, 7000 + rank)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(x, dims, eb, mode, dct, bs)
     if world > 1:
@@ -424,6 +429,91 @@ def run_batch(V, n_fields, seed, reps, sample_every=25):
             "plain_path": "vsz_compress per field on one stream (18 launches + host tree step each)",
             "batched_path": "vsz_batch_compress captured in a CUDA graph (one launch per stage / kernel class, "
                             "device tree build, one CTA per field)"}
+
+
+def run_serving(V, seconds, rate, seed, budget_gb=120, slots=8, pool=48):
+    """Poisson stream of compress (70 %) / decompress (30 %) requests through the request server.
+    Sizes log-uniform in bytes from 2D 256^2 to 3D 512^3, r2r eb from {1e-2, 1e-3, 1e-4, 1e-5}; a pool
+    of distinct fields (and their archives, for decompress requests) stands in for the stream."""
+    import threading
+    import torch
+    from vecsz_gb300 import fields
+    from vecsz_gb300.api import DecompressOpts
+    rng = np.random.default_rng(seed)
+    lo, hi = 256 * 256 * 4, 512 ** 3 * 4
+    items = []
+    for i in range(pool):
+        nbytes = math.exp(rng.uniform(math.log(lo), math.log(hi)))
+        n = max(65536, int(nbytes // 4))
+        nd = 2 if n <= (1 << 22) else 3
+        dims = fields._factor(n, nd, rng)
+        eb = float(rng.choice([1e-2, 1e-3, 1e-4, 1e-5]))
+        x = fields.grf_torch(tuple(reversed(dims)), seed=seed * 1000 + i).reshape(-1)
+        codec = V.DeviceCodec(dims, eb=eb, mode="r2r", dict_size=1024, block_size=8)
+        codec.compress(x)
+        a = codec.archive_bytes()
+        arc = torch.from_numpy(np.frombuffer(a + bytes(64), np.uint8).copy()).cuda()
+        items.append({"x": x, "dims": dims, "eb": eb, "bytes": 4 * x.numel(), "arc": arc, "desc": V.parse_archive(a)})
+        del codec
+    torch.cuda.synchronize()
+    opts = DecompressOpts(1024, 8, 1, 0.0)
+    srv = V.Server(budget_bytes=int(budget_gb * (1 << 30)), slots=slots)
+    n_req = int(seconds * rate)
+    gaps = rng.exponential(1.0 / rate, n_req)
+    kinds = rng.random(n_req) < 0.7
+    picks = rng.integers(0, pool, n_req)
+    tickets = [None] * n_req
+    done = []
+    errors = []
+
+    def waiter():
+        for i in range(n_req):
+            while tickets[i] is None:
+                time.sleep(1e-4)
+            t, nb = tickets[i]
+            c = srv.wait(t, timeout_s=120.0)
+            if c.status != 0:
+                errors.append(c.status)
+            done.append((c.t_submit, c.t_done, nb))
+            srv.release(t)
+
+    wt = threading.Thread(target=waiter)
+    wt.start()
+    t0 = time.perf_counter()
+    at = t0
+    for i in range(n_req):
+        at += gaps[i]
+        while True:
+            dt = at - time.perf_counter()
+            if dt <= 0:
+                break
+            if dt > 2e-4:
+                time.sleep(dt - 1.5e-4)
+        it = items[picks[i]]
+        if kinds[i]:
+            t = srv.submit_compress(it["x"], it["dims"], it["eb"], "r2r", 1024, 8)
+        else:
+            t = srv.submit_decompress(it["arc"], it["desc"], opts)
+        tickets[i] = (t, it["bytes"])
+    t_sub = time.perf_counter() - t0
+    wt.join()
+    srv.close()
+    lat = np.array([d - s for s, d, _ in done]) * 1e3
+    t_first = min(s for s, _, _ in done)
+    t_last = max(d for _, d, _ in done)
+    total = sum(nb for _, _, nb in done)
+    offered = sum(items[p]["bytes"] for p in picks) / max(t_sub, 1e-9)
+    del items
+    torch.cuda.empty_cache()
+    return {"requests": n_req, "compress": int(kinds.sum()), "decompress": int(n_req - kinds.sum()),
+            "rate_req_s": rate, "arrival_seconds": round(t_sub, 3), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat, 99)), 3), "max_ms": round(float(lat.max()), 3),
+            "sustained_gbs": round(total / (t_last - t_first) / 1e9, 2), "offered_gbs": round(offered / 1e9, 2),
+            "errors": len(errors), "budget_gb": budget_gb, "slots": slots,
+            "workload": f"Poisson {rate} req/s for {seconds} s, 70/30 compress/decompress, sizes log-uniform in "
+                        f"bytes from 256^2 (2D) to 512^3 (3D) over a pool of {pool} fields, r2r eb in "
+                        f"{{1e-2, 1e-3, 1e-4, 1e-5}}, dict 1024, block 8",
+            "latency": "submit to completion (host clock), including queueing for slots and memory"}
 
 
 def run_e2e(V, x, dims, eb, mode, dct, bs, steps, bytes_in, world):
