@@ -387,7 +387,8 @@ def run_batch(V, n_fields, seed, reps, sample_every=25):
     sample = list(range(0, n_fields, sample_every))
     want = {i: b.archives[i][: int(pres[8 * i]) + int(pres[8 * i + 1])].cpu().numpy().tobytes() for i in sample}
     want_res = pres.view(-1, 8)[:, [0, 2, 4, 5]].cpu().clone()
-    # batched path, eager once, then captured and replayed
+    # batched path: task sizes autotuned, eager once, then captured and replayed
+    tuned = b.autotune(iterations=1, stream=stream)
     b.compress(stream)
     stream.synchronize()
     e0.record(stream)
@@ -421,6 +422,7 @@ def run_batch(V, n_fields, seed, reps, sample_every=25):
             "plain_gbs": round(total / (plain_ms * 1e-3) / 1e9, 2),
             "batched_vs_plain": round(plain_ms / graph_ms, 3),
             "batched_ms": round(graph_ms, 3), "plain_ms": round(plain_ms, 3),
+            "task_sizes": {"dq_warp_units": tuned[0], "enc_chunks": tuned[1], "chosen_by": "vsz_batch_autotune"},
             "verified": ok, "check": f"per-field results identical to the plain path for all fields, archives "
                                      f"byte-identical for every {sample_every}th field",
             "workload": f"{n_fields} mixed fields: 1D/2D/3D 20/40/40 %, 16K-16M elements log-uniform, random "

@@ -239,6 +239,27 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
                             uint64_t* d_results, vsz_batch** batch);
 vsz_status vsz_batch_compress(vsz_batch* batch, void* stream);
 void vsz_batch_destroy(vsz_batch* batch);
+/* Work per block-wide task: dual-quant warp units (default 32) and encoder 512-code chunks
+ * (default 64).  Rebuilds and uploads the task lists (synchronous): call before capturing
+ * vsz_batch_compress in a graph.  vsz_batch_autotune times vsz_batch_compress over dual-quant sizes
+ * {8, 16, 32, 64, 128}, then encoder sizes {16, 32, 64, 128, 256} (`iterations` timed runs each
+ * after one warm-up, CUDA events on `stream`, synchronising), keeps the fastest pair and reports it;
+ * the fields' archives are overwritten by the runs.  Archives do not depend on the task sizes. */
+vsz_status vsz_batch_set_task_sizes(vsz_batch* batch, int dq_units, int enc_chunks);
+vsz_status vsz_batch_autotune(vsz_batch* batch, int iterations, int* best_dq_units, int* best_enc_chunks,
+                              void* stream);
+
+/* GPU block-size autotuner (autotune_block_sizes, src/autotune.hh:80-96; the CLI's -a): times the
+ * dual-quant kernel on a leading slab of the field (sample_percent of the slowest axis, at least 64
+ * planes / rows, 64K elements in 1D) at block sizes 8, 16, 32 and 64, `iterations` runs each after
+ * one warm-up, with CUDA events on `stream` (synchronising), and returns the fastest in
+ * *best_block_size (timings_ms[4], optional: ms per run).  The block size changes the archive, as
+ * with the reference's -a.  d_ws: vsz_autotune_workspace_bytes. */
+vsz_status vsz_autotune_workspace_bytes(const vsz_params* p, int ndim, const size_t dims[3], double sample_percent,
+                                        size_t* ws_bytes);
+vsz_status vsz_autotune_block_size(const vsz_params* p, int ndim, const size_t dims[3], const float* d_in,
+                                   double sample_percent, int iterations, void* d_ws, size_t ws_bytes,
+                                   int* best_block_size, double timings_ms[4], void* stream);
 
 /* ---- request server ---------------------------------------------------------------------------
  * Continuous admission of compress / decompress requests under a device-memory budget, their work

@@ -88,3 +88,26 @@ def test_batch_replays_from_cuda_graph(cuda):
             want, _ = _plain(f)
             assert b.archive_bytes(i) == want
     b.close()
+
+
+def test_batch_autotune_keeps_archives(cuda):
+    """Task sizes change how units are handed out, never the archives."""
+    fs = _mixed_fields(cuda, 11, 10)
+    b = V.BatchCompressor(fs)
+    dq, enc = b.autotune(iterations=1)
+    assert dq in (8, 16, 32, 64, 128) and enc in (16, 32, 64, 128, 256)
+    for sizes in ((8, 16), (128, 256), (dq, enc)):
+        b.set_task_sizes(*sizes)
+        b.compress()
+        cuda.cuda.synchronize()
+        for i, f in enumerate(fs):
+            assert b.archive_bytes(i) == _plain(f)[0]
+    b.close()
+
+
+def test_block_size_autotuner(cuda):
+    from vecsz_gb300.api import autotune_block_size
+    x = fields.grf_torch((96, 80, 128), seed=4).reshape(-1)
+    best, t = autotune_block_size(x, (128, 80, 96), eb=1e-4, mode="r2r", sample_percent=50.0, iterations=2)
+    assert best in (8, 16, 32, 64) and all(v > 0 for v in t.values())
+    assert t[best] == min(t.values())

@@ -105,6 +105,11 @@ _PROTOS = {
     "vsz_batch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
     "vsz_batch_compress": ([_p, _p], _i),
     "vsz_batch_destroy": ([_p], None),
+    "vsz_batch_set_task_sizes": ([_p, _i, _i], _i),
+    "vsz_batch_autotune": ([_p, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _p], _i),
+    "vsz_autotune_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t), _d, C.POINTER(C.c_size_t)], _i),
+    "vsz_autotune_block_size": ([_p, _i, C.POINTER(C.c_size_t), _p, _d, _i, _p, _sz, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double), _p], _i),
     "vsz_server_create": ([_sz, _i, C.POINTER(C.c_void_p)], _i),
     "vsz_server_submit": ([_p, _p, C.POINTER(C.c_uint64)], _i),
     "vsz_server_wait": ([_p, C.c_uint64, _d, _p], _i),

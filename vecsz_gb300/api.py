@@ -207,6 +207,16 @@ class BatchCompressor:
     def compress(self, stream=None) -> None:
         check(lib().vsz_batch_compress(self._h, _stream_ptr(stream)), "batch_compress")
 
+    def set_task_sizes(self, dq_units: int, enc_chunks: int) -> None:
+        check(lib().vsz_batch_set_task_sizes(self._h, int(dq_units), int(enc_chunks)), "batch_set_task_sizes")
+
+    def autotune(self, iterations: int = 2, stream=None):
+        """Search the task sizes (vsz_batch_autotune); returns (dq_units, enc_chunks)."""
+        a, b = C.c_int(0), C.c_int(0)
+        check(lib().vsz_batch_autotune(self._h, int(iterations), C.byref(a), C.byref(b), _stream_ptr(stream)),
+              "batch_autotune")
+        return a.value, b.value
+
     def result(self, i) -> Result:
         r = self.results[8 * i: 8 * i + 8].cpu().numpy().view(np.uint64)
         return Result(*[int(v) for v in r])
@@ -227,6 +237,24 @@ class BatchCompressor:
             self.close()
         except Exception:
             pass
+
+
+def autotune_block_size(d_in, dims, eb=1e-4, mode="abs", dict_size=1024, sample_percent=10.0, iterations=3):
+    """GPU block-size autotuner (vsz_autotune_block_size, the CLI's -a): (best block size,
+    {8: ms, 16: ms, 32: ms, 64: ms})."""
+    torch = _torch()
+    dims = tuple(int(v) for v in dims)
+    p = make_params(eb, mode, dict_size, 8)
+    ws = C.c_size_t(0)
+    check(lib().vsz_autotune_workspace_bytes(C.byref(p), len(dims), dims_arg(dims), float(sample_percent),
+                                             C.byref(ws)), "autotune_workspace_bytes")
+    tmp = torch.empty(ws.value, dtype=torch.uint8, device=d_in.device)
+    best = C.c_int(0)
+    t = (C.c_double * 4)()
+    check(lib().vsz_autotune_block_size(C.byref(p), len(dims), dims_arg(dims), _ptr(d_in), float(sample_percent),
+                                        int(iterations), _ptr(tmp), ws.value, C.byref(best), t, _stream_ptr()),
+          "autotune_block_size")
+    return best.value, dict(zip((8, 16, 32, 64), list(t)))
 
 
 class _CudaArray:

@@ -35,7 +35,8 @@ constexpr size_t kCtlBits    = 96;   // u64 payload bits
 constexpr size_t kCtlNOut    = 104;  // u64 outliers
 constexpr size_t kCtlTicket  = 112;  // u32 gather look-back ticket
 
-// Work per task (autotuned defaults): dual-quant warp units, encoder chunks, min/max elements.
+// Work per task (defaults; vsz_batch_autotune searches the first two): dual-quant warp units,
+// encoder chunks, min/max elements.
 constexpr uint64_t kDqUnitsPerTask  = 32;
 constexpr uint64_t kEncChunksPerTask = 64;
 constexpr uint64_t kMinmaxPerTask    = 1 << 20;
@@ -72,6 +73,12 @@ struct vsz_batch {
     int cb_dict_max = 0;
     uint32_t gather_off = 0, gather_n = 0;
     size_t total_chunks = 0;
+    // task lists (own buffer, rebuilt by vsz_batch_set_task_sizes) and what they are built from
+    BatchTask* d_tasks = nullptr;
+    size_t tasks_cap   = 0;
+    uint64_t dq_per = 32, enc_per = 64;
+    std::vector<uint64_t> minmax_units, dq_units, enc_units, gather_units;  // per field
+    std::vector<std::pair<DqGroup, std::vector<uint32_t>>> classes;
     // workspace regions zeroed per call
     uint8_t* ctl = nullptr;
     size_t ctl_bytes = 0;
@@ -191,6 +198,42 @@ int launch_finalize_batch(const FinalizeArgs* args, uint32_t nfields, cudaStream
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
+// Task lists from the per-field unit counts at the batch's task sizes, uploaded (synchronous).
+int upload_tasks(vsz_batch* B) {
+    std::vector<BatchTask> tasks;
+    const uint32_t nf = (uint32_t)B->nfields;
+    B->minmax_off = 0;
+    for (uint32_t f = 0; f < nf; f++)
+        if (B->minmax_units[f]) add_tasks(tasks, f, B->minmax_units[f], kMinmaxPerTask);
+    B->minmax_n = (uint32_t)tasks.size();
+    B->dq_groups.clear();
+    for (auto& kv : B->classes) {
+        DqGroup grp  = kv.first;
+        grp.task_off = (uint32_t)tasks.size();
+        for (uint32_t f : kv.second) add_tasks(tasks, f, B->dq_units[f], B->dq_per);
+        grp.ntasks = (uint32_t)tasks.size() - grp.task_off;
+        B->dq_groups.push_back(grp);
+    }
+    B->enc_off = (uint32_t)tasks.size();
+    for (uint32_t f = 0; f < nf; f++) add_tasks(tasks, f, B->enc_units[f], B->enc_per);
+    B->enc_n      = (uint32_t)tasks.size() - B->enc_off;
+    B->gather_off = (uint32_t)tasks.size();
+    for (uint32_t f = 0; f < nf; f++) add_tasks(tasks, f, B->gather_units[f], 1);
+    B->gather_n = (uint32_t)tasks.size() - B->gather_off;
+    if (tasks.size() > B->tasks_cap) {
+        if (B->d_tasks) cudaFree(B->d_tasks);
+        B->d_tasks   = nullptr;
+        B->tasks_cap = 0;
+        if (cudaMalloc(reinterpret_cast<void**>(&B->d_tasks), sizeof(BatchTask) * tasks.size()) != cudaSuccess)
+            return VSZ_ERR_NOMEM;
+        B->tasks_cap = tasks.size();
+    }
+    if (cudaMemcpy(B->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return VSZ_ERR_CUDA;
+    B->tasks = B->d_tasks;
+    return VSZ_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -222,7 +265,6 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
     std::vector<GatherArgs> ga(nf);
     std::vector<FinalizeArgs> fin(nf);
     std::vector<HuffBuildArgs> build_smem, build_glob;
-    std::vector<BatchTask> tasks;
     vsz_batch* B = new vsz_batch();
     B->nfields   = nfields;
     cudaGetDevice(&B->device);
@@ -320,11 +362,13 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
         fa.chunk_bits    = he.chunk_bits;
         fa.n_chunks      = G.nch;
     }
-    // ---- task lists
-    B->minmax_off = (uint32_t)tasks.size();
-    for (uint32_t f = 0; f < nf; f++)
-        if (fg[f].r2r) add_tasks(tasks, f, fg[f].g.n, kMinmaxPerTask);
-    B->minmax_n = (uint32_t)tasks.size() - B->minmax_off;
+    // ---- what the task lists are built from
+    for (uint32_t f = 0; f < nf; f++) {
+        B->minmax_units.push_back(fg[f].r2r ? fg[f].g.n : 0);
+        B->dq_units.push_back(dq[f].nunits);
+        B->enc_units.push_back(fg[f].nch);
+        B->gather_units.push_back(fg[f].ntiles);
+    }
     std::map<std::tuple<int, int, bool, bool>, std::vector<uint32_t>> classes;
     for (uint32_t f = 0; f < nf; f++) {
         const FieldGeom& G = fg[f];
@@ -335,20 +379,12 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
     for (auto& kv : classes) {
         DqGroup grp{};
         std::tie(grp.ndim, grp.bs, grp.vec, grp.tail) = kv.first;
-        grp.task_off = (uint32_t)tasks.size();
-        for (uint32_t f : kv.second) {
+        for (uint32_t f : kv.second)
             if (dq[f].smem_hist) grp.hist_words = std::max(grp.hist_words, (uint32_t)((dq[f].dict + 3) & ~3));
-            add_tasks(tasks, f, dq[f].nunits, kDqUnitsPerTask);
-        }
-        grp.ntasks = (uint32_t)tasks.size() - grp.task_off;
-        B->dq_groups.push_back(grp);
+        B->classes.emplace_back(grp, kv.second);
     }
-    B->enc_off = (uint32_t)tasks.size();
-    for (uint32_t f = 0; f < nf; f++) add_tasks(tasks, f, fg[f].nch, kEncChunksPerTask);
-    B->enc_n = (uint32_t)tasks.size() - B->enc_off;
-    B->gather_off = (uint32_t)tasks.size();
-    for (uint32_t f = 0; f < nf; f++) add_tasks(tasks, f, fg[f].ntiles, 1);
-    B->gather_n = (uint32_t)tasks.size() - B->gather_off;
+    B->dq_per  = kDqUnitsPerTask;
+    B->enc_per = kEncChunksPerTask;
     B->total_chunks = L.chunk_base.empty() ? 0 : L.chunk_base.back() + fg.back().nch;
     // ---- upload
     std::vector<HuffBuildArgs> build = build_smem;
@@ -364,7 +400,7 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
     const size_t o_mm = place(sizeof(MinmaxField) * nf), o_cs = place(sizeof(ConstsField) * nf),
                  o_dq = place(sizeof(DqArgs) * nf), o_bd = place(sizeof(HuffBuildArgs) * nf),
                  o_en = place(sizeof(HuffEncodeArgs) * nf), o_ga = place(sizeof(GatherArgs) * nf),
-                 o_fi = place(sizeof(FinalizeArgs) * nf), o_tk = place(sizeof(BatchTask) * tasks.size());
+                 o_fi = place(sizeof(FinalizeArgs) * nf);
     const size_t table_bytes = off + 256;
     std::vector<uint8_t> h(table_bytes, 0);
     memcpy(h.data() + o_mm, mm.data(), sizeof(MinmaxField) * nf);
@@ -374,7 +410,6 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
     memcpy(h.data() + o_en, enc.data(), sizeof(HuffEncodeArgs) * nf);
     memcpy(h.data() + o_ga, ga.data(), sizeof(GatherArgs) * nf);
     memcpy(h.data() + o_fi, fin.data(), sizeof(FinalizeArgs) * nf);
-    memcpy(h.data() + o_tk, tasks.data(), sizeof(BatchTask) * tasks.size());
     if (cudaMalloc(reinterpret_cast<void**>(&B->d_tables), table_bytes) != cudaSuccess) {
         delete B;
         return VSZ_ERR_NOMEM;
@@ -391,7 +426,6 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
     B->enc    = reinterpret_cast<const HuffEncodeArgs*>(B->d_tables + o_en);
     B->gather = reinterpret_cast<const GatherArgs*>(B->d_tables + o_ga);
     B->fin    = reinterpret_cast<const FinalizeArgs*>(B->d_tables + o_fi);
-    B->tasks  = reinterpret_cast<const BatchTask*>(B->d_tables + o_tk);
     B->ctl           = L.ctl;
     B->ctl_bytes     = (size_t)nf * kCtlBytes + 256;
     B->batch_status  = L.batch_status;
@@ -405,8 +439,65 @@ vsz_status vsz_batch_create(const vsz_batch_field* fields, int nfields, void* d_
     B->all_off      = L.all_off;
     B->scan_status  = L.scan_status;
     B->scan_counter = L.scan_counter;
+    const int rc    = upload_tasks(B);
+    if (rc != VSZ_OK) {
+        vsz_batch_destroy(B);
+        return rc;
+    }
     *out = B;
     return VSZ_OK;
+}
+
+vsz_status vsz_batch_set_task_sizes(vsz_batch* B, int dq_units, int enc_chunks) {
+    if (!B || dq_units < 1 || enc_chunks < 1) return VSZ_ERR_INVALID;
+    B->dq_per  = (uint64_t)dq_units;
+    B->enc_per = (uint64_t)enc_chunks;
+    return upload_tasks(B);
+}
+
+vsz_status vsz_batch_autotune(vsz_batch* B, int iterations, int* best_dq_units, int* best_enc_chunks, void* stream) {
+    if (!B || iterations < 1) return VSZ_ERR_INVALID;
+    cudaStream_t st = S(stream);
+    cudaEvent_t e0, e1;
+    VSZ_CUDA(cudaEventCreate(&e0));
+    VSZ_CUDA(cudaEventCreate(&e1));
+    auto time_cfg = [&](uint64_t dq, uint64_t enc, float* ms) -> int {
+        VSZ_TRY(vsz_batch_set_task_sizes(B, (int)dq, (int)enc));
+        VSZ_TRY(vsz_batch_compress(B, stream));  // warm-up
+        VSZ_CUDA(cudaEventRecord(e0, st));
+        for (int i = 0; i < iterations; i++) VSZ_TRY(vsz_batch_compress(B, stream));
+        VSZ_CUDA(cudaEventRecord(e1, st));
+        VSZ_CUDA(cudaEventSynchronize(e1));
+        VSZ_CUDA(cudaEventElapsedTime(ms, e0, e1));
+        return VSZ_OK;
+    };
+    // coordinate search: dual-quant task size first, then the encoder's
+    static const uint64_t kDq[]  = {8, 16, 32, 64, 128};
+    static const uint64_t kEnc[] = {16, 32, 64, 128, 256};
+    uint64_t bdq = B->dq_per, benc = B->enc_per;
+    float best = 3.4e38f, ms = 0.f;
+    int rc = VSZ_OK;
+    for (uint64_t dq : kDq) {
+        if ((rc = time_cfg(dq, benc, &ms)) != VSZ_OK) break;
+        if (ms < best) {
+            best = ms;
+            bdq  = dq;
+        }
+    }
+    best = 3.4e38f;
+    for (uint64_t enc : kEnc) {
+        if (rc != VSZ_OK || (rc = time_cfg(bdq, enc, &ms)) != VSZ_OK) break;
+        if (ms < best) {
+            best = ms;
+            benc = enc;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != VSZ_OK) return rc;
+    if (best_dq_units) *best_dq_units = (int)bdq;
+    if (best_enc_chunks) *best_enc_chunks = (int)benc;
+    return vsz_batch_set_task_sizes(B, (int)bdq, (int)benc);
 }
 
 vsz_status vsz_batch_compress(vsz_batch* B, void* stream) {
@@ -457,6 +548,7 @@ vsz_status vsz_batch_compress(vsz_batch* B, void* stream) {
 void vsz_batch_destroy(vsz_batch* B) {
     if (!B) return;
     if (B->d_tables) cudaFree(B->d_tables);
+    if (B->d_tasks) cudaFree(B->d_tasks);
     delete B;
 }
 
