@@ -50,7 +50,15 @@ typedef struct vsz_params {
     int dict_size;  /* -d: number of quant bins, even, 2..65536 */
     int block_size; /* -b: Lorenzo block edge: 8, 16, 32 or 64 */
     int lossless;   /* -L: VSZ_LOSSLESS_* (applied by the host entry points only) */
+    int flags;      /* VSZ_FLAG_*; 0 = the reference's behaviour */
 } vsz_params;
+
+/* Strict error-bound mode (opt-in; no counterpart in the reference).  Every element satisfies
+ * |x - x^| <= eb: an element whose reconstruction would miss eb -- rounding overshoot, |x| / 2eb
+ * beyond float precision, the reference's dropped 2D tail columns -- is stored as an outlier
+ * carrying its input value.  Such archives are not byte-compatible with the reference's (their
+ * outliers are input values, recorded in this library's trailer); single-field entry points only. */
+#define VSZ_FLAG_STRICT_EB 1
 
 /* What a compress produced (device-side vsz_compress writes these 8 u64 into d_result). */
 typedef struct vsz_result {
@@ -87,6 +95,7 @@ typedef struct vsz_archive_desc {
     uint64_t n_chunks;
     uint64_t index_offset;  /* trailer: byte offset of u16 bits-per-chunk, 8-byte aligned */
     uint64_t trailer_size;
+    int strict;             /* trailer: written in strict error-bound mode (VSZ_FLAG_STRICT_EB) */
 } vsz_archive_desc;
 
 /* Options a decompressor needs that the packed block does not store (the reference takes them

@@ -22,6 +22,7 @@ VSZ_ERR_NO_DEVICE = 9
 
 MODE_ABS = 0
 MODE_R2R = 1
+FLAG_STRICT_EB = 1
 
 TREE_DEVICE = 1
 TREE_HOST = 2
@@ -40,7 +41,7 @@ class VszError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("eb", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
-                ("lossless", C.c_int)]
+                ("lossless", C.c_int), ("flags", C.c_int)]
 
 
 class BatchField(C.Structure):
@@ -61,7 +62,7 @@ class ArchiveDesc(C.Structure):
                 ("data_size", C.c_uint64), ("has_trailer", C.c_int), ("eb_final", C.c_double),
                 ("value_range", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
                 ("chunk_syms", C.c_uint32), ("n_chunks", C.c_uint64), ("index_offset", C.c_uint64),
-                ("trailer_size", C.c_uint64)]
+                ("trailer_size", C.c_uint64), ("strict", C.c_int)]
 
 
 class DecompressOpts(C.Structure):

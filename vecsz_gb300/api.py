@@ -19,10 +19,10 @@ _MODES = {"abs": L.MODE_ABS, "r2r": L.MODE_R2R}
 _LOSSLESS = {None: L.LOSSLESS_NONE, "none": L.LOSSLESS_NONE, "zstd": L.LOSSLESS_ZSTD, "gzip": L.LOSSLESS_GZIP}
 
 
-def make_params(eb=1e-4, mode="abs", dict_size=4096, block_size=8, lossless=None) -> Params:
+def make_params(eb=1e-4, mode="abs", dict_size=4096, block_size=8, lossless=None, strict=False) -> Params:
     m = _MODES[mode] if isinstance(mode, str) else int(mode)
     ll = _LOSSLESS[lossless] if (lossless is None or isinstance(lossless, str)) else int(lossless)
-    return Params(float(eb), m, int(dict_size), int(block_size), ll)
+    return Params(float(eb), m, int(dict_size), int(block_size), ll, 1 if strict else 0)
 
 
 @dataclass
@@ -39,12 +39,12 @@ class Compressed:
 
 
 def compress(data: np.ndarray, dims=None, eb: float = 1e-4, mode="abs", dict_size: int = 4096, block_size: int = 8,
-             lossless=None) -> Compressed:
+             lossless=None, strict: bool = False) -> Compressed:
     """Compress a float32 field held in host memory (vecsz::interface::Compress)."""
     x = np.ascontiguousarray(data, dtype=np.float32)
     if dims is None:
         dims = tuple(reversed(x.shape))  # numpy (z, y, x) -> reference (x, y, z)
-    p = make_params(eb, mode, dict_size, block_size, lossless)
+    p = make_params(eb, mode, dict_size, block_size, lossless, strict)
     out = C.c_void_p(0)
     ob, ds, ls, no = C.c_size_t(0), C.c_size_t(0), C.c_size_t(0), C.c_size_t(0)
     check(lib().vsz_compress_host(C.byref(p), len(dims), dims_arg(dims), x.ctypes.data_as(C.c_void_p), C.byref(out),
@@ -115,11 +115,11 @@ class DeviceCodec:
     compress(d_in) writes the archive into self.archive (a uint8 CUDA tensor) and the vsz_result
     record into self.result (8 uint64); nothing is copied to the host unless you ask."""
 
-    def __init__(self, dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8, device="cuda"):
+    def __init__(self, dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8, device="cuda", strict=False):
         torch = _torch()
         self.dims = tuple(int(v) for v in dims)
         self.n = int(np.prod(self.dims))
-        self.params = make_params(eb, mode, dict_size, block_size)
+        self.params = make_params(eb, mode, dict_size, block_size, strict=strict)
         ws, cap = C.c_size_t(0), C.c_size_t(0)
         check(lib().vsz_compress_bounds(C.byref(self.params), len(self.dims), dims_arg(self.dims), C.byref(ws),
                                         C.byref(cap)), "compress_bounds")
@@ -182,7 +182,8 @@ class BatchCompressor:
         self.archives = []
         for i, f in enumerate(fields):
             dims = tuple(int(v) for v in f["dims"])
-            p = make_params(f.get("eb", 1e-4), f.get("mode", "abs"), f.get("dict_size", 1024), f.get("block_size", 8))
+            p = make_params(f.get("eb", 1e-4), f.get("mode", "abs"), f.get("dict_size", 1024), f.get("block_size", 8),
+                            strict=f.get("strict", False))
             ws, cap = C.c_size_t(0), C.c_size_t(0)
             check(lib().vsz_compress_bounds(C.byref(p), len(dims), dims_arg(dims), C.byref(ws), C.byref(cap)),
                   "compress_bounds")

@@ -68,6 +68,7 @@ inline int check_params(const vsz_params* p, int ndim, const size_t* dims) {
     if (!valid_dict(p->dict_size)) return VSZ_ERR_INVALID;
     if (p->block_size <= 0) return VSZ_ERR_INVALID;
     if (!valid_bs(p->block_size)) return VSZ_ERR_UNSUPPORTED;
+    if (p->flags & ~VSZ_FLAG_STRICT_EB) return VSZ_ERR_INVALID;
     return VSZ_OK;
 }
 
@@ -105,6 +106,7 @@ struct FinalizeArgs {
     uint32_t dims[3];
     double eb;  // user eb (header field)
     int mode, dict, bs;
+    int strict;
     size_t hdr;
     const Consts* consts;
     const uint32_t* build_info;             // node count, tree bytes, max len
@@ -162,7 +164,7 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
         double ebf = f.consts->eb_final, vr = f.consts->range;
         put_bytes(t + 16, &ebf, 8);
         put_bytes(t + 24, &vr, 8);
-        int32_t i32[3] = {f.mode, f.dict, f.bs};
+        int32_t i32[3] = {f.mode | (f.strict ? 0x100 : 0), f.dict, f.bs};  // bit 8: strict error-bound mode
         put_bytes(t + 32, i32, 12);
         uint32_t padu = (uint32_t)pad;
         put_bytes(t + 44, &padu, 4);

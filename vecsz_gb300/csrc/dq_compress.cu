@@ -272,6 +272,18 @@ __device__ __forceinline__ void prequant_row(const DqArgs& a, float4 v, bool row
 // current plane's once it has been used.  x - 1 neighbours come from the lane to the left.
 typedef float PrevRows[8][4][32];
 
+// Strict error-bound mode: an element keeps its quant code only if the decompressor, predicting
+// from the same neighbours with its own operation order, reproduces the prequantized value `cur`
+// (pd + e == cur) and the dequantized value is within eb of the input.  Otherwise it becomes an
+// outlier carrying the input value, from which the decompressor re-derives `cur` by the same
+// prequant rule -- so both sides' predictor chains stay identical, element by element.
+__device__ __forceinline__ bool strict_keep(bool q, float pd, float e, float cur, float x, const Consts& c) {
+    if (!q) return false;
+    if (__fadd_rn(pd, e) != cur) return false;
+    const float xh = dequant(cur, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+    return fabs((double)x - (double)xh) <= c.eb_final;
+}
+
 // The histogram share of a block: the threads' private hot-code counters into shared memory, then
 // shared memory into the field's histogram.
 __device__ __forceinline__ void hist_flush_block(const DqArgs& a, uint32_t* s_hist, HistAcc& h) {
@@ -285,8 +297,9 @@ __device__ __forceinline__ void hist_flush_block(const DqArgs& a, uint32_t* s_hi
     }
 }
 
-// Warp units u0, u0 + ustep, ... < u1 of one field.
-template <int NDIM, int BS, bool VEC, bool TAIL>
+// Warp units u0, u0 + ustep, ... < u1 of one field.  STRICT: the strict error-bound mode (see
+// strict_keep).
+template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false>
 __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, unsigned long long u0,
                                            unsigned long long u1, unsigned long long ustep, uint32_t* s_hist,
                                            PrevRows* s_prev, HistAcc& h) {
@@ -376,7 +389,21 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
                     const bool q  = fabsf(e) < Rf;
                     code[j]       = q ? (int)__fadd_rn(e, Rf) : 0;
                     outv[j]       = cur;
-                    if (NDIM == 2 && tail) {
+                    if (STRICT) {
+                        const float xr = j == 0 ? raw.x : (j == 1 ? raw.y : (j == 2 ? raw.z : raw.w));
+                        float pd;  // the decompressor's prediction from the same (in-step) neighbours
+                        if (NDIM == 2) {
+                            pd = __fsub_rn(__fadd_rn(Y, X), XY);
+                        } else {
+                            const float Z   = Pc[j];
+                            const float XZ  = j ? Pc[j - 1] : PcL;
+                            const float YZ  = Pp[j];
+                            const float XYZ = j ? Pp[j - 1] : PpL;
+                            pd = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
+                        }
+                        if (!strict_keep(q, pd, e, cur, xr, c)) code[j] = 0;
+                        outv[j] = xr;  // strict outliers carry the input value
+                    } else if (NDIM == 2 && tail) {
                         code[j] = 0;
                         outv[j] = 0.0f;
                     }
@@ -401,7 +428,7 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
     }
 }
 
-template <int NDIM, int BS, bool VEC, bool TAIL>
+template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false>
 __global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
@@ -415,7 +442,7 @@ __global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     HistAcc h;
-    dq23_units<NDIM, BS, VEC, TAIL>(a, c, warp0, a.nunits, warps_total, s_hist, s_prev, h);
+    dq23_units<NDIM, BS, VEC, TAIL, STRICT>(a, c, warp0, a.nunits, warps_total, s_hist, s_prev, h);
     hist_flush_block(a, s_hist, h);
 }
 
@@ -447,7 +474,7 @@ __global__ void __launch_bounds__(256, 3)
 // 1D: 4 consecutive 128-element tiles per warp unit; the x - 1 neighbour comes from the lane to
 // the left or, at a tile start, from the previous tile's last lane.  Blocks start on multiples of
 // block_size (which divide 128), so tile starts are block starts.
-template <int BS, bool VEC>
+template <int BS, bool VEC, bool STRICT = false>
 __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, unsigned long long u0, unsigned long long u1,
                                            unsigned long long ustep, uint32_t* s_hist, HistAcc& h) {
     const float r_f     = c.r_f;
@@ -457,11 +484,14 @@ __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, uns
     constexpr int U     = 4;
     for (unsigned long long u = u0; u < u1; u += ustep) {
         float S[U][4];
+        float4 RW[STRICT ? U : 1];
 #pragma unroll
         for (int t = 0; t < U; t++) {
             const uint32_t xt = (uint32_t)(u * U + t);
             const uint32_t xb = xt * kTileX + lane * 4;
-            prequant_row<1, false>(a, load_raw<VEC>(a, 0, xt < a.nxt, xb), xt < a.nxt, xb, r_f, 0.0, S[t]);
+            const float4 rw   = load_raw<VEC>(a, 0, xt < a.nxt, xb);
+            if (STRICT) RW[STRICT ? t : 0] = rw;
+            prequant_row<1, false>(a, rw, xt < a.nxt, xb, r_f, 0.0, S[t]);
         }
 #pragma unroll
         for (int t = 0; t < U; t++) {
@@ -478,13 +508,19 @@ __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, uns
                 const bool q     = fabsf(e) < Rf;
                 code[j]          = q ? (int)__fadd_rn(e, Rf) : 0;
                 outv[j]          = S[t][j];
+                if (STRICT) {
+                    const float4 rw = RW[STRICT ? t : 0];
+                    const float xr  = j == 0 ? rw.x : (j == 1 ? rw.y : (j == 2 ? rw.z : rw.w));
+                    if (!strict_keep(q, pred, e, S[t][j], xr, c)) code[j] = 0;
+                    outv[j] = xr;
+                }
             }
             emit_row<VEC>(a, 0, xb, xt, xt < a.nxt, code, outv, h, s_hist);
         }
     }
 }
 
-template <int BS, bool VEC>
+template <int BS, bool VEC, bool STRICT = false>
 __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
     extern __shared__ uint32_t s_hist_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
@@ -497,7 +533,7 @@ __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     HistAcc h;
-    dq1d_units<BS, VEC>(a, c, warp0, a.nunits, warps_total, s_hist, h);
+    dq1d_units<BS, VEC, STRICT>(a, c, warp0, a.nunits, warps_total, s_hist, h);
     hist_flush_block(a, s_hist, h);
 }
 
@@ -735,20 +771,23 @@ static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStr
     if (a.smem_hist) smem = (size_t)((a.dict + 3) & ~3) * sizeof(uint32_t);
     if (NDIM == 3) smem += 8 * 8 * 4 * 32 * sizeof(float);
     static std::atomic<unsigned long long> attr[4];
-    auto go = [&](auto kern, int which) {
-        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[which]);
+    auto go = [&](auto kern, std::atomic<unsigned long long>& at) {
+        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, at);
         kern<<<grid, 256, smem, st>>>(a);
     };
-    if (vec && !tail) go(k_dq_compress_23d<NDIM, BS, true, false>, 0);
-    else if (vec) go(k_dq_compress_23d<NDIM, BS, true, true>, 1);
-    else if (!tail) go(k_dq_compress_23d<NDIM, BS, false, false>, 2);
-    else go(k_dq_compress_23d<NDIM, BS, false, true>, 3);
+    static std::atomic<unsigned long long> attr_strict{0};
+    if (a.strict) go(k_dq_compress_23d<NDIM, BS, false, true, true>, attr_strict);  // general loads, tails at run time
+    else if (vec && !tail) go(k_dq_compress_23d<NDIM, BS, true, false>, attr[0]);
+    else if (vec) go(k_dq_compress_23d<NDIM, BS, true, true>, attr[1]);
+    else if (!tail) go(k_dq_compress_23d<NDIM, BS, false, false>, attr[2]);
+    else go(k_dq_compress_23d<NDIM, BS, false, true>, attr[3]);
     count_launch();
 }
 
 template <int BS>
 static void launch_1d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
-    if (vec) k_dq_compress_1d<BS, true><<<grid, 256, smem, st>>>(a);
+    if (a.strict) k_dq_compress_1d<BS, false, true><<<grid, 256, smem, st>>>(a);
+    else if (vec) k_dq_compress_1d<BS, true><<<grid, 256, smem, st>>>(a);
     else k_dq_compress_1d<BS, false><<<grid, 256, smem, st>>>(a);
     count_launch();
 }

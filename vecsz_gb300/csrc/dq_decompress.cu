@@ -34,6 +34,14 @@ constexpr int kDSeg = 256;  // decompress row segment (one warp of 8-wide blocks
 // Any zero 16-bit half in a word (exact: a borrow out of the low half needs the low half zero).
 __device__ __forceinline__ uint32_t zero_halves(uint32_t w) { return (w - 0x00010001u) & ~w & 0x80008000u; }
 
+// Strict archives: an outlier is the input value; the Lorenzo chain continues from its
+// prequantized value, by the compressor's rule for that column.
+template <int NDIM>
+__device__ __forceinline__ float strict_prequant(float v, uint32_t col, const DqDecArgs& a, const Consts& c) {
+    if (NDIM == 3 && col >= a.xtail) return prequant_scalar(v, c.r_d);
+    return prequant_vec(v, c.r_f);
+}
+
 template <int NDIM, bool VEC>
 __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
@@ -169,6 +177,7 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                                 s = 0.f;
                                 if (oi < a.n_outliers) s = a.outliers[oi];
                                 else set_status(a.status, VSZ_ERR_CORRUPT);
+                                if (a.strict) s = strict_prequant<NDIM>(s, x0 + (uint32_t)k, a, c);
                             }
                         }
                         C[k] = in_at(k) ? s : 0.f;
@@ -182,6 +191,16 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                     float xo[4];
 #pragma unroll
                     for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                    if (a.strict && zm) {  // strict outliers are output as stored
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const int kk = 4 * h + k;
+                            if (zm & (1u << kk)) {
+                                const unsigned long long oi = obase + __popc(zm & ((1u << kk) - 1u));
+                                xo[k] = oi < a.n_outliers ? a.outliers[oi] : 0.f;
+                            }
+                        }
+                    }
                     if (VEC && all_in) {
                         __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
                     } else {
@@ -237,7 +256,7 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
             size_t x = x0 + k;
             if (x >= a.d0) break;
             uint32_t cd = a.codes[x];
-            float s;
+            float s, xo;
             if (cd == 0u) {
                 if ((x & (kDSeg - 1)) == 0) zb = 0;
                 unsigned long long oi = a.seg_off[x / kDSeg] + zb;
@@ -247,12 +266,16 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                     set_status(a.status, VSZ_ERR_CORRUPT);
                 }
                 zb++;
+                xo = s;  // strict: the stored input value
+                if (a.strict) s = strict_prequant<1>(s, (uint32_t)x, a, c);
+                else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
             } else {
                 if ((x & (kDSeg - 1)) == 0) zb = 0;
-                s = __fadd_rn(k ? prev : 0.f, (float)((int)cd - R));
+                s  = __fadd_rn(k ? prev : 0.f, (float)((int)cd - R));
+                xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
             }
             prev     = s;
-            a.out[x] = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+            a.out[x] = xo;
         }
         return;
     }
@@ -300,15 +323,20 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                     const float Z   = zp ? Sp[t * BS + xl] : 0.f;
                     pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
                 }
+                float xo;
                 if (cd == 0u) {
                     unsigned long long oi = a.seg_off[row * a.nxs + (x / kDSeg)] + zrun;
                     if (oi < a.n_outliers) s = a.outliers[oi];
                     else set_status(a.status, VSZ_ERR_CORRUPT);
                     zrun++;
+                    xo = s;  // strict: the stored input value
+                    if (a.strict) s = strict_prequant<NDIM>(s, x, a, c);
+                    else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
                 } else {
-                    s = __fadd_rn(pred, (float)((int)cd - R));
+                    s  = __fadd_rn(pred, (float)((int)cd - R));
+                    xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
                 }
-                a.out[row * a.d0 + x] = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                a.out[row * a.d0 + x] = xo;
             }
             Sc[t * BS + xl] = s;
         }

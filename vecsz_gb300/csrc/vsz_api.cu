@@ -680,6 +680,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     }
     // 2. dual-quant + histogram + outlier ranking
     DqArgs a = make_dq_args(g, p->block_size, dict, d_in, w.consts, w.code, w.scratch, w.seg_count, w.hist);
+    a.strict = (p->flags & VSZ_FLAG_STRICT_EB) ? 1 : 0;
     {
         StageTimer t(kStDualquant, st);
         VSZ_TRY(launch_dq_compress(a, ndim, p->block_size, st, num_sms()));
@@ -745,6 +746,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     f.dims[2] = g.d2;
     f.eb = p->eb;
     f.mode = p->mode;
+    f.strict = a.strict;
     f.dict = dict;
     f.bs = p->block_size;
     f.hdr = hdr;
@@ -818,7 +820,8 @@ vsz_status vsz_archive_parse(const uint8_t* h, size_t len, vsz_archive_desc* d) 
             memcpy(&d->value_range, t + 24, 8);
             int32_t i32[3];
             memcpy(i32, t + 32, 12);
-            d->mode = i32[0];
+            d->mode = i32[0] & 0xff;
+            d->strict = (i32[0] >> 8) & 1;
             d->dict_size = i32[1];
             d->block_size = i32[2];
             uint32_t pad;
@@ -935,6 +938,8 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.d2 = g.d2;
     a.n = g.n;
     a.R = dict / 2;
+    a.strict = d->has_trailer ? d->strict : 0;
+    a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

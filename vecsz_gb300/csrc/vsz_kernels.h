@@ -68,6 +68,7 @@ struct DqArgs {
     int dict;
     int smem_hist;               // 1: histogram privatised in shared memory
     unsigned long long nunits;   // warp work units
+    int strict;                  // strict error-bound mode (outliers carry input values)
 };
 
 struct GatherArgs {
@@ -101,6 +102,8 @@ struct DqDecArgs {
     uint32_t nyb;                        // Lorenzo blocks along y
     uint32_t nbx;                        // Lorenzo blocks along x (general kernel)
     unsigned long long nunits;
+    int strict;                          // strict archive: outliers are input values (re-prequantized)
+    uint32_t xtail;                      // 3D: first scalar-prequant column (d0 & ~7 when d0 % 8), else d0
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
