@@ -72,6 +72,14 @@ def lib():
         L.vso_compress_bound.argtypes = [i, sz, i]
         L.vso_compress_bound.restype = sz
         L.vso_compress.argtypes = [p, i, p, i, i, d, i, p, sz, p, p, p, p]
+        L.vso_compress_pad.argtypes = [p, i, p, i, i, d, i, i, i, C.c_float, p, sz, p, p, p, p]
+        L.vso_compress_bound_pad.argtypes = [i, p, i, i, i]
+        L.vso_compress_bound_pad.restype = sz
+        L.vso_pad_count.argtypes = [i, sz, sz, sz, i, i]
+        L.vso_pad_count.restype = sz
+        L.vso_pad_values.argtypes = [p, i, sz, sz, sz, i, i, i, C.c_float, d, p, p]
+        L.vso_dualquant_pad.argtypes = [p, i, sz, sz, sz, i, i, d, i, i, C.c_float, p, p, p]
+        L.vso_xlorenzo_pad.argtypes = [p, p, i, sz, sz, sz, i, i, d, p, sz, p]
         L.vso_decompress.argtypes = [p, sz, i, i, d, p, sz, p]
         L.vso_parse_header.argtypes = [p, sz, p, p, p, p]
         L.vso_tree_bytes_size.argtypes = [C.c_uint32]
@@ -123,6 +131,65 @@ def dualquant(x: np.ndarray, dims, bs: int, dict_size: int, eb_final: float):
     return code, outl
 
 
+# Padding (-p): modes and value types as the reference numbers them (src/utils/padding.hh:9-12).
+PAD_NONE, PAD_GLOBAL, PAD_BLOCK, PAD_EDGE = 0, 1, 2, 3
+PADV_MAX, PADV_MIN, PADV_AVG, PADV_CONST = 0, 1, 2, 3
+
+
+def pad_count(dims, bs: int, pad_mode: int) -> int:
+    d0, d1, d2 = _dims3(dims)
+    return lib().vso_pad_count(len(dims), d0, d1, d2, bs, pad_mode)
+
+
+def pad_values(x: np.ndarray, dims, bs: int, eb_final: float, pad_mode: int, pad_type: int,
+               pad_const: float = 0.0):
+    """(archive pad values, value the compressor predicts from in global mode)."""
+    x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+    d0, d1, d2 = _dims3(dims)
+    out = np.zeros(max(1, pad_count(dims, bs, pad_mode)), np.float32)
+    hg = C.c_float(0)
+    ebs = eb_family(eb_final)
+    _check(lib().vso_pad_values(_ptr(x), len(dims), d0, d1, d2, bs, pad_mode, pad_type, C.c_float(pad_const),
+                                float(ebs[3]), _ptr(out), C.byref(hg)), "pad_values")
+    return out[:pad_count(dims, bs, pad_mode)], hg.value
+
+
+def dualquant_pad(x: np.ndarray, dims, bs: int, dict_size: int, eb_final: float, pad_mode: int, pad_type: int,
+                  pad_const: float = 0.0):
+    """Dense codes, dense outliers and the pad section, with -p padding."""
+    x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+    d0, d1, d2 = _dims3(dims)
+    n = d0 * d1 * d2
+    code = np.zeros(n, np.int32)
+    outl = np.zeros(n, np.float32)
+    pads = np.zeros(max(1, pad_count(dims, bs, pad_mode)), np.float32)
+    ebs = eb_family(eb_final)
+    _check(lib().vso_dualquant_pad(_ptr(x), len(dims), d0, d1, d2, bs, dict_size // 2, float(ebs[3]), pad_mode,
+                                   pad_type, C.c_float(pad_const), _ptr(code), _ptr(outl), _ptr(pads)),
+           "dualquant_pad")
+    return code, outl, pads[:pad_count(dims, bs, pad_mode)]
+
+
+def ref_pinned_pads(dims, bs: int, pad_mode: int, pad_type: int) -> np.ndarray:
+    """Which pad values of an archive the reference computes deterministically: all of them in 1D
+    (its input is handed over zero-extended), for global mode and for constants; in 2D/3D
+    block/edge max/min/avg only those of blocks wholly inside the field -- for the others it
+    reads an uninitialised buffer (src/utils/padding.hh:18-36, fill_*_block)."""
+    nd = len(dims)
+    d = list(dims) + [1] * (3 - nd)
+    nb = [(v + bs + 1) // bs for v in d]
+    if pad_mode == PAD_GLOBAL:
+        return np.ones(1, bool)
+    per = nd if (pad_mode == PAD_EDGE and nd > 1) else 1
+    out = []
+    for b2 in range(nb[2]):
+        for b1 in range(nb[1]):
+            for b0 in range(nb[0]):
+                inside = all((b + 1) * bs <= v for b, v in zip((b0, b1, b2)[:nd], d[:nd]))
+                out += [nd == 1 or pad_type == PADV_CONST or inside] * per
+    return np.array(out, bool)
+
+
 def gather_outliers(code: np.ndarray, outlier_dense: np.ndarray) -> np.ndarray:
     code = np.ascontiguousarray(code, np.int32)
     outlier_dense = np.ascontiguousarray(outlier_dense, np.float32)
@@ -139,14 +206,17 @@ def scatter_outliers(code: np.ndarray, outliers: np.ndarray) -> np.ndarray:
     return dense
 
 
-def xlorenzo(code: np.ndarray, outlier_dense: np.ndarray, dims, bs: int, dict_size: int, eb_final: float):
+def xlorenzo(code: np.ndarray, outlier_dense: np.ndarray, dims, bs: int, dict_size: int, eb_final: float,
+             pads: np.ndarray | None = None):
     code = np.ascontiguousarray(code, np.int32).ravel()
     outlier_dense = np.ascontiguousarray(outlier_dense, np.float32).ravel()
     d0, d1, d2 = _dims3(dims)
     xhat = np.zeros(d0 * d1 * d2, np.float32)
     ebs = eb_family(eb_final)
-    _check(lib().vso_xlorenzo(_ptr(code), _ptr(outlier_dense), len(dims), d0, d1, d2, bs, dict_size // 2,
-                              float(ebs[2]), _ptr(xhat)), "xlorenzo")
+    npad = 0 if pads is None else int(np.asarray(pads).size)
+    pads = np.zeros(1, np.float32) if npad == 0 else np.ascontiguousarray(pads, np.float32).ravel()
+    _check(lib().vso_xlorenzo_pad(_ptr(code), _ptr(outlier_dense), len(dims), d0, d1, d2, bs, dict_size // 2,
+                                  float(ebs[2]), _ptr(pads), npad, _ptr(xhat)), "xlorenzo")
     return xhat
 
 
@@ -184,17 +254,19 @@ def huffman_decode(buf: bytes, n: int) -> np.ndarray:
 
 
 def compress(x: np.ndarray, dims, bs: int = 8, dict_size: int = 1024, eb: float = 1e-4, r2r: bool = False,
-             timings: np.ndarray | None = None):
+             timings: np.ndarray | None = None, pad_mode: int = PAD_NONE, pad_type: int = PADV_CONST,
+             pad_const: float = 0.0):
     """Packed block bytes (the reference's Compress output without -L), plus metadata dict."""
     x = np.ascontiguousarray(x, dtype=np.float32).ravel()
     ndim = len(dims)
     d = np.array(list(dims) + [1] * (3 - ndim), np.uint64)
-    cap = lib().vso_compress_bound(ndim, x.size, dict_size)
+    cap = lib().vso_compress_bound_pad(ndim, _ptr(d), bs, dict_size, pad_mode)
     out = np.zeros(cap, np.uint8)
     sz, nout, ebf = C.c_size_t(0), C.c_size_t(0), C.c_double(0)
     tp = _ptr(timings) if timings is not None else None
-    _check(lib().vso_compress(_ptr(x), ndim, _ptr(d), bs, dict_size, eb, int(r2r), _ptr(out), cap, C.byref(sz),
-                              C.byref(nout), C.byref(ebf), tp), "compress")
+    _check(lib().vso_compress_pad(_ptr(x), ndim, _ptr(d), bs, dict_size, eb, int(r2r), pad_mode, pad_type,
+                                  C.c_float(pad_const), _ptr(out), cap, C.byref(sz), C.byref(nout), C.byref(ebf),
+                                  tp), "compress")
     return out[:sz.value].tobytes(), {"n_outlier": nout.value, "eb_final": ebf.value}
 
 
@@ -245,6 +317,7 @@ def ref():
         L.vszref_huffman_decode.argtypes = [p, sz, i, p]
         L.vszref_xlorenzo.argtypes = [p, p, i, i, i, i, i, i, d, p]
         L.vszref_compress.argtypes = [p, i, i, i, i, i, i, d, i, i, C.c_char_p, p, p, p, p]
+        L.vszref_compress_pad.argtypes = [p, i, i, i, i, i, i, d, i, i, i, C.c_float, C.c_char_p, p, p, p]
         L.vszref_decompress.argtypes = [p, sz, sz, i, i, i, C.c_char_p, p, sz]
         L.vszref_free.argtypes = [p]
         _ref = L
@@ -308,6 +381,19 @@ def ref_compress(x, dims, bs, dict_size, eb, r2r, lossless, tmpfile):
     data = C.string_at(outp.value, nbytes)
     ref().vszref_free(outp)
     return data, dsz.value, lsz.value, nout.value
+
+
+def ref_compress_pad(x, dims, bs, dict_size, eb, r2r, pad_mode, pad_type, pad_const, tmpfile):
+    """The reference's Compress with -p (one OpenMP thread); (packed block, n_outlier)."""
+    x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+    d0, d1, d2 = _dims3(dims)
+    outp = C.c_void_p(0)
+    dsz, nout = C.c_size_t(0), C.c_size_t(0)
+    ref().vszref_compress_pad(_ptr(x), len(dims), d0, d1, d2, bs, dict_size, eb, int(r2r), pad_mode, pad_type,
+                              C.c_float(pad_const), tmpfile.encode(), C.byref(outp), C.byref(dsz), C.byref(nout))
+    data = C.string_at(outp.value, dsz.value)
+    ref().vszref_free(outp)
+    return data, nout.value
 
 
 def ref_decompress(buf: bytes, data_size: int, lossless_size: int, n: int, bs, dict_size, r2r=False,

@@ -12,12 +12,14 @@
 //   vszref_huffman_decode -> createHuffmanTree + decode_withTree (src/vecsz_interface.hh:307-308)
 //   vszref_xlorenzo       -> per-block x_lorenzo_{1,2,3}d1l (src/vecsz_interface.hh:323-354)
 //   vszref_compress       -> vecsz::interface::Compress<float,int> (src/vecsz_interface.hh:31)
+//   vszref_compress_pad   -> the same with -p padding, on one OpenMP thread
 //   vszref_decompress     -> vecsz::interface::Decompress<float,int> (src/vecsz_interface.hh:232)
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fcntl.h>
+#include <omp.h>
 #include <unistd.h>
 
 #include "vecsz_interface.hh"
@@ -162,7 +164,7 @@ int vszref_xlorenzo(const int32_t* code_in, const float* outlier_in, int ndim, i
     memcpy(code, code_in, len * sizeof(int32_t));
     memcpy(outlier, outlier_in, len * sizeof(float));
     size_t pad_idx = 0;
-    float zero_pad[1] = {0.0f};  // B.4: the reference reads pad_vals[0] from an empty array; use 0
+    float zero_pad[1] = {0.0f};  // the reference reads pad_vals[0] from an empty array here; use 0
     if (ndim == 1) {
         for (size_t b0 = 0; b0 < dims_L16[nBLK0]; b0++)
             vecsz::predictor_quantizer::x_lorenzo_1d1l<float, int>(xdata, outlier, code, dims_L16, ebs_L4[EBx2], b0, bs,
@@ -228,6 +230,44 @@ int vszref_compress(const float* in, int ndim, int d0, int d1, int d2, int bs, i
     return 0;
 }
 
+// Compress<float,int> with padding (-p): pad_mode 1 global, 2 block, 3 edge; pad_type as
+// src/utils/padding.hh:9-12.  Run on one OpenMP thread: the reference's blocks share one pad index
+// (src/dualquant.hh:41), so with more threads the pad order, and the archive, vary run to run.
+int vszref_compress_pad(const float* in, int ndim, int d0, int d1, int d2, int bs, int dict, double eb, int r2r,
+                        int pad_mode, int pad_type, float pad_constant, const char* tmpfile_path, uint8_t** out,
+                        size_t* data_size, size_t* n_outlier) {
+    auto ap               = make_args(ndim, d0, d1, d2, bs, dict, eb, r2r);
+    size_t len            = (size_t)d0 * d1 * d2;
+    ap->files.input_file  = tmpfile_path;
+    ap->szwf.global_padding = pad_mode == 1;
+    ap->szwf.block_padding  = pad_mode == 2;
+    ap->szwf.edge_padding   = pad_mode == 3;
+    ap->pad_type            = pad_type;
+    ap->pad_constant        = pad_constant;
+    FILE* f = fopen(tmpfile_path, "wb");
+    if (!f) return 1;
+    fwrite(in, sizeof(float), len, f);
+    fclose(f);
+    float* data       = padded_copy(in, len, overrun_pad(d0, d1, bs));
+    size_t nout       = 0, dsz = 0;
+    unsigned long lsz = 0;
+    unsigned char* res;
+    const int threads = omp_get_max_threads();
+    omp_set_num_threads(1);
+    {
+        QuietStdout quiet;
+        res = (unsigned char*)vecsz::interface::Compress<float, int>(ap, data, &nout, &dsz, &lsz);
+    }
+    omp_set_num_threads(threads);
+    *out = (uint8_t*)malloc(dsz ? dsz : 1);
+    memcpy(*out, res, dsz);
+    delete[] res;  // Compress deleted `data`
+    *data_size = dsz;
+    *n_outlier = nout;
+    delete ap;
+    return 0;
+}
+
 // Full Decompress<float,int> of a packed block (or lossless frame).  For r2r the reference reads
 // the ORIGINAL field from `orig_file` to recover the value range (src/vecsz_interface.hh:280-284),
 // which only the dry-run workflow supplies correctly.
@@ -243,10 +283,14 @@ int vszref_decompress(const uint8_t* payload, size_t data_size, size_t lossless_
     auto buf             = new unsigned char[bytes + 16]();
     memcpy(buf, payload, bytes);
     float* res;
+    // one OpenMP thread: with padding the blocks share one pad index (src/dualquant.hh:923)
+    const int threads = omp_get_max_threads();
+    omp_set_num_threads(1);
     {
         QuietStdout quiet;
         res = (float*)vecsz::interface::Decompress<float, int>(ap, buf, data_size, lossless_size);
     }
+    omp_set_num_threads(threads);
     memcpy(xdata, res, n * sizeof(float));
     delete[] res;
     delete ap;

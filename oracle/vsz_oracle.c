@@ -102,14 +102,172 @@ static inline void post_scalar(float cur, float pred, int R, int32_t* code, floa
 }
 
 /* ------------------------------------------------------------------------------------------ */
+/* Padding (-p): the value(s) that replace the zero halo of each Lorenzo block.                */
+/* src/utils/padding.hh (find_pad_value :122-143, find_edge_pad_value :145-207, block_pad       */
+/* :209-254, edge_pad :256-301, x_block_pad / x_edge_pad :303-373); call sites                  */
+/* src/vecsz_interface.hh:70-90 (global value, pad array sizes) and src/dualquant.hh:36-46,     */
+/* 224-246, 551-573 (compress), 916-1016 (decompress).                                          */
+/*                                                                                              */
+/* Rules (each one what the single-threaded reference computes):                                */
+/*  - Block grid: get_nblk = (d + bs + 1) / bs per axis (src/dimensions.hh:32), phantom blocks   */
+/*    past the field included; pad values are stored block by block, x fastest.                 */
+/*  - global: p = find_pad_value over the whole field; the archive holds                         */
+/*    (float)round((double)p * r_d) (interface:79); 1D predicts from that value, 2D/3D from      */
+/*    roundf((float)((double)p * r_d)) (block_pad's float multiply then round, padding.hh:219).  */
+/*  - block: one value per block.  1D: find_pad_value over the block's bs raw values, NOT        */
+/*    prequantized (dualquant.hh:40).  2D/3D: over the block's cells (x fastest), then           */
+/*    roundf((float)((double)v * r_d)).                                                          */
+/*  - edge: 1D as block.  2D: [top row y=0, left column x=0]; 3D: [front face z=0 (x, y),        */
+/*    left face x=0 (y, z), top face y=0 (x, z)], each prequantized like block values.           */
+/*    The halo takes them as (padding.hh:286-296): 2D x-halo (and corner) = v0, y-halo = v1;     */
+/*    3D z-halo plane = v0, y-halo = v1, x-halo = v2.                                             */
+/*  - max / min: m = v[0]; m = v[i] > m ? v[i] : m (first maximum wins; a leading NaN sticks).    */
+/*    avg: float running sum in order, divided by (float)count.  constant: the given value.      */
+/*  - Cells outside the field count as 0.0f.  The reference reads memory past the field there    */
+/*    (1D) or an uninitialised buffer (2D/3D fill_*_block); zeros are what it computes when that  */
+/*    memory is zero.                                                                             */
+/* ------------------------------------------------------------------------------------------ */
+
+#define VSO_PAD_NONE 0
+#define VSO_PAD_GLOBAL 1
+#define VSO_PAD_BLOCK 2
+#define VSO_PAD_EDGE 3
+#define VSO_PADV_MAX 0
+#define VSO_PADV_MIN 1
+#define VSO_PADV_AVG 2
+#define VSO_PADV_CONST 3
+
+static size_t nblk_of(size_t d, int bs) { return (d + (size_t)bs + 1) / (size_t)bs; }
+
+/* find_pad_value (padding.hh:122-143) over n values in visiting order. */
+static float find_pad(const float* v, size_t n, int type, float cst) {
+    if (type == VSO_PADV_CONST) return cst;
+    if (type == VSO_PADV_AVG) {
+        float s = 0.0f;
+        for (size_t i = 0; i < n; i++) s += v[i];
+        return s / (float)n;
+    }
+    float m = v[0];
+    for (size_t i = 0; i < n; i++) {
+        if (type == VSO_PADV_MAX) m = (v[i] > m) ? v[i] : m;
+        else m = (v[i] < m) ? v[i] : m;
+    }
+    return m;
+}
+
+static float field_at(const float* x, size_t d0, size_t d1, size_t d2, size_t g0, size_t g1, size_t g2) {
+    return (g0 < d0 && g1 < d1 && g2 < d2) ? x[g0 + d0 * (g1 + d1 * g2)] : 0.0f;
+}
+
+static float prequant_pad(float v, double r_d) {
+    float t = (float)((double)v * r_d); /* padValueLocal *= padValueModifier */
+    return roundf(t);
+}
+
+/* Number of pad values an archive of this geometry holds (interface:78-89). */
+size_t vso_pad_count(int ndim, size_t d0, size_t d1, size_t d2, int bs, int mode) {
+    size_t nb = nblk_of(d0, bs) * nblk_of(d1, bs) * nblk_of(d2, bs);
+    if (mode == VSO_PAD_GLOBAL) return 1;
+    if (mode == VSO_PAD_BLOCK) return nb;
+    if (mode == VSO_PAD_EDGE) return (ndim == 1 ? 1 : (size_t)ndim) * nb;
+    return 0;
+}
+
+/* Pad values: arch[vso_pad_count] as the archive stores them; *halo_global: the value the
+ * compressor predicts from in global mode. */
+int vso_pad_values(const float* x, int ndim, size_t d0, size_t d1, size_t d2, int bs, int mode, int type, float cst,
+                   double r_d, float* arch, float* halo_global) {
+    if (mode < VSO_PAD_NONE || mode > VSO_PAD_EDGE || type < VSO_PADV_MAX || type > VSO_PADV_CONST) return VSO_ERR_ARG;
+    if (halo_global) *halo_global = 0.0f;
+    if (mode == VSO_PAD_NONE) return VSO_OK;
+    if (mode == VSO_PAD_GLOBAL) {
+        float p    = find_pad(x, d0 * d1 * d2, type, cst);
+        arch[0]    = (float)round((double)p * r_d);
+        if (halo_global) *halo_global = (ndim == 1) ? arch[0] : prequant_pad(p, r_d);
+        return VSO_OK;
+    }
+    size_t nb0 = nblk_of(d0, bs), nb1 = nblk_of(d1, bs), nb2 = nblk_of(d2, bs);
+    size_t cells = (size_t)bs * (ndim >= 2 ? (size_t)bs : 1) * (ndim == 3 ? (size_t)bs : 1);
+    float* buf   = (float*)malloc(sizeof(float) * cells);
+    if (!buf) return VSO_ERR_ARG;
+    size_t k = 0;
+    for (size_t b2 = 0; b2 < nb2; b2++)
+        for (size_t b1 = 0; b1 < nb1; b1++)
+            for (size_t b0 = 0; b0 < nb0; b0++) {
+                size_t o0 = b0 * bs, o1 = b1 * bs, o2 = b2 * bs;
+                if (ndim == 1) {
+                    for (int i = 0; i < bs; i++) buf[i] = field_at(x, d0, d1, d2, o0 + i, 0, 0);
+                    arch[k++] = find_pad(buf, (size_t)bs, type, cst);
+                } else if (mode == VSO_PAD_BLOCK) {
+                    size_t c = 0;
+                    for (int j3 = 0; j3 < (ndim == 3 ? bs : 1); j3++)
+                        for (int j = 0; j < bs; j++)
+                            for (int i = 0; i < bs; i++) buf[c++] = field_at(x, d0, d1, d2, o0 + i, o1 + j, o2 + j3);
+                    arch[k++] = prequant_pad(find_pad(buf, cells, type, cst), r_d);
+                } else if (ndim == 2) {
+                    for (int i = 0; i < bs; i++) buf[i] = field_at(x, d0, d1, d2, o0 + i, o1, 0);
+                    arch[k++] = prequant_pad(find_pad(buf, (size_t)bs, type, cst), r_d);
+                    for (int i = 0; i < bs; i++) buf[i] = field_at(x, d0, d1, d2, o0, o1 + i, 0);
+                    arch[k++] = prequant_pad(find_pad(buf, (size_t)bs, type, cst), r_d);
+                } else {
+                    size_t f = (size_t)bs * bs;
+                    for (int j = 0; j < bs; j++)
+                        for (int i = 0; i < bs; i++) buf[i + j * bs] = field_at(x, d0, d1, d2, o0 + i, o1 + j, o2);
+                    arch[k++] = prequant_pad(find_pad(buf, f, type, cst), r_d);
+                    for (int j = 0; j < bs; j++)
+                        for (int i = 0; i < bs; i++) buf[i + j * bs] = field_at(x, d0, d1, d2, o0, o1 + i, o2 + j);
+                    arch[k++] = prequant_pad(find_pad(buf, f, type, cst), r_d);
+                    for (int j = 0; j < bs; j++)
+                        for (int i = 0; i < bs; i++) buf[i + j * bs] = field_at(x, d0, d1, d2, o0 + i, o1, o2 + j);
+                    arch[k++] = prequant_pad(find_pad(buf, f, type, cst), r_d);
+                }
+            }
+    free(buf);
+    return VSO_OK;
+}
+
+/* Halo values of block `blk` (pv[0..2], see the rules above).  mode: how the pad array is read --
+ * NONE (zero halo), GLOBAL (hg for every block), BLOCK (arch[blk]) or EDGE (ndim values). */
+static void block_halo(int ndim, int mode, const float* arch, float hg, size_t blk, float pv[3]) {
+    pv[0] = pv[1] = pv[2] = 0.0f;
+    if (mode == VSO_PAD_GLOBAL) pv[0] = pv[1] = pv[2] = hg;
+    else if (mode == VSO_PAD_BLOCK || (mode == VSO_PAD_EDGE && ndim == 1)) pv[0] = pv[1] = pv[2] = arch[blk];
+    else if (mode == VSO_PAD_EDGE)
+        for (int i = 0; i < ndim; i++) pv[i] = arch[(size_t)ndim * blk + (size_t)i];
+}
+
+/* x_block_pad / x_edge_pad layout of the (bs+1)^ndim block buffer (padding.hh:303-373). */
+static void fill_halo2(float* s, int W, const float pv[3]) {
+    memset(s, 0, sizeof(float) * (size_t)W * W);
+    for (int j = 0; j < W; j++)
+        for (int i = 0; i < W; i++)
+            if (i == 0) s[j * W + i] = pv[0];
+            else if (j == 0) s[j * W + i] = pv[1];
+}
+
+static void fill_halo3(float* s, int W, const float pv[3]) {
+    memset(s, 0, sizeof(float) * (size_t)W * W * W);
+    for (int k = 0; k < W; k++)
+        for (int j = 0; j < W; j++)
+            for (int i = 0; i < W; i++) {
+                float* c = &s[((size_t)k * W + j) * W + i];
+                if (k == 0) *c = pv[0];
+                else if (j == 0) *c = pv[1];
+                else if (i == 0) *c = pv[2];
+            }
+}
+
+/* ------------------------------------------------------------------------------------------ */
 /* c_lorenzo_{1,2,3}d1l, all blocks (src/dualquant.hh:19-913; driven by                        */
 /* src/vecsz_interface.hh:108-140).  Outputs are dense like the reference's `code`/`outlier`    */
 /* arrays: code[i] in [0, 2R), outlier[i] = prequantized value where code[i] == 0, else 0.      */
 /* Block counts follow get_nblk = (d + bs + 1) / bs (src/dimensions.hh:32); blocks wholly       */
 /* outside the field touch nothing.  Requires bs to be a positive multiple of 8.               */
+/* pmode / arch / hg: the halo (block_halo); VSO_PAD_NONE is the reference's zero halo.        */
 /* ------------------------------------------------------------------------------------------ */
 
-static void lorenzo_1d(const float* x, size_t d0, int bs, int R, double r_d, int32_t* code, float* outl) {
+static void lorenzo_1d(const float* x, size_t d0, int bs, int R, double r_d, int32_t* code, float* outl, int pmode,
+                       const float* arch, float hg) {
     const float r_f = (float)r_d, Rf = (float)R;
     long nblk       = (long)((d0 + bs + 1) / bs);
     (void)r_d;
@@ -119,9 +277,12 @@ static void lorenzo_1d(const float* x, size_t d0, int bs, int R, double r_d, int
         if (o >= d0) continue;
         /* Prequant runs on whole 8-wide AVX chunks (blocks start on multiples of 8), the
          * postquant on AVX chunks for blocks with o + bs < d0, scalar otherwise; the two postquant
-         * forms agree on integer-valued residuals (src/dualquant.hh:65-205). */
+         * forms agree on integer-valued residuals (src/dualquant.hh:65-205) -- and differ on the
+         * first element of a block padded with a raw, non-integer value (:155-187). */
         int full  = o + bs < d0;
-        float prev = 0.0f; /* zero halo: padding = 0 without -p */
+        float pv[3];
+        block_halo(1, pmode, arch, hg, (size_t)b0, pv);
+        float prev = pv[0]; /* the block's padding (0 without -p) */
         for (int k = 0; k < bs; k++) {
             size_t g = o + k;
             if (g >= d0) break;
@@ -134,7 +295,7 @@ static void lorenzo_1d(const float* x, size_t d0, int bs, int R, double r_d, int
 }
 
 static void lorenzo_2d(const float* x, size_t d0, size_t d1, int bs, int R, double r_d, int32_t* code,
-                       float* outl) {
+                       float* outl, int pmode, const float* arch, float hg) {
     const float r_f = (float)r_d, Rf = (float)R;
     long nb0 = (long)((d0 + bs + 1) / bs), nb1 = (long)((d1 + bs + 1) / bs);
     const int W = bs + 1;
@@ -146,7 +307,9 @@ static void lorenzo_2d(const float* x, size_t d0, size_t d1, int bs, int R, doub
             for (long b0 = 0; b0 < nb0; b0++) {
                 size_t o0 = (size_t)b0 * bs, o1 = (size_t)b1 * bs;
                 if (o0 >= d0 || o1 >= d1) continue;
-                memset(s, 0, sizeof(float) * W * W);
+                float pv[3];
+                block_halo(2, pmode, arch, hg, (size_t)b0 + (size_t)nb0 * (size_t)b1, pv);
+                fill_halo2(s, W, pv);
                 int interior = (o1 + bs < d1) && (o0 + bs < d0); /* src/dualquant.hh:252 */
                 /* Prequant: every cell of the block goes through the AVX form, edge blocks too
                  * (src/dualquant.hh:268-292,400-424); cells outside the field never feed an
@@ -187,7 +350,7 @@ static void lorenzo_2d(const float* x, size_t d0, size_t d1, int bs, int R, doub
 #define S3(z, y, x) s[((z) * W + (y)) * W + (x)]
 
 static void lorenzo_3d(const float* x, size_t d0, size_t d1, size_t d2, int bs, int R, double r_d, int32_t* code,
-                       float* outl) {
+                       float* outl, int pmode, const float* arch, float hg) {
     const float r_f = (float)r_d, Rf = (float)R;
     long nb0 = (long)((d0 + bs + 1) / bs), nb1 = (long)((d1 + bs + 1) / bs), nb2 = (long)((d2 + bs + 1) / bs);
     const int W = bs + 1;
@@ -200,7 +363,9 @@ static void lorenzo_3d(const float* x, size_t d0, size_t d1, size_t d2, int bs, 
                 for (long b0 = 0; b0 < nb0; b0++) {
                     size_t o0 = (size_t)b0 * bs, o1 = (size_t)b1 * bs, o2 = (size_t)b2 * bs;
                     if (o0 >= d0 || o1 >= d1 || o2 >= d2) continue;
-                    memset(s, 0, sizeof(float) * W * W * W);
+                    float pv[3];
+                    block_halo(3, pmode, arch, hg, (size_t)b0 + (size_t)nb0 * ((size_t)b1 + (size_t)nb1 * (size_t)b2), pv);
+                    fill_halo3(s, W, pv);
                     int interior = (o2 + bs < d2) && (o1 + bs < d1) && (o0 + bs < d0); /* :580 */
                     /* Number of leading AVX elements in each in-range row: interior blocks are all
                      * AVX; edge blocks run 8-wide chunks until the first chunk that is not wholly
@@ -256,9 +421,24 @@ static void lorenzo_3d(const float* x, size_t d0, size_t d1, size_t d2, int bs, 
 int vso_dualquant(const float* x, int ndim, size_t d0, size_t d1, size_t d2, int bs, int radius, double ebx2_r,
                   int32_t* code, float* outlier) {
     if (bs <= 0 || bs % 8) return VSO_ERR_ARG;
-    if (ndim == 1) lorenzo_1d(x, d0, bs, radius, ebx2_r, code, outlier);
-    else if (ndim == 2) lorenzo_2d(x, d0, d1, bs, radius, ebx2_r, code, outlier);
-    else if (ndim == 3) lorenzo_3d(x, d0, d1, d2, bs, radius, ebx2_r, code, outlier);
+    if (ndim == 1) lorenzo_1d(x, d0, bs, radius, ebx2_r, code, outlier, VSO_PAD_NONE, NULL, 0.0f);
+    else if (ndim == 2) lorenzo_2d(x, d0, d1, bs, radius, ebx2_r, code, outlier, VSO_PAD_NONE, NULL, 0.0f);
+    else if (ndim == 3) lorenzo_3d(x, d0, d1, d2, bs, radius, ebx2_r, code, outlier, VSO_PAD_NONE, NULL, 0.0f);
+    else return VSO_ERR_ARG;
+    return VSO_OK;
+}
+
+/* Dual-quant compress with padding: the pad values (vso_pad_values) are computed first, then every
+ * block predicts from its halo.  pad_out: vso_pad_count floats, the archive's pad section. */
+int vso_dualquant_pad(const float* x, int ndim, size_t d0, size_t d1, size_t d2, int bs, int radius, double ebx2_r,
+                      int pad_mode, int pad_type, float pad_const, int32_t* code, float* outlier, float* pad_out) {
+    if (bs <= 0 || bs % 8) return VSO_ERR_ARG;
+    float hg = 0.0f;
+    int rc   = vso_pad_values(x, ndim, d0, d1, d2, bs, pad_mode, pad_type, pad_const, ebx2_r, pad_out, &hg);
+    if (rc) return rc;
+    if (ndim == 1) lorenzo_1d(x, d0, bs, radius, ebx2_r, code, outlier, pad_mode, pad_out, hg);
+    else if (ndim == 2) lorenzo_2d(x, d0, d1, bs, radius, ebx2_r, code, outlier, pad_mode, pad_out, hg);
+    else if (ndim == 3) lorenzo_3d(x, d0, d1, d2, bs, radius, ebx2_r, code, outlier, pad_mode, pad_out, hg);
     else return VSO_ERR_ARG;
     return VSO_OK;
 }
@@ -283,17 +463,31 @@ size_t vso_scatter_outliers(const int32_t* code, const float* outliers, size_t n
 /* s = code == 0 ? outlier : (float)(pred + (code - R)); xhat = (float)((double)s * 2eb).       */
 /* ------------------------------------------------------------------------------------------ */
 
-int vso_xlorenzo(const int32_t* code, const float* outlier, int ndim, size_t d0, size_t d1, size_t d2, int bs,
-                 int radius, double ebx2, float* xhat) {
+/* How a decompressor reads n_pad values (src/vecsz_interface.hh:287-298): 1 -> global, one per
+ * block -> block, ndim per block -> edge, otherwise no padding (zero halo; 1D then reads pad[0]
+ * for every block, dualquant.hh:924-927, and 0 when the section is empty). */
+static int pad_mode_of(size_t npad, int ndim, size_t nb) {
+    if (npad == 1) return VSO_PAD_GLOBAL;
+    if (npad == nb) return VSO_PAD_BLOCK;
+    if (npad == (size_t)ndim * nb) return VSO_PAD_EDGE;
+    return VSO_PAD_NONE;
+}
+
+int vso_xlorenzo_pad(const int32_t* code, const float* outlier, int ndim, size_t d0, size_t d1, size_t d2, int bs,
+                     int radius, double ebx2, const float* pads, size_t npad, float* xhat) {
     if (bs <= 0) return VSO_ERR_ARG;
     const int R = radius;
+    long nb0 = (long)nblk_of(d0, bs), nb1 = (long)nblk_of(d1, bs), nb2 = (long)nblk_of(d2, bs);
+    int pmode = pad_mode_of(npad, ndim, (size_t)nb0 * nb1 * nb2);
     if (ndim == 1) {
-        long nblk = (long)((d0 + bs + 1) / bs);
 #pragma omp parallel for schedule(static)
-        for (long b0 = 0; b0 < nblk; b0++) {
+        for (long b0 = 0; b0 < nb0; b0++) {
             size_t o = (size_t)b0 * bs;
-            /* pad_vals[0] without padding is an empty array in the reference; treated as 0. */
+            /* block / edge: pad[b0]; otherwise pad[0] (0 for an empty pad section: the reference
+             * reads pad_vals[0] from an empty array there) */
             float pad = 0.0f;
+            if (pmode == VSO_PAD_BLOCK || pmode == VSO_PAD_EDGE) pad = pads[b0];
+            else if (npad > 0) pad = pads[0];
             for (int i0 = 0; i0 < bs; i0++) {
                 size_t id = o + i0;
                 if (id >= d0) continue;
@@ -309,15 +503,17 @@ int vso_xlorenzo(const int32_t* code, const float* outlier, int ndim, size_t d0,
         return VSO_OK;
     }
     const int W = bs + 1;
+    const float hg = (pmode == VSO_PAD_GLOBAL) ? pads[0] : 0.0f;
     if (ndim == 2) {
-        long nb0 = (long)((d0 + bs + 1) / bs), nb1 = (long)((d1 + bs + 1) / bs);
 #pragma omp parallel
         {
             float* s = (float*)malloc(sizeof(float) * W * W);
 #pragma omp for schedule(static)
             for (long b1 = 0; b1 < nb1; b1++)
                 for (long b0 = 0; b0 < nb0; b0++) {
-                    memset(s, 0, sizeof(float) * W * W);
+                    float pv[3];
+                    block_halo(2, pmode, pads, hg, (size_t)b0 + (size_t)nb0 * b1, pv);
+                    fill_halo2(s, W, pv);
                     size_t o0 = (size_t)b0 * bs, o1 = (size_t)b1 * bs;
                     for (int i1 = 0; i1 < bs; i1++)
                         for (int i0 = 0; i0 < bs; i0++) {
@@ -335,7 +531,6 @@ int vso_xlorenzo(const int32_t* code, const float* outlier, int ndim, size_t d0,
         return VSO_OK;
     }
     if (ndim == 3) {
-        long nb0 = (long)((d0 + bs + 1) / bs), nb1 = (long)((d1 + bs + 1) / bs), nb2 = (long)((d2 + bs + 1) / bs);
 #pragma omp parallel
         {
             float* s = (float*)malloc(sizeof(float) * W * W * W);
@@ -343,7 +538,9 @@ int vso_xlorenzo(const int32_t* code, const float* outlier, int ndim, size_t d0,
             for (long b2 = 0; b2 < nb2; b2++)
                 for (long b1 = 0; b1 < nb1; b1++)
                     for (long b0 = 0; b0 < nb0; b0++) {
-                        memset(s, 0, sizeof(float) * W * W * W);
+                        float pv[3];
+                        block_halo(3, pmode, pads, hg, (size_t)b0 + (size_t)nb0 * ((size_t)b1 + (size_t)nb1 * b2), pv);
+                        fill_halo3(s, W, pv);
                         size_t o0 = (size_t)b0 * bs, o1 = (size_t)b1 * bs, o2 = (size_t)b2 * bs;
                         for (int i2 = 0; i2 < bs; i2++)
                             for (int i1 = 0; i1 < bs; i1++)
@@ -364,6 +561,11 @@ int vso_xlorenzo(const int32_t* code, const float* outlier, int ndim, size_t d0,
         return VSO_OK;
     }
     return VSO_ERR_ARG;
+}
+
+int vso_xlorenzo(const int32_t* code, const float* outlier, int ndim, size_t d0, size_t d1, size_t d2, int bs,
+                 int radius, double ebx2, float* xhat) {
+    return vso_xlorenzo_pad(code, outlier, ndim, d0, d1, d2, bs, radius, ebx2, NULL, 0, xhat);
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -774,8 +976,8 @@ int vso_huffman_decode(const uint8_t* in, size_t in_len, size_t n, int32_t* out)
 }
 
 /* ------------------------------------------------------------------------------------------ */
-/* Whole-field compress / decompress (src/vecsz_interface.hh:31-229, 232-375) without padding    */
-/* and without the lossless pass.  The packed block (src/utils/datapack.hh:17-29):              */
+/* Whole-field compress / decompress (src/vecsz_interface.hh:31-229, 232-375), with optional    */
+/* padding, without the lossless pass.  The packed block (src/utils/datapack.hh:17-29):         */
 /*   i32 ndim; i32 dims[ndim]; f64 eb (the user's eb); u64 {n_pad, huff_bytes, n_outliers};     */
 /*   f32 pad[n_pad]; huffman bytes; f32 outliers[n_outliers]                                     */
 /* ------------------------------------------------------------------------------------------ */
@@ -784,9 +986,18 @@ size_t vso_compress_bound(int ndim, size_t n, int dict) {
     return 4 * (size_t)(ndim + 1) + 8 + 24 + vso_huffman_bound(n, dict) + 4 * n;
 }
 
-/* timings (optional, seconds): [0] value range, [1] dual-quant, [2] Huffman, [3] outlier gather */
-int vso_compress(const float* x, int ndim, const size_t* dims, int bs, int dict, double eb, int r2r, uint8_t* out,
-                 size_t cap, size_t* out_size, size_t* n_outlier, double* eb_final_out, double* timings) {
+/* ... plus the pad section of -p (vso_pad_count floats). */
+size_t vso_compress_bound_pad(int ndim, const size_t* dims, int bs, int dict, int pad_mode) {
+    size_t d0 = dims[0], d1 = ndim > 1 ? dims[1] : 1, d2 = ndim > 2 ? dims[2] : 1;
+    return vso_compress_bound(ndim, d0 * d1 * d2, dict) + 4 * vso_pad_count(ndim, d0, d1, d2, bs, pad_mode);
+}
+
+/* timings (optional, seconds): [0] value range, [1] dual-quant, [2] Huffman, [3] outlier gather.
+ * pad_mode / pad_type / pad_const: -p (VSO_PAD_*, VSO_PADV_*); the pad values follow the header
+ * (src/utils/datapack.hh:23). */
+int vso_compress_pad(const float* x, int ndim, const size_t* dims, int bs, int dict, double eb, int r2r, int pad_mode,
+                     int pad_type, float pad_const, uint8_t* out, size_t cap, size_t* out_size, size_t* n_outlier,
+                     double* eb_final_out, double* timings) {
     if (ndim < 1 || ndim > 3 || dict < 2 || dict > 65536 || eb <= 0) return VSO_ERR_ARG;
     size_t d0 = dims[0], d1 = ndim > 1 ? dims[1] : 1, d2 = ndim > 2 ? dims[2] : 1;
     size_t n  = d0 * d1 * d2;
@@ -803,14 +1014,21 @@ int vso_compress(const float* x, int ndim, const size_t* dims, int bs, int dict,
     double t1       = now_s();
     int32_t* code   = (int32_t*)calloc(n, sizeof(int32_t));
     float* outl     = (float*)calloc(n, sizeof(float));
-    int rc = vso_dualquant(x, ndim, d0, d1, d2, bs, dict / 2, ebs[3], code, outl);
+    size_t npad     = vso_pad_count(ndim, d0, d1, d2, bs, pad_mode);
+    float* pads     = (float*)calloc(npad ? npad : 1, sizeof(float));
+    int rc = vso_dualquant_pad(x, ndim, d0, d1, d2, bs, dict / 2, ebs[3], pad_mode, pad_type, pad_const, code, outl,
+                               pads);
+    size_t hdr = 4 * (size_t)(ndim + 1) + 8 + 24 + 4 * npad;
+    if (!rc && hdr > cap) rc = VSO_ERR_CAPACITY;
     if (rc) {
         free(code);
         free(outl);
+        free(pads);
         return rc;
     }
+    memcpy(out + hdr - 4 * npad, pads, 4 * npad);
+    free(pads);
     double t2 = now_s();
-    size_t hdr = 4 * (size_t)(ndim + 1) + 8 + 24;
     size_t hsz = 0;
     rc         = vso_huffman_encode(code, n, dict, out + hdr, cap > hdr ? cap - hdr : 0, &hsz);
     if (rc) {
@@ -835,7 +1053,7 @@ int vso_compress(const float* x, int ndim, const size_t* dims, int bs, int dict,
     int32_t meta[4] = {ndim, (int32_t)d0, (int32_t)d1, (int32_t)d2};
     memcpy(out, meta, 4 * (size_t)(ndim + 1));
     memcpy(out + 4 * (ndim + 1), &eb, 8);
-    uint64_t lens[3] = {0, (uint64_t)hsz, (uint64_t)k};
+    uint64_t lens[3] = {(uint64_t)npad, (uint64_t)hsz, (uint64_t)k};
     memcpy(out + 4 * (ndim + 1) + 8, lens, 24);
     *out_size = pos + 4 * k;
     if (n_outlier) *n_outlier = k;
@@ -849,6 +1067,12 @@ int vso_compress(const float* x, int ndim, const size_t* dims, int bs, int dict,
     free(code);
     free(outl);
     return VSO_OK;
+}
+
+int vso_compress(const float* x, int ndim, const size_t* dims, int bs, int dict, double eb, int r2r, uint8_t* out,
+                 size_t cap, size_t* out_size, size_t* n_outlier, double* eb_final_out, double* timings) {
+    return vso_compress_pad(x, ndim, dims, bs, dict, eb, r2r, VSO_PAD_NONE, VSO_PADV_CONST, 0.0f, out, cap, out_size,
+                            n_outlier, eb_final_out, timings);
 }
 
 /* Parse the packed block's header.  dims_out[3] (missing dims = 1). */
@@ -895,13 +1119,16 @@ int vso_decompress(const uint8_t* in, size_t len, int bs, int dict, double value
     int32_t* code      = (int32_t*)malloc(n * sizeof(int32_t));
     float* dense       = (float*)malloc(n * sizeof(float));
     float* outl_copy   = (float*)malloc((lens[2] ? lens[2] : 1) * sizeof(float));
+    float* pads        = (float*)malloc((lens[0] ? lens[0] : 1) * sizeof(float));
     memcpy(outl_copy, outs, lens[2] * sizeof(float));
+    memcpy(pads, in + hdr, lens[0] * sizeof(float));
     double t0 = now_s();
     rc        = vso_huffman_decode(hp, lens[1], n, code);
     if (rc) {
         free(code);
         free(dense);
         free(outl_copy);
+        free(pads);
         return rc;
     }
     double t1 = now_s();
@@ -911,11 +1138,12 @@ int vso_decompress(const uint8_t* in, size_t len, int bs, int dict, double value
         free(code);
         free(dense);
         free(outl_copy);
+        free(pads);
         return VSO_ERR_CORRUPT;
     }
     vso_scatter_outliers(code, outl_copy, n, dense);
     double t2 = now_s();
-    rc = vso_xlorenzo(code, dense, ndim, dims[0], dims[1], dims[2], bs, dict / 2, ebs[2], xhat);
+    rc = vso_xlorenzo_pad(code, dense, ndim, dims[0], dims[1], dims[2], bs, dict / 2, ebs[2], pads, lens[0], xhat);
     double t3 = now_s();
     if (timings) {
         timings[0] = t1 - t0;
@@ -925,6 +1153,7 @@ int vso_decompress(const uint8_t* in, size_t len, int bs, int dict, double value
     free(code);
     free(dense);
     free(outl_copy);
+    free(pads);
     return rc;
 }
 

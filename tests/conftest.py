@@ -16,17 +16,25 @@ def pytest_configure(config):
 
 
 def golden_cases():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Unpadded fixtures (stage outputs and archives)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("p"))
+
+
+def pad_golden_cases():
+    """Padded (-p) fixtures: archive and reconstruction."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("p"))
 
 
 def load_golden(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     g = {k: z[k] for k in z.files}
     g["dims"] = tuple(int(v) for v in g["dims"])
-    for k in ("bs", "dict_size", "r2r", "data_size", "n_outlier"):
-        g[k] = int(g[k])
-    for k in ("eb", "eb_final"):
-        g[k] = float(g[k])
+    for k in ("bs", "dict_size", "r2r", "data_size", "n_outlier", "pad_mode", "pad_type"):
+        if k in g:
+            g[k] = int(g[k])
+    for k in ("eb", "eb_final", "pad_const"):
+        if k in g:
+            g[k] = float(g[k])
     g["name"] = name
     return g
 

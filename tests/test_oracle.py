@@ -8,9 +8,61 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, load_golden, pad_golden_cases
 
 CASES = golden_cases()
+PAD_CASES = pad_golden_cases()
+
+
+def pad_section(archive: bytes, ndim: int, npad: int) -> np.ndarray:
+    hdr = 4 * (ndim + 1) + 8 + 24
+    return np.frombuffer(archive[hdr:hdr + 4 * npad], np.uint32)
+
+
+def assert_same_padded_archive(got: bytes, want: bytes, ndim: int, pinned: np.ndarray):
+    """Byte-equal packed blocks, except pad values the reference leaves unpinned."""
+    assert len(got) == len(want)
+    npad = pinned.size
+    hdr = 4 * (ndim + 1) + 8 + 24
+    assert got[:hdr] == want[:hdr]
+    np.testing.assert_array_equal(pad_section(got, ndim, npad)[pinned], pad_section(want, ndim, npad)[pinned])
+    assert got[hdr + 4 * npad:] == want[hdr + 4 * npad:]
+
+
+@pytest.mark.parametrize("name", PAD_CASES)
+def test_oracle_matches_golden_padded(name):
+    g = load_golden(name)
+    archive, meta = O.compress(g["x"], g["dims"], g["bs"], g["dict_size"], g["eb"], bool(g["r2r"]),
+                               pad_mode=g["pad_mode"], pad_type=g["pad_type"], pad_const=g["pad_const"])
+    assert_same_padded_archive(archive, g["archive"].tobytes(), len(g["dims"]), g["pad_pinned"])
+    assert meta["n_outlier"] == g["n_outlier"]
+    vr = O.value_range(g["x"]) if g["r2r"] else 0.0
+    # the reference's own archive decodes to the reference's reconstruction
+    xhat = O.decompress(g["archive"].tobytes(), g["bs"], g["dict_size"], vr)
+    np.testing.assert_array_equal(xhat.view(np.uint32), g["xhat"].view(np.uint32))
+
+
+def test_oracle_padding_corner_codes():
+    """1D raw block pads: code 2R (one past the dictionary) and a quantizable code 0."""
+    g = load_golden("p1_block_min_corner")
+    code, outl, pads = O.dualquant_pad(g["x"], g["dims"], g["bs"], g["dict_size"], g["eb"], O.PAD_BLOCK,
+                                       O.PADV_MIN)
+    assert code[0] == g["dict_size"]               # residual 513 - 1.3 = 511.7 -> rint(1023.7) = 1024
+    assert np.float32(pads[0]) == np.float32(1.3)  # raw block minimum, not prequantized
+    code, outl, pads = O.dualquant_pad(g["x"], g["dims"], g["bs"], g["dict_size"], g["eb"], O.PAD_BLOCK,
+                                       O.PADV_MAX)
+    assert code[8] == 0 and outl[8] == 0.0         # residual -510 - 1.7 = -511.7 -> rint(0.3) = 0, quantizable
+
+
+def test_oracle_pad_counts():
+    # get_nblk = (d + bs + 1) // bs per axis; edge mode stores ndim values per block (1 in 1D)
+    assert O.pad_count((16,), 8, O.PAD_BLOCK) == 3
+    assert O.pad_count((14,), 8, O.PAD_BLOCK) == 2
+    assert O.pad_count((16,), 8, O.PAD_EDGE) == 3
+    assert O.pad_count((16, 17), 8, O.PAD_EDGE) == 2 * 3 * 3
+    assert O.pad_count((8, 8, 8), 8, O.PAD_EDGE) == 3 * 8
+    assert O.pad_count((100, 7, 3), 16, O.PAD_GLOBAL) == 1
+    assert O.pad_count((100,), 16, O.PAD_NONE) == 0
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -99,3 +151,39 @@ def test_oracle_matches_reference_random_shapes(seed):
         y_ref = O.ref_decompress(a_ref, dsz, 0, n, bs, dct, r2r, f)
         y_or = O.decompress(a_or, bs, dct, O.value_range(x) if r2r else 0.0)
         np.testing.assert_array_equal(y_or.view(np.uint32), y_ref.view(np.uint32))
+
+
+@ref_only
+@pytest.mark.parametrize("seed", range(8))
+def test_oracle_matches_reference_padding(seed):
+    """Padded archives and reconstructions against the reference itself (one OpenMP thread)."""
+    if not O.ref_available():
+        if O.build_ref() is None:
+            pytest.skip("reference cannot be built on this machine")
+    rng = np.random.default_rng(300 + seed)
+    ndim = 1 + seed % 3
+    bs = int(rng.choice([8, 16]))
+    mode = 1 + seed % 3 if seed < 6 else int(rng.integers(1, 4))
+    ptype = int(rng.integers(0, 4))
+    whole = mode == 1 or ptype == 3 or ndim == 1
+    if ndim == 1:
+        dims = (int(rng.integers(50, 3000)),)
+    elif ndim == 2:
+        dims = (int(rng.integers(5, 120)), int(rng.integers(5, 90))) if whole else \
+            (bs * int(rng.integers(1, 8)), bs * int(rng.integers(1, 6)))
+    else:
+        dims = tuple(int(rng.integers(3, 30)) for _ in range(3)) if whole else \
+            tuple(bs * int(rng.integers(1, 4)) for _ in range(3))
+    n = int(np.prod(dims))
+    x = (np.cumsum(rng.standard_normal(n)) * 10 ** rng.uniform(-2, 1)).astype(np.float32)
+    eb = float(10 ** rng.uniform(-5, -2))
+    cst = float(rng.choice([0.0, 0.37, 12.5, -3.25]))
+    r2r = bool(seed % 2)
+    tmp = tempfile.mkdtemp()
+    f = os.path.join(tmp, "f.f32")
+    a_ref, nout = O.ref_compress_pad(x, dims, bs, 1024, eb, r2r, mode, ptype, cst, f)
+    a_or, meta = O.compress(x, dims, bs, 1024, eb, r2r, pad_mode=mode, pad_type=ptype, pad_const=cst)
+    assert_same_padded_archive(a_or, a_ref, ndim, O.ref_pinned_pads(dims, bs, mode, ptype))
+    y_ref = O.ref_decompress(a_ref, len(a_ref), 0, n, bs, 1024, r2r, f)
+    y_or = O.decompress(a_ref, bs, 1024, O.value_range(x) if r2r else 0.0)
+    np.testing.assert_array_equal(y_or.view(np.uint32), y_ref.view(np.uint32))
