@@ -51,7 +51,34 @@ typedef struct vsz_params {
     int block_size; /* -b: Lorenzo block edge: 8, 16, 32 or 64 */
     int lossless;   /* -L: VSZ_LOSSLESS_* (applied by the host entry points only) */
     int flags;      /* VSZ_FLAG_*; 0 = the reference's behaviour */
+    int pad_mode;   /* -p: VSZ_PAD_*; 0 = the zero halo (no -p) */
+    int pad_type;   /* -p: VSZ_PADV_* (the reference's default: constant) */
+    float pad_constant; /* -p constant value (the number in the -p string) */
 } vsz_params;
+
+/* Padding (-p; src/utils/padding.hh, src/argument_parser/argparse.cc:399-415): the value(s) that
+ * replace the zero halo of every Lorenzo block, stored in the packed block's pad section.
+ *   global: one value from the whole field; block: one per block; edge: one per block face
+ *   (1D: one per block).  Blocks are counted as the reference does, (d + bs + 1) / bs per axis.
+ *   1D block / edge values are raw (not prequantized), as in the reference; such fields may give
+ *   the code 2 * radius, so their dict_size must be at most 32768.
+ *   Cells outside the field count as 0 (the reference reads past the field there).
+ * Single-field entry points only (vsz_compress and the host / server paths built on it). */
+#define VSZ_PAD_NONE 0
+#define VSZ_PAD_GLOBAL 1
+#define VSZ_PAD_BLOCK 2
+#define VSZ_PAD_EDGE 3
+#define VSZ_PADV_MAX 0
+#define VSZ_PADV_MIN 1
+#define VSZ_PADV_AVG 2   /* float running sum in field order, as the reference (a serial pass) */
+#define VSZ_PADV_CONST 3
+/* Parses a -p string as the reference's command line does: "global" / "block" / "edge",
+ * "max" / "min" / "avg" / "constant" and the first number in it, into p->pad_*; global wins over
+ * block and edge, block over edge (argparse.cc:156-170).  The type stays constant when none is
+ * named. */
+vsz_status vsz_parse_padding(const char* spec, vsz_params* p);
+/* Number of pad values a packed block of this geometry holds (0 without padding). */
+size_t vsz_pad_count(int ndim, const size_t dims[3], int block_size, int pad_mode);
 
 /* Strict error-bound mode (opt-in; no counterpart in the reference).  Every element satisfies
  * |x - x^| <= eb: an element whose reconstruction would miss eb -- rounding overshoot, |x| / 2eb

@@ -277,3 +277,24 @@ def test_general_kernels_match_oracle(cuda, monkeypatch, seed):
 def test_long_codewords_general_decoder(cuda, monkeypatch):
     monkeypatch.setenv("VSZ_DECODE_NO_WINDOW", "1")
     test_long_codewords_match_oracle(cuda)
+
+
+@pytest.mark.parametrize("dims,bs", [((96, 40), 8), ((37, 41, 43), 8), ((5000,), 16), ((64, 64, 16), 16)])
+def test_nan_inputs_keep_reference_bits(cuda, dims, bs):
+    """NaN inputs (quiet with payloads, negative, signalling): the reference's arithmetic keeps a
+    NaN operand's bits, quieted, where the GPU's would give its canonical NaN; outliers and
+    reconstructions must carry the reference's bits."""
+    rng = np.random.default_rng(sum(dims) + bs)
+    n = int(np.prod(dims))
+    x = (np.cumsum(rng.standard_normal(n)) * 0.1).astype(np.float32)
+    bits = x.view(np.uint32)
+    idx = rng.choice(n, 12, replace=False)
+    bits[idx[:4]] = 0x7fc01234
+    bits[idx[4:8]] = 0xffc00001
+    bits[idx[8:]] = 0x7f800005   # signalling
+    bits[0] = 0x7fc0beef
+    c = V.compress(x, dims, eb=1e-3, dict_size=1024, block_size=bs)
+    oa, _ = O.compress(x, dims, bs, 1024, 1e-3, False)
+    assert c.data[:c.data_size] == oa
+    y = V.decompress(c)
+    np.testing.assert_array_equal(y.view(np.uint32), O.decompress(oa, bs, 1024).view(np.uint32))

@@ -190,3 +190,45 @@ def test_tree_builder_switch():
     assert lib.vsz_set_tree_builder(L.TREE_DEVICE) == prev
     assert lib.vsz_set_tree_builder(-1) == L.TREE_DEVICE
     lib.vsz_set_tree_builder(prev)
+
+
+@pytest.mark.parametrize("spec,want", [
+    ("block,max", (L.PAD_BLOCK, L.PADV_MAX, 0.0)),
+    ("global", (L.PAD_GLOBAL, L.PADV_CONST, 0.0)),
+    ("edge,avg", (L.PAD_EDGE, L.PADV_AVG, 0.0)),
+    ("block,edge,min", (L.PAD_BLOCK, L.PADV_MIN, 0.0)),        # block wins over edge
+    ("global,block,avg", (L.PAD_GLOBAL, L.PADV_AVG, 0.0)),     # global wins over block / edge
+    ("block,constant,12.5", (L.PAD_BLOCK, L.PADV_CONST, 12.5)),
+    ("edge,constant,-3.25", (L.PAD_EDGE, L.PADV_CONST, 3.25)),  # the reference's regex reads no sign
+    ("global,constant,.5", (L.PAD_GLOBAL, L.PADV_CONST, 0.5)),
+    ("block,constant,7.x", (L.PAD_BLOCK, L.PADV_CONST, 7.0)),
+    ("max,min", (L.PAD_NONE, L.PADV_MIN, 0.0)),                # later type names win; no mode named
+])
+def test_parse_padding_like_reference_cli(spec, want):
+    p = V.make_params(padding=spec)
+    assert (p.pad_mode, p.pad_type) == want[:2]
+    assert p.pad_constant == pytest.approx(want[2])
+
+
+def test_padding_argument_checks_and_counts():
+    def bounds(ndim, dims, dict_size=1024, padding="block,max", strict=False):
+        p = V.make_params(eb=1e-3, dict_size=dict_size, block_size=8, padding=padding, strict=strict)
+        ws, cap = C.c_size_t(0), C.c_size_t(0)
+        rc = V.lib().vsz_compress_bounds(C.byref(p), ndim, L.dims_arg(dims), C.byref(ws), C.byref(cap))
+        return rc, cap.value
+    rc0, cap0 = bounds(2, (64, 64), padding=None)
+    rc1, cap1 = bounds(2, (64, 64), padding="edge,max")
+    assert rc0 == rc1 == L.VSZ_OK
+    assert cap1 >= cap0 + 4 * 2 * 9 * 9   # 9 x 9 blocks of the reference grid, 2 values each
+    assert bounds(1, (1000,), dict_size=65536)[0] == L.VSZ_ERR_UNSUPPORTED      # code 2R must fit u16
+    assert bounds(1, (1000,), dict_size=65536, padding="global,max")[0] == L.VSZ_OK
+    assert bounds(2, (64, 64), strict=True)[0] == L.VSZ_ERR_UNSUPPORTED
+    p = V.make_params(padding="block,max")
+    p.pad_type = 9
+    ws, cap = C.c_size_t(0), C.c_size_t(0)
+    assert V.lib().vsz_compress_bounds(C.byref(p), 1, L.dims_arg((100,)), C.byref(ws), C.byref(cap)) == \
+        L.VSZ_ERR_INVALID
+    for dims, mode in [((16,), "block"), ((14,), "block"), ((16, 17), "edge"), ((8, 8, 8), "edge"),
+                       ((100, 7, 3), "global"), ((100,), None)]:
+        mcode = {"block": O.PAD_BLOCK, "edge": O.PAD_EDGE, "global": O.PAD_GLOBAL, None: O.PAD_NONE}[mode]
+        assert V.pad_count(dims, 8, mode and mode + ",max") == O.pad_count(dims, 8, mcode)

@@ -5,7 +5,7 @@ include/vecsz_gb300.h); this package binds it with ctypes.  There is no CPU fall
 """
 from ._lib import VszError, lib, library_path  # noqa: F401
 from .api import (BatchCompressor, Compressed, DeviceCodec, Server, compress, decompress,  # noqa: F401
-                  make_params, parse_archive, read_sz_file)
+                  make_params, pad_count, parse_archive, read_sz_file)
 
 __all__ = ["VszError", "lib", "library_path", "BatchCompressor", "Compressed", "DeviceCodec", "Server",
-           "compress", "decompress", "make_params", "parse_archive", "read_sz_file"]
+           "compress", "decompress", "make_params", "pad_count", "parse_archive", "read_sz_file"]

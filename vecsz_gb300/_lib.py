@@ -24,6 +24,10 @@ MODE_ABS = 0
 MODE_R2R = 1
 FLAG_STRICT_EB = 1
 
+# -p padding (include/vecsz_gb300.h VSZ_PAD_*, VSZ_PADV_*)
+PAD_NONE, PAD_GLOBAL, PAD_BLOCK, PAD_EDGE = 0, 1, 2, 3
+PADV_MAX, PADV_MIN, PADV_AVG, PADV_CONST = 0, 1, 2, 3
+
 TREE_DEVICE = 1
 TREE_HOST = 2
 LOSSLESS_NONE = 0
@@ -41,7 +45,8 @@ class VszError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("eb", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
-                ("lossless", C.c_int), ("flags", C.c_int)]
+                ("lossless", C.c_int), ("flags", C.c_int), ("pad_mode", C.c_int), ("pad_type", C.c_int),
+                ("pad_constant", C.c_float)]
 
 
 class BatchField(C.Structure):
@@ -88,6 +93,8 @@ _p, _sz, _i, _d, _u64p, _u32p = C.c_void_p, C.c_size_t, C.c_int, C.c_double, C.c
 _PROTOS = {
     "vsz_status_string": ([_i], C.c_char_p),
     "vsz_version": ([], C.c_char_p),
+    "vsz_parse_padding": ([C.c_char_p, C.POINTER(Params)], _i),
+    "vsz_pad_count": ([_i, C.POINTER(C.c_size_t), _i, _i], _sz),
     "vsz_eb_setup": ([C.POINTER(Params), _p, _sz, _p, _p, _p], _i),
     "vsz_consts_read": ([_p, C.POINTER(C.c_double), C.POINTER(C.c_int), _p], _i),
     "vsz_outlier_segments": ([_i, C.POINTER(C.c_size_t)], _sz),

@@ -19,10 +19,33 @@ _MODES = {"abs": L.MODE_ABS, "r2r": L.MODE_R2R}
 _LOSSLESS = {None: L.LOSSLESS_NONE, "none": L.LOSSLESS_NONE, "zstd": L.LOSSLESS_ZSTD, "gzip": L.LOSSLESS_GZIP}
 
 
-def make_params(eb=1e-4, mode="abs", dict_size=4096, block_size=8, lossless=None, strict=False) -> Params:
+_PAD_MODES = {"none": L.PAD_NONE, "global": L.PAD_GLOBAL, "block": L.PAD_BLOCK, "edge": L.PAD_EDGE}
+_PAD_TYPES = {"max": L.PADV_MAX, "min": L.PADV_MIN, "avg": L.PADV_AVG, "constant": L.PADV_CONST}
+
+
+def make_params(eb=1e-4, mode="abs", dict_size=4096, block_size=8, lossless=None, strict=False,
+                padding=None) -> Params:
+    """Settings of one compress.  padding: the reference's -p string ("block,max", "global,avg",
+    "edge,constant,2.5", ...; src/argument_parser/argparse.cc:399-415, which reads no sign), or a
+    (mode, type, constant) tuple ("block", "avg", 0.0) that also takes negative constants; None
+    for the zero halo."""
     m = _MODES[mode] if isinstance(mode, str) else int(mode)
     ll = _LOSSLESS[lossless] if (lossless is None or isinstance(lossless, str)) else int(lossless)
-    return Params(float(eb), m, int(dict_size), int(block_size), ll, 1 if strict else 0)
+    p = Params(float(eb), m, int(dict_size), int(block_size), ll, 1 if strict else 0, L.PAD_NONE, L.PADV_CONST, 0.0)
+    if isinstance(padding, str):
+        check(lib().vsz_parse_padding(padding.encode(), C.byref(p)), "parse_padding")
+    elif padding is not None:
+        pm, pt, pc = padding
+        p.pad_mode = _PAD_MODES[pm] if isinstance(pm, str) else int(pm)
+        p.pad_type = _PAD_TYPES[pt] if isinstance(pt, str) else int(pt)
+        p.pad_constant = float(pc)
+    return p
+
+
+def pad_count(dims, block_size: int, padding) -> int:
+    """Pad values a packed block of this geometry holds with this padding (see make_params)."""
+    p = make_params(block_size=block_size, padding=padding)
+    return int(lib().vsz_pad_count(len(dims), dims_arg(dims), int(block_size), p.pad_mode))
 
 
 @dataclass
@@ -39,12 +62,13 @@ class Compressed:
 
 
 def compress(data: np.ndarray, dims=None, eb: float = 1e-4, mode="abs", dict_size: int = 4096, block_size: int = 8,
-             lossless=None, strict: bool = False) -> Compressed:
-    """Compress a float32 field held in host memory (vecsz::interface::Compress)."""
+             lossless=None, strict: bool = False, padding=None) -> Compressed:
+    """Compress a float32 field held in host memory (vecsz::interface::Compress).  padding: the
+    reference's -p string, see make_params."""
     x = np.ascontiguousarray(data, dtype=np.float32)
     if dims is None:
         dims = tuple(reversed(x.shape))  # numpy (z, y, x) -> reference (x, y, z)
-    p = make_params(eb, mode, dict_size, block_size, lossless, strict)
+    p = make_params(eb, mode, dict_size, block_size, lossless, strict, padding)
     out = C.c_void_p(0)
     ob, ds, ls, no = C.c_size_t(0), C.c_size_t(0), C.c_size_t(0), C.c_size_t(0)
     check(lib().vsz_compress_host(C.byref(p), len(dims), dims_arg(dims), x.ctypes.data_as(C.c_void_p), C.byref(out),
@@ -115,11 +139,12 @@ class DeviceCodec:
     compress(d_in) writes the archive into self.archive (a uint8 CUDA tensor) and the vsz_result
     record into self.result (8 uint64); nothing is copied to the host unless you ask."""
 
-    def __init__(self, dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8, device="cuda", strict=False):
+    def __init__(self, dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8, device="cuda", strict=False,
+                 padding=None):
         torch = _torch()
         self.dims = tuple(int(v) for v in dims)
         self.n = int(np.prod(self.dims))
-        self.params = make_params(eb, mode, dict_size, block_size, strict=strict)
+        self.params = make_params(eb, mode, dict_size, block_size, strict=strict, padding=padding)
         ws, cap = C.c_size_t(0), C.c_size_t(0)
         check(lib().vsz_compress_bounds(C.byref(self.params), len(self.dims), dims_arg(self.dims), C.byref(ws),
                                         C.byref(cap)), "compress_bounds")

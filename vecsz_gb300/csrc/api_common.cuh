@@ -69,7 +69,21 @@ inline int check_params(const vsz_params* p, int ndim, const size_t* dims) {
     if (p->block_size <= 0) return VSZ_ERR_INVALID;
     if (!valid_bs(p->block_size)) return VSZ_ERR_UNSUPPORTED;
     if (p->flags & ~VSZ_FLAG_STRICT_EB) return VSZ_ERR_INVALID;
+    if (p->pad_mode < VSZ_PAD_NONE || p->pad_mode > VSZ_PAD_EDGE) return VSZ_ERR_INVALID;
+    if (p->pad_mode != VSZ_PAD_NONE) {
+        if (p->pad_type < VSZ_PADV_MAX || p->pad_type > VSZ_PADV_CONST) return VSZ_ERR_INVALID;
+        if (p->flags & VSZ_FLAG_STRICT_EB) return VSZ_ERR_UNSUPPORTED;  // strict mode keeps the zero halo
+        // 1D block / edge values are raw: codes reach 2 * radius, which must fit the u16 codes
+        if (ndim == 1 && p->pad_mode != VSZ_PAD_GLOBAL && p->dict_size > 32768) return VSZ_ERR_UNSUPPORTED;
+    }
     return VSZ_OK;
+}
+
+// Histogram / codebook symbols: the dictionary, plus the code 2 * radius that a 1D field padded
+// with raw block values can produce (the reference's tree takes 2 * dict symbols,
+// src/vecsz_interface.hh:160).
+inline int symbol_count(int dict, int ndim, int pad_mode) {
+    return (ndim == 1 && (pad_mode == VSZ_PAD_BLOCK || pad_mode == VSZ_PAD_EDGE)) ? dict + 1 : dict;
 }
 
 inline size_t hdr_bytes(int ndim) { return 4 * (size_t)(ndim + 1) + 8 + 24; }
@@ -108,6 +122,7 @@ struct FinalizeArgs {
     int mode, dict, bs;
     int strict;
     size_t hdr;
+    size_t npad;  // pad values after the header (written by the padding stage)
     const Consts* consts;
     const uint32_t* build_info;             // node count, tree bytes, max len
     const unsigned long long* payload_bits;
@@ -135,7 +150,7 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
     const unsigned long long nout = *f.n_out;
     const uint32_t tree           = f.build_info[1];
     const size_t huff_bytes       = 8 + (size_t)tree + (size_t)((bits + 7) >> 3);
-    const size_t data_size        = f.hdr + huff_bytes + 4 * (size_t)nout;
+    const size_t data_size        = f.hdr + 4 * f.npad + huff_bytes + 4 * (size_t)nout;
     const size_t pad              = trailer_index_pad(data_size);
     const size_t trailer          = ((pad + 2 * (size_t)f.n_chunks) + 7) & ~(size_t)7;
     uint8_t* t                    = f.archive + data_size;
@@ -156,7 +171,7 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
             put_bytes(f.archive + 4 * (1 + i), &d, 4);
         }
         put_bytes(f.archive + 4 * (f.ndim + 1), &f.eb, 8);
-        unsigned long long lens[3] = {0ull, (unsigned long long)huff_bytes, nout};
+        unsigned long long lens[3] = {(unsigned long long)f.npad, (unsigned long long)huff_bytes, nout};
         put_bytes(f.archive + 4 * (f.ndim + 1) + 8, lens, 24);
         // trailer fixed part
         uint32_t u32[4] = {kTrailerMagic, kTrailerVersion, kTrailerFixed, (uint32_t)kChunkSyms};
@@ -195,10 +210,11 @@ inline size_t codebook_block_bytes(int dict) { return 9 * (size_t)dict + 16; }
 // [BE nc][BE dict] + the largest serialised tree a dictionary can give
 inline size_t tree_head_max(int dict) { return 8 + tree_bytes_size((uint32_t)(2 * dict - 1)); }
 
-inline size_t archive_capacity(const Geometry& g, int dict) {
+// dict: histogram symbols (symbol_count); npad: pad values (pad_count)
+inline size_t archive_capacity(const Geometry& g, int dict, size_t npad = 0) {
     size_t tree_max = tree_bytes_size((uint32_t)(2 * dict - 1));
     size_t n_chunks = (g.n + kChunkSyms - 1) / kChunkSyms;
-    return hdr_bytes(g.ndim) + 8 + tree_max + 8 * g.n + 4 * g.n + kTrailerFixed + 8 + 2 * n_chunks + 64;
+    return hdr_bytes(g.ndim) + 4 * npad + 8 + tree_max + 8 * g.n + 4 * g.n + kTrailerFixed + 8 + 2 * n_chunks + 64;
 }
 
 }  // namespace api

@@ -11,7 +11,8 @@
 //   s   = rint(x *f32 r_f)                       all 1D/2D elements, 3D columns x < d0 & ~7
 //   s   = (float) round((double) x * r_d)        3D tail columns x >= d0 & ~7 when d0 % 8 != 0
 //   pred: 1D s[x-1]; 2D W + (N - NW); 3D (XYZ - (XY + (XZ + YZ))) + (X + (Y + Z)),
-//         3D tail columns left to right XYZ - XY - XZ - YZ + X + Y + Z; zero halo per block
+//         3D tail columns left to right XYZ - XY - XZ - YZ + X + Y + Z; zero halo per block,
+//         or with padding (-p) the block's pad values (dq_pad.cu)
 //   e   = s - pred (always integer valued, so the reference's sqrt(e*e) < R is |e| < R)
 //   code = |e| < R ? e + R : 0;  outlier value = s where code == 0
 //   2D tail columns (d0 % 8 != 0): code 0, outlier 0.0 -- the reference skips those AVX chunks
@@ -29,16 +30,6 @@ namespace vsz {
 // ------------------------------------------------------------------------------------------
 // K0: min / max of the field for r2r (GetDatumValueRange, src/types.cc:28-35)
 // ------------------------------------------------------------------------------------------
-
-// Order-preserving map of floats onto unsigned integers (NaNs are skipped by the caller).
-__device__ __forceinline__ uint32_t f2key(float f) {
-    uint32_t b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-__device__ __forceinline__ float key2f(uint32_t k) {
-    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
-    return __uint_as_float(b);
-}
 
 __global__ void __launch_bounds__(256) k_minmax(const float* __restrict__ x, size_t n, uint32_t* __restrict__ mm) {
     uint32_t kmax = 0u, kmin = 0xffffffffu;
@@ -225,7 +216,16 @@ __device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t x
         unsigned r = before;
 #pragma unroll
         for (int j = 0; j < 4; j++)
-            if (o[j]) dst[r++] = outv[j];
+            if (o[j]) {
+                float v = outv[j];
+                // a NaN input's prequantized value is that NaN, quieted (the GPU multiply would
+                // give its canonical NaN); strict outliers are input values already
+                if (v != v && !a.strict) {
+                    const float xv = a.x[row * a.d0 + xb + j];
+                    if (xv != xv) v = quiet_nan(xv);
+                }
+                dst[r++] = v;
+            }
     }
 }
 
@@ -298,8 +298,8 @@ __device__ __forceinline__ void hist_flush_block(const DqArgs& a, uint32_t* s_hi
 }
 
 // Warp units u0, u0 + ustep, ... < u1 of one field.  STRICT: the strict error-bound mode (see
-// strict_keep).
-template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false>
+// strict_keep).  PAD: padding (-p), the halo of each block from a.pad instead of zeros.
+template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false, bool PAD = false>
 __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, unsigned long long u0,
                                            unsigned long long u1, unsigned long long ustep, uint32_t* s_hist,
                                            PrevRows* s_prev, HistAcc& h) {
@@ -309,9 +309,9 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
     const unsigned lane = lane_id();
     const unsigned wib  = threadIdx.x >> 5;
     const bool xbound   = ((lane * 4) % BS) == 0;  // my first column starts a Lorenzo block
-    auto left = [&](float v) {                     // x - 1 neighbour of my first column
+    auto left = [&](float v, float halo) {         // x - 1 neighbour of my first column
         const float t = __shfl_up_sync(0xffffffffu, v, 1);
-        return xbound ? 0.f : t;
+        return xbound ? halo : t;
     };
     for (unsigned long long u = u0; u < u1; u += ustep) {
         const uint32_t xt = (uint32_t)(u % a.nxt);
@@ -320,20 +320,33 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
         const uint32_t zb = (uint32_t)(r / a.nyg);
         const uint32_t xb = xt * kTileX + lane * 4;
         const uint32_t y0 = yg * 8;
-        const bool yhalo  = (BS > 8) && (y0 % BS) != 0;
+        const bool yhalo  = (BS > 8) && (y0 % BS) != 0;  // the row above is inside the block
         const uint32_t z0 = (NDIM == 3) ? zb * BS : 0;
         const int nz      = (NDIM == 3) ? (int)min((uint32_t)BS, a.d2 - z0) : 1;
 
-        float Ph[4] = {0.f, 0.f, 0.f, 0.f}, PhL = 0.f;  // previous plane's halo row (y0 - 1)
+        // halo values of my block: x-, y- and z-halo cells (zero without padding; lanes past the
+        // field read none); hxy: the (x-1, y-1) neighbour of my first column when the row above is
+        // the halo row -- the corner cell at a block start (2D: x-halo, 3D: y-halo), else a y-halo
+        // cell of the lane to the left, same block
+        float hx = 0.f, hy = 0.f, hz = 0.f;
+        if (PAD && xb < a.d0) {
+            const Halo hv = halo_of(a.pad, NDIM, xb / BS, y0 / BS, zb);
+            hx = hv.x;
+            hy = hv.y;
+            hz = hv.z;
+        }
+        const float hxy = (xbound && NDIM == 2) ? hx : hy;
+
+        float Ph[4] = {hz, hz, hz, hz}, PhL = hz;  // previous plane's halo row (y0 - 1)
         float4 nxt = load_raw<VEC>(a, (size_t)z0 * a.d1 + y0, y0 < a.d1, xb);
         for (int zz = 0; zz < nz; zz++) {
             const uint32_t z = z0 + zz;
             const bool zp    = zz > 0;  // a previous plane inside the block
-            float Sp[4] = {0.f, 0.f, 0.f, 0.f}, SpL = 0.f;  // row above, this plane (halo row at i = 0)
+            float Sp[4] = {hy, hy, hy, hy}, SpL = hxy;  // row above, this plane (halo row at i = 0)
             if (yhalo) {
                 prequant_row<NDIM, TAIL>(a, load_raw<VEC>(a, (size_t)z * a.d1 + (y0 - 1), true, xb), true, xb, r_f,
                                          r_d, Sp);
-                SpL = left(Sp[3]);
+                SpL = left(Sp[3], hx);
             }
             const float ShNext[4] = {Sp[0], Sp[1], Sp[2], Sp[3]};
             const float ShNextL   = SpL;
@@ -351,12 +364,12 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
                 }
                 float S[4];
                 prequant_row<NDIM, TAIL>(a, raw, row_in, xb, r_f, r_d, S);
-                const float SL = left(S[3]);
-                float Pc[4] = {0.f, 0.f, 0.f, 0.f}, PcL = 0.f;  // this row, previous plane
+                const float SL = left(S[3], hx);
+                float Pc[4] = {hz, hz, hz, hz}, PcL = hz;  // this row, previous plane
                 if (NDIM == 3) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) Pc[j] = zp ? s_prev[wib][i][j][lane] : 0.f;
-                    PcL = left(Pc[3]);
+                    for (int j = 0; j < 4; j++) Pc[j] = zp ? s_prev[wib][i][j][lane] : hz;
+                    PcL = left(Pc[3], zp ? hx : hz);
                 }
                 int code[4];
                 float outv[4];
@@ -428,7 +441,7 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
     }
 }
 
-template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false>
+template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false, bool PAD = false>
 __global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
@@ -442,7 +455,7 @@ __global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     HistAcc h;
-    dq23_units<NDIM, BS, VEC, TAIL, STRICT>(a, c, warp0, a.nunits, warps_total, s_hist, s_prev, h);
+    dq23_units<NDIM, BS, VEC, TAIL, STRICT, PAD>(a, c, warp0, a.nunits, warps_total, s_hist, s_prev, h);
     hist_flush_block(a, s_hist, h);
 }
 
@@ -474,7 +487,7 @@ __global__ void __launch_bounds__(256, 3)
 // 1D: 4 consecutive 128-element tiles per warp unit; the x - 1 neighbour comes from the lane to
 // the left or, at a tile start, from the previous tile's last lane.  Blocks start on multiples of
 // block_size (which divide 128), so tile starts are block starts.
-template <int BS, bool VEC, bool STRICT = false>
+template <int BS, bool VEC, bool STRICT = false, bool PAD = false>
 __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, unsigned long long u0, unsigned long long u1,
                                            unsigned long long ustep, uint32_t* s_hist, HistAcc& h) {
     const float r_f     = c.r_f;
@@ -498,13 +511,30 @@ __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, uns
             const uint32_t xt = (uint32_t)(u * U + t);
             const uint32_t xb = xt * kTileX + lane * 4;
             float L           = __shfl_up_sync(0xffffffffu, S[t][3], 1);
-            if (xbound) L = 0.f;
+            if (xbound) L = (PAD && xb < a.d0) ? halo_of(a.pad, 1, xb / BS, 0, 0).x : 0.f;
+            // PAD: the reference's two postquant forms, which differ once a raw (non-integer) pad
+            // value makes the first residual of a block fractional -- AVX for blocks ending before
+            // the last element (sqrt(e*e) < R, code rint(e + R), outlier andnot(q, s)), scalar for
+            // the others (|e| < R, code (int)(e + R), outlier (1 - q) * s); src/dualquant.hh:112-205.
+            const bool full = PAD && (xb / BS) * BS + BS < a.d0;
             int code[4];
             float outv[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const float pred = j ? S[t][j - 1] : L;
                 const float e    = __fsub_rn(S[t][j], pred);
+                if (PAD) {
+                    if (full) {
+                        const bool q = __fsqrt_rn(__fmul_rn(e, e)) < Rf;
+                        code[j]      = q ? __float2int_rn(__fadd_rn(e, Rf)) : 0;
+                        outv[j]      = q ? 0.0f : S[t][j];
+                    } else {
+                        const bool q = fabsf(e) < Rf;
+                        code[j]      = q ? __float2int_rz(__fadd_rn(e, Rf)) : 0;
+                        outv[j]      = q ? __fmul_rn(0.0f, S[t][j]) : S[t][j];
+                    }
+                    continue;
+                }
                 const bool q     = fabsf(e) < Rf;
                 code[j]          = q ? (int)__fadd_rn(e, Rf) : 0;
                 outv[j]          = S[t][j];
@@ -520,7 +550,7 @@ __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, uns
     }
 }
 
-template <int BS, bool VEC, bool STRICT = false>
+template <int BS, bool VEC, bool STRICT = false, bool PAD = false>
 __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
     extern __shared__ uint32_t s_hist_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_hist_dyn : nullptr;
@@ -533,7 +563,7 @@ __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
     const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     HistAcc h;
-    dq1d_units<BS, VEC, STRICT>(a, c, warp0, a.nunits, warps_total, s_hist, h);
+    dq1d_units<BS, VEC, STRICT, PAD>(a, c, warp0, a.nunits, warps_total, s_hist, h);
     hist_flush_block(a, s_hist, h);
 }
 
@@ -775,8 +805,10 @@ static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStr
         if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, at);
         kern<<<grid, 256, smem, st>>>(a);
     };
-    static std::atomic<unsigned long long> attr_strict{0};
-    if (a.strict) go(k_dq_compress_23d<NDIM, BS, false, true, true>, attr_strict);  // general loads, tails at run time
+    static std::atomic<unsigned long long> attr_strict{0}, attr_pad{0};
+    // strict and padded fields: general loads, tail columns decided at run time
+    if (a.strict) go(k_dq_compress_23d<NDIM, BS, false, true, true>, attr_strict);
+    else if (a.pad.vals) go(k_dq_compress_23d<NDIM, BS, false, true, false, true>, attr_pad);
     else if (vec && !tail) go(k_dq_compress_23d<NDIM, BS, true, false>, attr[0]);
     else if (vec) go(k_dq_compress_23d<NDIM, BS, true, true>, attr[1]);
     else if (!tail) go(k_dq_compress_23d<NDIM, BS, false, false>, attr[2]);
@@ -787,6 +819,7 @@ static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStr
 template <int BS>
 static void launch_1d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
     if (a.strict) k_dq_compress_1d<BS, false, true><<<grid, 256, smem, st>>>(a);
+    else if (a.pad.vals) k_dq_compress_1d<BS, false, false, true><<<grid, 256, smem, st>>>(a);
     else if (vec) k_dq_compress_1d<BS, true><<<grid, 256, smem, st>>>(a);
     else k_dq_compress_1d<BS, false><<<grid, 256, smem, st>>>(a);
     count_launch();

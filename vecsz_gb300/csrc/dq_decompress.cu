@@ -4,7 +4,8 @@
 //   outlier scatter           src/vecsz_interface.hh:313-317
 //   x_lorenzo_{1,2,3}d1l      src/dualquant.hh:915-1043
 //
-// Per element, in the reference's FP32 operation order (zero halo per block):
+// Per element, in the reference's FP32 operation order (zero halo per block, or with padding the
+// block's pad values from the archive's pad section, src/dualquant.hh:946-1016):
 //   s = code == 0 ? outlier : (float)(pred + (float)(code - R))
 //   pred: 1D s[x-1]; 2D (N + W) - NW; 3D XYZ - XY - XZ - YZ + X + Y + Z, left to right
 //   xhat = (float)((double) s * 2eb)                 (dequant(), vsz_device.cuh)
@@ -42,7 +43,7 @@ __device__ __forceinline__ float strict_prequant(float v, uint32_t col, const Dq
     return prequant_vec(v, c.r_f);
 }
 
-template <int NDIM, bool VEC>
+template <int NDIM, bool VEC, bool PAD = false>
 __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     typedef float PrevT[8][8][32];
@@ -68,6 +69,15 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
         const int ny = (NDIM >= 2) ? (int)min(8u, a.d1 - y0) : 1;
         const int nz = (NDIM == 3) ? (int)min(8u, a.d2 - z0) : 1;
         const bool col_in = x0 < a.d0;  // VEC: d0 % 8 == 0, so all 8 columns or none
+        // halo of my block (zero without padding): x-, y- and z-halo cells; in 3D the (x-1, y-1)
+        // cell of a halo row is the y-halo's, in 2D the x-halo's
+        float hx = 0.f, hy = 0.f, hz = 0.f;
+        if (PAD && col_in) {
+            const Halo hv = halo_of(a.pad, NDIM, x0 / 8, yb, zb);
+            hx = hv.x;
+            hy = hv.y;
+            hz = hv.z;
+        }
 
         // VEC: the 8 codes of this lane's columns in one 16-byte load; rows outside the field
         // read as R (no zero codes, so they never enter the outlier path)
@@ -82,13 +92,13 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
 #pragma unroll
             for (int i = 0; i < 8; i++)
 #pragma unroll
-                for (int k = 0; k < 8; k++) s_prev[wib][i][k][lane] = 0.f;
+                for (int k = 0; k < 8; k++) s_prev[wib][i][k][lane] = hz;
         }
 
         for (int zz = 0; zz < nz; zz++) {
-            float Cm[8];  // row y - 1 of this plane (zeros above the block)
+            float Cm[8];  // row y - 1 of this plane (the halo row above the block)
 #pragma unroll
-            for (int k = 0; k < 8; k++) Cm[k] = 0.f;
+            for (int k = 0; k < 8; k++) Cm[k] = hy;
 #pragma unroll 2
             for (int y = 0; y < 8; y++) {
                 const bool row_in = y < ny;
@@ -150,22 +160,22 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                     for (int k = 0; k < 8; k++) {
                         float pred;
                         if (NDIM == 1) {
-                            pred = k ? C[k - 1] : 0.f;
+                            pred = k ? C[k - 1] : hx;
                         } else if (NDIM == 2) {
-                            const float X  = k ? C[k - 1] : 0.f;
-                            const float XY = k ? Cm[k - 1] : 0.f;
+                            const float X  = k ? C[k - 1] : hx;
+                            const float XY = k ? Cm[k - 1] : hx;
                             pred           = __fsub_rn(__fadd_rn(Cm[k], X), XY);  // (N + W) - NW
                         } else {
                             // previous plane: this row (z-1, y) and the row above (z-1, y-1), rolled along x
                             const float Z   = s_prev[wib][y][k][lane];
                             const float yz  = s_prev[wib][ym1][k][lane];
-                            const float YZ  = y ? yz : 0.f;
-                            const float XYZ = k ? pYZ : 0.f;
-                            const float XZ  = k ? pZ : 0.f;
+                            const float YZ  = y ? yz : (zz ? hy : hz);
+                            const float XYZ = k ? pYZ : (zz ? (y ? hx : hy) : hz);
+                            const float XZ  = k ? pZ : (zz ? hx : hz);
                             pZ              = Z;
                             pYZ             = YZ;
-                            const float XY  = k ? Cm[k - 1] : 0.f;
-                            const float X   = k ? C[k - 1] : 0.f;
+                            const float XY  = k ? Cm[k - 1] : (y ? hx : hy);
+                            const float X   = k ? C[k - 1] : hx;
                             pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Cm[k]),
                                              Z);
                         }
@@ -238,7 +248,7 @@ __device__ __forceinline__ uint32_t zeros_before(const uint16_t* crow, uint32_t 
     return n;
 }
 
-template <int NDIM, int BS>
+template <int NDIM, int BS, bool PAD = false>
 __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
     constexpr int G = (128 / BS) > 0 ? (128 / BS) : 1;
     extern __shared__ float s_buf[];  // G blocks x 2 planes x BS x BS
@@ -251,6 +261,7 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
         if (x0 >= a.d0) return;
         uint32_t seg_x0 = (uint32_t)(x0 & ~(size_t)(kDSeg - 1));
         uint32_t zb = zeros_before(a.codes, seg_x0, (uint32_t)x0);
+        const float hx = PAD ? halo_of(a.pad, 1, (uint32_t)(x0 / BS), 0, 0).x : 0.f;
         float prev = 0.f;
         for (int k = 0; k < BS; k++) {
             size_t x = x0 + k;
@@ -271,7 +282,7 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                 else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
             } else {
                 if ((x & (kDSeg - 1)) == 0) zb = 0;
-                s  = __fadd_rn(k ? prev : 0.f, (float)((int)cd - R));
+                s  = __fadd_rn(k ? prev : hx, (float)((int)cd - R));
                 xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
             }
             prev     = s;
@@ -287,6 +298,13 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
     const uint32_t by = (uint32_t)(rr % a.nyb);
     const uint32_t bz = (NDIM == 3) ? (uint32_t)(rr / a.nyb) : 0u;
     const uint32_t x0 = bx * BS, y = by * BS + t, z0 = bz * BS;
+    float hx = 0.f, hy = 0.f, hz = 0.f;  // halo of this block (zero without padding)
+    if (PAD && active) {
+        const Halo hv = halo_of(a.pad, NDIM, bx, by, bz);
+        hx = hv.x;
+        hy = hv.y;
+        hz = hv.z;
+    }
     float* S0 = s_buf + (size_t)g * 2 * BS * BS;
     float* S1 = S0 + BS * BS;
     for (int i = t; i < 2 * BS * BS; i += BS) S0[i] = 0.f;
@@ -310,17 +328,19 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                 else if ((x & (kDSeg - 1)) == 0) zrun = 0;
                 uint32_t cd = crow[x];
                 float pred;
-                const float X  = xl ? Sc[t * BS + xl - 1] : 0.f;
-                const float Y  = t ? Sc[(t - 1) * BS + xl] : 0.f;
-                const float XY = (t && xl) ? Sc[(t - 1) * BS + xl - 1] : 0.f;
+                // halo cells: 2D (x-1, y-1) is the x-halo's, 3D the y-halo's; z - 1 = halo: hz
+                const float X  = xl ? Sc[t * BS + xl - 1] : hx;
+                const float Y  = t ? Sc[(t - 1) * BS + xl] : hy;
+                const float XY = (t && xl) ? Sc[(t - 1) * BS + xl - 1]
+                                           : (NDIM == 2 ? (xl ? hy : hx) : (t ? hx : hy));
                 if (NDIM == 2) {
                     pred = __fsub_rn(__fadd_rn(Y, X), XY);
                 } else {
                     const bool zp   = zl > 0;
-                    const float XYZ = (zp && t && xl) ? Sp[(t - 1) * BS + xl - 1] : 0.f;
-                    const float XZ  = (zp && xl) ? Sp[t * BS + xl - 1] : 0.f;
-                    const float YZ  = (zp && t) ? Sp[(t - 1) * BS + xl] : 0.f;
-                    const float Z   = zp ? Sp[t * BS + xl] : 0.f;
+                    const float XYZ = (zp && t && xl) ? Sp[(t - 1) * BS + xl - 1] : (zp ? (t ? hx : hy) : hz);
+                    const float XZ  = (zp && xl) ? Sp[t * BS + xl - 1] : (zp ? hx : hz);
+                    const float YZ  = (zp && t) ? Sp[(t - 1) * BS + xl] : (zp ? hy : hz);
+                    const float Z   = zp ? Sp[t * BS + xl] : hz;
                     pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
                 }
                 float xo;
@@ -374,19 +394,19 @@ int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
-template <int NDIM, int BS>
+template <int NDIM, int BS, bool PAD>
 static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
     constexpr int G = (128 / BS) > 0 ? (128 / BS) : 1;
     if (NDIM == 1) {
         size_t nblk = (a.d0 + BS - 1) / BS;
-        k_dq_decompress_gen<1, BS><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(a);
+        k_dq_decompress_gen<1, BS, PAD><<<(unsigned)((nblk + 127) / 128), 128, 0, st>>>(a);
         count_launch();
     } else {
         size_t smem = (size_t)G * 2 * BS * BS * sizeof(float);
         static std::atomic<unsigned long long> attr{0};
-        smem_limit_once(k_dq_decompress_gen<NDIM, BS>, (int)smem, attr);
+        smem_limit_once(k_dq_decompress_gen<NDIM, BS, PAD>, (int)smem, attr);
         unsigned grid = (unsigned)((a.nunits + G - 1) / G);
-        k_dq_decompress_gen<NDIM, BS><<<grid, G * BS, smem, st>>>(a);
+        k_dq_decompress_gen<NDIM, BS, PAD><<<grid, G * BS, smem, st>>>(a);
         count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
@@ -405,16 +425,24 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
         long long cap  = (long long)num_sms * 16;
         int grid = (int)(want < cap ? want : cap);
         if (grid < 1) grid = 1;
-        static std::atomic<unsigned long long> attr[6];
+        static std::atomic<unsigned long long> attr[12];
+        const bool pad = a.pad.vals != nullptr;
         auto go = [&](auto kern, int nd) {
             const size_t smem = (nd == 3) ? 4 * 8 * 8 * 32 * 4 : 0;  // previous plane per warp
-            if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[(nd - 1) * 2 + (vec ? 1 : 0)]);
+            if (smem > 48 * 1024)
+                smem_limit_once(kern, (int)smem, attr[(nd - 1) * 4 + (vec ? 1 : 0) + (pad ? 2 : 0)]);
             kern<<<grid, 128, smem, st>>>(a);
             count_launch();
         };
-        if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);
-        else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true>, 2) : go(k_dq_decompress_b8<2, false>, 2);
-        else vec ? go(k_dq_decompress_b8<1, true>, 1) : go(k_dq_decompress_b8<1, false>, 1);
+        if (pad) {
+            if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true, true>, 3) : go(k_dq_decompress_b8<3, false, true>, 3);
+            else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true, true>, 2) : go(k_dq_decompress_b8<2, false, true>, 2);
+            else vec ? go(k_dq_decompress_b8<1, true, true>, 1) : go(k_dq_decompress_b8<1, false, true>, 1);
+        } else {
+            if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);
+            else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true>, 2) : go(k_dq_decompress_b8<2, false>, 2);
+            else vec ? go(k_dq_decompress_b8<1, true>, 1) : go(k_dq_decompress_b8<1, false>, 1);
+        }
         return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
     }
     a.nxs = (a.d0 + kDSeg - 1) / kDSeg;
@@ -424,9 +452,14 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
     a.nunits = (unsigned long long)a.nbx * a.nyb * nzb;
     auto go = [&](auto bs_c) -> int {
         constexpr int B = decltype(bs_c)::value;
-        if (ndim == 3) return launch_gen<3, B>(a, st);
-        if (ndim == 2) return launch_gen<2, B>(a, st);
-        return launch_gen<1, B>(a, st);
+        if (a.pad.vals) {
+            if (ndim == 3) return launch_gen<3, B, true>(a, st);
+            if (ndim == 2) return launch_gen<2, B, true>(a, st);
+            return launch_gen<1, B, true>(a, st);
+        }
+        if (ndim == 3) return launch_gen<3, B, false>(a, st);
+        if (ndim == 2) return launch_gen<2, B, false>(a, st);
+        return launch_gen<1, B, false>(a, st);
     };
     switch (bs) {
         case 8: return go(std::integral_constant<int, 8>{});

@@ -22,7 +22,7 @@ size_t host_tree_bytes(uint32_t nc) {
 }
 
 int host_huffman_build(const uint64_t* hist, int dict, uint64_t* cb_word, uint8_t* cb_len, uint32_t* info,
-                       uint8_t* head) {
+                       uint8_t* head, int hdr_dict) {
     std::vector<uint32_t> used;
     used.reserve((size_t)dict);
     for (int s = 0; s < dict; s++)
@@ -95,10 +95,11 @@ int host_huffman_build(const uint64_t* hist, int dict, uint64_t* cb_word, uint8_
     head[1] = (uint8_t)(nc >> 16);
     head[2] = (uint8_t)(nc >> 8);
     head[3] = (uint8_t)nc;
-    head[4] = (uint8_t)((uint32_t)dict >> 24);
-    head[5] = (uint8_t)((uint32_t)dict >> 16);
-    head[6] = (uint8_t)((uint32_t)dict >> 8);
-    head[7] = (uint8_t)dict;
+    const uint32_t dh = (uint32_t)(hdr_dict ? hdr_dict : dict);
+    head[4] = (uint8_t)(dh >> 24);
+    head[5] = (uint8_t)(dh >> 16);
+    head[6] = (uint8_t)(dh >> 8);
+    head[7] = (uint8_t)dh;
     head[8] = 0;
     uint8_t* pL = head + 9;
     uint8_t* pR = pL + (size_t)w * nc;

@@ -11,9 +11,10 @@ namespace vsz {
 size_t host_tree_bytes(uint32_t nc);
 
 // hist[dict] -> cb_word/cb_len[dict] (right-aligned codeword, length; 0 = unused symbol),
-// info[4] = {node count, tree bytes, max code length, node count}, head = [BE nc][BE dict][tree].
-// Returns 0, or 1 when no symbol occurs (info is then all zero and head is not written).
+// info[4] = {node count, tree bytes, max code length, node count}, head = [BE nc][BE hdr_dict][tree]
+// (hdr_dict 0: dict).  Returns 0, or 1 when no symbol occurs (info is then all zero and head is
+// not written).
 int host_huffman_build(const uint64_t* hist, int dict, uint64_t* cb_word, uint8_t* cb_len, uint32_t* info,
-                       uint8_t* head);
+                       uint8_t* head, int hdr_dict = 0);
 
 }  // namespace vsz

@@ -246,7 +246,7 @@ __device__ __forceinline__ void build_field(const HuffBuildArgs& a, uint8_t* s_b
         o[1] = (uint8_t)(nc >> 16);
         o[2] = (uint8_t)(nc >> 8);
         o[3] = (uint8_t)nc;
-        uint32_t dh = (uint32_t)dict;
+        uint32_t dh = (uint32_t)(a.hdr_dict ? a.hdr_dict : dict);
         o[4] = (uint8_t)(dh >> 24);
         o[5] = (uint8_t)(dh >> 16);
         o[6] = (uint8_t)(dh >> 8);

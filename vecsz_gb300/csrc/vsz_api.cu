@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "api_common.cuh"
@@ -73,9 +74,12 @@ struct CompressWs {
     unsigned long long* total_bits;
     uint16_t* chunk_bits;
     size_t n_chunks;
+    uint8_t* pad_ws;   // padding: reduction state of the global value
+    float* halo_g;     // padding, global mode: the value the blocks predict from
     size_t bytes;
 };
 
+// dict: histogram / codebook symbols (symbol_count)
 CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t cap) {
     Bump b{base, cap};
     CompressWs w{};
@@ -106,6 +110,8 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     w.e_counter  = b.take<uint32_t>(4);
     w.total_bits = b.take<unsigned long long>(1);
     w.chunk_bits = b.take<uint16_t>(w.n_chunks + 8);
+    w.pad_ws     = b.take<uint8_t>(pad_ws_bytes());
+    w.halo_g     = b.take<float>(4);
     w.bytes      = b.off + 256;
     return w;
 }
@@ -319,6 +325,7 @@ struct TreeSlot {
     int device    = -1;
     int dict_cap  = 0;
     int dict      = 0;
+    int hdr_dict  = 0;
     bool reserved = false;
     uint8_t* pinned = nullptr;
     cudaEvent_t done = nullptr;
@@ -334,7 +341,7 @@ void host_tree_callback(void* p) {
     uint8_t* cb    = s->pinned + s->cb_off;
     host_huffman_build(reinterpret_cast<const uint64_t*>(s->pinned + s->hist_off), dict,
                        reinterpret_cast<uint64_t*>(cb), cb + 8 * (size_t)dict + 16,
-                       reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict), s->pinned + s->head_off);
+                       reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict), s->pinned + s->head_off, s->hdr_dict);
 }
 
 TreeSlot* acquire_tree_slot(int dict) {
@@ -374,13 +381,14 @@ void release_tree_slot(TreeSlot* s) {
 }
 
 // Enqueue the host build: hist (device) -> codebook block (device workspace) and
-// [BE nc][BE dict][tree] at huff_out (device archive; up to tree_head_max(dict) bytes are written,
-// the bytes past the tree are overwritten by the encoder that follows).
-int enqueue_host_tree(const unsigned long long* hist, int dict, uint8_t* cb_block, uint8_t* huff_out,
+// [BE nc][BE hdr_dict][tree] at huff_out (device archive; up to tree_head_max(dict) bytes are
+// written, the bytes past the tree are overwritten by the encoder that follows).
+int enqueue_host_tree(const unsigned long long* hist, int dict, int hdr_dict, uint8_t* cb_block, uint8_t* huff_out,
                       cudaStream_t st) {
     TreeSlot* s = acquire_tree_slot(dict);
     if (!s) return VSZ_ERR_CUDA;
-    s->dict = dict;
+    s->dict     = dict;
+    s->hdr_dict = hdr_dict;
     int rc  = VSZ_OK;
     if (cudaMemcpyAsync(s->pinned + s->hist_off, hist, 8 * (size_t)dict, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaLaunchHostFunc(st, host_tree_callback, s) != cudaSuccess ||
@@ -423,6 +431,50 @@ const char* vsz_status_string(vsz_status s) {
 }
 
 const char* vsz_version(void) { return "vecsz_gb300 0.1 (sm_103a)"; }
+
+// The -p string, as src/argument_parser/argparse.cc:399-415 reads it: substrings select the mode
+// and the value type, the first match of [0-9]*[.][0-9]+|[0-9]+ is the constant (so a sign is not
+// part of it); then one mode is kept (argparse.cc:156-170).
+vsz_status vsz_parse_padding(const char* spec, vsz_params* p) {
+    if (!spec || !p) return VSZ_ERR_INVALID;
+    const std::string t(spec);
+    const bool global = t.find("global") != std::string::npos;
+    const bool block  = t.find("block") != std::string::npos;
+    const bool edge   = t.find("edge") != std::string::npos;
+    int type          = VSZ_PADV_CONST;
+    if (t.find("max") != std::string::npos) type = VSZ_PADV_MAX;
+    if (t.find("min") != std::string::npos) type = VSZ_PADV_MIN;
+    if (t.find("avg") != std::string::npos) type = VSZ_PADV_AVG;
+    if (t.find("constant") != std::string::npos) type = VSZ_PADV_CONST;
+    float cst = 0.0f;
+    auto digit = [&](size_t i) { return i < t.size() && t[i] >= '0' && t[i] <= '9'; };
+    for (size_t i = 0; i < t.size(); i++) {
+        size_t j = i;
+        while (digit(j)) j++;
+        size_t end = 0;
+        if (j < t.size() && t[j] == '.' && digit(j + 1)) {  // [0-9]*[.][0-9]+
+            end = j + 1;
+            while (digit(end)) end++;
+        } else if (j > i) {  // [0-9]+
+            end = j;
+        }
+        if (end) {
+            cst = strtof(t.substr(i, end - i).c_str(), nullptr);
+            break;
+        }
+    }
+    p->pad_mode     = global ? VSZ_PAD_GLOBAL : (block ? VSZ_PAD_BLOCK : (edge ? VSZ_PAD_EDGE : VSZ_PAD_NONE));
+    p->pad_type     = type;
+    p->pad_constant = cst;
+    return VSZ_OK;
+}
+
+size_t vsz_pad_count(int ndim, const size_t dims[3], int block_size, int pad_mode) {
+    if (!valid_dims(ndim, dims) || block_size <= 0) return 0;
+    Geometry g = make_geometry(ndim, dims);
+    const uint32_t d3[3] = {g.d0, g.d1, g.d2};
+    return pad_count(ndim, d3, block_size, pad_mode);
+}
 
 vsz_status vsz_eb_setup(const vsz_params* p, const float* d_in, size_t n, void* d_consts, void* d_tmp, void* stream) {
     if (!p || !d_consts || !d_tmp) return VSZ_ERR_INVALID;
@@ -652,8 +704,10 @@ vsz_status vsz_compress_bounds(const vsz_params* p, int ndim, const size_t dims[
                                size_t* archive_cap) {
     VSZ_TRY(check_params(p, ndim, dims));
     Geometry g = make_geometry(ndim, dims);
-    if (ws_bytes) *ws_bytes = layout_compress(g, p->dict_size, nullptr, 0).bytes;
-    if (archive_cap) *archive_cap = archive_capacity(g, p->dict_size);
+    const int nsym = symbol_count(p->dict_size, ndim, p->pad_mode);
+    const uint32_t d3[3] = {g.d0, g.d1, g.d2};
+    if (ws_bytes) *ws_bytes = layout_compress(g, nsym, nullptr, 0).bytes;
+    if (archive_cap) *archive_cap = archive_capacity(g, nsym, pad_count(ndim, d3, p->block_size, p->pad_mode));
     return VSZ_OK;
 }
 
@@ -662,14 +716,18 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     VSZ_TRY(check_params(p, ndim, dims));
     if (!d_in || !d_ws || !d_archive || !d_result) return VSZ_ERR_INVALID;
     Geometry g   = make_geometry(ndim, dims);
-    CompressWs w = layout_compress(g, p->dict_size, reinterpret_cast<uint8_t*>(d_ws), ws_bytes);
+    const int dict = p->dict_size;
+    const int nsym = symbol_count(dict, ndim, p->pad_mode);  // histogram / codebook symbols
+    const uint32_t d3[3] = {g.d0, g.d1, g.d2};
+    const size_t npad    = pad_count(ndim, d3, p->block_size, p->pad_mode);
+    CompressWs w = layout_compress(g, nsym, reinterpret_cast<uint8_t*>(d_ws), ws_bytes);
     if (w.bytes > ws_bytes) return VSZ_ERR_CAPACITY;
-    if (archive_cap < archive_capacity(g, p->dict_size)) return VSZ_ERR_CAPACITY;
+    if (archive_cap < archive_capacity(g, nsym, npad)) return VSZ_ERR_CAPACITY;
     cudaStream_t st = S(stream);
-    const int dict  = p->dict_size;
     const size_t hdr = hdr_bytes(ndim);
+    const size_t huff_off = hdr + 4 * npad;  // the Huffman section follows the pad values
     VSZ_CUDA(cudaMemsetAsync(w.status, 0, sizeof(int), st));
-    VSZ_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(unsigned long long) * dict, st));
+    VSZ_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(unsigned long long) * nsym, st));
     VSZ_CUDA(cudaMemsetAsync(w.build_info, 0, 4 * sizeof(uint32_t), st));
     VSZ_CUDA(cudaMemsetAsync(w.total_bits, 0, sizeof(unsigned long long), st));
     VSZ_CUDA(cudaMemsetAsync(w.n_out, 0, sizeof(unsigned long long), st));
@@ -678,20 +736,49 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
         StageTimer t(kStEbSetup, st);
         VSZ_TRY(launch_eb_setup(p->mode, p->eb, d_in, g.n, w.consts, w.mm, st, w.status));
     }
-    // 2. dual-quant + histogram + outlier ranking
+    // 1b. padding (-p): pad values into the archive's pad section (and the global halo value)
     DqArgs a = make_dq_args(g, p->block_size, dict, d_in, w.consts, w.code, w.scratch, w.seg_count, w.hist);
+    if (p->pad_mode != VSZ_PAD_NONE) {
+        PadArgs pa{};
+        pa.x = d_in;
+        pa.ndim = ndim;
+        pa.bs = p->block_size;
+        pa.mode = p->pad_mode;
+        pa.type = p->pad_type;
+        pa.cst = p->pad_constant;
+        pa.d0 = g.d0;
+        pa.d1 = g.d1;
+        pa.d2 = g.d2;
+        pa.nb0 = (g.d0 + p->block_size + 1) / p->block_size;
+        pa.nb1 = (g.d1 + p->block_size + 1) / p->block_size;
+        pa.nb2 = (g.d2 + p->block_size + 1) / p->block_size;
+        pa.consts = w.consts;
+        pa.arch = d_archive + hdr;
+        pa.halo_g = w.halo_g;
+        pa.ws = w.pad_ws;
+        VSZ_TRY(launch_pad_values(pa, st, num_sms()));
+        const bool global = p->pad_mode == VSZ_PAD_GLOBAL;
+        a.pad.vals   = global ? reinterpret_cast<const uint8_t*>(w.halo_g) : d_archive + hdr;
+        a.pad.stride = global ? 0 : ((p->pad_mode == VSZ_PAD_EDGE && ndim > 1) ? ndim : 1);
+        a.pad.nb0    = pa.nb0;
+        a.pad.nb1    = pa.nb1;
+        a.dict       = nsym;
+        a.smem_hist  = nsym <= 16384 ? 1 : 0;
+    }
+    // 2. dual-quant + histogram + outlier ranking
     a.strict = (p->flags & VSZ_FLAG_STRICT_EB) ? 1 : 0;
     {
         StageTimer t(kStDualquant, st);
         VSZ_TRY(launch_dq_compress(a, ndim, p->block_size, st, num_sms()));
     }
-    // 3. tree + codebook; the Huffman section starts right after the header (no padding values)
+    // 3. tree + codebook; the Huffman section starts after the header and the pad values
     HuffBuildArgs hb{};
     hb.hist = w.hist;
-    hb.dict = dict;
+    hb.dict = nsym;
+    hb.hdr_dict = dict;
     hb.cb_word = w.cb_word;
     hb.cb_len = w.cb_len;
-    hb.out = d_archive + hdr;
+    hb.out = d_archive + huff_off;
     hb.info = w.build_info;
     hb.scratch = w.build_scratch;
     hb.status = w.status;
@@ -699,7 +786,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
         StageTimer t(kStHuffBuild, st);
         if (tree_builder() == VSZ_TREE_HOST && !stream_capturing(st)) {
             huff_build_prepare();  // a later captured call takes the device builder
-            VSZ_TRY(enqueue_host_tree(w.hist, dict, w.cb_block, d_archive + hdr, st));
+            VSZ_TRY(enqueue_host_tree(w.hist, nsym, dict, w.cb_block, d_archive + huff_off, st));
         } else
             VSZ_TRY(launch_huff_build(hb, st));
     }
@@ -709,9 +796,9 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     he.n = g.n;
     he.cb_word = w.cb_word;
     he.cb_len = w.cb_len;
-    he.dict = dict;
+    he.dict = nsym;
     he.out = d_archive;
-    he.out_off = DevOffset{hdr + 8, w.build_info + 1, nullptr};
+    he.out_off = DevOffset{huff_off + 8, w.build_info + 1, nullptr};
     he.total_bits = w.total_bits;
     he.chunk_bits = w.chunk_bits;
     he.chunk_off = w.e_chunk_off;
@@ -728,7 +815,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     ga.scratch = w.scratch;
     ga.nseg = g.nseg;
     ga.out_bytes = d_archive;
-    ga.out_off = DevOffset{hdr + 8, w.build_info + 1, w.total_bits};
+    ga.out_off = DevOffset{huff_off + 8, w.build_info + 1, w.total_bits};
     ga.total = w.n_out;
     ga.tile_status = w.g_tile_status;
     ga.tile_counter = w.g_counter;
@@ -750,6 +837,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     f.dict = dict;
     f.bs = p->block_size;
     f.hdr = hdr;
+    f.npad = npad;
     f.consts = w.consts;
     f.build_info = w.build_info;
     f.payload_bits = w.total_bits;
@@ -863,6 +951,31 @@ static int resolve_decode_params(const vsz_archive_desc* d, const vsz_decompress
     return VSZ_OK;
 }
 
+// Symbols a decoder accepts: the dictionary, plus 2 * radius in a padded 1D archive (raw block
+// pad values can produce it), while it fits the u16 codes.
+static int decode_symbols(const vsz_archive_desc* d, int dict) {
+    return (d->ndim == 1 && d->n_pad > 0 && dict < 65536) ? dict + 1 : dict;
+}
+
+// How a decompressor reads the pad section (src/vecsz_interface.hh:287-298): one value -> global,
+// one per block -> block, ndim per block -> edge; in 2D / 3D any other count means the zero halo,
+// in 1D value 0 for every block (src/dualquant.hh:924-927).
+static PadView pad_view_of(const vsz_archive_desc* d, int bs, const uint8_t* d_archive) {
+    PadView v{};
+    if (d->n_pad == 0) return v;
+    const uint64_t nb0 = (d->dims[0] + bs + 1) / bs, nb1 = (d->dims[1] + bs + 1) / bs;
+    const uint64_t nb = nb0 * nb1 * ((d->dims[2] + bs + 1) / bs);
+    v.nb0 = (uint32_t)nb0;
+    v.nb1 = (uint32_t)nb1;
+    v.vals = d_archive + d->header_bytes;
+    if (d->n_pad == 1) v.stride = 0;
+    else if (d->n_pad == nb) v.stride = 1;
+    else if (d->n_pad == (uint64_t)d->ndim * nb) v.stride = d->ndim == 1 ? 1 : d->ndim;
+    else if (d->ndim == 1) v.stride = 0;
+    else v.vals = nullptr;
+    return v;
+}
+
 vsz_status vsz_decompress_bounds(const vsz_archive_desc* d, const vsz_decompress_opts* o, size_t* ws_bytes) {
     if (!d) return VSZ_ERR_INVALID;
     int dict, bs;
@@ -871,8 +984,8 @@ vsz_status vsz_decompress_bounds(const vsz_archive_desc* d, const vsz_decompress
     size_t dims[3] = {d->dims[0], d->dims[1], d->dims[2]};
     Geometry g = make_geometry(d->ndim, dims);
     if (ws_bytes)
-        *ws_bytes = layout_decompress(g, dict, d->payload_bytes, d->n_outlier, d->has_trailer ? d->n_chunks : 0,
-                                      nullptr, 0).bytes;
+        *ws_bytes = layout_decompress(g, decode_symbols(d, dict), d->payload_bytes, d->n_outlier,
+                                      d->has_trailer ? d->n_chunks : 0, nullptr, 0).bytes;
     return VSZ_OK;
 }
 
@@ -882,12 +995,12 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     int dict, bs;
     double ebf;
     VSZ_TRY(resolve_decode_params(d, o, &dict, &bs, &ebf));
-    if (d->n_pad != 0) return VSZ_ERR_UNSUPPORTED;  // padding modes (-p) are not built
     size_t dims[3] = {d->dims[0], d->dims[1], d->dims[2]};
     if (!valid_dims(d->ndim, dims)) return VSZ_ERR_CORRUPT;
     Geometry g = make_geometry(d->ndim, dims);
-    if (d->node_count > (uint32_t)(2 * dict - 1)) return VSZ_ERR_CORRUPT;
-    DecompressWs w = layout_decompress(g, dict, d->payload_bytes, d->n_outlier, d->has_trailer ? d->n_chunks : 0,
+    const int nsym = decode_symbols(d, dict);
+    if (d->node_count > (uint32_t)(2 * nsym - 1)) return VSZ_ERR_CORRUPT;
+    DecompressWs w = layout_decompress(g, nsym, d->payload_bytes, d->n_outlier, d->has_trailer ? d->n_chunks : 0,
                                        reinterpret_cast<uint8_t*>(d_ws), ws_bytes);
     if (w.bytes > ws_bytes) return VSZ_ERR_CAPACITY;
     cudaStream_t st = S(stream);
@@ -897,7 +1010,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     VSZ_CUDA(cudaMemsetAsync(w.seg_zero, 0, 4 * nsegd, st));
     VSZ_TRY(launch_eb_setup(VSZ_MODE_ABS, ebf, nullptr, 0, w.consts, w.mm, st, w.status));
     const uint16_t* idx = d->has_trailer ? reinterpret_cast<const uint16_t*>(d_archive + d->index_offset) : nullptr;
-    VSZ_TRY(decode_codes(d_archive + d->huff_offset, d->huff_bytes, d->node_count, d->tree_bytes, g.n, dict, idx,
+    VSZ_TRY(decode_codes(d_archive + d->huff_offset, d->huff_bytes, d->node_count, d->tree_bytes, g.n, nsym, idx,
                          d->has_trailer ? d->n_chunks : 0, d->chunk_syms, w, idx ? nullptr : w.seg_zero, g.d0, st));
     // outlier ranks: per 512-code chunk from the indexed decoder (block size 8), else per 256-wide
     // row segment
@@ -940,6 +1053,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.R = dict / 2;
     a.strict = d->has_trailer ? d->strict : 0;
     a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
+    a.pad    = pad_view_of(d, bs, d_archive);
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

@@ -164,7 +164,8 @@ int field_geoms(const vsz_batch_field* fields, int nfields, std::vector<FieldGeo
     for (int i = 0; i < nfields; i++) {
         const vsz_batch_field& f = fields[i];
         VSZ_TRY(check_params(&f.params, f.ndim, f.dims));
-        if (f.params.flags & VSZ_FLAG_STRICT_EB) return VSZ_ERR_UNSUPPORTED;  // single-field entry points only
+        // strict mode and padding: single-field entry points only
+        if ((f.params.flags & VSZ_FLAG_STRICT_EB) || f.params.pad_mode != VSZ_PAD_NONE) return VSZ_ERR_UNSUPPORTED;
         FieldGeom fg{};
         fg.g      = make_geometry(f.ndim, f.dims);
         fg.p      = f.params;

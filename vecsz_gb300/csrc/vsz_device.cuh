@@ -83,7 +83,15 @@ __device__ __forceinline__ float prequant_scalar(float x, double r_d) {
 //   the double path.  tests/test_gpu_exact.py checks every integer s in [-2^24, 2^24] against
 //   the double multiply on the device.
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ float dequant_fp64(float s, double c_d) { return __double2float_rn(__dmul_rn((double)s, c_d)); }
+// NaN bits as the reference's x86 arithmetic leaves them: an operation on a NaN operand returns that
+// NaN, quieted (payload kept), where the GPU's FP32 arithmetic returns its canonical NaN.  Applied
+// where a NaN can reach the archive or the output: outlier values, pad values, reconstructions.
+__device__ __forceinline__ float quiet_nan(float v) { return __uint_as_float(__float_as_uint(v) | 0x00400000u); }
+
+__device__ __forceinline__ float dequant_fp64(float s, double c_d) {
+    if (s != s) return quiet_nan(s);
+    return __double2float_rn(__dmul_rn((double)s, c_d));
+}
 
 __device__ __forceinline__ float dequant(float s, double c_d, float c_hi, float c_lo, int fast) {
     if (!fast) return dequant_fp64(s, c_d);
@@ -106,6 +114,29 @@ __device__ __forceinline__ float dequant(float s, double c_d, float c_hi, float 
     }
     if (ok) return y;
     return dequant_fp64(s, c_d);
+}
+
+// Order-preserving map of floats onto unsigned integers (NaNs are skipped by the caller).
+__device__ __forceinline__ uint32_t f2key(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+// A float at any byte address (archive sections need not be 4-byte aligned).
+__device__ __forceinline__ float ld_f32_bytes(const uint8_t* p) {
+    const uint32_t b = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+    return __uint_as_float(b);
+}
+__device__ __forceinline__ void st_f32_bytes(uint8_t* p, float v) {
+    const uint32_t b = __float_as_uint(v);
+    p[0] = (uint8_t)b;
+    p[1] = (uint8_t)(b >> 8);
+    p[2] = (uint8_t)(b >> 16);
+    p[3] = (uint8_t)(b >> 24);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -37,7 +37,8 @@ __host__ __device__ inline size_t tree_bytes_size(uint32_t nc) {
 
 struct HuffBuildArgs {
     const unsigned long long* hist;
-    int dict;
+    int dict;                     // symbols [0, dict) (a 1D padded field adds one: 2 * radius)
+    int hdr_dict;                 // dictionary size written into the head; 0: dict
     unsigned long long* cb_word;  // right-aligned codeword per symbol
     uint8_t* cb_len;              // codeword length per symbol (0 = unused)
     uint8_t* out;                 // [BE nc][BE dict][tree bytes], any alignment

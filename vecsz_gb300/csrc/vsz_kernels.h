@@ -27,6 +27,44 @@ struct DevOffset {
 #endif
 };
 
+// ---- padding (-p) ----------------------------------------------------------------------------
+// Where a dual-quant kernel finds the halo values of each Lorenzo block.  Blocks are numbered on
+// the reference's grid, get_nblk = (d + bs + 1) / bs per axis (src/dimensions.hh:32), x fastest.
+struct PadView {
+    const uint8_t* vals;  // f32 values at any byte address; null: the zero halo (no padding)
+    int stride;           // values per block: 0 (every block reads value 0), 1, or ndim (edge)
+    uint32_t nb0, nb1;    // grid blocks along x and y
+};
+
+// Halo values of one block: x-, y- and z-halo cells (src/utils/padding.hh:286-296, 342-373): a
+// single value in global / block mode; edge mode 2D {x: v0, y: v1}, 3D {z: v0, y: v1, x: v2}.
+// Corner cells take 2D x (x wins), 3D y (y wins in a plane), and z wherever z is the halo.
+struct Halo {
+    float x, y, z;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ float pad_value_at(const uint8_t* p, size_t i) {
+    const uint8_t* q = p + 4 * i;
+    const uint32_t b = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
+    return __uint_as_float(b);
+}
+__device__ __forceinline__ Halo halo_of(const PadView& p, int ndim, uint32_t bx, uint32_t by, uint32_t bz) {
+    if (p.stride == 0) {
+        const float v = pad_value_at(p.vals, 0);
+        return Halo{v, v, v};
+    }
+    const size_t blk = (size_t)bx + (size_t)p.nb0 * ((size_t)by + (size_t)p.nb1 * bz);
+    if (p.stride == 1) {
+        const float v = pad_value_at(p.vals, blk);
+        return Halo{v, v, v};
+    }
+    const size_t o = blk * (size_t)p.stride;
+    if (ndim == 2) return Halo{pad_value_at(p.vals, o), pad_value_at(p.vals, o + 1), 0.0f};
+    return Halo{pad_value_at(p.vals, o + 2), pad_value_at(p.vals, o + 1), pad_value_at(p.vals, o)};
+}
+#endif
+
 // ---- many fields in one launch -------------------------------------------------------------
 // A block-wide unit of work: one field of a batch and a range [u0, u1) of that field's work units
 // (warp tiles, 512-code chunks, elements or look-back tiles, by stage).  Tasks are built on the
@@ -69,6 +107,7 @@ struct DqArgs {
     int smem_hist;               // 1: histogram privatised in shared memory
     unsigned long long nunits;   // warp work units
     int strict;                  // strict error-bound mode (outliers carry input values)
+    PadView pad;                 // padding (-p): the halo each block predicts from
 };
 
 struct GatherArgs {
@@ -104,6 +143,7 @@ struct DqDecArgs {
     unsigned long long nunits;
     int strict;                          // strict archive: outliers are input values (re-prequantized)
     uint32_t xtail;                      // 3D: first scalar-prequant column (d0 & ~7 when d0 % 8), else d0
+    PadView pad;                         // padded archive: the halo of each block (vals = pad section)
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
@@ -114,6 +154,23 @@ int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_
                     cudaStream_t st, int* status_word = nullptr);
 int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms);
 int launch_outlier_gather(GatherArgs g, cudaStream_t st);
+
+// Pad values of a field (-p).  Writes the archive's pad section (`arch`, any alignment) and, in
+// global mode, the value the compressor's 2D/3D blocks predict from (`halo_g`).  ws: pad_ws_bytes.
+struct PadArgs {
+    const float* x;
+    int ndim, bs, mode, type;
+    float cst;
+    uint32_t d0, d1, d2;
+    uint32_t nb0, nb1, nb2;      // reference grid
+    const Consts* consts;
+    uint8_t* arch;
+    float* halo_g;
+    void* ws;
+};
+size_t pad_ws_bytes();
+size_t pad_count(int ndim, const uint32_t d[3], int bs, int mode);
+int launch_pad_values(const PadArgs& a, cudaStream_t st, int num_sms);
 
 // Batched launchers (device arrays of per-field arguments and of tasks).  A dual-quant batch
 // holds fields of one kernel class: ndim, block size, vec (d0 % 4 == 0 and aligned), tail
