@@ -144,40 +144,35 @@ __global__ void k_consts(int mode, double eb, const uint32_t* __restrict__ mm, c
 // ------------------------------------------------------------------------------------------
 
 struct HistAcc {
-    // Private counters for the three most frequent codes of a smooth field (R-1, R, R+1); all
-    // other codes go to the block's shared-memory histogram.
-    uint32_t c0 = 0, c1 = 0, c2 = 0;
+    // A private counter for the code R (zero residual), the most frequent code of a smooth field,
+    // so a warp of smooth data does not serialise on one shared-memory bin; every other code goes
+    // to the block's shared-memory histogram (the field's global one when dict is large).
+    uint32_t c1 = 0;
     __device__ __forceinline__ void add(int code, int R, uint32_t* s_hist, int dict, unsigned long long* g_hist) {
-        const uint32_t d = (uint32_t)(code - R + 1);
-        c0 += (d == 0u);
-        c1 += (d == 1u);
-        c2 += (d == 2u);
-        if (d > 2u) {
-            if (s_hist) atomicAdd(&s_hist[code], 1u);
-            else atomicAdd(&g_hist[code], 1ull);
+        if (code == R) {
+            c1++;
+        } else if (s_hist) {
+            atomicAdd(&s_hist[code], 1u);
+        } else {
+            atomicAdd(&g_hist[code], 1ull);
         }
     }
     __device__ __forceinline__ void flush(int R, uint32_t* s_hist, int dict, unsigned long long* g_hist) {
-        if (s_hist) {
-            if (c1) atomicAdd(&s_hist[R], c1);
-            if (c0) atomicAdd(&s_hist[R - 1], c0);
-            if (c2 && R + 1 < dict) atomicAdd(&s_hist[R + 1], c2);
-        } else {
-            if (c1) atomicAdd(&g_hist[R], (unsigned long long)c1);
-            if (c0) atomicAdd(&g_hist[R - 1], (unsigned long long)c0);
-            if (c2 && R + 1 < dict) atomicAdd(&g_hist[R + 1], (unsigned long long)c2);
-        }
+        if (!c1) return;
+        if (s_hist) atomicAdd(&s_hist[R], c1);
+        else atomicAdd(&g_hist[R], (unsigned long long)c1);
     }
 };
 
 // One row of 4 elements per lane: store codes, count histogram, rank and write outliers.
-template <bool VEC>
+template <bool VEC, bool FULL = false>
 __device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t xb, uint32_t xt, bool row_in,
                                          const int code[4], const float outv[4], HistAcc& h, uint32_t* s_hist) {
     const unsigned lane = lane_id();
+    if (FULL) row_in = true;
     bool in[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) in[j] = row_in && (xb + j < a.d0);
+    for (int j = 0; j < 4; j++) in[j] = FULL || (row_in && (xb + j < a.d0));
     uint16_t* crow = a.code + row * a.d0;
     if (VEC && in[0]) {
         // d0 % 4 == 0: all four columns are in range together; 8-byte aligned store.
@@ -236,13 +231,13 @@ __device__ __forceinline__ float prequant_at(float v, uint32_t col, uint32_t xta
 }
 
 // Raw values of 4 consecutive columns [xb, xb+4) of one row (zeros outside the field).
-template <bool VEC>
+template <bool VEC, bool FULL = false>
 __device__ __forceinline__ float4 load_raw(const DqArgs& a, size_t row, bool row_in, uint32_t xb) {
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!row_in) return v;
+    if (!FULL && !row_in) return v;
     const float* rowp = a.x + row * a.d0;
     if (VEC) {
-        if (xb < a.d0) v = __ldcs(reinterpret_cast<const float4*>(rowp + xb));
+        if (FULL || xb < a.d0) v = __ldcs(reinterpret_cast<const float4*>(rowp + xb));
     } else {
         if (xb < a.d0) v.x = __ldcs(rowp + xb);
         if (xb + 1 < a.d0) v.y = __ldcs(rowp + xb + 1);
@@ -253,13 +248,13 @@ __device__ __forceinline__ float4 load_raw(const DqArgs& a, size_t row, bool row
 }
 
 // Prequantized values of a raw row; zero outside the field.
-template <int NDIM, bool TAIL>
+template <int NDIM, bool TAIL, bool FULL = false>
 __device__ __forceinline__ void prequant_row(const DqArgs& a, float4 v, bool row_in, uint32_t xb, float r_f, double r_d,
                                              float S[4]) {
     const float t[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        const bool in = row_in && (xb + j < a.d0);
+        const bool in = FULL || (row_in && (xb + j < a.d0));
         S[j]          = in ? prequant_at<NDIM, TAIL>(t[j], xb + j, a.xtail, r_f, r_d) : 0.0f;
     }
 }
@@ -313,131 +308,139 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
         const float t = __shfl_up_sync(0xffffffffu, v, 1);
         return xbound ? halo : t;
     };
-    for (unsigned long long u = u0; u < u1; u += ustep) {
-        const uint32_t xt = (uint32_t)(u % a.nxt);
-        const unsigned long long r = u / a.nxt;
-        const uint32_t yg = (uint32_t)(r % a.nyg);
-        const uint32_t zb = (uint32_t)(r / a.nyg);
+    // unit indices fit 32 bits (n <= 2^36 elements, 1024 per unit): 32-bit divisions only
+    for (uint32_t u = (uint32_t)u0; u < (uint32_t)u1; u += (uint32_t)ustep) {
+        const uint32_t xt = u % a.nxt;
+        const uint32_t r = u / a.nxt;
+        const uint32_t yg = r % a.nyg;
+        const uint32_t zb = r / a.nyg;
         const uint32_t xb = xt * kTileX + lane * 4;
         const uint32_t y0 = yg * 8;
         const bool yhalo  = (BS > 8) && (y0 % BS) != 0;  // the row above is inside the block
         const uint32_t z0 = (NDIM == 3) ? zb * BS : 0;
         const int nz      = (NDIM == 3) ? (int)min((uint32_t)BS, a.d2 - z0) : 1;
 
-        // halo values of my block: x-, y- and z-halo cells (zero without padding; lanes past the
-        // field read none); hxy: the (x-1, y-1) neighbour of my first column when the row above is
-        // the halo row -- the corner cell at a block start (2D: x-halo, 3D: y-halo), else a y-halo
-        // cell of the lane to the left, same block
-        float hx = 0.f, hy = 0.f, hz = 0.f;
-        if (PAD && xb < a.d0) {
-            const Halo hv = halo_of(a.pad, NDIM, xb / BS, y0 / BS, zb);
-            hx = hv.x;
-            hy = hv.y;
-            hz = hv.z;
-        }
-        const float hxy = (xbound && NDIM == 2) ? hx : hy;
-
-        float Ph[4] = {hz, hz, hz, hz}, PhL = hz;  // previous plane's halo row (y0 - 1)
-        float4 nxt = load_raw<VEC>(a, (size_t)z0 * a.d1 + y0, y0 < a.d1, xb);
-        for (int zz = 0; zz < nz; zz++) {
-            const uint32_t z = z0 + zz;
-            const bool zp    = zz > 0;  // a previous plane inside the block
-            float Sp[4] = {hy, hy, hy, hy}, SpL = hxy;  // row above, this plane (halo row at i = 0)
-            if (yhalo) {
-                prequant_row<NDIM, TAIL>(a, load_raw<VEC>(a, (size_t)z * a.d1 + (y0 - 1), true, xb), true, xb, r_f,
-                                         r_d, Sp);
-                SpL = left(Sp[3], hx);
+        // a tile wholly inside the field (the common case) runs without per-element range checks
+        const bool full = VEC && (xt + 1) * kTileX <= a.d0 && y0 + 8 <= a.d1;
+        auto unit_body = [&](auto full_c) {
+            constexpr bool FULL = decltype(full_c)::value;
+            // halo values of my block: x-, y- and z-halo cells (zero without padding; lanes past the
+            // field read none); hxy: the (x-1, y-1) neighbour of my first column when the row above is
+            // the halo row -- the corner cell at a block start (2D: x-halo, 3D: y-halo), else a y-halo
+            // cell of the lane to the left, same block
+            float hx = 0.f, hy = 0.f, hz = 0.f;
+            if (PAD && xb < a.d0) {
+                const Halo hv = halo_of(a.pad, NDIM, xb / BS, y0 / BS, zb);
+                hx = hv.x;
+                hy = hv.y;
+                hz = hv.z;
             }
-            const float ShNext[4] = {Sp[0], Sp[1], Sp[2], Sp[3]};
-            const float ShNextL   = SpL;
-            float Pp[4] = {Ph[0], Ph[1], Ph[2], Ph[3]}, PpL = PhL;  // row above, previous plane
+            const float hxy = (xbound && NDIM == 2) ? hx : hy;
+
+            float Ph[4] = {hz, hz, hz, hz}, PhL = hz;  // previous plane's halo row (y0 - 1)
+            float4 nxt = load_raw<VEC, FULL>(a, (size_t)z0 * a.d1 + y0, y0 < a.d1, xb);
+            for (int zz = 0; zz < nz; zz++) {
+                const uint32_t z = z0 + zz;
+                const bool zp    = zz > 0;  // a previous plane inside the block
+                float Sp[4] = {hy, hy, hy, hy}, SpL = hxy;  // row above, this plane (halo row at i = 0)
+                if (yhalo) {
+                    prequant_row<NDIM, TAIL, FULL>(a, load_raw<VEC, FULL>(a, (size_t)z * a.d1 + (y0 - 1), true, xb), true, xb, r_f,
+                                             r_d, Sp);
+                    SpL = left(Sp[3], hx);
+                }
+                const float ShNext[4] = {Sp[0], Sp[1], Sp[2], Sp[3]};
+                const float ShNextL   = SpL;
+                float Pp[4] = {Ph[0], Ph[1], Ph[2], Ph[3]}, PpL = PhL;  // row above, previous plane
 #pragma unroll 2
-            for (int i = 0; i < 8; i++) {
-                const uint32_t y  = y0 + i;
-                const bool row_in = y < a.d1;
-                const float4 raw  = nxt;
-                {  // the next row of this plane, or the first row of the next plane
-                    const bool last_row = (i == 7);
-                    const uint32_t zn = last_row ? z + 1 : z, yn = last_row ? y0 : y + 1;
-                    const bool more = !last_row || zz + 1 < nz;
-                    nxt = more ? load_raw<VEC>(a, (size_t)zn * a.d1 + yn, yn < a.d1, xb) : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
-                float S[4];
-                prequant_row<NDIM, TAIL>(a, raw, row_in, xb, r_f, r_d, S);
-                const float SL = left(S[3], hx);
-                float Pc[4] = {hz, hz, hz, hz}, PcL = hz;  // this row, previous plane
-                if (NDIM == 3) {
-#pragma unroll
-                    for (int j = 0; j < 4; j++) Pc[j] = zp ? s_prev[wib][i][j][lane] : hz;
-                    PcL = left(Pc[3], zp ? hx : hz);
-                }
-                int code[4];
-                float outv[4];
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const uint32_t col = xb + j;
-                    const float cur    = S[j];
-                    const float X      = j ? S[j - 1] : SL;
-                    const float Y      = Sp[j];
-                    const float XY     = j ? Sp[j - 1] : SpL;
-                    const bool tail    = TAIL && col >= a.xtail;
-                    float pred;
-                    if (NDIM == 2) {
-                        pred = __fadd_rn(X, __fsub_rn(Y, XY));  // W + (N - NW)
-                    } else {
-                        const float Z   = Pc[j];
-                        const float XZ  = j ? Pc[j - 1] : PcL;
-                        const float YZ  = Pp[j];
-                        const float XYZ = j ? Pp[j - 1] : PpL;
-                        if (!tail) {
-                            float dist1 = __fadd_rn(X, __fadd_rn(Y, Z));
-                            float dist2 = __fadd_rn(XY, __fadd_rn(XZ, YZ));
-                            pred        = __fadd_rn(__fsub_rn(XYZ, dist2), dist1);
-                        } else {
-                            pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y),
-                                             Z);
-                        }
+                for (int i = 0; i < 8; i++) {
+                    const uint32_t y  = y0 + i;
+                    const bool row_in = y < a.d1;
+                    const float4 raw  = nxt;
+                    {  // the next row of this plane, or the first row of the next plane
+                        const bool last_row = (i == 7);
+                        const uint32_t zn = last_row ? z + 1 : z, yn = last_row ? y0 : y + 1;
+                        const bool more = !last_row || zz + 1 < nz;
+                        nxt = more ? load_raw<VEC, FULL>(a, (size_t)zn * a.d1 + yn, yn < a.d1, xb) : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
-                    const float e = __fsub_rn(cur, pred);
-                    const bool q  = fabsf(e) < Rf;
-                    code[j]       = q ? (int)__fadd_rn(e, Rf) : 0;
-                    outv[j]       = cur;
-                    if (STRICT) {
-                        const float xr = j == 0 ? raw.x : (j == 1 ? raw.y : (j == 2 ? raw.z : raw.w));
-                        float pd;  // the decompressor's prediction from the same (in-step) neighbours
+                    float S[4];
+                    prequant_row<NDIM, TAIL, FULL>(a, raw, row_in, xb, r_f, r_d, S);
+                    const float SL = left(S[3], hx);
+                    float Pc[4] = {hz, hz, hz, hz}, PcL = hz;  // this row, previous plane
+                    if (NDIM == 3) {
+#pragma unroll
+                        for (int j = 0; j < 4; j++) Pc[j] = zp ? s_prev[wib][i][j][lane] : hz;
+                        PcL = left(Pc[3], zp ? hx : hz);
+                    }
+                    int code[4];
+                    float outv[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const uint32_t col = xb + j;
+                        const float cur    = S[j];
+                        const float X      = j ? S[j - 1] : SL;
+                        const float Y      = Sp[j];
+                        const float XY     = j ? Sp[j - 1] : SpL;
+                        const bool tail    = TAIL && col >= a.xtail;
+                        float pred;
                         if (NDIM == 2) {
-                            pd = __fsub_rn(__fadd_rn(Y, X), XY);
+                            pred = __fadd_rn(X, __fsub_rn(Y, XY));  // W + (N - NW)
                         } else {
                             const float Z   = Pc[j];
                             const float XZ  = j ? Pc[j - 1] : PcL;
                             const float YZ  = Pp[j];
                             const float XYZ = j ? Pp[j - 1] : PpL;
-                            pd = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
+                            if (!tail) {
+                                float dist1 = __fadd_rn(X, __fadd_rn(Y, Z));
+                                float dist2 = __fadd_rn(XY, __fadd_rn(XZ, YZ));
+                                pred        = __fadd_rn(__fsub_rn(XYZ, dist2), dist1);
+                            } else {
+                                pred = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y),
+                                                 Z);
+                            }
                         }
-                        if (!strict_keep(q, pd, e, cur, xr, c)) code[j] = 0;
-                        outv[j] = xr;  // strict outliers carry the input value
-                    } else if (NDIM == 2 && tail) {
-                        code[j] = 0;
-                        outv[j] = 0.0f;
+                        const float e = __fsub_rn(cur, pred);
+                        const bool q  = fabsf(e) < Rf;
+                        code[j]       = q ? (int)__fadd_rn(e, Rf) : 0;
+                        outv[j]       = cur;
+                        if (STRICT) {
+                            const float xr = j == 0 ? raw.x : (j == 1 ? raw.y : (j == 2 ? raw.z : raw.w));
+                            float pd;  // the decompressor's prediction from the same (in-step) neighbours
+                            if (NDIM == 2) {
+                                pd = __fsub_rn(__fadd_rn(Y, X), XY);
+                            } else {
+                                const float Z   = Pc[j];
+                                const float XZ  = j ? Pc[j - 1] : PcL;
+                                const float YZ  = Pp[j];
+                                const float XYZ = j ? Pp[j - 1] : PpL;
+                                pd = __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), YZ), X), Y), Z);
+                            }
+                            if (!strict_keep(q, pd, e, cur, xr, c)) code[j] = 0;
+                            outv[j] = xr;  // strict outliers carry the input value
+                        } else if (NDIM == 2 && tail) {
+                            code[j] = 0;
+                            outv[j] = 0.0f;
+                        }
                     }
-                }
-                emit_row<VEC>(a, (size_t)z * a.d1 + y, xb, xt, row_in, code, outv, h, s_hist);
-                if (NDIM == 3) {
+                    emit_row<VEC, FULL>(a, (size_t)z * a.d1 + y, xb, xt, row_in, code, outv, h, s_hist);
+                    if (NDIM == 3) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) s_prev[wib][i][j][lane] = S[j];  // row i of plane z
+                        for (int j = 0; j < 4; j++) s_prev[wib][i][j][lane] = S[j];  // row i of plane z
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        Sp[j] = S[j];
+                        Pp[j] = Pc[j];
+                    }
+                    SpL = SL;
+                    PpL = PcL;
                 }
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    Sp[j] = S[j];
-                    Pp[j] = Pc[j];
-                }
-                SpL = SL;
-                PpL = PcL;
+                for (int j = 0; j < 4; j++) Ph[j] = ShNext[j];
+                PhL = ShNextL;
             }
-#pragma unroll
-            for (int j = 0; j < 4; j++) Ph[j] = ShNext[j];
-            PhL = ShNextL;
-        }
+        };
+        if (full) unit_body(std::true_type{});
+        else unit_body(std::false_type{});
     }
 }
 

@@ -56,14 +56,15 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
     const uint32_t rpair  = (uint32_t)R | ((uint32_t)R << 16);
     const unsigned lane   = lane_id();
     const unsigned wib    = threadIdx.x >> 5;  // warp in block (4 warps)
-    const unsigned long long warps_total = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    const unsigned long long warp0       = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
+    const uint32_t warp0       = blockIdx.x * (blockDim.x >> 5) + wib;
 
-    for (unsigned long long u = warp0; u < a.nunits; u += warps_total) {
-        const uint32_t xs = (uint32_t)(u % a.nxs);
-        const unsigned long long r = u / a.nxs;
-        const uint32_t yb = (NDIM >= 2) ? (uint32_t)(r % a.nyb) : 0u;
-        const uint32_t zb = (NDIM == 3) ? (uint32_t)(r / a.nyb) : 0u;
+    // unit indices fit 32 bits (n <= 2^36 elements, 2048 per unit): 32-bit divisions only
+    for (uint32_t u = warp0; u < (uint32_t)a.nunits; u += warps_total) {
+        const uint32_t xs = u % a.nxs;
+        const uint32_t r  = u / a.nxs;
+        const uint32_t yb = (NDIM >= 2) ? r % a.nyb : 0u;
+        const uint32_t zb = (NDIM == 3) ? r / a.nyb : 0u;
         const uint32_t x0 = xs * kDSeg + lane * 8;
         const uint32_t y0 = yb * 8, z0 = zb * 8;
         const int ny = (NDIM >= 2) ? (int)min(8u, a.d1 - y0) : 1;
