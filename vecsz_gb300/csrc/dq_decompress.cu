@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
 
         for (int zz = 0; zz < nz; zz++) {
             float Cm[8];  // row y - 1 of this plane (the halo row above the block)
+            float Zm[8], Zn[8];  // 3D: row y - 1 and row y of plane z - 1
 #pragma unroll
             for (int k = 0; k < 8; k++) Cm[k] = hy;
 #pragma unroll 2
@@ -119,11 +120,13 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                 const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
                 auto code_at = [&](int k) -> uint32_t { return (cw[k >> 1] >> (16 * (k & 1))) & 0xffffu; };
                 auto in_at   = [&](int k) -> bool { return all_in || (row_in && x0 + (uint32_t)k < a.d0); };
-                // ---- outliers of this row segment, ranked in row-major order
+                // ---- outliers of this row segment, ranked in row-major order.  Cells outside the
+                // field read code R (never 0), so no range test is needed here or in the row pass:
+                // their values only ever feed other cells outside the field.
                 uint32_t zm = 0;
                 if (zero_halves(cv.x) | zero_halves(cv.y) | zero_halves(cv.z) | zero_halves(cv.w)) {
 #pragma unroll
-                    for (int k = 0; k < 8; k++) zm |= (in_at(k) && code_at(k) == 0u) ? (1u << k) : 0u;
+                    for (int k = 0; k < 8; k++) zm |= (code_at(k) == 0u) ? (1u << k) : 0u;
                 }
                 unsigned long long obase = 0;
                 if (__any_sync(0xffffffffu, zm != 0u)) {
@@ -156,7 +159,6 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                 float C[8];
                 auto row_pass = [&](auto with_outliers) {
                     float pZ = 0.f, pYZ = 0.f;
-                    const int ym1 = y ? y - 1 : 0;
 #pragma unroll
                     for (int k = 0; k < 8; k++) {
                         float pred;
@@ -167,10 +169,11 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                             const float XY = k ? Cm[k - 1] : hx;
                             pred           = __fsub_rn(__fadd_rn(Cm[k], X), XY);  // (N + W) - NW
                         } else {
-                            // previous plane: this row (z-1, y) and the row above (z-1, y-1), rolled along x
+                            // previous plane: this row (z-1, y) from shared memory, the row above
+                            // (z-1, y-1) kept from the row before; both rolled along x
                             const float Z   = s_prev[wib][y][k][lane];
-                            const float yz  = s_prev[wib][ym1][k][lane];
-                            const float YZ  = y ? yz : (zz ? hy : hz);
+                            const float YZ  = y ? Zm[k] : (zz ? hy : hz);
+                            Zn[k]           = Z;
                             const float XYZ = k ? pYZ : (zz ? (y ? hx : hy) : hz);
                             const float XZ  = k ? pZ : (zz ? hx : hz);
                             pZ              = Z;
@@ -191,7 +194,7 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                                 if (a.strict) s = strict_prequant<NDIM>(s, x0 + (uint32_t)k, a, c);
                             }
                         }
-                        C[k] = in_at(k) ? s : 0.f;
+                        C[k] = s;
                     }
                 };
                 if (zm) row_pass(std::true_type{});
@@ -225,7 +228,10 @@ __global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
                     for (int k = 0; k < 8; k++) s_prev[wib][y - 1][k][lane] = Cm[k];
                 }
 #pragma unroll
-                for (int k = 0; k < 8; k++) Cm[k] = C[k];
+                for (int k = 0; k < 8; k++) {
+                    Cm[k] = C[k];
+                    if (NDIM == 3) Zm[k] = Zn[k];
+                }
                 if (NDIM == 1) break;
             }
             if (NDIM == 3) {

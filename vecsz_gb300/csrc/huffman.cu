@@ -505,11 +505,97 @@ __device__ __forceinline__ void pack_chunks(const HuffEncodeArgs& a, size_t c, s
     }
 }
 
+// Codewords of at most kPackFastLen bits: the codebook is one u32 per symbol in shared memory,
+// (codeword << 6) | length, and a lane appends its 16 codewords to a right-aligned 64-bit
+// accumulator with no per-code branches but the word flush -- the same words as pack_chunks.
+constexpr uint32_t kPackFastLen = 26;
+
+__device__ __forceinline__ void pack_chunks_fast(const HuffEncodeArgs& a, size_t c, size_t c1, size_t cstep,
+                                                 uint8_t* s_dyn) {
+    uint32_t* s_words = reinterpret_cast<uint32_t*>(s_dyn);      // 8 x kEncWarpWords
+    uint32_t* s_tab   = s_words + 8 * kEncWarpWords;             // dict entries
+    for (int i = threadIdx.x; i < a.dict; i += blockDim.x) {
+        const uint32_t l = a.cb_len[i];
+        s_tab[i]         = l ? ((uint32_t)a.cb_word[i] << 6) | l : 0u;
+    }
+    __syncthreads();
+    const unsigned lane  = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t* sw         = s_words + warp * kEncWarpWords;
+    uint8_t* out         = a.out + a.out_off.eval();
+    const uint32_t base0 = (uint32_t)(reinterpret_cast<uintptr_t>(out) & 3u) * 8u;
+    uint32_t* gw         = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
+    const unsigned long long off0 = a.chunk_off[0];
+    Codes16 nxt                   = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
+    for (; c < c1; c += cstep) {
+        const Codes16 cc = nxt;
+        if (c + cstep < c1) nxt = load_codes16(a, (c + cstep) * kEncChunk + lane * kEncPerThread);
+        uint32_t e[kEncPerThread], bits = 0;
+#pragma unroll
+        for (int k = 0; k < kEncPerThread; k++) {
+            e[k] = ((uint32_t)k < cc.nvalid) ? s_tab[code_k(cc, k)] : 0u;
+            bits += e[k] & 63u;
+        }
+        uint32_t incl = bits;  // warp inclusive scan of lane bit counts
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (unsigned)o) incl += t;
+        }
+        const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
+        const unsigned long long gstart = base0 + (a.chunk_off[c] - off0);
+        const uint32_t r0               = (uint32_t)(gstart & 31u);
+        const unsigned long long F      = gstart >> 5;
+        const uint32_t nwords           = tot ? (r0 + tot + 31) >> 5 : 0u;
+        for (uint32_t i = lane; i < nwords; i += 32) sw[i] = 0u;
+        __syncwarp();
+        if (bits) {
+            const uint32_t pos = r0 + incl - bits;
+            uint32_t wi        = pos >> 5;
+            uint32_t nb        = pos & 31u;  // bits pending in acc; the leading ones belong to the lane before
+            const bool shared0 = nb != 0;    // my first word is shared with the lane before
+            unsigned long long acc = 0;      // right-aligned pending bits
+#pragma unroll
+            for (int k = 0; k < kEncPerThread; k++) {
+                const uint32_t l = e[k] & 63u;
+                acc = (acc << l) | (e[k] >> 6);
+                nb += l;
+                if (nb >= 32) {
+                    nb -= 32;
+                    const uint32_t w = (uint32_t)(acc >> nb);
+                    if (shared0 && wi == (pos >> 5)) atomicOr(&sw[wi], w);
+                    else sw[wi] = w;
+                    wi++;
+                }
+            }
+            if (nb > 0) atomicOr(&sw[wi], (uint32_t)(acc << (32 - nb)));
+        }
+        __syncwarp();
+        const bool first_partial = (r0 != 0);
+        const bool last_partial  = ((r0 + tot) & 31u) != 0;
+        for (uint32_t i = lane; i < nwords; i += 32) {
+            if (i == 0 && first_partial) continue;
+            if (i == nwords - 1 && last_partial) continue;
+            gw[F + i] = bswap32(sw[i]);
+        }
+        if (lane == 0) {
+            const unsigned long long none = ~0ull;
+            a.edge_idx[2 * c]      = (nwords && first_partial) ? F : none;
+            a.edge_bits[2 * c]     = nwords ? bswap32(sw[0]) : 0u;
+            a.edge_idx[2 * c + 1]  = (nwords && last_partial) ? F + nwords - 1 : none;
+            a.edge_bits[2 * c + 1] = nwords ? bswap32(sw[nwords - 1]) : 0u;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void __launch_bounds__(kEncThreads, 4) k_huff_pack(HuffEncodeArgs a) {
     extern __shared__ uint8_t s_dyn[];
     if (*a.status != VSZ_OK) return;  // set before this launch: uniform across the grid
-    pack_chunks(a, blockIdx.x * (size_t)(kEncThreads / 32) + (threadIdx.x >> 5), a.nchunks,
-                (size_t)gridDim.x * (kEncThreads / 32), s_dyn);
+    const size_t c0 = blockIdx.x * (size_t)(kEncThreads / 32) + (threadIdx.x >> 5);
+    const size_t cs = (size_t)gridDim.x * (kEncThreads / 32);
+    // max code length from the tree build (device-resident); uniform
+    if (a.cb_in_smem && a.build_info && a.build_info[2] <= kPackFastLen) pack_chunks_fast(a, c0, a.nchunks, cs, s_dyn);
+    else pack_chunks(a, c0, a.nchunks, cs, s_dyn);
 }
 
 __global__ void __launch_bounds__(kEncThreads, 4)
