@@ -44,7 +44,7 @@ __device__ __forceinline__ float strict_prequant(float v, uint32_t col, const Dq
 }
 
 template <int NDIM, bool VEC, bool PAD = false>
-__global__ void __launch_bounds__(128, 4) k_dq_decompress_b8(DqDecArgs a) {
+__global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     typedef float PrevT[8][8][32];
     PrevT* s_prev  = reinterpret_cast<PrevT*>(s_dq_dyn);  // 3D only

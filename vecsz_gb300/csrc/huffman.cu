@@ -1040,7 +1040,8 @@ __global__ void __launch_bounds__(256, 4) k_huff_decode_win(HuffDecodeArgs a) {
         w2 = ring_word(wn + 2);
         wn += 3;
     }
-    uint32_t used = 0, zeros = 0;
+    const unsigned long long pos_first = wn * 32ull + off;  // the first bit (wn counts the 3 window words)
+    uint32_t zeros = 0;
     uint16_t* dst = a.codes + out0;
     for (uint32_t r0 = 0; r0 < (uint32_t)kChunkSyms; r0 += kWinRound) {
         const uint32_t m = (live && cnt > r0) ? min((uint32_t)kWinRound, cnt - r0) : 0u;
@@ -1050,68 +1051,74 @@ __global__ void __launch_bounds__(256, 4) k_huff_decode_win(HuffDecodeArgs a) {
         }
         cp_async_wait<kWinRing / 2>();
         uint32_t pk[kWinRound / 2] = {0u, 0u, 0u, 0u};
-#pragma unroll
-        for (int k = 0; k < kWinRound; k++) {
-            if ((uint32_t)k < m) {
-                const uint32_t win = __funnelshift_l(w1, w0, off);  // 32 bits from the current position
-                const uint32_t e   = s_table[win >> (32 - kDecBits)];
-                uint32_t len       = e & 0x7fu;
-                uint32_t sy        = e >> 8;
+        // one codeword; a full round (m == kWinRound) runs it without per-code guards
+        auto step = [&](int k) {
+            const uint32_t win = __funnelshift_l(w1, w0, off);  // 32 bits from the current position
+            const uint32_t e   = s_table[win >> (32 - kDecBits)];
+            uint32_t len       = e & 0x7fu;
+            uint32_t sy        = e >> 8;
+            if (!len) {
+                uint32_t node = e >> 8, usedb = kDecBits;
+                if (e & 0x80u) {
+                    const uint32_t w2b = (e >> 8) & 0xfu;
+                    const uint32_t e2 =
+                        __ldg(&a.table2[(e >> 12) + ((win >> (32 - kDecBits - w2b)) & ((1u << w2b) - 1u))]);
+                    len   = e2 & 0xffu;
+                    sy    = e2 >> 8;
+                    node  = e2 >> 8;
+                    usedb = kDecBits + w2b;
+                }
                 if (!len) {
-                    uint32_t node = e >> 8, usedb = kDecBits;
-                    if (e & 0x80u) {
-                        const uint32_t w2b = (e >> 8) & 0xfu;
-                        const uint32_t e2 =
-                            __ldg(&a.table2[(e >> 12) + ((win >> (32 - kDecBits - w2b)) & ((1u << w2b) - 1u))]);
-                        len   = e2 & 0xffu;
-                        sy    = e2 >> 8;
-                        node  = e2 >> 8;
-                        usedb = kDecBits + w2b;
-                    }
-                    if (!len) {
-                        // longer than both tables: walk the tree over a 64-bit view of the window
-                        unsigned long long v = ((((unsigned long long)w0) << 32) | w1) << off;
-                        if (off) v |= (unsigned long long)w2 >> (32 - off);
-                        sy = 0xffffffffu;
-                        if (node != 0 && node < a.max_nodes) {
-                            for (uint32_t d = usedb; d < (uint32_t)kWinMaxLen; d++) {
-                                node = __ldg(&a.child[2 * (size_t)node + (uint32_t)((v >> (63 - d)) & 1ull)]);
-                                if (node == 0 || node >= a.max_nodes) break;
-                                const uint32_t ns = __ldg(&a.node_sym[node]);
-                                if (ns & 0x80000000u) {
-                                    sy  = ns & 0xffffu;
-                                    len = d + 1;
-                                    break;
-                                }
+                    // longer than both tables: walk the tree over a 64-bit view of the window
+                    unsigned long long v = ((((unsigned long long)w0) << 32) | w1) << off;
+                    if (off) v |= (unsigned long long)w2 >> (32 - off);
+                    sy = 0xffffffffu;
+                    if (node != 0 && node < a.max_nodes) {
+                        for (uint32_t d = usedb; d < (uint32_t)kWinMaxLen; d++) {
+                            node = __ldg(&a.child[2 * (size_t)node + (uint32_t)((v >> (63 - d)) & 1ull)]);
+                            if (node == 0 || node >= a.max_nodes) break;
+                            const uint32_t ns = __ldg(&a.node_sym[node]);
+                            if (ns & 0x80000000u) {
+                                sy  = ns & 0xffffu;
+                                len = d + 1;
+                                break;
                             }
                         }
-                        if (sy == 0xffffffffu) {
-                            bad = true;
-                            sy  = 0;
-                            len = 0;
-                        }
+                    }
+                    if (sy == 0xffffffffu) {
+                        bad = true;
+                        sy  = 0;
+                        len = 0;
                     }
                 }
-                pk[k >> 1] |= (sy & 0xffffu) << (16 * (k & 1));
-                zeros += (sy == 0u);
-                used += len;
-                off += len;
-                if (off >= 32u) {  // at most one word per codeword (len <= 32)
-                    off -= 32u;
-                    w0 = w1;
-                    w1 = w2;
-                    w2 = ring_word(wn);
-                    wn++;
-                }
             }
-        }
+            pk[k >> 1] |= (sy & 0xffffu) << (16 * (k & 1));
+            zeros += (sy == 0u);
+            off += len;
+            // at most one word per codeword (len <= 32); refilled without a branch, because some
+            // lane of the warp crosses a word boundary on nearly every step
+            const bool adv    = off >= 32u;
+            const uint32_t nw = ring_word(wn);  // a slot not yet landed is read but not used
+            off = adv ? off - 32u : off;
+            w0  = adv ? w1 : w0;
+            w1  = adv ? w2 : w1;
+            w2  = adv ? nw : w2;
+            wn += adv ? 1u : 0u;
+        };
         if (m == (uint32_t)kWinRound) {
+#pragma unroll
+            for (int k = 0; k < kWinRound; k++) step(k);
             *reinterpret_cast<uint4*>(dst + r0) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
         } else {
+#pragma unroll
+            for (int k = 0; k < kWinRound; k++)
+                if ((uint32_t)k < m) step(k);
             for (uint32_t k = 0; k < m; k++) dst[r0 + k] = (uint16_t)(pk[k >> 1] >> (16 * (k & 1)));
         }
     }
     cp_async_wait<0>();  // no copy into this CTA's shared memory may outlive it
+    // bits consumed: the position now minus the first
+    const unsigned long long used = live ? wn * 32ull + off - pos_first : 0ull;
     if (cnt && (bad || used != cb)) set_status(a.status, VSZ_ERR_CORRUPT);  // must fill exactly its length
     if (j < a.nchunks && a.chunk_zero) a.chunk_zero[j] = zeros;
 }
