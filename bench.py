@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain mixed field set")
     ap.add_argument("--batch-fields", type=int, default=1000)
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server stream")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip the 1e-3, CESM-like and adversarial single-field configurations")
     ap.add_argument("--serving-seconds", type=float, default=8.0)
     ap.add_argument("--no-stage-profile", action="store_true",
                     help="no per-stage CUDA events in the timed loop (no roofline / stages)")
@@ -325,6 +327,8 @@ def run_ours(args):
     }
     if not args.no_e2e:
         line["e2e"] = run_e2e(V, x, dims, eb, mode, dct, bs, args.e2e_steps, bytes_in, world, want=out)
+    if not args.no_other_configs and args.workload == "nyx512":
+        line["other_configs"] = run_other_configs(V, x, dims, stream)
     if not args.no_batch:
         line["batched"] = run_batch(V, args.batch_fields, 1000 + rank, reps=3)
     if not args.no_serving:
@@ -335,6 +339,58 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_other_configs(V, x512, dims512, stream, reps=5):
+    """The reference's other single-field configurations, timed like the headline one (device
+    buffers, CUDA events on the stream, median of `reps` runs after 2 warm-ups): the 512^3
+    NYX-like field at r2r eb 1e-3, the 1800x3600 CESM-like field (abs 1e-4) and the adversarial
+    256x384x384 field (abs 1e-6); each with its compression ratio and error-bound check."""
+    import torch
+
+    def one(x, dims, eb, mode):
+        codec = V.DeviceCodec(dims, eb=eb, mode=mode, dict_size=1024, block_size=8)
+        out = torch.empty_like(x)
+        with torch.cuda.stream(stream):
+            codec.compress(x, stream)
+        stream.synchronize()
+        codec.prepare_decompress(codec.archive_bytes())
+        res = codec.result_host()
+        for _ in range(2):
+            codec.compress(x, stream)
+            codec.decompress(codec.archive, out, stream)
+        cm, dm = [], []
+        for _ in range(reps):
+            a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a.record(stream)
+            codec.compress(x, stream)
+            b.record(stream)
+            codec.decompress(codec.archive, out, stream)
+            c.record(stream)
+            stream.synchronize()
+            cm.append(a.elapsed_time(b))
+            dm.append(b.elapsed_time(c))
+        ebf = codec._desc.eb_final
+        err = (out.double() - x.double()).abs()
+        bound = ebf + 2.0 * torch.abs(x.double()) * 2.0 ** -23
+        nbytes = 4 * x.numel()
+        return {"dims_xyz": list(dims), "eb": eb, "mode": mode,
+                "compress_gbs": round(nbytes / (statistics.median(cm) * 1e-3) / 1e9, 1),
+                "decompress_gbs": round(nbytes / (statistics.median(dm) * 1e-3) / 1e9, 1),
+                "compression_ratio": round(nbytes / res.data_size, 3), "n_outlier": int(res.n_outlier),
+                "max_code_len": int(res.max_code_len), "verified_error_bound": bool((err <= bound).all()),
+                "max_err_over_eb": round(float(err.max().item()) / ebf, 6)}
+
+    outd = {"nyx512_r2r_1e-3": one(x512, dims512, 1e-3, "r2r")}
+    xc = make_field_torch("cesm", seed=1)
+    outd["cesm_1800x3600_abs_1e-4"] = one(xc.reshape(-1), ref_dims("cesm"), 1e-4, "abs")
+    del xc
+    xa = make_field_torch("adversarial", seed=1)
+    outd["adversarial_256x384x384_abs_1e-6"] = one(xa.reshape(-1), ref_dims("adversarial"), 1e-6, "abs")
+    outd["note"] = ("abs 1e-6 on the adversarial field and 2D fields whose width is not a multiple of 8 "
+                    "reproduce the reference's own overshoot and dropped tail columns; strict mode "
+                    "(VSZ_FLAG_STRICT_EB) bounds them")
+    return outd
 
 
 def run_batch(V, n_fields, seed, reps, sample_every=25):

@@ -604,6 +604,35 @@ constexpr int kGatherTile = kGatherThreads * kGatherPerThread;  // segments per 
 
 // One tile of 4096 row segments of one field: the next ticket of the field's look-back.  The
 // status is read once per block, so the early exit is uniform.
+// Copies the n outliers of segment s from scratch to outlier index dst0 of the destination (one
+// warp).  A byte destination is written as whole aligned words, each the bytes of two neighbouring
+// values (funnel shift); only the partial words at the run's two ends, shared with the
+// neighbouring runs, are written byte by byte.
+__device__ __forceinline__ void copy_segment(const GatherArgs& g, uint8_t* out_bytes, size_t s, uint32_t n,
+                                             unsigned long long dst0) {
+    const unsigned lane = lane_id();
+    const float* src    = g.scratch + s * kSegX;
+    if (g.out_f32) {
+        for (uint32_t i = lane; i < n; i += 32) g.out_f32[dst0 + i] = src[i];
+        return;
+    }
+    uint8_t* d          = out_bytes + 4 * dst0;
+    const uint32_t a    = (uint32_t)(reinterpret_cast<uintptr_t>(d) & 3u);
+    const uint32_t* s32 = reinterpret_cast<const uint32_t*>(src);
+    if (a == 0) {
+        uint32_t* dw = reinterpret_cast<uint32_t*>(d);
+        for (uint32_t i = lane; i < n; i += 32) dw[i] = s32[i];
+        return;
+    }
+    uint32_t* dw = reinterpret_cast<uint32_t*>(d + (4 - a));  // word j: top a bytes of value j, low 4 - a of j + 1
+    for (uint32_t j = lane; j + 1 < n; j += 32) dw[j] = __funnelshift_r(s32[j], s32[j + 1], 8 * (4 - a));
+    if (lane == 0) {
+        const uint32_t b0 = s32[0], bl = s32[n - 1];
+        for (uint32_t t = 0; t < 4 - a; t++) d[t] = (uint8_t)(b0 >> (8 * t));                    // value 0, low bytes
+        for (uint32_t t = 0; t < a; t++) d[4 * n - a + t] = (uint8_t)(bl >> (8 * (4 - a + t)));  // value n-1, top bytes
+    }
+}
+
 __device__ __forceinline__ void gather_tile(const GatherArgs& g) {
     __shared__ uint32_t s_off[kGatherTile];
     __shared__ uint8_t s_cnt[kGatherTile];
@@ -672,39 +701,50 @@ __device__ __forceinline__ void gather_tile(const GatherArgs& g) {
     }
     __syncthreads();
     const unsigned long long base = s_base;
+    const size_t tseg0            = (size_t)tile * kGatherTile;
+    if (g.seg_off) {  // split copy: record the offsets, k_outlier_copy moves the values
+        for (int k = threadIdx.x; k < kGatherTile; k += kGatherThreads)
+            if (tseg0 + k < g.nseg) g.seg_off[tseg0 + k] = s_off[k];
+        if (threadIdx.x == 0) g.tile_base[tile] = base;
+        return;
+    }
     uint8_t* out_bytes = g.out_bytes ? g.out_bytes + g.out_off.eval() : nullptr;
     // warp-cooperative copies of the non-empty segments: each warp scans 32 segment counts at a
     // time from shared memory and visits only those with outliers
-    const size_t tseg0 = (size_t)tile * kGatherTile;
     for (int k0 = w * 32; k0 < kGatherTile; k0 += kGatherThreads) {
         const int kk = k0 + (int)lane;
         const bool has = (tseg0 + kk < g.nseg) && s_cnt[kk] != 0;
         unsigned nz = __ballot_sync(0xffffffffu, has);
         while (nz) {
-        const int k = k0 + __ffs(nz) - 1;
-        nz &= nz - 1;
-        const size_t s = tseg0 + k;
-        const uint32_t n = s_cnt[k];
-        const float* src          = g.scratch + s * kSegX;
-        unsigned long long dst0   = base + s_off[k];
-        for (uint32_t i = lane; i < n; i += 32) {
-            float v = src[i];
-            if (g.out_f32) {
-                g.out_f32[dst0 + i] = v;
-            } else {
-                uint8_t* d = out_bytes + 4 * (dst0 + i);
-                uint32_t b = __float_as_uint(v);
-                d[0]       = (uint8_t)b;
-                d[1]       = (uint8_t)(b >> 8);
-                d[2]       = (uint8_t)(b >> 16);
-                d[3]       = (uint8_t)(b >> 24);
-            }
-        }
+            const int k = k0 + __ffs(nz) - 1;
+            nz &= nz - 1;
+            copy_segment(g, out_bytes, tseg0 + k, s_cnt[k], base + s_off[k]);
         }
     }
 }
 
 __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g) { gather_tile(g); }
+
+// Split copy: every warp of the grid takes 32 segments at a time and copies the non-empty ones.
+__global__ void __launch_bounds__(256) k_outlier_copy(GatherArgs g) {
+    if (*g.status != VSZ_OK) return;
+    const unsigned lane = lane_id();
+    uint8_t* out_bytes  = g.out_bytes ? g.out_bytes + g.out_off.eval() : nullptr;
+    const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t s0 = ((size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; s0 < g.nseg;
+         s0 += nwarps * 32) {
+        const size_t s    = s0 + lane;
+        const uint32_t cn = (s < g.nseg) ? g.seg_count[s] : 0u;
+        unsigned nz       = __ballot_sync(0xffffffffu, cn != 0u);
+        while (nz) {
+            const int k = __ffs(nz) - 1;
+            nz &= nz - 1;
+            const size_t sk = s0 + k;
+            const uint32_t n = __shfl_sync(0xffffffffu, cn, k);
+            copy_segment(g, out_bytes, sk, n, g.tile_base[sk / kGatherTile] + g.seg_off[sk]);
+        }
+    }
+}
 
 // Many fields: one task per tile of each field (tasks[t].field; the field's tickets keep its tiles
 // in look-back order, and the holder of every earlier ticket is already running).
@@ -862,7 +902,7 @@ int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms)
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
-int launch_outlier_gather(GatherArgs g, cudaStream_t st) {
+int launch_outlier_gather(GatherArgs g, cudaStream_t st, int num_sms) {
     g.ntiles = (uint32_t)((g.nseg + kGatherTile - 1) / kGatherTile);
     if (g.ntiles == 0) {
         return cudaMemsetAsync(g.total, 0, sizeof(unsigned long long), st) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
@@ -871,6 +911,11 @@ int launch_outlier_gather(GatherArgs g, cudaStream_t st) {
     if (cudaMemsetAsync(g.tile_counter, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
     k_outlier_gather<<<g.ntiles, kGatherThreads, 0, st>>>(g);
     count_launch();
+    if (g.seg_off) {
+        const long long want = (long long)((g.nseg + 255) / 256), cap = (long long)(num_sms > 0 ? num_sms : 152) * 8;
+        k_outlier_copy<<<(unsigned)(want < cap ? want : cap), 256, 0, st>>>(g);
+        count_launch();
+    }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 

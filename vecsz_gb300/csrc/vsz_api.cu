@@ -60,6 +60,8 @@ struct CompressWs {
     float* scratch;
     unsigned long long* g_tile_status;
     uint32_t* g_counter;
+    uint32_t* g_seg_off;              // split outlier copy: offset of each segment within its tile
+    unsigned long long* g_tile_base;  // and each tile's first outlier
     unsigned long long* n_out;
     uint8_t* build_scratch;
     uint8_t* cb_block;
@@ -93,6 +95,8 @@ CompressWs layout_compress(const Geometry& g, int dict, uint8_t* base, size_t ca
     size_t gt   = (g.nseg + 4095) / 4096 + 1;
     w.g_tile_status = b.take<unsigned long long>(gt);
     w.g_counter = b.take<uint32_t>(4);
+    w.g_seg_off = b.take<uint32_t>(g.nseg + 16);
+    w.g_tile_base = b.take<unsigned long long>(gt);
     w.n_out     = b.take<unsigned long long>(1);
     w.build_scratch = b.take<uint8_t>(huff_build_scratch_bytes(dict));
     // codebook block [cb_word dict x u64][info 4 x u32][cb_len dict x u8]: one copy from the host
@@ -820,9 +824,11 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
     ga.tile_status = w.g_tile_status;
     ga.tile_counter = w.g_counter;
     ga.status = w.status;
+    ga.seg_off = w.g_seg_off;
+    ga.tile_base = w.g_tile_base;
     {
         StageTimer t(kStOutlierGather, st);
-        VSZ_TRY(launch_outlier_gather(ga, st));
+        VSZ_TRY(launch_outlier_gather(ga, st, num_sms()));
     }
     // 6. header, result record, trailer with the decode index
     FinalizeArgs f{};

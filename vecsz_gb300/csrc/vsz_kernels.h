@@ -122,6 +122,11 @@ struct GatherArgs {
     uint32_t* tile_counter;
     int* status;
     uint32_t ntiles;
+    // optional split copy: the look-back kernel records each segment's outlier offset within its
+    // tile (seg_off, nseg) and each tile's first outlier (tile_base, ntiles), and k_outlier_copy
+    // moves the values with the whole grid -- for fields with many outliers
+    uint32_t* seg_off;
+    unsigned long long* tile_base;
 };
 
 // ---- dual-quant decompress ----------------------------------------------------------------
@@ -153,7 +158,7 @@ int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_
 int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_consts, uint32_t* d_mm,
                     cudaStream_t st, int* status_word = nullptr);
 int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms);
-int launch_outlier_gather(GatherArgs g, cudaStream_t st);
+int launch_outlier_gather(GatherArgs g, cudaStream_t st, int num_sms = 0);
 
 // Pad values of a field (-p).  Writes the archive's pad section (`arch`, any alignment) and, in
 // global mode, the value the compressor's 2D/3D blocks predict from (`halo_g`).  ws: pad_ws_bytes.
