@@ -1023,8 +1023,11 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     // VSZ_FORCE_GENERAL_DECOMPRESS: the general reverse-Lorenzo kernel for every block size (tests
     // of that path); it ranks outliers by row segment only
     const bool force_general = getenv("VSZ_FORCE_GENERAL_DECOMPRESS") != nullptr;
-    // the block-8 kernel ranks outliers from the decoder's per-chunk zero counts directly
-    const bool chunk_rank = idx != nullptr && bs == 8 && d->node_count > 1 && !force_general;
+    // the block-8 kernel ranks outliers from the decoder's per-chunk zero counts directly, which
+    // costs a recount from the chunk start in every row segment holding outliers; with dense
+    // outliers (over 1 in 1024 elements) the per-segment zero counts are cheaper
+    const bool dense_outliers = d->n_outlier > g.n / 1024;
+    const bool chunk_rank     = idx != nullptr && bs == 8 && d->node_count > 1 && !force_general && !dense_outliers;
     {
         StageTimer t(kStZeroScan, st);
         if (chunk_rank) {
