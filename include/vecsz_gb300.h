@@ -374,6 +374,28 @@ vsz_status vsz_decompress_host_into(const uint8_t* h_archive, size_t len, size_t
                                     const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, size_t* n);
 void vsz_free_host(void* p);
 
+/* Stream-ordered host-buffer operations.  A vsz_host_op owns a CUDA stream and device buffers
+ * (grown on demand, kept between calls); its compress / decompress enqueue all their work and
+ * return without synchronising, so several ops overlap their host<->device copies and kernels
+ * (host-to-device and device-to-host copies run concurrently on the link).  Host buffers must be
+ * pinned (cudaHostAlloc / cudaHostRegister).  No lossless pass (VSZ_ERR_UNSUPPORTED).
+ *   compress:   h_in (n floats) -> h_out (the packed block and this library's trailer;
+ *               out_capacity from vsz_compress_host_bound) and h_result (the 8-u64 vsz_result:
+ *               data_size + trailer_size bytes of h_out are valid; status VSZ_ERR_CAPACITY when
+ *               they did not fit).  The archive's size is known only on the device: a kernel
+ *               copies exactly those bytes into h_out.
+ *   decompress: h_archive (len bytes, complete: the host parses its header) -> h_out (n floats),
+ *               *h_status = VSZ_OK or the device-side error.
+ *   wait:       blocks until the op's enqueued work is done; returns VSZ_ERR_CUDA if it failed. */
+typedef struct vsz_host_op vsz_host_op;
+vsz_status vsz_host_op_create(vsz_host_op** op);
+void vsz_host_op_destroy(vsz_host_op* op);
+vsz_status vsz_host_op_compress(vsz_host_op* op, const vsz_params* p, int ndim, const size_t dims[3], const float* h_in,
+                                uint8_t* h_out, size_t out_capacity, uint64_t* h_result);
+vsz_status vsz_host_op_decompress(vsz_host_op* op, const uint8_t* h_archive, size_t len,
+                                  const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, int* h_status);
+vsz_status vsz_host_op_wait(vsz_host_op* op);
+
 /* Lossless pass on host memory (src/lossless.hh:179-221): level 3 zstd or zlib through the
  * system libzstd / libz.  *h_out malloc'd.  VSZ_ERR_UNSUPPORTED when the library is absent. */
 vsz_status vsz_lossless_compress(int which, const uint8_t* h_in, size_t len, uint8_t** h_out, size_t* out_len);

@@ -298,3 +298,50 @@ def test_nan_inputs_keep_reference_bits(cuda, dims, bs):
     assert c.data[:c.data_size] == oa
     y = V.decompress(c)
     np.testing.assert_array_equal(y.view(np.uint32), O.decompress(oa, bs, 1024).view(np.uint32))
+
+
+def test_host_ops_match_host_entry_points(cuda):
+    """Stream-ordered host-buffer ops: the same archive bytes and reconstruction as the one-call
+    host entry points, with two ops in flight on different fields."""
+    import ctypes as C
+
+    from vecsz_gb300 import _lib as L
+    from vecsz_gb300.api import HostOp
+    torch = cuda
+    fields_ = [(fields.grf_3d(40, 48, 64, seed=31).ravel(), (64, 48, 40), "r2r", 1e-3),
+               (fields.bump_field_2d(90, 200, seed=32).ravel(), (200, 90), "abs", 1e-4)]
+    ops = [HostOp(), HostOp()]
+    pinned = []
+    for x, dims, mode, eb in fields_:
+        p = V.make_params(eb, mode, 1024, 8)
+        cap = C.c_size_t(0)
+        L.check(L.lib().vsz_compress_host_bound(C.byref(p), len(dims), L.dims_arg(dims), C.byref(cap)))
+        h_in = torch.from_numpy(x).pin_memory()
+        h_arch = torch.zeros(cap.value, dtype=torch.uint8).pin_memory()
+        h_res = torch.zeros(8, dtype=torch.int64).pin_memory()
+        h_out = torch.zeros(x.size, dtype=torch.float32).pin_memory()
+        h_st = torch.zeros(1, dtype=torch.int32).pin_memory()
+        pinned.append((x, dims, mode, eb, p, cap.value, h_in, h_arch, h_res, h_out, h_st))
+    for op, (x, dims, mode, eb, p, cap, h_in, h_arch, h_res, h_out, h_st) in zip(ops, pinned):
+        op.compress(p, dims, h_in.data_ptr(), h_arch.data_ptr(), cap, h_res.data_ptr())
+    for op, (x, dims, mode, eb, p, cap, h_in, h_arch, h_res, h_out, h_st) in zip(ops, pinned):
+        op.wait()
+        r = h_res.numpy()
+        assert int(r[5]) == 0
+        total = int(r[0] + r[1])
+        ref = V.compress(x, dims, eb=eb, mode=mode, dict_size=1024, block_size=8)
+        assert h_arch.numpy()[:total].tobytes() == ref.data
+        opts = L.DecompressOpts(1024, 8, 1 if mode == "r2r" else 0, 0.0)
+        op.decompress(h_arch.data_ptr(), total, opts, h_out.data_ptr(), x.size, h_st.data_ptr())
+    for op, (x, dims, mode, eb, p, cap, h_in, h_arch, h_res, h_out, h_st) in zip(ops, pinned):
+        op.wait()
+        assert int(h_st.item()) == 0
+        ref = V.compress(x, dims, eb=eb, mode=mode, dict_size=1024, block_size=8)
+        np.testing.assert_array_equal(h_out.numpy().view(np.uint32), V.decompress(ref).view(np.uint32))
+    # an archive that does not fit is reported, not written past the buffer
+    x, dims, mode, eb, p, cap, h_in, h_arch, h_res, h_out, h_st = pinned[0]
+    ops[0].compress(p, dims, h_in.data_ptr(), h_arch.data_ptr(), 16, h_res.data_ptr())
+    ops[0].wait()
+    assert int(h_res.numpy()[5]) == L.VSZ_ERR_CAPACITY
+    for op in ops:
+        op.close()

@@ -147,6 +147,11 @@ _PROTOS = {
                              C.POINTER(C.c_size_t)], _i),
     "vsz_decompress_host_into": ([_p, _sz, _sz, _sz, C.POINTER(DecompressOpts), _p, _sz, C.POINTER(C.c_size_t)], _i),
     "vsz_free_host": ([_p], None),
+    "vsz_host_op_create": ([C.POINTER(_p)], _i),
+    "vsz_host_op_destroy": ([_p], None),
+    "vsz_host_op_compress": ([_p, C.POINTER(Params), _i, C.POINTER(C.c_size_t), _p, _p, _sz, _p], _i),
+    "vsz_host_op_decompress": ([_p, _p, _sz, _p, _p, _sz, _p], _i),
+    "vsz_host_op_wait": ([_p], _i),
     "vsz_lossless_compress": ([_i, _p, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_lossless_decompress": ([_p, _sz, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_lossless_detect": ([_p, _sz], _i),

@@ -191,6 +191,42 @@ class DeviceCodec:
         return int(self._dstatus.item())
 
 
+class HostOp:
+    """One stream-ordered compress or decompress on pinned host buffers (vsz_host_op_*): calls
+    enqueue the copies and kernels and return at once; wait() blocks until they are done.  Several
+    ops overlap their host-to-device and device-to-host copies."""
+
+    def __init__(self):
+        h = C.c_void_p(0)
+        check(lib().vsz_host_op_create(C.byref(h)), "host_op_create")
+        self._h = h
+
+    def compress(self, p: Params, dims, h_in_ptr: int, h_out_ptr: int, out_capacity: int, h_result_ptr: int):
+        check(lib().vsz_host_op_compress(self._h, C.byref(p), len(dims), dims_arg(dims), C.c_void_p(h_in_ptr),
+                                         C.c_void_p(h_out_ptr), int(out_capacity), C.c_void_p(h_result_ptr)),
+              "host_op_compress")
+
+    def decompress(self, h_archive_ptr: int, length: int, opts: DecompressOpts, h_out_ptr: int, out_capacity: int,
+                   h_status_ptr: int):
+        check(lib().vsz_host_op_decompress(self._h, C.c_void_p(h_archive_ptr), int(length), C.byref(opts),
+                                           C.c_void_p(h_out_ptr), int(out_capacity), C.c_void_p(h_status_ptr)),
+              "host_op_decompress")
+
+    def wait(self):
+        check(lib().vsz_host_op_wait(self._h), "host_op_wait")
+
+    def close(self):
+        if self._h:
+            lib().vsz_host_op_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class BatchCompressor:
     """Many device fields compressed in one launch sequence (vsz_batch_*).
 

@@ -309,6 +309,11 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
 // the tree into pinned staging, and two async copies put the codebook into the workspace and the
 // serialised tree into the archive.  Nothing returns to the caller's thread and nothing
 // synchronises.  Under stream capture (a CUDA graph) the device builder k_huff_build is used.
+//
+// The three small transfers are made by a kernel's loads and stores to the mapped pinned area,
+// not by the copy engines: a copy engine serves its queue in order, so with several streams in
+// flight a few-KB histogram or codebook copy would wait behind another stream's field-sized
+// transfer, and the Huffman stage of this compress with it.
 
 std::atomic<int> g_tree_builder{-1};
 
@@ -332,9 +337,32 @@ struct TreeSlot {
     int hdr_dict  = 0;
     bool reserved = false;
     uint8_t* pinned = nullptr;
+    uint8_t* pinned_dev = nullptr;  // the same area as the device addresses it
     cudaEvent_t done = nullptr;
     size_t hist_off = 0, cb_off = 0, head_off = 0;
 };
+
+__global__ void __launch_bounds__(256) k_link_copy(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
+                                                   size_t bytes) {
+    const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t nt  = (size_t)gridDim.x * blockDim.x;
+    size_t head      = 0;
+    if ((((uintptr_t)dst | (uintptr_t)src) & 15) == 0) {
+        head = bytes & ~(size_t)15;
+        for (size_t i = tid; i < head / 16; i += nt)
+            reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
+    }
+    for (size_t i = head + tid; i < bytes; i += nt) dst[i] = src[i];
+    __threadfence_system();
+}
+
+int launch_link_copy(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes == 0) return VSZ_OK;
+    const unsigned blocks = (unsigned)std::min<size_t>(32, (bytes + 4095) / 4096);
+    k_link_copy<<<blocks, 256, 0, st>>>(static_cast<uint8_t*>(dst), static_cast<const uint8_t*>(src), bytes);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
 
 std::mutex g_slot_mu;
 std::vector<TreeSlot*> g_slots;
@@ -369,7 +397,9 @@ TreeSlot* acquire_tree_slot(int dict) {
         delete s;
         return nullptr;
     }
-    if (cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->pinned_dev), s->pinned, 0) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
         cudaFreeHost(s->pinned);
         delete s;
         return nullptr;
@@ -394,12 +424,10 @@ int enqueue_host_tree(const unsigned long long* hist, int dict, int hdr_dict, ui
     s->dict     = dict;
     s->hdr_dict = hdr_dict;
     int rc  = VSZ_OK;
-    if (cudaMemcpyAsync(s->pinned + s->hist_off, hist, 8 * (size_t)dict, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+    if (launch_link_copy(s->pinned_dev + s->hist_off, hist, 8 * (size_t)dict, st) != VSZ_OK ||
         cudaLaunchHostFunc(st, host_tree_callback, s) != cudaSuccess ||
-        cudaMemcpyAsync(cb_block, s->pinned + s->cb_off, codebook_block_bytes(dict), cudaMemcpyHostToDevice, st) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(huff_out, s->pinned + s->head_off, tree_head_max(dict), cudaMemcpyHostToDevice, st) !=
-            cudaSuccess)
+        launch_link_copy(cb_block, s->pinned_dev + s->cb_off, codebook_block_bytes(dict), st) != VSZ_OK ||
+        launch_link_copy(huff_out, s->pinned_dev + s->head_off, tree_head_max(dict), st) != VSZ_OK)
         rc = VSZ_ERR_CUDA;
     // recorded even after a failed enqueue, so the slot is not reused while anything queued reads it
     if (cudaEventRecord(s->done, st) != cudaSuccess) rc = VSZ_ERR_CUDA;

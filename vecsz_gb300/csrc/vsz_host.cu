@@ -13,6 +13,10 @@
 
 #include "vsz_types.h"
 
+namespace vsz {
+void count_launch();  // vsz_profile.cu
+}
+
 namespace {
 
 #define VSZ_TRY(x)                     \
@@ -126,6 +130,41 @@ bool zlib_magic(const uint8_t* b, size_t len) {
     return false;
 }
 
+}  // namespace
+
+// ---- stream-ordered host-buffer operations (vsz_host_op_*) ---------------------------------------
+
+struct vsz_host_op {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf in, ws, archive, out, result;
+};
+
+namespace {
+// The archive (data_size + trailer_size bytes, known only on the device) and the result record
+// into pinned host memory: 16-byte pieces where both ends allow, bytes otherwise.
+__global__ void __launch_bounds__(256) k_archive_to_host(const uint8_t* __restrict__ a, const uint64_t* __restrict__ r,
+                                                         uint8_t* __restrict__ h_out, size_t cap, uint64_t* h_result) {
+    const uint64_t total = r[5] == VSZ_OK ? r[0] + r[1] : 0;
+    const bool fits      = total <= cap;
+    if (blockIdx.x == 0 && threadIdx.x < 8) {
+        uint64_t v = r[threadIdx.x];
+        if (threadIdx.x == 5 && r[5] == VSZ_OK && !fits) v = VSZ_ERR_CAPACITY;
+        h_result[threadIdx.x] = v;
+    }
+    if (!fits || total == 0) return;
+    const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const bool vec   = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(h_out)) & 15u) == 0;
+    size_t done      = 0;
+    if (vec) {
+        const size_t n16 = (size_t)(total / 16);
+        const uint4* s   = reinterpret_cast<const uint4*>(a);
+        uint4* d         = reinterpret_cast<uint4*>(h_out);
+        for (size_t i = tid; i < n16; i += stride) d[i] = s[i];
+        done = n16 * 16;
+    }
+    for (size_t i = done + tid; i < total; i += stride) h_out[i] = a[i];
+}
 }  // namespace
 
 extern "C" {
@@ -370,6 +409,80 @@ vsz_status vsz_decompress_host(const uint8_t* h_archive, size_t len, size_t data
     }
     *h_out = o;
     return VSZ_OK;
+}
+
+vsz_status vsz_host_op_create(vsz_host_op** op) {
+    if (!op) return VSZ_ERR_INVALID;
+    vsz_host_op* o = new vsz_host_op();
+    if (cudaGetDevice(&o->device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&o->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete o;
+        return VSZ_ERR_CUDA;
+    }
+    *op = o;
+    return VSZ_OK;
+}
+
+void vsz_host_op_destroy(vsz_host_op* op) {
+    if (!op) return;
+    if (op->stream) {
+        cudaStreamSynchronize(op->stream);
+        cudaStreamDestroy(op->stream);
+    }
+    for (DevBuf* b : {&op->in, &op->ws, &op->archive, &op->out, &op->result})
+        if (b->p) cudaFree(b->p);
+    delete op;
+}
+
+vsz_status vsz_host_op_compress(vsz_host_op* op, const vsz_params* p, int ndim, const size_t dims[3], const float* h_in,
+                                uint8_t* h_out, size_t out_capacity, uint64_t* h_result) {
+    if (!op || !p || !h_in || !h_out || !h_result) return VSZ_ERR_INVALID;
+    if (p->lossless != VSZ_LOSSLESS_NONE) return VSZ_ERR_UNSUPPORTED;
+    size_t ws = 0, cap = 0;
+    VSZ_TRY(vsz_compress_bounds(p, ndim, dims, &ws, &cap));
+    size_t n = dims[0] * (ndim > 1 ? dims[1] : 1) * (ndim > 2 ? dims[2] : 1);
+    VSZ_TRY(op->in.grow(n * sizeof(float)));
+    VSZ_TRY(op->ws.grow(ws));
+    VSZ_TRY(op->archive.grow(cap));
+    VSZ_TRY(op->result.grow(64));
+    VSZ_CUDA(cudaMemcpyAsync(op->in.p, h_in, n * sizeof(float), cudaMemcpyHostToDevice, op->stream));
+    VSZ_TRY(vsz_compress(p, ndim, dims, (const float*)op->in.p, op->ws.p, op->ws.cap, (uint8_t*)op->archive.p,
+                         op->archive.cap, (uint64_t*)op->result.p, op->stream));
+    // enough CTAs to keep the link busy; the kernel strides over what the device says the size is
+    k_archive_to_host<<<256, 256, 0, op->stream>>>((const uint8_t*)op->archive.p, (const uint64_t*)op->result.p,
+                                                   h_out, out_capacity, h_result);
+    vsz::count_launch();
+    VSZ_CUDA(cudaGetLastError());
+    return VSZ_OK;
+}
+
+vsz_status vsz_host_op_decompress(vsz_host_op* op, const uint8_t* h_archive, size_t len,
+                                  const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, int* h_status) {
+    if (!op || !h_archive || !h_out || !h_status) return VSZ_ERR_INVALID;
+    vsz_archive_desc d;
+    VSZ_TRY(vsz_archive_parse(h_archive, len, &d));
+    size_t n = d.dims[0] * d.dims[1] * d.dims[2];
+    if (n > out_capacity) return VSZ_ERR_CAPACITY;
+    size_t ws = 0;
+    VSZ_TRY(vsz_decompress_bounds(&d, opts, &ws));
+    size_t used = d.has_trailer ? (size_t)(d.index_offset + 2 * d.n_chunks) : (size_t)d.data_size;
+    if (used > len) return VSZ_ERR_CORRUPT;
+    VSZ_TRY(op->archive.grow(used + 64));
+    VSZ_TRY(op->ws.grow(ws));
+    VSZ_TRY(op->out.grow(n * sizeof(float)));
+    VSZ_TRY(op->result.grow(64));
+    VSZ_CUDA(cudaMemcpyAsync(op->archive.p, h_archive, used, cudaMemcpyHostToDevice, op->stream));
+    VSZ_CUDA(cudaMemsetAsync((uint8_t*)op->archive.p + used, 0, 64, op->stream));
+    VSZ_TRY(vsz_decompress(&d, opts, (const uint8_t*)op->archive.p, op->ws.p, op->ws.cap, (float*)op->out.p,
+                           (int*)op->result.p, op->stream));
+    VSZ_CUDA(cudaMemcpyAsync(h_status, op->result.p, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+    VSZ_CUDA(cudaMemcpyAsync(h_out, op->out.p, n * sizeof(float), cudaMemcpyDeviceToHost, op->stream));
+    return VSZ_OK;
+}
+
+vsz_status vsz_host_op_wait(vsz_host_op* op) {
+    if (!op) return VSZ_ERR_INVALID;
+    return cudaStreamSynchronize(op->stream) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
 }  // extern "C"
