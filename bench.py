@@ -325,6 +325,7 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks.summary(t_wall0, t_wall1),
     }
+    line["lossless"] = run_device_gzip(V, codec.archive, int(res.data_size), stream)
     if not args.no_e2e:
         line["e2e"] = run_e2e(V, x, dims, eb, mode, dct, bs, args.e2e_steps, bytes_in, world, want=out)
     if not args.no_other_configs and args.workload == "nyx512":
@@ -339,6 +340,54 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_device_gzip(V, d_archive, nbytes, stream, reps=5, host_sample=16 << 20):
+    """The -L gzip pass on the device (vsz_deflate) over a packed block already in device memory:
+    GB/s of input by CUDA events (median of `reps` after 2 warm-ups), the frame's size, a check
+    that host zlib inflates it to the block, and host zlib level 3 (the reference's -L gzip pass,
+    one core) timed on the block's first `host_sample` bytes."""
+    import ctypes as C
+    import zlib
+
+    import torch
+    from vecsz_gb300 import _lib as L
+    from vecsz_gb300.api import _ptr
+    lib = L.lib()
+    ws, cap = C.c_size_t(0), C.c_size_t(0)
+    L.check(lib.vsz_deflate_bounds(nbytes, C.byref(ws), C.byref(cap)))
+    d_ws = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
+    d_out = torch.empty(cap.value, dtype=torch.uint8, device="cuda")
+    d_res = torch.zeros(8, dtype=torch.int64, device="cuda")
+
+    def once():
+        L.check(lib.vsz_deflate(_ptr(d_archive), nbytes, _ptr(d_ws), ws.value, _ptr(d_out), cap.value, _ptr(d_res),
+                                C.c_void_p(stream.cuda_stream)), "deflate")
+
+    for _ in range(2):
+        once()
+    ms = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        once()
+        b.record(stream)
+        stream.synchronize()
+        ms.append(a.elapsed_time(b))
+    r = d_res.cpu().numpy()
+    frame = d_out[: int(r[0])].cpu().numpy().tobytes()
+    block = d_archive[:nbytes].cpu().numpy().tobytes()
+    ok = int(r[1]) == 0 and zlib.decompress(frame) == block
+    sample = block[:host_sample]
+    t0 = time.perf_counter()
+    z3 = zlib.compress(sample, 3)
+    t_host = time.perf_counter() - t0
+    return {"api": "vsz_deflate (device, zlib stream)", "input_bytes": nbytes,
+            "gbs": round(nbytes / (statistics.median(ms) * 1e-3) / 1e9, 2), "ms": round(statistics.median(ms), 4),
+            "frame_bytes": int(r[0]), "frame_ratio": round(int(r[0]) / max(nbytes, 1), 4),
+            "chunks": {"stored": int(r[3]), "fixed": int(r[4]), "dynamic": int(r[5])}, "verified_inflate": ok,
+            "host_zlib3": {"sample_bytes": len(sample), "ratio": round(len(z3) / max(len(sample), 1), 4),
+                           "gbs": round(len(sample) / t_host / 1e9, 4), "cores": 1, "bytes": len(z3)}}
 
 
 def run_other_configs(V, x512, dims512, stream, reps=5):
@@ -374,7 +423,8 @@ def run_other_configs(V, x512, dims512, stream, reps=5):
         err = (out.double() - x.double()).abs()
         bound = ebf + 2.0 * torch.abs(x.double()) * 2.0 ** -23
         nbytes = 4 * x.numel()
-        return {"dims_xyz": list(dims), "eb": eb, "mode": mode,
+        gz = run_device_gzip(V, codec.archive, int(res.data_size), stream)
+        return {"dims_xyz": list(dims), "eb": eb, "mode": mode, "lossless": gz,
                 "compress_gbs": round(nbytes / (statistics.median(cm) * 1e-3) / 1e9, 1),
                 "decompress_gbs": round(nbytes / (statistics.median(dm) * 1e-3) / 1e9, 1),
                 "compression_ratio": round(nbytes / res.data_size, 3), "n_outlier": int(res.n_outlier),

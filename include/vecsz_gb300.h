@@ -41,6 +41,9 @@ typedef int vsz_status;
 #define VSZ_LOSSLESS_NONE 0
 #define VSZ_LOSSLESS_ZSTD 1 /* -L zstd: host library, level 3 (src/lossless.hh:179-200) */
 #define VSZ_LOSSLESS_GZIP 2 /* -L gzip: host library, level 3 */
+/* -L gzip on the GPU (vsz_deflate): a zlib stream that the reference's lossless pass detects and
+ * decodes (src/lossless.hh:40-76), with bytes of its own (not zlib's level 3 output). */
+#define VSZ_LOSSLESS_GZIP_DEVICE 3
 
 /* Compression settings: the ArgParse fields that reach the path
  * (src/argument_parser/argparse.hh:62-77; reference defaults eb 1e-4, dict 4096, block 8). */
@@ -402,6 +405,16 @@ vsz_status vsz_lossless_compress(int which, const uint8_t* h_in, size_t len, uin
 vsz_status vsz_lossless_decompress(const uint8_t* h_in, size_t len, size_t target, uint8_t** h_out, size_t* out_len);
 /* 1 zstd frame, 2 zlib stream, 0 neither (is_lossless_compressed_data, src/lossless.hh:59-76). */
 int vsz_lossless_detect(const uint8_t* h_in, size_t len);
+
+/* The gzip pass on the device (replaces zlib_compress, src/lossless.hh:84-142, for -L gzip):
+ * d_in[len] -> a zlib stream (RFC 1950 around RFC 1951 deflate) in d_out.  32 KiB chunks are
+ * encoded independently (one CTA each: hash-chain match search, dynamic, fixed or stored block,
+ * whichever is shortest, then an empty stored block so the next chunk starts on a byte).
+ * d_result (device, 8 x u64): [0] stream bytes, [1] status (VSZ_ERR_CAPACITY when out_capacity is
+ * too small), [2] chunks, [3] stored, [4] fixed, [5] dynamic chunks.  Stream-ordered, no sync. */
+vsz_status vsz_deflate_bounds(size_t len, size_t* ws_bytes, size_t* out_capacity);
+vsz_status vsz_deflate(const uint8_t* d_in, size_t len, void* d_ws, size_t ws_bytes, uint8_t* d_out,
+                       size_t out_capacity, uint64_t* d_result, void* stream);
 
 /* Per-stage device timing: when enabled, the whole-field entry points record a CUDA event pair
  * around each stage on the launching stream.  vsz_profile_read synchronises, returns the number of

@@ -33,6 +33,7 @@ TREE_HOST = 2
 LOSSLESS_NONE = 0
 LOSSLESS_ZSTD = 1
 LOSSLESS_GZIP = 2
+LOSSLESS_GZIP_DEVICE = 3
 CONSTS_BYTES = 64
 
 
@@ -155,6 +156,8 @@ _PROTOS = {
     "vsz_lossless_compress": ([_i, _p, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_lossless_decompress": ([_p, _sz, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_lossless_detect": ([_p, _sz], _i),
+    "vsz_deflate_bounds": ([_sz, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], _i),
+    "vsz_deflate": ([_p, _sz, _p, _sz, _p, _sz, _p, _p], _i),
     "vsz_profile_enable": ([_i], None),
     "vsz_profile_reset": ([], None),
     "vsz_profile_read": ([_p, _p, _p, _i], _i),

@@ -16,7 +16,8 @@ from . import _lib as L
 from ._lib import (ArchiveDesc, DecompressOpts, Params, Result, VszError, check, dims_arg, lib)
 
 _MODES = {"abs": L.MODE_ABS, "r2r": L.MODE_R2R}
-_LOSSLESS = {None: L.LOSSLESS_NONE, "none": L.LOSSLESS_NONE, "zstd": L.LOSSLESS_ZSTD, "gzip": L.LOSSLESS_GZIP}
+_LOSSLESS = {None: L.LOSSLESS_NONE, "none": L.LOSSLESS_NONE, "zstd": L.LOSSLESS_ZSTD, "gzip": L.LOSSLESS_GZIP,
+             "gzip-device": L.LOSSLESS_GZIP_DEVICE}
 
 
 _PAD_MODES = {"none": L.PAD_NONE, "global": L.PAD_GLOBAL, "block": L.PAD_BLOCK, "edge": L.PAD_EDGE}
@@ -131,6 +132,31 @@ def _stream_ptr(stream=None) -> C.c_void_p:
     torch = _torch()
     s = stream if stream is not None else torch.cuda.current_stream()
     return C.c_void_p(s.cuda_stream)
+
+
+def deflate(data, stream=None):
+    """The gzip pass on the device (vsz_deflate): bytes, a uint8 numpy array or a uint8 CUDA tensor
+    -> (zlib stream bytes, stats {chunks, stored, fixed, dynamic})."""
+    torch = _torch()
+    if isinstance(data, torch.Tensor):
+        d_in = data.contiguous().view(-1)
+        n = int(d_in.numel())
+    else:
+        a = data.view(np.uint8).ravel() if isinstance(data, np.ndarray) else np.frombuffer(bytes(data), np.uint8)
+        n = int(a.size)
+        d_in = torch.from_numpy(a.copy()).cuda() if n else torch.zeros(1, dtype=torch.uint8, device="cuda")
+    ws, cap = C.c_size_t(0), C.c_size_t(0)
+    check(lib().vsz_deflate_bounds(n, C.byref(ws), C.byref(cap)), "deflate_bounds")
+    d_ws = torch.empty(max(1, ws.value), dtype=torch.uint8, device=d_in.device)
+    d_out = torch.empty(cap.value, dtype=torch.uint8, device=d_in.device)
+    res = torch.zeros(8, dtype=torch.int64, device=d_in.device)
+    check(lib().vsz_deflate(_ptr(d_in), n, _ptr(d_ws), ws.value, _ptr(d_out), cap.value, _ptr(res),
+                            _stream_ptr(stream)), "deflate")
+    r = res.cpu().numpy()
+    if int(r[1]) != 0:
+        raise VszError(int(r[1]), "deflate (device)")
+    out = d_out[: int(r[0])].cpu().numpy().tobytes()
+    return out, {"chunks": int(r[2]), "stored": int(r[3]), "fixed": int(r[4]), "dynamic": int(r[5])}
 
 
 class DeviceCodec:

@@ -52,6 +52,7 @@ struct HostCtx {
     std::mutex mu;
     cudaStream_t stream = nullptr;
     DevBuf in, ws, archive, out, result;
+    DevBuf dws, dframe;  // the device gzip pass: workspace and zlib stream
 };
 
 HostCtx* ctx_for_device() {
@@ -255,6 +256,9 @@ vsz_status vsz_lossless_decompress(const uint8_t* h_in, size_t len, size_t targe
 vsz_status vsz_compress_host_bound(const vsz_params* p, int ndim, const size_t dims[3], size_t* out_capacity) {
     size_t ws = 0, cap = 0;
     VSZ_TRY(vsz_compress_bounds(p, ndim, dims, &ws, &cap));
+    // a lossless frame of incompressible bytes is slightly longer than its input (zstd's bound is
+    // len + len / 256 + a few KB; zlib's and the device pass's are smaller)
+    if (p && p->lossless != VSZ_LOSSLESS_NONE) cap += cap / 128 + 4096;
     if (out_capacity) *out_capacity = cap;
     return VSZ_OK;
 }
@@ -282,7 +286,27 @@ vsz_status vsz_compress_host_into(const vsz_params* p, int ndim, const size_t di
     VSZ_CUDA(cudaStreamSynchronize(c->stream));
     if (r.status != VSZ_OK) return (vsz_status)r.status;
     size_t total = r.data_size + r.trailer_size;
-    if (p->lossless == VSZ_LOSSLESS_NONE) {
+    if (p->lossless == VSZ_LOSSLESS_GZIP_DEVICE) {
+        // the gzip pass on the device: only the zlib stream and the trailer come back
+        size_t dws = 0, fcap = 0;
+        VSZ_TRY(vsz_deflate_bounds(r.data_size, &dws, &fcap));
+        VSZ_TRY(c->dws.grow(dws));
+        VSZ_TRY(c->dframe.grow(fcap));
+        VSZ_TRY(vsz_deflate((const uint8_t*)c->archive.p, r.data_size, c->dws.p, c->dws.cap, (uint8_t*)c->dframe.p,
+                            c->dframe.cap, (uint64_t*)c->result.p, c->stream));
+        uint64_t dr[8];
+        VSZ_CUDA(cudaMemcpyAsync(dr, c->result.p, sizeof(dr), cudaMemcpyDeviceToHost, c->stream));
+        VSZ_CUDA(cudaStreamSynchronize(c->stream));
+        if (dr[1] != VSZ_OK) return (vsz_status)dr[1];
+        const size_t flen = dr[0];
+        if (flen + r.trailer_size > out_capacity) return VSZ_ERR_CAPACITY;
+        VSZ_CUDA(cudaMemcpyAsync(h_out, c->dframe.p, flen, cudaMemcpyDeviceToHost, c->stream));
+        VSZ_CUDA(cudaMemcpyAsync(h_out + flen, (const uint8_t*)c->archive.p + r.data_size, r.trailer_size,
+                                 cudaMemcpyDeviceToHost, c->stream));
+        VSZ_CUDA(cudaStreamSynchronize(c->stream));
+        if (out_bytes) *out_bytes = flen + r.trailer_size;
+        if (lossless_size) *lossless_size = flen;
+    } else if (p->lossless == VSZ_LOSSLESS_NONE) {
         if (total > out_capacity) return VSZ_ERR_CAPACITY;
         VSZ_CUDA(cudaMemcpyAsync(h_out, c->archive.p, total, cudaMemcpyDeviceToHost, c->stream));
         VSZ_CUDA(cudaStreamSynchronize(c->stream));
