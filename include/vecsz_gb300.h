@@ -339,6 +339,10 @@ vsz_status vsz_server_stats(vsz_server* server, uint64_t* completed, uint64_t* i
                             size_t* arena_bytes_in_use, int* queued);
 void vsz_server_destroy(vsz_server* server);
 
+/* The same parse from the block's first head_len bytes (the header, the pad values and the Huffman
+ * head) and the bytes from the block's end on (the trailer), for a block that lives on the device. */
+vsz_status vsz_archive_parse_split(const uint8_t* head, size_t head_len, const uint8_t* tail, size_t tail_len,
+                                   vsz_archive_desc* d);
 /* Parse a packed block (+ optional trailer) held in host memory. */
 vsz_status vsz_archive_parse(const uint8_t* h_archive, size_t len, vsz_archive_desc* desc);
 vsz_status vsz_decompress_bounds(const vsz_archive_desc* desc, const vsz_decompress_opts* opts, size_t* ws_bytes);
@@ -415,6 +419,20 @@ int vsz_lossless_detect(const uint8_t* h_in, size_t len);
 vsz_status vsz_deflate_bounds(size_t len, size_t* ws_bytes, size_t* out_capacity);
 vsz_status vsz_deflate(const uint8_t* d_in, size_t len, void* d_ws, size_t ws_bytes, uint8_t* d_out,
                        size_t out_capacity, uint64_t* d_result, void* stream);
+/* Compressed bytes of each 32 KiB chunk of the last vsz_deflate on this workspace (u32 per chunk,
+ * host or device dst, stream-ordered): the deflate index the host entry points append after the
+ * trailer of a VSZ_LOSSLESS_GZIP_DEVICE archive. */
+vsz_status vsz_deflate_chunk_sizes(const void* d_ws, size_t len, uint32_t* dst, void* stream);
+
+/* Inflate on the device for streams written by vsz_deflate (replaces zlib_uncompress,
+ * src/lossless.hh:144-177, for them): chunk c (its compressed bytes at d_chunk_offsets[c] in the
+ * stream, d_chunk_bytes[c] of them) inflates to d_out[32768 c ..], one thread per chunk; the
+ * Adler-32 of the output is checked against adler32.  *d_status (device int) = VSZ_ERR_CORRUPT for
+ * anything that is not such a stream; reads and writes stay inside the given buffers. */
+vsz_status vsz_inflate_bounds(size_t n_chunks, size_t* ws_bytes);
+vsz_status vsz_inflate(const uint8_t* d_stream, size_t stream_len, const unsigned long long* d_chunk_offsets,
+                       const uint32_t* d_chunk_bytes, size_t n_chunks, uint32_t adler32, uint8_t* d_out,
+                       size_t out_len, void* d_ws, size_t ws_bytes, int* d_status, void* stream);
 
 /* Per-stage device timing: when enabled, the whole-field entry points record a CUDA event pair
  * around each stage on the launching stream.  vsz_profile_read synchronises, returns the number of

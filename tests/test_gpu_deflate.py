@@ -34,7 +34,8 @@ def test_deflate_sizes_random_and_runs(cuda, n):
 def test_deflate_block_types(cuda):
     rng = np.random.default_rng(5)
     _, st = roundtrip(rng.integers(0, 256, 5 * 32768, dtype=np.uint8).tobytes())
-    assert st == {"chunks": 5, "stored": 5, "fixed": 0, "dynamic": 0}
+    assert (st["chunks"], st["stored"], st["fixed"], st["dynamic"]) == (5, 5, 0, 0)
+    assert list(st["chunk_bytes"]) == [32773] * 5  # stored: 5 header bytes + the chunk
     _, st = roundtrip(bytes(3 * 32768))
     assert st["chunks"] == 3 and st["stored"] == 0
     text = (b"the quick brown fox jumps over the lazy dog " * 2000)[:70000]
@@ -91,9 +92,93 @@ def test_host_compress_with_device_gzip(cuda, mode, eb):
     assert dev.lossless_size > 0 and dev.data[:2] == b"\x78\x01"
     assert dev.data_size == plain.data_size
     assert zlib.decompress(dev.data[: dev.lossless_size]) == plain.data[: plain.data_size]
-    assert dev.data[dev.lossless_size:] == plain.data[plain.data_size:]  # the same trailer
+    trailer = plain.data[plain.data_size:]
+    assert dev.data[dev.lossless_size:dev.lossless_size + len(trailer)] == trailer  # the same trailer
+    index = dev.data[dev.lossless_size + len(trailer):]
+    assert index[:4] == b"VSZD" and len(index) % 8 == 0
     np.testing.assert_array_equal(V.decompress(dev).view(np.uint32), V.decompress(plain).view(np.uint32))
     # the oracle reads the inflated block
     y = O.decompress(zlib.decompress(dev.data[: dev.lossless_size]), 8, 1024,
                      O.value_range(x) if mode == "r2r" else 0.0)
     np.testing.assert_array_equal(y.view(np.uint32), V.decompress(plain).view(np.uint32))
+
+
+def inflate_roundtrip(data):
+    out, st = api.deflate(data)
+    y, status = api.inflate(out, st["chunk_bytes"], len(data))
+    assert status == 0
+    assert y == bytes(data)
+    return out, st
+
+
+@pytest.mark.parametrize("n", [0, 1, 3, 4096, 32767, 32768, 32769, 100003, 1 << 20])
+def test_inflate_device_streams(cuda, n):
+    rng = np.random.default_rng(100 + n)
+    inflate_roundtrip(rng.integers(0, 256, n, dtype=np.uint8).tobytes())
+    inflate_roundtrip(bytes(n))
+    inflate_roundtrip(np.repeat(rng.choice([0, 1, 255, 7], size=n // 5 + 1, p=[0.7, 0.1, 0.1, 0.1]).astype(np.uint8),
+                                5)[:n].tobytes())
+    words = [bytes(rng.integers(97, 123, int(k), dtype=np.uint8)) for k in rng.integers(2, 9, 300)]
+    text = b" ".join(words[int(i)] for i in rng.integers(0, 300, n // 5 + 1))[:n]
+    inflate_roundtrip(text)
+
+
+def test_inflate_archives_and_fixed_blocks(cuda):
+    x = fields.bump_field_2d(600, 1200, seed=1).ravel()
+    a = V.compress(x, (1200, 600), eb=1e-4, mode="abs", dict_size=1024, block_size=8)
+    _, st = inflate_roundtrip(a.data[: a.data_size])
+    assert st["dynamic"] > 0
+    rng = np.random.default_rng(3)
+    # a skewed but wide literal alphabet with short runs, where fixed codes can win
+    inflate_roundtrip(np.clip(rng.normal(100, 30, 200000), 0, 255).astype(np.uint8).tobytes())
+
+
+def test_inflate_rejects_other_streams(cuda):
+    """Damaged streams and streams of other encoders: VSZ_ERR_CORRUPT, never a fault."""
+    x = fields.bump_field_2d(300, 700, seed=5).ravel()
+    block = V.compress(x, (700, 300), eb=1e-4, mode="abs", dict_size=1024, block_size=8).data
+    out, st = api.deflate(block)
+    sizes = st["chunk_bytes"]
+    rng = np.random.default_rng(7)
+    for k in range(12):
+        bad = bytearray(out)
+        pos = int(rng.integers(2, len(out) - 6))
+        bad[pos] ^= int(rng.integers(1, 256))
+        y, status = api.inflate(bytes(bad), sizes, len(block))
+        assert status in (0, 3)
+        if status == 0:  # a flip that still decodes is caught by the Adler-32, so only a no-op passes
+            assert y == block
+    bad = bytearray(out)
+    bad[-1] ^= 1  # Adler-32
+    assert api.inflate(bytes(bad), sizes, len(block))[1] == 3
+    z = zlib.compress(block, 6)  # zlib's stream: a final block inside the "chunk"
+    assert api.inflate(z, np.array([len(z) - 6], np.uint32), len(block) if len(block) <= 32768 else 32768)[1] == 3
+    wrong = sizes.copy()
+    wrong[0] += 1
+    assert api.inflate(out, wrong, len(block))[1] == 3
+    huge = sizes.copy()
+    huge[-1] = 1 << 30
+    assert api.inflate(out, huge, len(block))[1] == 3
+
+
+def test_host_decompress_inflates_on_device(cuda):
+    """With the deflate index the host entry point inflates on the device (two more launches than
+    the plain archive's decompress); without it, through the host library; the same floats."""
+    x = fields.bump_field_2d(400, 900, seed=6).ravel()
+    plain = V.compress(x, (900, 400), eb=1e-4, mode="abs", dict_size=1024, block_size=8)
+    dev = V.compress(x, (900, 400), eb=1e-4, mode="abs", dict_size=1024, block_size=8, lossless="gzip-device")
+    lib = V.lib()
+    want = V.decompress(plain)
+    l0 = lib.vsz_launch_count()
+    V.decompress(plain)
+    l1 = lib.vsz_launch_count()
+    got = V.decompress(dev)
+    l2 = lib.vsz_launch_count()
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert (l2 - l1) - (l1 - l0) == 2
+    trailer_len = len(plain.data) - plain.data_size
+    stripped = api.Compressed(dev.data[: dev.lossless_size + trailer_len], dev.data_size, dev.lossless_size,
+                              dev.n_outlier)
+    l3 = lib.vsz_launch_count()
+    np.testing.assert_array_equal(V.decompress(stripped).view(np.uint32), want.view(np.uint32))
+    assert lib.vsz_launch_count() - l3 == l1 - l0

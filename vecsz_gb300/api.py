@@ -156,7 +156,35 @@ def deflate(data, stream=None):
     if int(r[1]) != 0:
         raise VszError(int(r[1]), "deflate (device)")
     out = d_out[: int(r[0])].cpu().numpy().tobytes()
-    return out, {"chunks": int(r[2]), "stored": int(r[3]), "fixed": int(r[4]), "dynamic": int(r[5])}
+    sizes = np.zeros(int(r[2]), np.uint32)
+    if sizes.size:
+        check(lib().vsz_deflate_chunk_sizes(_ptr(d_ws), n, sizes.ctypes.data_as(C.c_void_p), _stream_ptr(stream)),
+              "deflate_chunk_sizes")
+        _torch().cuda.synchronize()
+    return out, {"chunks": int(r[2]), "stored": int(r[3]), "fixed": int(r[4]), "dynamic": int(r[5]),
+                 "chunk_bytes": sizes}
+
+
+def inflate(stream_bytes: bytes, chunk_bytes, out_len: int) -> tuple[bytes, int]:
+    """Inflate on the device (vsz_inflate) a stream vsz_deflate wrote, from its chunk sizes:
+    (bytes, status); status VSZ_ERR_CORRUPT for streams it does not take."""
+    torch = _torch()
+    sizes = np.ascontiguousarray(chunk_bytes, np.uint32)
+    offs = (2 + np.concatenate([[0], np.cumsum(sizes.astype(np.uint64))[:-1]])).astype(np.uint64) if sizes.size \
+        else np.zeros(0, np.uint64)
+    a = np.frombuffer(stream_bytes, np.uint8)
+    d_s = torch.from_numpy(np.concatenate([a, np.zeros(16, np.uint8)])).cuda()
+    d_off = torch.from_numpy(offs.view(np.int64).copy() if offs.size else np.zeros(1, np.int64)).cuda()
+    d_sz = torch.from_numpy(sizes.view(np.int32).copy() if sizes.size else np.zeros(1, np.int32)).cuda()
+    ws = C.c_size_t(0)
+    check(lib().vsz_inflate_bounds(sizes.size, C.byref(ws)), "inflate_bounds")
+    d_ws = torch.empty(ws.value, dtype=torch.uint8, device="cuda")
+    d_out = torch.zeros(max(1, out_len), dtype=torch.uint8, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    adler = int.from_bytes(stream_bytes[-4:], "big") if len(stream_bytes) >= 4 else 0
+    check(lib().vsz_inflate(_ptr(d_s), a.size, _ptr(d_off), _ptr(d_sz), sizes.size, adler, _ptr(d_out), out_len,
+                            _ptr(d_ws), ws.value, _ptr(st), _stream_ptr()), "inflate")
+    return d_out[:out_len].cpu().numpy().tobytes(), int(st.item())
 
 
 class DeviceCodec:

@@ -835,6 +835,17 @@ vsz_status vsz_deflate_bounds(size_t len, size_t* ws_bytes, size_t* out_capacity
     return VSZ_OK;
 }
 
+vsz_status vsz_deflate_chunk_sizes(const void* d_ws, size_t len, uint32_t* dst, void* stream) {
+    if (!d_ws || !dst) return VSZ_ERR_INVALID;
+    const size_t nchunks = (len + kChunk - 1) / kChunk;
+    DeflateWs w = deflate_ws(static_cast<uint8_t*>(const_cast<void*>(d_ws)), nchunks);
+    if (!nchunks) return VSZ_OK;
+    return cudaMemcpyAsync(dst, w.sizes, 4 * nchunks, cudaMemcpyDefault, static_cast<cudaStream_t>(stream)) ==
+                   cudaSuccess
+               ? VSZ_OK
+               : VSZ_ERR_CUDA;
+}
+
 vsz_status vsz_deflate(const uint8_t* d_in, size_t len, void* d_ws, size_t ws_bytes, uint8_t* d_out,
                        size_t out_capacity, uint64_t* d_result, void* stream) {
     if ((!d_in && len) || !d_ws || !d_out || !d_result) return VSZ_ERR_INVALID;

@@ -894,15 +894,33 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
 
 // ---- archive parsing (host) ---------------------------------------------------------------------
 
+// The archive as its first head_len bytes and the bytes from data_size on (tail, tail_len of them):
+// the header, the Huffman head and the trailer are all the parse reads.
+static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* tail, size_t tail_len, size_t len,
+                              vsz_archive_desc* d);
+
 vsz_status vsz_archive_parse(const uint8_t* h, size_t len, vsz_archive_desc* d) {
     if (!h || !d) return VSZ_ERR_INVALID;
+    return parse_split(h, len, nullptr, 0, len, d);
+}
+
+vsz_status vsz_archive_parse_split(const uint8_t* head, size_t head_len, const uint8_t* tail, size_t tail_len,
+                                   vsz_archive_desc* d) {
+    if (!head || !d || (!tail && tail_len)) return VSZ_ERR_INVALID;
+    return parse_split(head, head_len, tail, tail_len, 0, d);
+}
+
+// len == 0: split form (the archive is data_size + tail_len bytes long); else h holds all len bytes
+static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* tail, size_t tail_len, size_t len,
+                              vsz_archive_desc* d) {
     memset(d, 0, sizeof(*d));
-    if (len < 4) return VSZ_ERR_CORRUPT;
+    const bool split = len == 0;
+    if (head_len < 4) return VSZ_ERR_CORRUPT;
     int32_t nd;
     memcpy(&nd, h, 4);
     if (nd < 1 || nd > 3) return VSZ_ERR_CORRUPT;
     size_t hdr = hdr_bytes(nd);
-    if (len < hdr) return VSZ_ERR_CORRUPT;
+    if (head_len < hdr) return VSZ_ERR_CORRUPT;
     d->ndim = nd;
     d->dims[0] = d->dims[1] = d->dims[2] = 1;
     for (int i = 0; i < nd; i++) {
@@ -921,7 +939,8 @@ vsz_status vsz_archive_parse(const uint8_t* h, size_t len, vsz_archive_desc* d) 
     if (d->n_pad > (1ull << 40) || d->huff_bytes > (1ull << 44) || d->n_outlier > (1ull << 40)) return VSZ_ERR_CORRUPT;
     d->huff_offset = hdr + 4 * d->n_pad;
     d->data_size = d->huff_offset + d->huff_bytes + 4 * d->n_outlier;
-    if (d->data_size > len || d->huff_bytes < 8) return VSZ_ERR_CORRUPT;
+    if (split) len = d->data_size + tail_len;
+    if (d->data_size > len || d->huff_bytes < 8 || d->huff_offset + 8 > head_len) return VSZ_ERR_CORRUPT;
     const uint8_t* hh = h + d->huff_offset;
     uint32_t nc = ((uint32_t)hh[0] << 24) | ((uint32_t)hh[1] << 16) | ((uint32_t)hh[2] << 8) | hh[3];
     if (nc == 0) return VSZ_ERR_CORRUPT;
@@ -933,7 +952,7 @@ vsz_status vsz_archive_parse(const uint8_t* h, size_t len, vsz_archive_desc* d) 
     d->outlier_offset = d->huff_offset + d->huff_bytes;
     // this library's trailer
     if (len >= d->data_size + kTrailerFixed) {
-        const uint8_t* t = h + d->data_size;
+        const uint8_t* t = split ? tail : h + d->data_size;
         uint32_t u32[4];
         memcpy(u32, t, 16);
         if (u32[0] == kTrailerMagic && u32[1] == kTrailerVersion && u32[2] == kTrailerFixed) {

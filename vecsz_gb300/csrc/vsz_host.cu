@@ -3,6 +3,7 @@
 // (src/lossless.hh) through the system zstd / zlib libraries loaded at run time.
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -120,6 +121,64 @@ Zlib* zlib() {
         }
     }
     return g_zlib.ok ? &g_zlib : nullptr;
+}
+
+// ---- deflate index --------------------------------------------------------------------------
+// Written after the trailer when the gzip pass ran on the device, so the decompressor can inflate
+// the chunks independently on the device: [u32 magic "VSZD"][u32 version][u32 chunk bytes]
+// [u32 head bytes][u64 chunks][u64 inflated bytes][u64 values][u32 compressed bytes per chunk],
+// padded to 8.  Readers that do not know it ignore it (the reference reads lossless_size bytes).
+constexpr uint32_t kDeflateIndexMagic   = 0x445A5356u;
+constexpr uint32_t kDeflateIndexVersion = 1;
+constexpr uint32_t kDeflateIndexHead    = 40;
+constexpr uint32_t kDeflateChunk        = 32768;
+
+size_t deflate_index_bytes(size_t nchunks) { return (kDeflateIndexHead + 4 * nchunks + 7) & ~(size_t)7; }
+
+struct DeflateIndex {
+    size_t nchunks = 0, raw = 0, values = 0;
+    std::vector<uint32_t> sizes;
+    std::vector<unsigned long long> offsets;  // of each chunk in the stream
+    uint32_t adler = 0;
+};
+
+// The index of an archive [frame (lossless_size)][trailer][index], checked against the frame.
+bool read_deflate_index(const uint8_t* h, size_t len, size_t lossless_size, DeflateIndex* ix) {
+    if (lossless_size < 8 || len < lossless_size + 64 || h[0] != 0x78 || h[1] != 0x01) return false;
+    const uint8_t* t = h + lossless_size;
+    uint32_t tu[3];
+    memcpy(tu, t, 12);
+    if (tu[0] != 0x545A5356u || tu[1] != 1 || tu[2] != 64) return false;  // this library's trailer
+    uint64_t tsz;
+    memcpy(&tsz, t + 56, 8);
+    if (tsz > len - lossless_size || len - lossless_size - tsz < kDeflateIndexHead) return false;
+    const uint8_t* di = t + tsz;
+    uint32_t u32[4];
+    uint64_t u64[3];
+    memcpy(u32, di, 16);
+    memcpy(u64, di + 16, 24);
+    if (u32[0] != kDeflateIndexMagic || u32[1] != kDeflateIndexVersion || u32[2] != kDeflateChunk ||
+        u32[3] != kDeflateIndexHead)
+        return false;
+    const size_t nch = u64[0], raw = u64[1];
+    if (nch != (raw + kDeflateChunk - 1) / kDeflateChunk || nch > (len >> 2)) return false;
+    if (deflate_index_bytes(nch) > len - lossless_size - tsz) return false;
+    ix->nchunks = nch;
+    ix->raw     = raw;
+    ix->values  = u64[2];
+    ix->sizes.resize(nch);
+    ix->offsets.resize(nch);
+    if (nch) memcpy(ix->sizes.data(), di + kDeflateIndexHead, 4 * nch);
+    unsigned long long off = 2;
+    for (size_t c = 0; c < nch; c++) {
+        if (ix->sizes[c] == 0 || ix->sizes[c] > kDeflateChunk + 5) return false;
+        ix->offsets[c] = off;
+        off += ix->sizes[c];
+    }
+    if (off + 6 != lossless_size) return false;  // final empty block (2 bytes) and Adler-32
+    const uint8_t* a = h + lossless_size - 4;
+    ix->adler = ((uint32_t)a[0] << 24) | ((uint32_t)a[1] << 16) | ((uint32_t)a[2] << 8) | a[3];
+    return true;
 }
 
 // zlib header check of isZlibFormat (src/lossless.hh:40-57)
@@ -298,13 +357,22 @@ vsz_status vsz_compress_host_into(const vsz_params* p, int ndim, const size_t di
         VSZ_CUDA(cudaMemcpyAsync(dr, c->result.p, sizeof(dr), cudaMemcpyDeviceToHost, c->stream));
         VSZ_CUDA(cudaStreamSynchronize(c->stream));
         if (dr[1] != VSZ_OK) return (vsz_status)dr[1];
-        const size_t flen = dr[0];
-        if (flen + r.trailer_size > out_capacity) return VSZ_ERR_CAPACITY;
+        const size_t flen = dr[0], nch = dr[2];
+        const size_t ib   = deflate_index_bytes(nch);
+        if (flen + r.trailer_size + ib > out_capacity) return VSZ_ERR_CAPACITY;
         VSZ_CUDA(cudaMemcpyAsync(h_out, c->dframe.p, flen, cudaMemcpyDeviceToHost, c->stream));
         VSZ_CUDA(cudaMemcpyAsync(h_out + flen, (const uint8_t*)c->archive.p + r.data_size, r.trailer_size,
                                  cudaMemcpyDeviceToHost, c->stream));
+        uint8_t* di = h_out + flen + r.trailer_size;
+        memset(di, 0, ib);
+        const uint32_t head[4] = {kDeflateIndexMagic, kDeflateIndexVersion, kDeflateChunk, kDeflateIndexHead};
+        const uint64_t counts[3] = {nch, r.data_size, n};
+        memcpy(di, head, 16);
+        memcpy(di + 16, counts, 24);
+        VSZ_TRY(vsz_deflate_chunk_sizes(c->dws.p, r.data_size, reinterpret_cast<uint32_t*>(di + kDeflateIndexHead),
+                                        c->stream));
         VSZ_CUDA(cudaStreamSynchronize(c->stream));
-        if (out_bytes) *out_bytes = flen + r.trailer_size;
+        if (out_bytes) *out_bytes = flen + r.trailer_size + ib;
         if (lossless_size) *lossless_size = flen;
     } else if (p->lossless == VSZ_LOSSLESS_NONE) {
         if (total > out_capacity) return VSZ_ERR_CAPACITY;
@@ -353,9 +421,103 @@ vsz_status vsz_compress_host(const vsz_params* p, int ndim, const size_t dims[3]
     return VSZ_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The archive is on the device (c->archive, `used` bytes and 64 zero bytes after them): decode it
+// into h_out.  The caller holds c->mu.
+int decode_resident(HostCtx* c, const vsz_archive_desc& d, const vsz_decompress_opts* opts, float* h_out,
+                    size_t out_capacity, size_t* n_out) {
+    const size_t n = d.dims[0] * d.dims[1] * d.dims[2];
+    if (n > out_capacity) return VSZ_ERR_CAPACITY;
+    size_t ws = 0;
+    VSZ_TRY(vsz_decompress_bounds(&d, opts, &ws));
+    VSZ_TRY(c->ws.grow(ws));
+    VSZ_TRY(c->out.grow(n * sizeof(float)));
+    VSZ_TRY(c->result.grow(64));
+    VSZ_TRY(vsz_decompress(&d, opts, (const uint8_t*)c->archive.p, c->ws.p, c->ws.cap, (float*)c->out.p,
+                           (int*)c->result.p, c->stream));
+    int st = 0;
+    VSZ_CUDA(cudaMemcpyAsync(&st, c->result.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaMemcpyAsync(h_out, c->out.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaStreamSynchronize(c->stream));
+    if (st != VSZ_OK) return st;
+    if (n_out) *n_out = n;
+    return VSZ_OK;
+}
+
+// -L archives whose frame came from the device gzip pass: inflate on the device from the deflate
+// index.  Returns 1 when the archive has no usable index or the stream does not inflate (the
+// caller then takes the host library path), else a status.
+int decompress_device_inflate(const uint8_t* h, size_t len, size_t data_size, size_t lossless_size,
+                              const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, size_t* n_out) {
+    DeflateIndex ix;
+    if (!read_deflate_index(h, len, lossless_size, &ix)) return 1;
+    if (data_size && ix.raw != data_size) return VSZ_ERR_CORRUPT;
+    const uint8_t* trailer = h + lossless_size;
+    uint64_t tsz;
+    memcpy(&tsz, trailer + 56, 8);
+    HostCtx* c = ctx_for_device();
+    if (!c) return VSZ_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lk(c->mu);
+    VSZ_TRY(ensure_stream(c));
+    size_t iws = 0;
+    VSZ_TRY(vsz_inflate_bounds(ix.nchunks, &iws));
+    const size_t tab = (12 * ix.nchunks + 255) & ~(size_t)255;
+    VSZ_TRY(c->dframe.grow(lossless_size + 64));
+    VSZ_TRY(c->dws.grow(tab + iws));
+    VSZ_TRY(c->archive.grow(ix.raw + tsz + 64));
+    VSZ_TRY(c->result.grow(64));
+    uint8_t* dws = (uint8_t*)c->dws.p;
+    VSZ_CUDA(cudaMemcpyAsync(c->dframe.p, h, lossless_size, cudaMemcpyHostToDevice, c->stream));
+    VSZ_CUDA(cudaMemcpyAsync(dws, ix.offsets.data(), 8 * ix.nchunks, cudaMemcpyHostToDevice, c->stream));
+    VSZ_CUDA(cudaMemcpyAsync(dws + 8 * ix.nchunks, ix.sizes.data(), 4 * ix.nchunks, cudaMemcpyHostToDevice,
+                             c->stream));
+    VSZ_TRY(vsz_inflate((const uint8_t*)c->dframe.p, lossless_size, (const unsigned long long*)dws,
+                        (const uint32_t*)(dws + 8 * ix.nchunks), ix.nchunks, ix.adler, (uint8_t*)c->archive.p, ix.raw,
+                        dws + tab, iws, (int*)c->result.p, c->stream));
+    VSZ_CUDA(cudaMemcpyAsync((uint8_t*)c->archive.p + ix.raw, trailer, tsz, cudaMemcpyHostToDevice, c->stream));
+    VSZ_CUDA(cudaMemsetAsync((uint8_t*)c->archive.p + ix.raw + tsz, 0, 64, c->stream));
+    // the header and the Huffman head come back for the parse
+    int st = 0;
+    std::vector<uint8_t> head(std::min<size_t>(ix.raw, 64));
+    VSZ_CUDA(cudaMemcpyAsync(&st, c->result.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaMemcpyAsync(head.data(), c->archive.p, head.size(), cudaMemcpyDeviceToHost, c->stream));
+    VSZ_CUDA(cudaStreamSynchronize(c->stream));
+    if (st != VSZ_OK) return 1;  // not a stream this inflater takes: the host library decides
+    if (head.size() >= 4) {
+        int32_t nd;
+        memcpy(&nd, head.data(), 4);
+        if (nd >= 1 && nd <= 3) {
+            uint64_t npad;
+            memcpy(&npad, head.data() + 4 * (nd + 1) + 8, 8);
+            const size_t need = 4 * (size_t)(nd + 1) + 32 + 4 * (size_t)std::min<uint64_t>(npad, 1ull << 40) + 8;
+            if (need > head.size() && need <= ix.raw) {
+                head.resize(need);
+                VSZ_CUDA(cudaMemcpyAsync(head.data(), c->archive.p, need, cudaMemcpyDeviceToHost, c->stream));
+                VSZ_CUDA(cudaStreamSynchronize(c->stream));
+            }
+        }
+    }
+    vsz_archive_desc d;
+    VSZ_TRY(vsz_archive_parse_split(head.data(), head.size(), trailer, len - lossless_size, &d));
+    if (d.data_size != ix.raw) return VSZ_ERR_CORRUPT;
+    return decode_resident(c, d, opts, h_out, out_capacity, n_out);
+}
+
+}  // namespace
+
+extern "C" {
+
 vsz_status vsz_decompress_host_into(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
                                     const vsz_decompress_opts* opts, float* h_out, size_t out_capacity, size_t* n_out) {
     if (!h_archive || !h_out) return VSZ_ERR_INVALID;
+    if (lossless_size > 0 && lossless_size <= len) {
+        const int rc = decompress_device_inflate(h_archive, len, data_size, lossless_size, opts, h_out, out_capacity,
+                                                 n_out);
+        if (rc != 1) return rc;
+    }
     // 1. undo the lossless pass; the trailer (if any) follows the frame
     std::vector<uint8_t> packed;
     const uint8_t* block = h_archive;
@@ -381,28 +543,15 @@ vsz_status vsz_decompress_host_into(const uint8_t* h_archive, size_t len, size_t
     if (data_size && d.data_size != data_size) return VSZ_ERR_CORRUPT;
     size_t n = d.dims[0] * d.dims[1] * d.dims[2];
     if (n > out_capacity) return VSZ_ERR_CAPACITY;
-    size_t ws = 0;
-    VSZ_TRY(vsz_decompress_bounds(&d, opts, &ws));
     HostCtx* c = ctx_for_device();
     if (!c) return VSZ_ERR_NO_DEVICE;
     std::lock_guard<std::mutex> lk(c->mu);
     VSZ_TRY(ensure_stream(c));
     size_t used = d.has_trailer ? (size_t)(d.index_offset + 2 * d.n_chunks) : (size_t)d.data_size;
     VSZ_TRY(c->archive.grow(used + 64));
-    VSZ_TRY(c->ws.grow(ws));
-    VSZ_TRY(c->out.grow(n * sizeof(float)));
-    VSZ_TRY(c->result.grow(64));
     VSZ_CUDA(cudaMemcpyAsync(c->archive.p, block, used, cudaMemcpyHostToDevice, c->stream));
     VSZ_CUDA(cudaMemsetAsync((uint8_t*)c->archive.p + used, 0, 64, c->stream));
-    VSZ_TRY(vsz_decompress(&d, opts, (const uint8_t*)c->archive.p, c->ws.p, c->ws.cap, (float*)c->out.p,
-                           (int*)c->result.p, c->stream));
-    int st = 0;
-    VSZ_CUDA(cudaMemcpyAsync(&st, c->result.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    VSZ_CUDA(cudaMemcpyAsync(h_out, c->out.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    VSZ_CUDA(cudaStreamSynchronize(c->stream));
-    if (st != VSZ_OK) return st;
-    if (n_out) *n_out = n;
-    return VSZ_OK;
+    return decode_resident(c, d, opts, h_out, out_capacity, n_out);
 }
 
 vsz_status vsz_decompress_host(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
@@ -410,10 +559,13 @@ vsz_status vsz_decompress_host(const uint8_t* h_archive, size_t len, size_t data
     if (!h_out) return VSZ_ERR_INVALID;
     // size the output from the header (after the lossless pass if any)
     size_t cap = 0;
+    DeflateIndex ix;
     if (lossless_size == 0) {
         vsz_archive_desc d;
         VSZ_TRY(vsz_archive_parse(h_archive, len, &d));
         cap = d.dims[0] * d.dims[1] * d.dims[2];
+    } else if (lossless_size <= len && read_deflate_index(h_archive, len, lossless_size, &ix) && ix.values) {
+        cap = ix.values;  // the device gzip pass recorded it
     } else {
         uint8_t* raw = nullptr;
         size_t rl    = 0;
