@@ -1,11 +1,14 @@
 // Inflate on the device for the zlib streams vsz_deflate writes: the decompress side of the -L gzip
 // pass (replaces zlib_uncompress, src/lossless.hh:144-177, for those streams).  vsz_deflate's
 // chunks are independent (no match reaches before its chunk, every chunk starts on a byte), so
-// with the chunk sizes from the archive's deflate index each chunk inflates on its own: one thread
-// per chunk, a 9-bit primary table per Huffman code in shared memory and a canonical walk for
-// longer codewords.  Every read is bounded by the chunk's bytes, every write by its output size;
-// anything else (another encoder's stream, a damaged one) sets VSZ_ERR_CORRUPT and the host falls
-// back to the host library.  The Adler-32 of the output is checked against the stream's.
+// with the chunk sizes from the archive's deflate index each chunk inflates on its own: one warp
+// per chunk, the chunk's compressed bytes and its 32 KiB of output in shared memory.  All lanes
+// run the same decode (broadcast reads, no divergence), lane 0 builds the code tables (a 9-bit
+// primary table and a canonical walk for longer codewords) and writes literals, the warp copies
+// matches and stored blocks together.  Every read is bounded by the chunk's bytes, every write by
+// its output size; anything else (another encoder's stream, a damaged one) sets VSZ_ERR_CORRUPT and
+// the host falls back to the host library.  The Adler-32 of the output is checked against the
+// stream's.
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -19,12 +22,12 @@ void count_launch();  // vsz_profile.cu
 namespace {
 
 constexpr int kChunk         = 32768;  // output bytes per chunk, as vsz_deflate writes them
-constexpr int kThreads       = 32;     // chunks per CTA
+constexpr int kInBytes       = kChunk + 5 + 64;  // a chunk's compressed bytes (stored: kChunk + 5), skew, padding
 constexpr int kLitBits       = 9;      // primary table of the literal/length code
 constexpr int kDistBits      = 6;      // primary table of the distance code
 constexpr uint32_t kAdlerMod = 65521;
 
-// per-thread decoding state in shared memory
+// code tables of a warp's chunk, in shared memory
 struct LaneTables {
     uint16_t lit[1 << kLitBits];    // symbol | len << 9; 0: codeword longer than kLitBits
     uint16_t dist[1 << kDistBits];  // symbol | len << 9
@@ -41,37 +44,45 @@ __constant__ uint16_t kDistBase[30] = {1,   2,   3,   4,   5,   7,    9,    13, 
 __constant__ uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
 __constant__ uint8_t kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
-// LSB-first bit reader over [p, p + n) bytes; bytes past the end read as zero and are counted
+// LSB-first bit reader over the chunk's bytes in shared memory (little-endian words, the chunk
+// starting `base` bits into them), with a 64-bit window in registers refilled a word at a time;
+// positions past the chunk read zero padding and are caught by the caller's position checks
 struct Bits {
-    const uint8_t* p;
-    size_t n, next;  // next byte to load
+    const uint32_t* w;
+    uint32_t base;  // bit offset of the chunk's first byte
+    uint32_t pos;   // bits consumed
+    uint32_t nw;    // next word to enter the window
+    uint32_t cnt;   // valid bits in the window
     uint64_t buf;
-    uint32_t cnt;    // valid bits in buf
-    size_t consumed;  // bits consumed
-    __device__ void fill() {
-        while (cnt <= 56) {
-            const uint64_t b = next < n ? p[next] : 0;
-            next++;
-            buf |= b << cnt;
-            cnt += 8;
+    __device__ __forceinline__ void seek(uint32_t p) {
+        pos = p;
+        const uint32_t b = base + p;
+        buf = w[b >> 5] >> (b & 31);
+        cnt = 32 - (b & 31);
+        nw  = (b >> 5) + 1;
+    }
+    __device__ __forceinline__ uint32_t peek() {  // at least 32 valid bits
+        if (cnt < 32) {
+            buf |= (uint64_t)w[nw++] << cnt;
+            cnt += 32;
         }
+        return (uint32_t)buf;
     }
-    __device__ uint32_t peek(uint32_t k) {
-        if (cnt < k) fill();
-        return (uint32_t)(buf & ((1ull << k) - 1));
-    }
-    __device__ void drop(uint32_t k) {
+    __device__ __forceinline__ void drop(uint32_t k) {
         buf >>= k;
         cnt -= k;
-        consumed += k;
+        pos += k;
     }
-    __device__ uint32_t get(uint32_t k) {
+    __device__ __forceinline__ uint32_t get(uint32_t k) {
         if (k == 0) return 0;
-        const uint32_t v = peek(k);
+        const uint32_t v = peek() & ((1u << k) - 1);
         drop(k);
         return v;
     }
-    __device__ void align_byte() { drop((8 - (uint32_t)(consumed & 7)) & 7); }
+    __device__ __forceinline__ void align_byte() {
+        peek();
+        drop((8 - (pos & 7)) & 7);
+    }
 };
 
 __device__ __forceinline__ uint32_t reverse_bits(uint32_t code, uint32_t len) { return __brev(code) >> (32 - len); }
@@ -114,7 +125,7 @@ __device__ bool build_table(const uint8_t* len, int n, int pbits, uint16_t* prim
 // One codeword: primary table, else the canonical walk over up to 15 bits.  -1 on a bad code.
 __device__ __forceinline__ int decode_sym(Bits& br, const uint16_t* primary, int pbits, const uint16_t* count,
                                           const uint16_t* sym) {
-    const uint32_t bits = br.peek(15);
+    const uint32_t bits = br.peek();
     const uint16_t e    = primary[bits & ((1u << pbits) - 1)];
     if (e) {
         br.drop(e >> 9);
@@ -135,75 +146,96 @@ __device__ __forceinline__ int decode_sym(Bits& br, const uint16_t* primary, int
     return -1;
 }
 
-__global__ void __launch_bounds__(kThreads)
+// dynamic shared memory of a CTA (one warp, one chunk)
+struct InflateSmem {
+    uint8_t out[kChunk];
+    uint32_t in[kInBytes / 4 + 2];
+    LaneTables t;
+    int bad;
+};
+
+__global__ void __launch_bounds__(32)
     k_inflate_chunks(const uint8_t* __restrict__ stream, size_t stream_len, const unsigned long long* __restrict__ chunk_off,
                      const uint32_t* __restrict__ chunk_bytes, size_t nchunks, uint8_t* __restrict__ out,
                      size_t out_len, uint32_t* __restrict__ adler, int* __restrict__ status) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    LaneTables& t = reinterpret_cast<LaneTables*>(smem)[threadIdx.x];
-    const size_t c = blockIdx.x * (size_t)kThreads + threadIdx.x;
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    InflateSmem& m    = *reinterpret_cast<InflateSmem*>(smem_raw);
+    LaneTables& t     = m.t;
+    const uint32_t lane = threadIdx.x;
+    const size_t c    = blockIdx.x;
     if (c >= nchunks) return;
-    const size_t o0   = c * kChunk;
+    const size_t o0     = c * (size_t)kChunk;
     const uint32_t want = (uint32_t)min((size_t)kChunk, out_len - o0);
-    uint8_t* dst       = out + o0;
     const unsigned long long off = chunk_off[c];
     const uint32_t cb            = chunk_bytes[c];
-    if (off > stream_len || cb > stream_len - off) {  // an index that does not fit the stream
-        atomicExch(status, VSZ_ERR_CORRUPT);
-        adler[2 * c] = adler[2 * c + 1] = 0;
+    if (off > stream_len || cb > stream_len - off || cb > (uint32_t)(kChunk + 5)) {  // an index that does not fit
+        if (lane == 0) {
+            atomicExch(status, VSZ_ERR_CORRUPT);
+            adler[2 * c] = adler[2 * c + 1] = 0;
+        }
         return;
     }
-    Bits br{stream + off, cb, 0, 0, 0, 0};
-    const size_t end_bits = 8 * (size_t)cb;
+    // the compressed bytes into shared memory, `skew` bytes in so 16-byte loads stay aligned
+    const uint8_t* src  = stream + off;
+    const uint32_t skew = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
+    uint8_t* inb        = reinterpret_cast<uint8_t*>(m.in);
+    {
+        const uint32_t span = (skew + cb + 15) & ~15u;  // whole 16-byte blocks covering the chunk
+        const uint4* g16    = reinterpret_cast<const uint4*>(src - skew);
+        for (uint32_t k = lane; k < span / 16; k += 32) {
+            const uint32_t lo = 16 * k, hi = lo + 16;
+            if (lo >= skew && hi <= skew + cb) {
+                reinterpret_cast<uint4*>(inb)[k] = g16[k];
+            } else {
+                for (uint32_t q = lo; q < hi; q++) inb[q] = (q >= skew && q < skew + cb) ? src[q - skew] : 0;
+            }
+        }
+        for (uint32_t q = span + lane; q < (uint32_t)sizeof(m.in); q += 32) inb[q] = 0;
+        if (lane == 0) m.bad = 0;
+    }
+    __syncwarp();
+    Bits br{m.in, 8 * skew, 0, 0, 0, 0};
+    br.seek(0);
+    const uint32_t end_bits = 8 * cb;
     uint32_t have = 0;
     bool bad      = false;
-    uint64_t S = 0, T = 0;  // Adler-32 parts of this chunk (reduced at the end)
-    auto emit = [&](uint8_t b) {
-        dst[have++] = b;
-        S += b;
-        T += S;
-    };
     // blocks until the chunk's bytes are used up; a dynamic or fixed block is followed by an
     // empty stored block, a stored block of data ends on a byte itself
-    for (int guard = 0; !bad && br.consumed < end_bits; guard++) {
+    for (int guard = 0; !bad && br.pos < end_bits; guard++) {
         if (guard > 64) {
             bad = true;
             break;
         }
         const uint32_t final = br.get(1);
         const uint32_t type  = br.get(2);
-        if (final) {  // chunks never hold the final block
+        if (final || type == 3) {  // chunks never hold the final block
             bad = true;
             break;
         }
         if (type == 0) {
             br.align_byte();
             const uint32_t len = br.get(16), nlen = br.get(16);
-            if ((len ^ 0xFFFFu) != nlen || len > want - have || br.consumed + 8ull * len > end_bits) {
+            if ((len ^ 0xFFFFu) != nlen || len > want - have || br.pos + 8 * len > end_bits) {
                 bad = true;
                 break;
             }
-            // the block's bytes straight from the stream; the reader restarts after them
-            const size_t bp = br.consumed / 8;
-            for (uint32_t k = 0; k < len; k++) emit(br.p[bp + k]);
-            br.next = bp + len;
-            br.buf  = 0;
-            br.cnt  = 0;
-            br.consumed += 8ull * len;
+            const uint32_t bp = skew + br.pos / 8;
+            for (uint32_t k = lane; k < len; k += 32) m.out[have + k] = inb[bp + k];
+            __syncwarp();
+            have += len;
+            br.seek(br.pos + 8 * len);
             continue;
         }
-        if (type == 3) {
-            bad = true;
-            break;
-        }
+        bool ok = true;
         if (type == 1) {  // fixed codes (RFC 1951 3.2.6)
-            for (int i = 0; i < 288; i++) t.lens[i] = i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8;
-            for (int i = 0; i < 30; i++) t.lens[288 + i] = 5;
-            if (!build_table(t.lens, 288, kLitBits, t.lit, t.lcount, t.lsym, false) ||
-                !build_table(t.lens + 288, 30, kDistBits, t.dist, t.dcount, t.dsym, true)) {
-                bad = true;
-                break;
+            if (lane == 0) {
+                for (int i = 0; i < 288; i++) t.lens[i] = i < 144 ? 8 : i < 256 ? 9 : i < 280 ? 7 : 8;
+                for (int i = 0; i < 30; i++) t.lens[288 + i] = 5;
+                m.bad = !build_table(t.lens, 288, kLitBits, t.lit, t.lcount, t.lsym, false) ||
+                        !build_table(t.lens + 288, 30, kDistBits, t.dist, t.dcount, t.dsym, true);
             }
+            __syncwarp();
+            ok = !m.bad;
         } else {  // dynamic codes (RFC 1951 3.2.7)
             const int nlit = (int)br.get(5) + 257, ndist = (int)br.get(5) + 1, ncl = (int)br.get(4) + 4;
             if (nlit > 286 || ndist > 30) {
@@ -214,58 +246,67 @@ __global__ void __launch_bounds__(kThreads)
             for (int i = 0; i < 19; i++) cl[i] = 0;
             for (int i = 0; i < ncl; i++) cl[kClOrder[i]] = (uint8_t)br.get(3);
             // the code-length code goes through the literal tables' space
-            if (!build_table(cl, 19, 7, t.lit, t.lcount, t.lsym, false)) {
+            if (lane == 0) m.bad = !build_table(cl, 19, 7, t.lit, t.lcount, t.lsym, false);
+            __syncwarp();
+            if (m.bad) {
                 bad = true;
                 break;
             }
+            // every lane decodes the lengths (the reader positions stay equal); lane 0 stores them
             int k = 0;
+            uint8_t prev = 0;
             while (k < nlit + ndist) {
                 const int sy = decode_sym(br, t.lit, 7, t.lcount, t.lsym);
-                if (sy < 0 || br.consumed > end_bits) {
+                if (sy < 0 || br.pos > end_bits) {
                     bad = true;
                     break;
                 }
-                if (sy < 16) {
-                    t.lens[k++] = (uint8_t)sy;
-                    continue;
-                }
                 int rep;
-                uint8_t v = 0;
-                if (sy == 16) {
+                uint8_t v;
+                if (sy < 16) {
+                    rep = 1;
+                    v   = (uint8_t)sy;
+                } else if (sy == 16) {
                     if (k == 0) {
                         bad = true;
                         break;
                     }
-                    v   = t.lens[k - 1];
+                    v   = prev;
                     rep = 3 + (int)br.get(2);
-                } else if (sy == 17) {
-                    rep = 3 + (int)br.get(3);
                 } else {
-                    rep = 11 + (int)br.get(7);
+                    v   = 0;
+                    rep = sy == 17 ? 3 + (int)br.get(3) : 11 + (int)br.get(7);
                 }
                 if (k + rep > nlit + ndist) {
                     bad = true;
                     break;
                 }
-                for (int r = 0; r < rep; r++) t.lens[k++] = v;
+                if (lane == 0)
+                    for (int r = 0; r < rep; r++) {
+                        const int at = k + r;  // literal/length lengths at [0, nlit), distance ones at 288 +
+                        t.lens[at < nlit ? at : 288 + (at - nlit)] = v;
+                    }
+                k += rep;
+                prev = v;
             }
             if (bad) break;
-            // the lengths sit at lens[0..nlit) and lens[nlit..nlit+ndist); move the distance
-            // lengths to lens[288..) and clear the rest
-            uint8_t dl[30];
-            for (int i = 0; i < 30; i++) dl[i] = i < ndist ? t.lens[nlit + i] : 0;
-            for (int i = nlit; i < 288; i++) t.lens[i] = 0;
-            for (int i = 0; i < 30; i++) t.lens[288 + i] = dl[i];
-            if (t.lens[256] == 0 || !build_table(t.lens, 288, kLitBits, t.lit, t.lcount, t.lsym, false) ||
-                !build_table(t.lens + 288, 30, kDistBits, t.dist, t.dcount, t.dsym, true)) {
-                bad = true;
-                break;
+            if (lane == 0) {
+                for (int i = nlit; i < 288; i++) t.lens[i] = 0;
+                for (int i = ndist; i < 32; i++) t.lens[288 + i] = 0;
+                m.bad = t.lens[256] == 0 || !build_table(t.lens, 288, kLitBits, t.lit, t.lcount, t.lsym, false) ||
+                        !build_table(t.lens + 288, 30, kDistBits, t.dist, t.dcount, t.dsym, true);
             }
+            __syncwarp();
+            ok = !m.bad;
+        }
+        if (!ok) {
+            bad = true;
+            break;
         }
         // symbols up to the end of the block
         while (true) {
             const int sy = decode_sym(br, t.lit, kLitBits, t.lcount, t.lsym);
-            if (sy < 0 || br.consumed > end_bits) {
+            if (sy < 0 || br.pos > end_bits) {
                 bad = true;
                 break;
             }
@@ -274,7 +315,8 @@ __global__ void __launch_bounds__(kThreads)
                     bad = true;
                     break;
                 }
-                emit((uint8_t)sy);
+                if (lane == 0) m.out[have] = (uint8_t)sy;
+                have++;
                 continue;
             }
             if (sy == 256) break;
@@ -293,14 +335,53 @@ __global__ void __launch_bounds__(kThreads)
                 bad = true;
                 break;
             }
-            for (uint32_t k = 0; k < len; k++) emit(dst[have - dist]);
+            __syncwarp();  // the literals lane 0 wrote are read below
+            for (uint32_t k = lane; k < len; k += 32)
+                m.out[have + k] = m.out[have - dist + (k < dist ? k : k % dist)];
+            __syncwarp();
+            have += len;
+        }
+        __syncwarp();
+    }
+    if (br.pos != end_bits) bad = true;
+    if (have != want) bad = true;
+    __syncwarp();
+    // Adler-32 parts of the chunk: lane l sums bytes [1024 l, 1024 l + 1024), then an ordered scan
+    uint64_t S = 0, T = 0, N = 0;
+    if (!bad) {
+        const uint32_t b0 = lane * 1024, b1 = min(want, b0 + 1024);
+        for (uint32_t i = b0; i < b1; i++) {
+            S += m.out[i];
+            T += S;
+        }
+        N = b1 > b0 ? b1 - b0 : 0;
+        S %= kAdlerMod;
+        T %= kAdlerMod;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t S_l = __shfl_up_sync(0xFFFFFFFFu, S, o);
+            const uint64_t T_l = __shfl_up_sync(0xFFFFFFFFu, T, o);
+            const uint64_t N_l = __shfl_up_sync(0xFFFFFFFFu, N, o);
+            if (lane >= (uint32_t)o) {
+                T = (T_l + T + (N % kAdlerMod) * S_l) % kAdlerMod;
+                S = (S_l + S) % kAdlerMod;
+                N = N_l + N;
+            }
+        }
+        // the chunk's output to global memory
+        uint8_t* dst = out + o0;
+        if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+            for (uint32_t k = lane; k < want / 16; k += 32)
+                reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(m.out)[k];
+            for (uint32_t k = (want & ~15u) + lane; k < want; k += 32) dst[k] = m.out[k];
+        } else {
+            for (uint32_t k = lane; k < want; k += 32) dst[k] = m.out[k];
         }
     }
-    if (br.consumed != end_bits && !bad) bad = true;
-    if (have != want) bad = true;
-    if (bad) atomicExch(status, VSZ_ERR_CORRUPT);
-    adler[2 * c]     = (uint32_t)(S % kAdlerMod);
-    adler[2 * c + 1] = (uint32_t)(T % kAdlerMod);
+    if (lane == 31) {
+        if (bad) atomicExch(status, VSZ_ERR_CORRUPT);
+        adler[2 * c]     = (uint32_t)S;
+        adler[2 * c + 1] = (uint32_t)T;
+    }
 }
 
 // One CTA: the Adler-32 of the whole output from the per-chunk parts, against the stream's.
@@ -350,11 +431,11 @@ vsz_status vsz_inflate(const uint8_t* d_stream, size_t stream_len, const unsigne
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(d_status, 0, sizeof(int), st) != cudaSuccess) return VSZ_ERR_CUDA;
     uint32_t* adler = static_cast<uint32_t*>(d_ws);
-    const size_t smem = sizeof(LaneTables) * kThreads;
+    const size_t smem = sizeof(InflateSmem);
     if (cudaFuncSetAttribute(k_inflate_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return VSZ_ERR_CUDA;
     if (n_chunks) {
-        k_inflate_chunks<<<(unsigned)((n_chunks + kThreads - 1) / kThreads), kThreads, smem, st>>>(
+        k_inflate_chunks<<<(unsigned)n_chunks, 32, smem, st>>>(
             d_stream, stream_len, d_chunk_offsets, d_chunk_bytes, n_chunks, d_out, out_len, adler, d_status);
         vsz::count_launch();
     }
