@@ -67,6 +67,7 @@ def parse_args():
     ap.add_argument("--no-serving", action="store_true", help="skip the request-server stream")
     ap.add_argument("--no-other-configs", action="store_true",
                     help="skip the 1e-3, CESM-like and adversarial single-field configurations")
+    ap.add_argument("--no-lossless", action="store_true", help="skip the device gzip / inflate timing")
     ap.add_argument("--serving-seconds", type=float, default=8.0)
     ap.add_argument("--no-stage-profile", action="store_true",
                     help="no per-stage CUDA events in the timed loop (no roofline / stages)")
@@ -325,11 +326,12 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks.summary(t_wall0, t_wall1),
     }
-    line["lossless"] = run_device_gzip(V, codec.archive, int(res.data_size), stream)
+    if not args.no_lossless:
+        line["lossless"] = run_device_gzip(V, codec.archive, int(res.data_size), stream)
     if not args.no_e2e:
         line["e2e"] = run_e2e(V, x, dims, eb, mode, dct, bs, args.e2e_steps, bytes_in, world, want=out)
     if not args.no_other_configs and args.workload == "nyx512":
-        line["other_configs"] = run_other_configs(V, x, dims, stream)
+        line["other_configs"] = run_other_configs(V, x, dims, stream, lossless=not args.no_lossless)
     if not args.no_batch:
         line["batched"] = run_batch(V, args.batch_fields, 1000 + rank, reps=3)
     if not args.no_serving:
@@ -426,7 +428,7 @@ def run_device_gzip(V, d_archive, nbytes, stream, reps=5, host_sample=16 << 20):
                            "gbs": round(len(sample) / t_host / 1e9, 4), "cores": 1, "bytes": len(z3)}}
 
 
-def run_other_configs(V, x512, dims512, stream, reps=5):
+def run_other_configs(V, x512, dims512, stream, reps=5, lossless=True):
     """The reference's other single-field configurations, timed like the headline one (device
     buffers, CUDA events on the stream, median of `reps` runs after 2 warm-ups): the 512^3
     NYX-like field at r2r eb 1e-3, the 1800x3600 CESM-like field (abs 1e-4) and the adversarial
@@ -459,7 +461,7 @@ def run_other_configs(V, x512, dims512, stream, reps=5):
         err = (out.double() - x.double()).abs()
         bound = ebf + 2.0 * torch.abs(x.double()) * 2.0 ** -23
         nbytes = 4 * x.numel()
-        gz = run_device_gzip(V, codec.archive, int(res.data_size), stream)
+        gz = run_device_gzip(V, codec.archive, int(res.data_size), stream) if lossless else None
         return {"dims_xyz": list(dims), "eb": eb, "mode": mode, "lossless": gz,
                 "compress_gbs": round(nbytes / (statistics.median(cm) * 1e-3) / 1e9, 1),
                 "decompress_gbs": round(nbytes / (statistics.median(dm) * 1e-3) / 1e9, 1),

@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(kGatherThreads) k_outlier_gather(GatherArgs g)
 
 // Split copy: every warp of the grid takes 32 segments at a time and copies the non-empty ones.
 __global__ void __launch_bounds__(256) k_outlier_copy(GatherArgs g) {
-    if (*g.status != VSZ_OK) return;
+    if (*g.status != VSZ_OK || *g.total == 0) return;  // a field without outliers returns at once
     const unsigned lane = lane_id();
     uint8_t* out_bytes  = g.out_bytes ? g.out_bytes + g.out_off.eval() : nullptr;
     const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
