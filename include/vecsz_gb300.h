@@ -300,6 +300,12 @@ vsz_status vsz_autotune_block_size(const vsz_params* p, int ndim, const size_t d
                                    double sample_percent, int iterations, void* d_ws, size_t ws_bytes,
                                    int* best_block_size, double timings_ms[4], void* stream);
 
+/* The same search on a field in host memory (copied to the device first): what the command line's
+ * -a runs. */
+vsz_status vsz_autotune_block_size_host(const vsz_params* p, int ndim, const size_t dims[3], const float* h_in,
+                                        double sample_percent, int iterations, int* best_block_size,
+                                        double timings_ms[4]);
+
 /* ---- request server ---------------------------------------------------------------------------
  * Continuous admission of compress / decompress requests under a device-memory budget, their work
  * overlapping on the device.  Requests queue in arrival order; a dispatcher thread admits the head

@@ -17,6 +17,8 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libvecsz_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+CLI_SRC = os.path.join(HERE, "cli", "vecsz_cli.cpp")
+CLI = os.path.join(LIBDIR, "vecsz")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no contraction -- every FP step must round like the reference's separate operations.
@@ -54,8 +56,27 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def build_cli(force: bool = False) -> str:
+    """The `vecsz` command line (host C++ over the library's C ABI), linked next to the library."""
+    deps = [CLI_SRC, LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))
+    if not force and os.path.exists(CLI) and all(os.path.getmtime(d) <= os.path.getmtime(CLI) for d in deps):
+        return CLI
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("g++ not found: needed for the vecsz command line")
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", f"-I{INCLUDE}", CLI_SRC, "-o", tmp, f"-L{LIBDIR}", "-lvecsz_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"vecsz command line failed to build:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, CLI)
+    return CLI
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and not _stale():
+        build_cli()
         return LIB
     nv = nvcc()
     os.makedirs(OBJ, exist_ok=True)
@@ -81,6 +102,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_cli(force=True)
     return LIB
 
 

@@ -587,6 +587,24 @@ vsz_status vsz_decompress_host(const uint8_t* h_archive, size_t len, size_t data
     return VSZ_OK;
 }
 
+vsz_status vsz_autotune_block_size_host(const vsz_params* p, int ndim, const size_t dims[3], const float* h_in,
+                                        double sample_percent, int iterations, int* best_block_size,
+                                        double timings_ms[4]) {
+    if (!p || !dims || !h_in || !best_block_size) return VSZ_ERR_INVALID;
+    size_t ws = 0;
+    VSZ_TRY(vsz_autotune_workspace_bytes(p, ndim, dims, sample_percent, &ws));
+    HostCtx* c = ctx_for_device();
+    if (!c) return VSZ_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> lk(c->mu);
+    VSZ_TRY(ensure_stream(c));
+    size_t n = dims[0] * (ndim > 1 ? dims[1] : 1) * (ndim > 2 ? dims[2] : 1);
+    VSZ_TRY(c->in.grow(n * sizeof(float)));
+    VSZ_TRY(c->ws.grow(ws));
+    VSZ_CUDA(cudaMemcpyAsync(c->in.p, h_in, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    return vsz_autotune_block_size(p, ndim, dims, (const float*)c->in.p, sample_percent, iterations, c->ws.p,
+                                   c->ws.cap, best_block_size, timings_ms, c->stream);
+}
+
 vsz_status vsz_host_op_create(vsz_host_op** op) {
     if (!op) return VSZ_ERR_INVALID;
     vsz_host_op* o = new vsz_host_op();
