@@ -119,6 +119,8 @@ _PROTOS = {
     "vsz_autotune_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t), _d, C.POINTER(C.c_size_t)], _i),
     "vsz_autotune_block_size": ([_p, _i, C.POINTER(C.c_size_t), _p, _d, _i, _p, _sz, C.POINTER(C.c_int),
                                  C.POINTER(C.c_double), _p], _i),
+    "vsz_autotune_block_size_host": ([_p, _i, C.POINTER(C.c_size_t), _p, _d, _i, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_double)], _i),
     "vsz_server_create": ([_sz, _i, C.POINTER(C.c_void_p)], _i),
     "vsz_server_submit": ([_p, _p, C.POINTER(C.c_uint64)], _i),
     "vsz_server_wait": ([_p, C.c_uint64, _d, _p], _i),
