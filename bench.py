@@ -201,6 +201,22 @@ def algorithmic_bytes(stage, n, res, desc):
     return table.get(stage)
 
 
+def max_over_ranks(ms: float, world: int, device: str) -> float:
+    """The slowest rank's time; every rank calls it (one rank: unchanged)."""
+    if world == 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbs(bytes_per_rank_step: int, world: int, steps: int, total_ms: float) -> float:
+    """Input bytes of all ranks and steps per second of the slowest rank's time (weak scaling)."""
+    return world * steps * bytes_per_rank_step / (total_ms * 1e-3) / 1e9
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -271,11 +287,7 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     L.lib().vsz_profile_enable(0)
-    total_ms = start.elapsed_time(stop)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(start.elapsed_time(stop), world, "cuda")
     time.sleep(0.3)
     clocks.stop()
     comp_ms = [a.elapsed_time(b) for a, b, _ in ev]
@@ -309,7 +321,7 @@ def run_ours(args):
                   "share": round(v[0] / max(sum(w[0] for w in prof.values()), 1e-9), 4)}
               for k, v in prof.items()}
     bytes_in = 4 * n
-    value = world * args.steps * bytes_in / (total_ms * 1e-3) / 1e9
+    value = whole_job_gbs(bytes_in, world, args.steps, total_ms)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
