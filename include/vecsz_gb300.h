@@ -34,6 +34,7 @@ typedef int vsz_status;
 #define VSZ_ERR_RANGE 7       /* r2r with zero value range: the reference exits (src/types.cc:51-54) */
 #define VSZ_ERR_NOMEM 8       /* device or host allocation failed */
 #define VSZ_ERR_NO_DEVICE 9   /* no CUDA device */
+#define VSZ_ERR_CANCELLED 10  /* request server: withdrawn by vsz_server_cancel before it ran */
 
 #define VSZ_MODE_ABS 0 /* -m abs */
 #define VSZ_MODE_R2R 1 /* -m r2r: eb relative to the value range */
@@ -341,6 +342,10 @@ vsz_status vsz_server_submit(vsz_server* server, const vsz_request* request, uin
 /* Blocks until the request completed (VSZ_ERR_TIMEOUT after timeout_s). */
 vsz_status vsz_server_wait(vsz_server* server, uint64_t ticket, double timeout_s, vsz_completion* done);
 vsz_status vsz_server_release(vsz_server* server, uint64_t ticket);
+/* Withdraws a request that is still queued: it completes at once with status VSZ_ERR_CANCELLED and
+ * no output (wait returns it; release it as any other).  VSZ_ERR_UNSUPPORTED once the request has
+ * been admitted (it runs to completion), VSZ_ERR_INVALID for an unknown ticket. */
+vsz_status vsz_server_cancel(vsz_server* server, uint64_t ticket);
 vsz_status vsz_server_stats(vsz_server* server, uint64_t* completed, uint64_t* input_bytes_completed,
                             size_t* arena_bytes_in_use, int* queued);
 void vsz_server_destroy(vsz_server* server);

@@ -86,3 +86,38 @@ def test_budget_admission(cuda):
         srv.release(t)  # frees memory for the requests still queued
     assert srv.stats()["arena_bytes_in_use"] == 0
     srv.close()
+
+
+def test_cancel_queued_request(cuda):
+    """A request held back by the memory budget can be withdrawn: it completes at once as
+    cancelled with no output; an admitted or finished request cannot be; the rest are unaffected."""
+    import ctypes as C
+    torch = cuda
+    x = fields.grf_torch((64, 64, 64), seed=77).reshape(-1)
+    dims = (64, 64, 64)
+    p, ws, cap = make_params(1e-4, "r2r", 1024, 8), C.c_size_t(0), C.c_size_t(0)
+    V.lib().vsz_compress_bounds(C.byref(p), 3, V.api.dims_arg(dims), C.byref(ws), C.byref(cap))
+    # room for one request, not for a second while the first one's archive is kept
+    budget = max(ws.value + cap.value + (64 << 10), 1 << 20)
+    alone = _alone_compress({"x": x, "dims": dims, "eb": 1e-4, "mode": "r2r"})
+    srv = V.Server(budget_bytes=budget, slots=2)
+    t1 = srv.submit_compress(x, dims, 1e-4, "r2r", 1024, 8)
+    t2 = srv.submit_compress(x, dims, 1e-4, "r2r", 1024, 8)
+    c1 = srv.wait(t1)
+    assert c1.status == 0 and srv.output_bytes(c1) == alone
+    assert srv.stats()["queued"] == 1  # t2 waits for t1's archive to be released
+    assert srv.cancel(t2) == 0
+    c2 = srv.wait(t2, timeout_s=5)
+    assert c2.status == 10  # VSZ_ERR_CANCELLED
+    assert c2.out_bytes == 0
+    assert srv.cancel(t1) == 6  # already ran
+    assert srv.cancel(987654) == 1
+    srv.release(t1)
+    srv.release(t2)
+    t3 = srv.submit_compress(x, dims, 1e-4, "r2r", 1024, 8)
+    c3 = srv.wait(t3)
+    assert c3.status == 0 and srv.output_bytes(c3) == alone
+    srv.release(t3)
+    s = srv.stats()
+    assert s["queued"] == 0 and s["arena_bytes_in_use"] == 0
+    srv.close()

@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_status_strings():
     lib = V.lib()
-    for s in range(10):
+    for s in range(11):
         assert lib.vsz_status_string(s)
     assert b"sm_103a" in lib.vsz_version()
 

@@ -19,6 +19,7 @@ VSZ_ERR_UNSUPPORTED = 6
 VSZ_ERR_RANGE = 7
 VSZ_ERR_NOMEM = 8
 VSZ_ERR_NO_DEVICE = 9
+VSZ_ERR_CANCELLED = 10
 
 MODE_ABS = 0
 MODE_R2R = 1
@@ -125,6 +126,7 @@ _PROTOS = {
     "vsz_server_submit": ([_p, _p, C.POINTER(C.c_uint64)], _i),
     "vsz_server_wait": ([_p, C.c_uint64, _d, _p], _i),
     "vsz_server_release": ([_p, C.c_uint64], _i),
+    "vsz_server_cancel": ([_p, C.c_uint64], _i),
     "vsz_server_stats": ([_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_size_t),
                           C.POINTER(C.c_int)], _i),
     "vsz_server_destroy": ([_p], None),

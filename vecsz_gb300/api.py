@@ -443,6 +443,10 @@ class Server:
         check(lib().vsz_server_release(self._h, C.c_uint64(ticket)), "server_release")
         self._keep.pop(ticket, None)
 
+    def cancel(self, ticket) -> int:
+        """Withdraw a queued request (vsz_server_cancel): 0, or the status why it could not be."""
+        return int(lib().vsz_server_cancel(self._h, C.c_uint64(ticket)))
+
     def stats(self):
         d, b, u, q = C.c_uint64(0), C.c_uint64(0), C.c_size_t(0), C.c_int(0)
         check(lib().vsz_server_stats(self._h, C.byref(d), C.byref(b), C.byref(u), C.byref(q)), "server_stats")

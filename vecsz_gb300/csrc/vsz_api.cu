@@ -458,6 +458,7 @@ const char* vsz_status_string(vsz_status s) {
         case VSZ_ERR_RANGE: return "zero value range (r2r)";
         case VSZ_ERR_NOMEM: return "out of memory";
         case VSZ_ERR_NO_DEVICE: return "no CUDA device";
+        case VSZ_ERR_CANCELLED: return "request cancelled";
         default: return "unknown status";
     }
 }

@@ -1,9 +1,12 @@
 // Per-stage CUDA-event timing (see vsz_profile.h).  Event pairs are kept until vsz_profile_read,
-// which synchronises on them and accumulates elapsed times.
+// which synchronises on them and accumulates elapsed times.  Every stage is also an NVTX range
+// (named as in vsz_profile_read), so a timeline tool shows the stages around their launches.
 #include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "vsz_profile.h"
 #include "vsz_types.h"
@@ -34,6 +37,7 @@ std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 StageTimer::StageTimer(int s, cudaStream_t stream) : stage(s), st(stream) {
+    nvtxRangePushA(g_names[s]);
     if (!g_on) return;
     if (cudaEventCreate(&a) != cudaSuccess) {
         a = nullptr;
@@ -43,6 +47,7 @@ StageTimer::StageTimer(int s, cudaStream_t stream) : stage(s), st(stream) {
 }
 
 StageTimer::~StageTimer() {
+    nvtxRangePop();
     if (!a) return;
     cudaEvent_t b;
     if (cudaEventCreate(&b) != cudaSuccess) {

@@ -9,6 +9,7 @@
 // allocator, so admission never calls cudaMalloc.  A completed request frees its workspace at
 // once and keeps its output (compress: shrunk to the archive's real size) until released.
 #include <chrono>
+#include <algorithm>
 #include <condition_variable>
 #include <cstdint>
 #include <cstring>
@@ -324,6 +325,24 @@ vsz_status vsz_server_release(vsz_server* s, uint64_t ticket) {
     s->arena->release(j->out_off, j->out_bytes);
     s->jobs.erase(it);
     delete j;
+    s->cv.notify_all();
+    return VSZ_OK;
+}
+
+vsz_status vsz_server_cancel(vsz_server* s, uint64_t ticket) {
+    if (!s) return VSZ_ERR_INVALID;
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->jobs.find(ticket);
+    if (it == s->jobs.end()) return VSZ_ERR_INVALID;
+    Job* j = it->second;
+    if (j->state != 0) return VSZ_ERR_UNSUPPORTED;  // admitted: its work is on the device
+    auto q = std::find(s->queue.begin(), s->queue.end(), j);
+    if (q != s->queue.end()) s->queue.erase(q);
+    j->status    = VSZ_ERR_CANCELLED;
+    j->out_bytes = 0;  // nothing was allocated for it
+    j->out_keep  = 0;
+    j->state     = 2;
+    j->t_start = j->t_done = now_s();
     s->cv.notify_all();
     return VSZ_OK;
 }
