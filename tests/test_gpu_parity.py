@@ -345,3 +345,27 @@ def test_host_ops_match_host_entry_points(cuda):
     assert int(h_res.numpy()[5]) == L.VSZ_ERR_CAPACITY
     for op in ops:
         op.close()
+
+
+@pytest.mark.parametrize("offset", ["none", "all", "half", "nan"])
+def test_separable_reverse_lorenzo_matches_oracle(cuda, offset):
+    """3D block-8 fields with few outliers take the separable reverse Lorenzo; blocks whose values
+    reach 2^21 (here: a large offset at abs 1e-3, all or half of the field) or hold a NaN are redone
+    in the reference's order.  Every case must match the oracle bit for bit."""
+    nz, ny, nx = 40, 48, 64
+    z, y, xx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    x = (np.sin(xx / 9.0) * np.cos(y / 7.0) + 0.3 * np.sin(z / 5.0 + xx / 13.0)).astype(np.float64)
+    if offset == "all":
+        x += 5000.0
+    elif offset == "half":
+        x[nz // 2:] += 5000.0
+    x = x.astype(np.float32).ravel()
+    if offset == "nan":
+        x[12345] = np.nan
+    dims = (nx, ny, nz)
+    c = V.compress(x, dims, eb=1e-3, mode="abs", dict_size=1024, block_size=8)
+    a_or, meta = O.compress(x, dims, 8, 1024, 1e-3, False)
+    assert c.data[: c.data_size] == a_or
+    assert meta["n_outlier"] * 64 < x.size  # the separable pass is taken
+    y_or = O.decompress(a_or, 8, 1024)
+    np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y_or.view(np.uint32))

@@ -43,7 +43,7 @@ __device__ __forceinline__ float strict_prequant(float v, uint32_t col, const Dq
     return prequant_vec(v, c.r_f);
 }
 
-template <int NDIM, bool VEC, bool PAD = false>
+template <int NDIM, bool VEC, bool PAD = false, bool REDO = false>
 __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     typedef float PrevT[8][8][32];
@@ -59,8 +59,11 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
     const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
     const uint32_t warp0       = blockIdx.x * (blockDim.x >> 5) + wib;
 
-    // unit indices fit 32 bits (n <= 2^36 elements, 2048 per unit): 32-bit divisions only
-    for (uint32_t u = warp0; u < (uint32_t)a.nunits; u += warps_total) {
+    // unit indices fit 32 bits (n <= 2^36 elements, 2048 per unit): 32-bit divisions only.
+    // REDO: only the units the separable kernel listed (its count is final: stream order).
+    const uint32_t nloop = REDO ? a.redo[0] : (uint32_t)a.nunits;
+    for (uint32_t ui = warp0; ui < nloop; ui += warps_total) {
+        const uint32_t u  = REDO ? a.redo[1 + ui] : ui;
         const uint32_t xs = u % a.nxs;
         const uint32_t r  = u / a.nxs;
         const uint32_t yb = (NDIM >= 2) ? r % a.nyb : 0u;
@@ -238,6 +241,144 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
 #pragma unroll
                 for (int k = 0; k < 8; k++) s_prev[wib][7][k][lane] = Cm[k];
             }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Separable pass, 3D, block 8, zero halo (no padding), not strict.  With a zero halo the Lorenzo
+// inverse is the block's 3D inclusive prefix sum of the residuals q = code - R, so an element takes
+// three adds -- A = A(z-1) + q, B = B(y-1) + A, s = s(x-1) + B -- instead of the predictor's seven.
+// While every value of the block stays below 2^21 in magnitude, every partial sum of the
+// reference's order and of this one is an integer below 2^24, exact in FP32, so both give the same
+// bits.  An outlier sets s; B and A are corrected from it (B = s - s(x-1), A = B - B(y-1)).  A warp
+// with a block whose values leave that range (or meet a NaN or an infinity) lists its unit in
+// a.redo, and the reference-order kernel redoes it afterwards.
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    typedef float PlaneT[8][8][32];
+    PlaneT* s_A    = reinterpret_cast<PlaneT*>(s_dq_dyn);  // A of the previous plane [row][column][lane]
+    const Consts c = *a.consts;
+    if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
+    const int R                = a.R;
+    const float rbias          = 8388608.0f + (float)R;
+    const uint32_t rpair       = (uint32_t)R | ((uint32_t)R << 16);
+    const unsigned lane        = lane_id();
+    const unsigned wib         = threadIdx.x >> 5;
+    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
+    const uint32_t warp0       = blockIdx.x * (blockDim.x >> 5) + wib;
+
+    for (uint32_t u = warp0; u < (uint32_t)a.nunits; u += warps_total) {
+        const uint32_t xs = u % a.nxs;
+        const uint32_t r  = u / a.nxs;
+        const uint32_t yb = r % a.nyb;
+        const uint32_t zb = r / a.nyb;
+        const uint32_t x0 = xs * kDSeg + lane * 8;
+        const uint32_t y0 = yb * 8, z0 = zb * 8;
+        const int ny      = (int)min(8u, a.d1 - y0);
+        const int nz      = (int)min(8u, a.d2 - z0);
+        const bool col_in = x0 < a.d0;  // d0 % 8 == 0: all 8 columns or none
+        auto load_row = [&](int zz, int y) -> uint4 {
+            if (!(col_in && y < ny && zz < nz)) return make_uint4(rpair, rpair, rpair, rpair);
+            const size_t row = (size_t)(z0 + zz) * a.d1 + (y0 + y);
+            return __ldcs(reinterpret_cast<const uint4*>(a.codes + row * a.d0 + x0));
+        };
+        uint4 cv_next = load_row(0, 0);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int k = 0; k < 8; k++) s_A[wib][i][k][lane] = 0.f;
+        uint32_t big = 0;  // largest |value| of the block, as float bits (NaN and infinity above all)
+
+        for (int zz = 0; zz < nz; zz++) {
+            float Bm[8];  // B of the row above (zero above the block)
+#pragma unroll
+            for (int k = 0; k < 8; k++) Bm[k] = 0.f;
+#pragma unroll 2
+            for (int y = 0; y < 8; y++) {
+                const bool row_in = y < ny;
+                const size_t row  = ((size_t)(z0 + zz) * a.d1 + (y0 + y));
+                const bool all_in = row_in && col_in;
+                const uint4 cv    = cv_next;
+                cv_next           = (y < 7) ? load_row(zz, y + 1) : load_row(zz + 1, 0);
+                const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
+                auto code_at = [&](int k) -> uint32_t { return (cw[k >> 1] >> (16 * (k & 1))) & 0xffffu; };
+                // outliers of this row segment, ranked in row-major order (as k_dq_decompress_b8)
+                uint32_t zm = 0;
+                if (zero_halves(cv.x) | zero_halves(cv.y) | zero_halves(cv.z) | zero_halves(cv.w)) {
+#pragma unroll
+                    for (int k = 0; k < 8; k++) zm |= (code_at(k) == 0u) ? (1u << k) : 0u;
+                }
+                unsigned long long obase = 0;
+                if (__any_sync(0xffffffffu, zm != 0u)) {
+                    uint32_t cnt = __popc(zm), incl = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= (unsigned)o) incl += t;
+                    }
+                    unsigned long long seg_base;
+                    if (a.chunk_off) {
+                        const unsigned long long q  = row * a.d0 + (unsigned long long)xs * kDSeg;
+                        const unsigned long long c0 = q & ~511ull;
+                        uint32_t zc = 0;
+                        const unsigned long long lo = c0 + (unsigned long long)lane * 16;
+#pragma unroll
+                        for (int t = 0; t < 16; t++)
+                            if (lo + t < q) zc += (a.codes[lo + t] == 0);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
+                        seg_base = a.chunk_off[q >> 9] + zc;
+                    } else {
+                        seg_base = a.seg_off[row * a.nxs + xs];
+                    }
+                    obase = seg_base + (incl - cnt);
+                }
+                float C[8];
+                auto row_pass = [&](auto with_outliers) {
+                    float sl = 0.f;  // s of the element to the left (zero left of the block)
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        const float q = __fsub_rn(__uint_as_float(0x4B000000u | code_at(k)), rbias);
+                        float A       = __fadd_rn(s_A[wib][y][k][lane], q);
+                        float B       = __fadd_rn(Bm[k], A);
+                        float sv      = __fadd_rn(sl, B);
+                        if (decltype(with_outliers)::value) {
+                            if (zm & (1u << k)) {
+                                const unsigned long long oi = obase + __popc(zm & ((1u << k) - 1u));
+                                sv = 0.f;
+                                if (oi < a.n_outliers) sv = a.outliers[oi];
+                                else set_status(a.status, VSZ_ERR_CORRUPT);
+                                B = __fsub_rn(sv, sl);
+                                A = __fsub_rn(B, Bm[k]);
+                            }
+                        }
+                        s_A[wib][y][k][lane] = A;
+                        Bm[k]                = B;
+                        sl                   = sv;
+                        C[k]                 = sv;
+                        big                  = max(big, __float_as_uint(sv) & 0x7fffffffu);
+                    }
+                };
+                if (zm) row_pass(std::true_type{});
+                else row_pass(std::false_type{});
+                if (all_in) {
+                    float* orow = a.out + row * a.d0;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        float xo[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                        __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
+                    }
+                }
+            }
+        }
+        // 0x4A000000 = 2^21: a block with a larger value (or a NaN / infinity) is redone
+        if (__any_sync(0xffffffffu, big >= 0x4A000000u) && lane == 0) {
+            const uint32_t i = atomicAdd(a.redo, 1u);
+            a.redo[1 + i]    = u;
         }
     }
 }
@@ -445,6 +586,11 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
             if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true, true>, 3) : go(k_dq_decompress_b8<3, false, true>, 3);
             else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true, true>, 2) : go(k_dq_decompress_b8<2, false, true>, 2);
             else vec ? go(k_dq_decompress_b8<1, true, true>, 1) : go(k_dq_decompress_b8<1, false, true>, 1);
+        } else if (ndim == 3 && vec && a.redo && !a.strict && a.n_outliers * 64 < a.n) {
+            // separable pass, then the reference-order kernel over the units it listed
+            if (cudaMemsetAsync(a.redo, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
+            go(k_dq_decompress_b8s, 3);
+            go(k_dq_decompress_b8<3, true, false, true>, 3);
         } else {
             if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);
             else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true>, 2) : go(k_dq_decompress_b8<2, false>, 2);

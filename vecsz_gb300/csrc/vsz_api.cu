@@ -148,6 +148,7 @@ struct DecompressWs {
     unsigned long long* s_out_begin;
     int* s_changed;
     float* outliers;
+    uint32_t* redo;  // units of the separable reverse Lorenzo that the reference-order kernel redoes
     size_t bytes;
 };
 
@@ -188,6 +189,10 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
     w.s_out_begin  = b.take<unsigned long long>(nsync);
     w.s_changed    = b.take<int>(4);
     w.outliers     = b.take<float>(n_out + 4);
+    {
+        const size_t units8 = (size_t)nxs * ((g.d1 + 7) / 8) * ((g.d2 + 7) / 8);  // block-8 warp units
+        w.redo = b.take<uint32_t>(units8 + 2);
+    }
     w.bytes        = b.off + 256;
     return w;
 }
@@ -1111,6 +1116,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.strict = d->has_trailer ? d->strict : 0;
     a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
     a.pad    = pad_view_of(d, bs, d_archive);
+    a.redo   = w.redo;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

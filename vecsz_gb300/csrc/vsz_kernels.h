@@ -149,6 +149,8 @@ struct DqDecArgs {
     int strict;                          // strict archive: outliers are input values (re-prequantized)
     uint32_t xtail;                      // 3D: first scalar-prequant column (d0 & ~7 when d0 % 8), else d0
     PadView pad;                         // padded archive: the halo of each block (vals = pad section)
+    uint32_t* redo;                      // 3D block 8, separable pass: [0] count, then units whose
+                                         // values left the exact range (null: reference order only)
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
