@@ -392,3 +392,22 @@ def test_3d_value_scales_match_oracle(cuda, case):
     assert c.data[: c.data_size] == a_or
     vr = O.value_range(x) if mode == "r2r" else 0.0
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(a_or, bs, 1024, vr).view(np.uint32))
+
+
+@pytest.mark.parametrize("dims,bs,mode", [((96, 40), 8, "abs"), ((37, 41, 43), 8, "abs"), ((64, 64, 16), 8, "abs"),
+                                          ((5000,), 16, "abs"), ((64, 48, 16), 16, "abs")])
+def test_infinite_and_huge_inputs_match_oracle(cuda, dims, bs, mode):
+    """Infinities and values near the float limit: outliers, codes and reconstructions follow the
+    reference's IEEE arithmetic (overflowing prequantization, infinite residuals)."""
+    rng = np.random.default_rng(7 * sum(dims) + bs)
+    n = int(np.prod(dims))
+    x = (np.cumsum(rng.standard_normal(n)) * 0.1).astype(np.float32)
+    idx = rng.choice(n, 12, replace=False)
+    x[idx[:3]] = np.inf
+    x[idx[3:6]] = -np.inf
+    x[idx[6:9]] = np.float32(3.0e38)
+    x[idx[9:]] = np.float32(-1.7e38)
+    c = V.compress(x, dims, eb=1e-3, mode=mode, dict_size=1024, block_size=bs)
+    oa, _ = O.compress(x, dims, bs, 1024, 1e-3, mode == "r2r")
+    assert c.data[:c.data_size] == oa
+    np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(oa, bs, 1024).view(np.uint32))
