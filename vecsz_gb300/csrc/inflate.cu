@@ -2,13 +2,13 @@
 // pass (replaces zlib_uncompress, src/lossless.hh:144-177, for those streams).  vsz_deflate's
 // chunks are independent (no match reaches before its chunk, every chunk starts on a byte), so
 // with the chunk sizes from the archive's deflate index each chunk inflates on its own: one warp
-// per chunk, the chunk's compressed bytes and its 32 KiB of output in shared memory.  All lanes
-// run the same decode (broadcast reads, no divergence), lane 0 builds the code tables (a 9-bit
-// primary table and a canonical walk for longer codewords) and writes literals, the warp copies
-// matches and stored blocks together.  Every read is bounded by the chunk's bytes, every write by
-// its output size; anything else (another encoder's stream, a damaged one) sets VSZ_ERR_CORRUPT and
-// the host falls back to the host library.  The Adler-32 of the output is checked against the
-// stream's.
+// per chunk, the chunk's 32 KiB of output in shared memory, its compressed bytes read through the
+// read-only cache.  All lanes run the same decode (broadcast reads, no divergence), lane 0 builds
+// the code tables (a 9-bit primary table and a canonical walk for longer codewords) and writes
+// literals, the warp copies matches and stored blocks together.  Every read is bounded by the
+// chunk's bytes, every write by its output size; anything else (another encoder's stream, a
+// damaged one) sets VSZ_ERR_CORRUPT and the host falls back to the host library.  The Adler-32 of
+// the output is checked against the stream's.
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -22,7 +22,6 @@ void count_launch();  // vsz_profile.cu
 namespace {
 
 constexpr int kChunk         = 32768;  // output bytes per chunk, as vsz_deflate writes them
-constexpr int kInBytes       = kChunk + 5 + 64;  // a chunk's compressed bytes (stored: kChunk + 5), skew, padding
 constexpr int kLitBits       = 9;      // primary table of the literal/length code
 constexpr int kDistBits      = 6;      // primary table of the distance code
 constexpr uint32_t kAdlerMod = 65521;
@@ -44,26 +43,39 @@ __constant__ uint16_t kDistBase[30] = {1,   2,   3,   4,   5,   7,    9,    13, 
 __constant__ uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
 __constant__ uint8_t kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
-// LSB-first bit reader over the chunk's bytes in shared memory (little-endian words, the chunk
-// starting `base` bits into them), with a 64-bit window in registers refilled a word at a time;
-// positions past the chunk read zero padding and are caught by the caller's position checks
+// LSB-first bit reader over the chunk's bytes in global memory (read-only, cached; every lane of
+// the warp reads the same word), with a 64-bit window in registers refilled a word at a time.
+// Words are aligned; bytes outside the chunk read as zero, and positions past its end are caught
+// by the caller's position checks.
 struct Bits {
-    const uint32_t* w;
-    uint32_t base;  // bit offset of the chunk's first byte
-    uint32_t pos;   // bits consumed
-    uint32_t nw;    // next word to enter the window
-    uint32_t cnt;   // valid bits in the window
+    const uint32_t* w;  // aligned words covering the chunk
+    uint32_t skew;      // bytes of the first word before the chunk
+    uint32_t cb;        // chunk bytes
+    uint32_t pos;       // bits consumed
+    uint32_t nw;        // next word to enter the window
+    uint32_t cnt;       // valid bits in the window
     uint64_t buf;
+    __device__ __forceinline__ uint32_t word(uint32_t i) const {
+        const uint32_t lo = 4 * i;  // byte offset of the word from w, the chunk starts at skew
+        if (lo >= skew && lo + 4 - skew <= cb) return __ldg(&w[i]);
+        const uint8_t* b = reinterpret_cast<const uint8_t*>(w);
+        uint32_t v = 0;
+        for (uint32_t q = 0; q < 4; q++) {
+            const uint32_t at = lo + q;
+            if (at >= skew && at - skew < cb) v |= (uint32_t)__ldg(&b[at]) << (8 * q);
+        }
+        return v;
+    }
     __device__ __forceinline__ void seek(uint32_t p) {
         pos = p;
-        const uint32_t b = base + p;
-        buf = w[b >> 5] >> (b & 31);
-        cnt = 32 - (b & 31);
-        nw  = (b >> 5) + 1;
+        const uint32_t bit = 8 * skew + p;
+        buf = word(bit >> 5) >> (bit & 31);
+        cnt = 32 - (bit & 31);
+        nw  = (bit >> 5) + 1;
     }
     __device__ __forceinline__ uint32_t peek() {  // at least 32 valid bits
         if (cnt < 32) {
-            buf |= (uint64_t)w[nw++] << cnt;
+            buf |= (uint64_t)word(nw++) << cnt;
             cnt += 32;
         }
         return (uint32_t)buf;
@@ -149,7 +161,6 @@ __device__ __forceinline__ int decode_sym(Bits& br, const uint16_t* primary, int
 // dynamic shared memory of a CTA (one warp, one chunk)
 struct InflateSmem {
     uint8_t out[kChunk];
-    uint32_t in[kInBytes / 4 + 2];
     LaneTables t;
     int bad;
 };
@@ -175,26 +186,11 @@ __global__ void __launch_bounds__(32)
         }
         return;
     }
-    // the compressed bytes into shared memory, `skew` bytes in so 16-byte loads stay aligned
     const uint8_t* src  = stream + off;
-    const uint32_t skew = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 15);
-    uint8_t* inb        = reinterpret_cast<uint8_t*>(m.in);
-    {
-        const uint32_t span = (skew + cb + 15) & ~15u;  // whole 16-byte blocks covering the chunk
-        const uint4* g16    = reinterpret_cast<const uint4*>(src - skew);
-        for (uint32_t k = lane; k < span / 16; k += 32) {
-            const uint32_t lo = 16 * k, hi = lo + 16;
-            if (lo >= skew && hi <= skew + cb) {
-                reinterpret_cast<uint4*>(inb)[k] = g16[k];
-            } else {
-                for (uint32_t q = lo; q < hi; q++) inb[q] = (q >= skew && q < skew + cb) ? src[q - skew] : 0;
-            }
-        }
-        for (uint32_t q = span + lane; q < (uint32_t)sizeof(m.in); q += 32) inb[q] = 0;
-        if (lane == 0) m.bad = 0;
-    }
+    const uint32_t skew = (uint32_t)(reinterpret_cast<uintptr_t>(src) & 3);
+    if (lane == 0) m.bad = 0;
     __syncwarp();
-    Bits br{m.in, 8 * skew, 0, 0, 0, 0};
+    Bits br{reinterpret_cast<const uint32_t*>(src - skew), skew, cb, 0, 0, 0, 0};
     br.seek(0);
     const uint32_t end_bits = 8 * cb;
     uint32_t have = 0;
@@ -219,8 +215,8 @@ __global__ void __launch_bounds__(32)
                 bad = true;
                 break;
             }
-            const uint32_t bp = skew + br.pos / 8;
-            for (uint32_t k = lane; k < len; k += 32) m.out[have + k] = inb[bp + k];
+            const uint32_t bp = br.pos / 8;  // the block's bytes start here in the chunk
+            for (uint32_t k = lane; k < len; k += 32) m.out[have + k] = __ldg(&src[bp + k]);
             __syncwarp();
             have += len;
             br.seek(br.pos + 8 * len);
