@@ -422,22 +422,24 @@ vsz_status vsz_lossless_decompress(const uint8_t* h_in, size_t len, size_t targe
 int vsz_lossless_detect(const uint8_t* h_in, size_t len);
 
 /* The gzip pass on the device (replaces zlib_compress, src/lossless.hh:84-142, for -L gzip):
- * d_in[len] -> a zlib stream (RFC 1950 around RFC 1951 deflate) in d_out.  32 KiB chunks are
- * encoded independently (one CTA each: hash-chain match search, dynamic, fixed or stored block,
+ * d_in[len] -> a zlib stream (RFC 1950 around RFC 1951 deflate) in d_out.  Chunks of
+ * vsz_deflate_chunk_bytes() (16 KiB) are encoded independently (one CTA each: hash-chain match search, dynamic, fixed or stored block,
  * whichever is shortest, then an empty stored block so the next chunk starts on a byte).
  * d_result (device, 8 x u64): [0] stream bytes, [1] status (VSZ_ERR_CAPACITY when out_capacity is
  * too small), [2] chunks, [3] stored, [4] fixed, [5] dynamic chunks.  Stream-ordered, no sync. */
 vsz_status vsz_deflate_bounds(size_t len, size_t* ws_bytes, size_t* out_capacity);
 vsz_status vsz_deflate(const uint8_t* d_in, size_t len, void* d_ws, size_t ws_bytes, uint8_t* d_out,
                        size_t out_capacity, uint64_t* d_result, void* stream);
-/* Compressed bytes of each 32 KiB chunk of the last vsz_deflate on this workspace (u32 per chunk,
+size_t vsz_deflate_chunk_bytes(void);
+/* Compressed bytes of each chunk of the last vsz_deflate on this workspace (u32 per chunk,
  * host or device dst, stream-ordered): the deflate index the host entry points append after the
  * trailer of a VSZ_LOSSLESS_GZIP_DEVICE archive. */
 vsz_status vsz_deflate_chunk_sizes(const void* d_ws, size_t len, uint32_t* dst, void* stream);
 
 /* Inflate on the device for streams written by vsz_deflate (replaces zlib_uncompress,
  * src/lossless.hh:144-177, for them): chunk c (its compressed bytes at d_chunk_offsets[c] in the
- * stream, d_chunk_bytes[c] of them) inflates to d_out[32768 c ..], one thread per chunk; the
+ * stream, d_chunk_bytes[c] of them) inflates to d_out[vsz_deflate_chunk_bytes() * c ..], one warp
+ * per chunk; the
  * Adler-32 of the output is checked against adler32.  *d_status (device int) = VSZ_ERR_CORRUPT for
  * anything that is not such a stream; reads and writes stay inside the given buffers. */
 vsz_status vsz_inflate_bounds(size_t n_chunks, size_t* ws_bytes);

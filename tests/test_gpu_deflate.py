@@ -11,6 +11,7 @@ import vecsz_gb300 as V
 from vecsz_gb300 import api, fields
 
 pytestmark = pytest.mark.gpu
+CH = 16384  # vsz_deflate_chunk_bytes(); checked below
 
 
 def roundtrip(data):
@@ -21,7 +22,12 @@ def roundtrip(data):
     return out, stats
 
 
-@pytest.mark.parametrize("n", [0, 1, 2, 3, 4, 5, 127, 128, 129, 4095, 4096, 4100, 32767, 32768, 32769, 65536, 100003])
+def test_chunk_size(cuda):
+    assert V.lib().vsz_deflate_chunk_bytes() == CH
+
+
+@pytest.mark.parametrize("n", [0, 1, 2, 3, 4, 5, 63, 64, 65, 127, 128, 129, 4095, 4096, 4100, CH - 1, CH, CH + 1,
+                               2 * CH + 7, 32768, 65536, 100003])
 def test_deflate_sizes_random_and_runs(cuda, n):
     rng = np.random.default_rng(n)
     roundtrip(rng.integers(0, 256, n, dtype=np.uint8).tobytes())
@@ -33,14 +39,14 @@ def test_deflate_sizes_random_and_runs(cuda, n):
 
 def test_deflate_block_types(cuda):
     rng = np.random.default_rng(5)
-    _, st = roundtrip(rng.integers(0, 256, 5 * 32768, dtype=np.uint8).tobytes())
+    _, st = roundtrip(rng.integers(0, 256, 5 * CH, dtype=np.uint8).tobytes())
     assert (st["chunks"], st["stored"], st["fixed"], st["dynamic"]) == (5, 5, 0, 0)
-    assert list(st["chunk_bytes"]) == [32773] * 5  # stored: 5 header bytes + the chunk
-    _, st = roundtrip(bytes(3 * 32768))
+    assert list(st["chunk_bytes"]) == [CH + 5] * 5  # stored: 5 header bytes + the chunk
+    _, st = roundtrip(bytes(3 * CH))
     assert st["chunks"] == 3 and st["stored"] == 0
     text = (b"the quick brown fox jumps over the lazy dog " * 2000)[:70000]
     out, st = roundtrip(text)
-    assert st["dynamic"] + st["fixed"] == 3 and len(out) < len(text) // 20
+    assert st["dynamic"] + st["fixed"] == (len(text) + CH - 1) // CH and len(out) < len(text) // 12
 
 
 def test_deflate_patterns_and_long_matches(cuda):
@@ -49,8 +55,10 @@ def test_deflate_patterns_and_long_matches(cuda):
         unit = rng.integers(0, 256, period, dtype=np.uint8).tobytes()
         data = (unit * (100000 // period + 2))[:100000]
         out, _ = roundtrip(data)
-        if period <= 4097:
+        if period <= 1000:
             assert len(out) < len(data) // 4
+        elif period <= 4097:  # each chunk's first period is literals
+            assert len(out) < len(data) * (period + 2048) // CH
     # text with many 3-byte repeats at large distances, and a skewed literal alphabet
     words = [bytes(rng.integers(97, 123, int(k), dtype=np.uint8)) for k in rng.integers(2, 9, 400)]
     roundtrip(b" ".join(words[int(i)] for i in rng.integers(0, 400, 30000)))
@@ -78,7 +86,7 @@ def test_deflate_large_input(cuda):
     base = np.repeat(rng.integers(0, 4, 2_000_000, dtype=np.uint8), 3)
     base[::97] = rng.integers(0, 256, base[::97].size, dtype=np.uint8)
     out, st = api.deflate(torch.from_numpy(base).cuda())
-    assert st["chunks"] == (base.size + 32767) // 32768
+    assert st["chunks"] == (base.size + CH - 1) // CH
     assert zlib.decompress(out) == base.tobytes()
 
 
@@ -111,7 +119,7 @@ def inflate_roundtrip(data):
     return out, st
 
 
-@pytest.mark.parametrize("n", [0, 1, 3, 4096, 32767, 32768, 32769, 100003, 1 << 20])
+@pytest.mark.parametrize("n", [0, 1, 3, 4096, CH - 1, CH, CH + 1, 32769, 100003, 1 << 20])
 def test_inflate_device_streams(cuda, n):
     rng = np.random.default_rng(100 + n)
     inflate_roundtrip(rng.integers(0, 256, n, dtype=np.uint8).tobytes())
@@ -152,7 +160,7 @@ def test_inflate_rejects_other_streams(cuda):
     bad[-1] ^= 1  # Adler-32
     assert api.inflate(bytes(bad), sizes, len(block))[1] == 3
     z = zlib.compress(block, 6)  # zlib's stream: a final block inside the "chunk"
-    assert api.inflate(z, np.array([len(z) - 6], np.uint32), len(block) if len(block) <= 32768 else 32768)[1] == 3
+    assert api.inflate(z, np.array([len(z) - 6], np.uint32), min(len(block), CH))[1] == 3
     wrong = sizes.copy()
     wrong[0] += 1
     assert api.inflate(out, wrong, len(block))[1] == 3

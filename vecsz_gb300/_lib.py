@@ -163,6 +163,7 @@ _PROTOS = {
     "vsz_deflate_bounds": ([_sz, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], _i),
     "vsz_deflate": ([_p, _sz, _p, _sz, _p, _sz, _p, _p], _i),
     "vsz_deflate_chunk_sizes": ([_p, _sz, _p, _p], _i),
+    "vsz_deflate_chunk_bytes": ([], _sz),
     "vsz_inflate_bounds": ([_sz, C.POINTER(C.c_size_t)], _i),
     "vsz_inflate": ([_p, _sz, _p, _p, _sz, C.c_uint32, _p, _sz, _p, _sz, _p, _p], _i),
     "vsz_archive_parse_split": ([_p, _sz, _p, _sz, C.POINTER(ArchiveDesc)], _i),

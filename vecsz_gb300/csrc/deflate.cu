@@ -3,14 +3,14 @@
 // :84-142 zlib_compress at level 3; src/vecsz_interface.hh:206-217, :237-243).  The stream decodes
 // with any inflate, the reference's included; its bytes are not zlib's (a different match search).
 //
-// Layout of the work.  The input is cut into 32 KiB chunks, one CTA each.  Matches never reach
-// back before their chunk, so chunks are independent:
-//   1. candidates: eight warps each sweep 4 KiB of the chunk, 32 positions a step, and record for
+// Layout of the work.  The input is cut into 16 KiB chunks (kDeflateChunk), one CTA each, two CTAs
+// per SM.  Matches never reach back before their chunk, so chunks are independent:
+//   1. candidates: eight warps each sweep 2 KiB of the chunk, 32 positions a step, and record for
 //      every position the previous position with the same 4-byte hash (within the step by
 //      __match_any_sync, before it from the warp's hash head table); a position without one
-//      takes the last occurrence in the nearest earlier 4 KiB range from that range's final head
+//      takes the last occurrence in the nearest earlier 2 KiB range from that range's final head
 //      table.  The records form hash chains, as zlib's prev[] does.
-//   2. parse: thread t parses bytes [128 t, 128 t + 128) greedily, following up to kChain chain
+//   2. parse: thread t parses bytes [64 t, 64 t + 64) greedily, following up to kChain chain
 //      links per position; matches end at the thread's range end.  Tokens go to shared memory,
 //      symbol counts to shared histograms.
 //   3. codes: length-limited (15-bit) Huffman codes for literal/length and distance symbols and
@@ -25,6 +25,7 @@
 
 #include <cuda_runtime.h>
 
+#include "deflate_format.h"
 #include "vsz_types.h"
 
 namespace vsz {
@@ -33,12 +34,12 @@ void count_launch();  // vsz_profile.cu
 
 namespace {
 
-constexpr int kChunk      = 32768;   // input bytes per chunk (= the deflate window)
+constexpr int kChunk      = vsz::kDeflateChunk;  // input bytes per chunk
 constexpr int kThreads    = 256;
-constexpr int kSeg        = kChunk / kThreads;  // 128 bytes parsed per thread
+constexpr int kSeg        = kChunk / kThreads;  // 64 bytes parsed per thread
 constexpr int kWarps      = kThreads / 32;
-constexpr int kRange      = kChunk / kWarps;    // 4096 positions swept per warp
-constexpr int kHashBits   = 12;
+constexpr int kRange      = kChunk / kWarps;    // 2048 positions swept per warp
+constexpr int kHashBits   = 11;                 // a head table of kRange entries per warp
 constexpr int kHashSize   = 1 << kHashBits;
 constexpr int kChain      = 4;
 constexpr int kTooFar     = 4096;    // 3-byte matches farther than this are not worth it (zlib's rule)
@@ -58,6 +59,7 @@ constexpr int kPrevBytes = 2 * kChunk;           // prev[] (phases 1-2), then th
 constexpr int kHeadBytes = 2 * kHashSize * kWarps;  // head tables (phase 1), then the tokens
 constexpr int kTagBytes  = kHashSize * kWarps;      // per-warp lane tags of the candidate sweep
 static_assert(kHeadBytes == 2 * kChunk, "one u16 token slot per position");
+static_assert(kChunk <= 32768 && kSeg * kThreads == kChunk, "distances within the zlib window");
 static_assert(kPrevBytes >= kChunk + 256, "bit buffer holds any block shorter than a stored one");
 
 struct DeflateSmem {
@@ -243,7 +245,7 @@ __device__ __forceinline__ void put_bits(uint32_t* out, uint32_t& pos, uint32_t 
     pos += n;
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_deflate_chunks(const uint8_t* __restrict__ in, size_t len, uint8_t* __restrict__ staging,
                      uint32_t* __restrict__ sizes, uint32_t* __restrict__ adler, uint32_t* __restrict__ kinds) {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -827,6 +829,8 @@ DeflateWs deflate_ws(uint8_t* base, size_t nchunks) {
 }  // namespace
 
 extern "C" {
+
+size_t vsz_deflate_chunk_bytes(void) { return (size_t)kChunk; }
 
 vsz_status vsz_deflate_bounds(size_t len, size_t* ws_bytes, size_t* out_capacity) {
     const size_t nchunks = (len + kChunk - 1) / kChunk;

@@ -2,7 +2,7 @@
 // pass (replaces zlib_uncompress, src/lossless.hh:144-177, for those streams).  vsz_deflate's
 // chunks are independent (no match reaches before its chunk, every chunk starts on a byte), so
 // with the chunk sizes from the archive's deflate index each chunk inflates on its own: one warp
-// per chunk, the chunk's 32 KiB of output in shared memory, its compressed bytes read through the
+// per chunk, the chunk's output (16 KiB) in shared memory, its compressed bytes read through the
 // read-only cache.  All lanes run the same decode (broadcast reads, no divergence), lane 0 builds
 // the code tables (a 9-bit primary table and a canonical walk for longer codewords) and writes
 // literals, the warp copies matches and stored blocks together.  Every read is bounded by the
@@ -13,6 +13,7 @@
 
 #include <cuda_runtime.h>
 
+#include "deflate_format.h"
 #include "vsz_types.h"
 
 namespace vsz {
@@ -21,7 +22,7 @@ void count_launch();  // vsz_profile.cu
 
 namespace {
 
-constexpr int kChunk         = 32768;  // output bytes per chunk, as vsz_deflate writes them
+constexpr int kChunk         = vsz::kDeflateChunk;  // output bytes per chunk, as vsz_deflate writes them
 constexpr int kLitBits       = 9;      // primary table of the literal/length code
 constexpr int kDistBits      = 6;      // primary table of the distance code
 constexpr uint32_t kAdlerMod = 65521;
@@ -342,10 +343,10 @@ __global__ void __launch_bounds__(32)
     if (br.pos != end_bits) bad = true;
     if (have != want) bad = true;
     __syncwarp();
-    // Adler-32 parts of the chunk: lane l sums bytes [1024 l, 1024 l + 1024), then an ordered scan
+    // Adler-32 parts of the chunk: lane l sums bytes [kChunk / 32 * l, ...), then an ordered scan
     uint64_t S = 0, T = 0, N = 0;
     if (!bad) {
-        const uint32_t b0 = lane * 1024, b1 = min(want, b0 + 1024);
+        const uint32_t b0 = lane * (kChunk / 32), b1 = min(want, b0 + kChunk / 32);
         for (uint32_t i = b0; i < b1; i++) {
             S += m.out[i];
             T += S;

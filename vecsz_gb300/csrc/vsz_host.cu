@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 
+#include "deflate_format.h"
 #include "vsz_types.h"
 
 namespace vsz {
@@ -131,7 +132,7 @@ Zlib* zlib() {
 constexpr uint32_t kDeflateIndexMagic   = 0x445A5356u;
 constexpr uint32_t kDeflateIndexVersion = 1;
 constexpr uint32_t kDeflateIndexHead    = 40;
-constexpr uint32_t kDeflateChunk        = 32768;
+constexpr uint32_t kDeflateChunk        = (uint32_t)vsz::kDeflateChunk;
 
 size_t deflate_index_bytes(size_t nchunks) { return (kDeflateIndexHead + 4 * nchunks + 7) & ~(size_t)7; }
 
