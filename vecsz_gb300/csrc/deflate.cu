@@ -95,7 +95,10 @@ struct DeflateSmem {
     uint64_t fixed_bits;
     int skip_dynamic;
     int nlit, ndist, ncl;
-    int btype;  // 0 stored, 1 fixed, 2 dynamic
+    int btype;   // 0 stored, 1 fixed, 2 dynamic
+    int dyn_ok;  // the dynamic codes were built
+    uint64_t pb_part[kWarps];          // per-warp payload bits of the dynamic codes
+    uint32_t cnt[3][16], next[3][16];  // per alphabet (literal/length, distance, code length): codes per length, first code
 };
 
 constexpr size_t kSmemBytes = kDataBytes + kPrevBytes + kHeadBytes + kTagBytes;  // dynamic part
@@ -158,11 +161,11 @@ __device__ __forceinline__ int rank_symbols(const uint32_t* freq, int n, uint16_
 }
 
 // Length-limited Huffman code lengths (one thread).  sorted[0..m) holds the symbols in use by
-// ascending (frequency, symbol), m >= 2; other symbols get length 0.  Returns false if the limit
+// ascending (frequency, symbol), m >= 2; len[] is zero on entry and stays zero for the others.  Returns false if the limit
 // cannot be met with a complete code (the caller then uses another block type).
 __device__ __forceinline__ bool lengths_from_sorted(const uint32_t* freq, const uint16_t* sorted, int m, int n, int limit,
                                     uint8_t* len, DeflateSmem& s) {
-    for (int i = 0; i < n; i++) len[i] = 0;
+    (void)n;  // len[0..n) is zero on entry: only the used symbols are written
     if (m < 2) return false;
     // two-queue Huffman: leaves 0..m-1 by ascending weight, internal nodes m..2m-2 in creation
     // order (their weights come out nondecreasing, so the queue head is the lightest)
@@ -220,20 +223,6 @@ __device__ __forceinline__ bool lengths_from_sorted(const uint32_t* freq, const 
     for (int l = limit; l >= 1; l--)
         for (int c = 0; c < s.bl_count[l]; c++) len[sorted[k++]] = (uint8_t)l;
     return true;
-}
-
-// canonical codes (RFC 1951 3.2.2), stored bit-reversed for the LSB-first stream
-__device__ __forceinline__ void build_codes(const uint8_t* len, int n, uint16_t* code) {
-    uint32_t count[16] = {0};
-    for (int i = 0; i < n; i++) count[len[i]]++;
-    count[0] = 0;
-    uint32_t next[16];
-    uint32_t c = 0;
-    for (int l = 1; l < 16; l++) {
-        c       = (c + count[l - 1]) << 1;
-        next[l] = c;
-    }
-    for (int i = 0; i < n; i++) code[i] = len[i] ? (uint16_t)reverse_bits(next[len[i]]++, len[i]) : 0;
 }
 
 // shared-memory bit writer: atomics because neighbouring threads share boundary words
@@ -450,15 +439,19 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     const bool try_dynamic = !s.skip_dynamic;
     int m_lit = 0, m_dist = 0;
+    for (int k = tid; k < kLitSyms + kDistSyms + kClSyms + 4; k += kThreads) {
+        if (k < kLitSyms + 2) s.lit_len[k] = 0;
+        else if (k < kLitSyms + kDistSyms + 4) s.dist_len[k - kLitSyms - 2] = 0;
+        else if (k - kLitSyms - kDistSyms - 4 < kClSyms + 1) s.cl_len[k - kLitSyms - kDistSyms - 4] = 0;
+    }
+    __syncthreads();
     if (try_dynamic) {
         m_lit  = rank_symbols(s.lf, kLitSyms, s.sorted_lit);
         m_dist = rank_symbols(s.df, kDistSyms, s.sorted_dist);
     }
-    if (tid == 0) {
-        const uint64_t fixed_bits = s.fixed_bits;
+    if (tid == 0) {  // the code lengths and the dynamic header: serial, on small alphabets
         bool dyn_ok = try_dynamic && lengths_from_sorted(s.lf, s.sorted_lit, m_lit, kLitSyms, 15, s.lit_len, s) &&
                       lengths_from_sorted(s.df, s.sorted_dist, m_dist, kDistSyms, 15, s.dist_len, s);
-        uint64_t dyn_bits = ~0ull;
         if (dyn_ok) {
             int nlit = kLitSyms, ndist = kDistSyms;
             while (nlit > 257 && s.lit_len[nlit - 1] == 0) nlit--;
@@ -533,39 +526,82 @@ __global__ void __launch_bounds__(kThreads, 2)
                     const uint32_t sym = s.rle[r] & 31;
                     hb += s.cl_len[sym] + (sym == 16 ? 2 : sym == 17 ? 3 : sym == 18 ? 7 : 0);
                 }
-                uint64_t pb = s.extra_bits;
-                for (int k = 0; k < kLitSyms; k++) pb += (uint64_t)s.lit_freq[k] * s.lit_len[k];
-                for (int k = 0; k < kDistSyms; k++) pb += (uint64_t)s.dist_freq[k] * s.dist_len[k];
-                dyn_bits      = hb + pb;
                 s.nlit        = nlit;
                 s.ndist       = ndist;
                 s.ncl         = ncl;
                 s.header_bits = (uint32_t)hb;
             }
         }
+        s.dyn_ok = dyn_ok;
+    }
+    __syncthreads();
+    // payload bits of the dynamic codes (block reduction), then the block type (thread 0)
+    if (s.dyn_ok) {
+        uint64_t pb = 0;
+        for (int k = tid; k < kLitSyms + kDistSyms; k += kThreads)
+            pb += k < kLitSyms ? (uint64_t)s.lit_freq[k] * s.lit_len[k]
+                               : (uint64_t)s.dist_freq[k - kLitSyms] * s.dist_len[k - kLitSyms];
+        for (int off = 16; off > 0; off >>= 1) pb += __shfl_xor_sync(0xffffffffu, pb, off);
+        if (lane == 0) s.pb_part[warp] = pb;
+    }
+    for (int i = tid; i < 3 * 16; i += kThreads) (&s.cnt[0][0])[i] = 0u;
+    __syncthreads();
+    if (tid == 0) {
+        uint64_t dyn_bits = ~0ull;
+        if (s.dyn_ok) {
+            dyn_bits = (uint64_t)s.header_bits + s.extra_bits;
+            for (int w = 0; w < kWarps; w++) dyn_bits += s.pb_part[w];
+        }
         // a dynamic or fixed block is followed by an empty stored block: 3 bits, pad, 4 bytes
         const uint64_t flush       = 3 + 7 + 32;
         const uint64_t stored_bits = 8 * (uint64_t)(5 + n);
         int bt        = 0;
         uint64_t best = stored_bits;
-        if (fixed_bits + flush < best) bt = 1, best = fixed_bits + flush;
-        if (dyn_ok && dyn_bits + flush < best) bt = 2, best = dyn_bits + flush;
+        if (s.fixed_bits + flush < best) bt = 1, best = s.fixed_bits + flush;
+        if (s.dyn_ok && dyn_bits + flush < best) bt = 2, best = dyn_bits + flush;
         s.btype = bt;
-        if (bt == 1) {
-            for (int k = 0; k < kLitSyms; k++) {
+        if (bt == 1) s.header_bits = 3;
+    }
+    __syncthreads();
+    if (s.btype == 1) {  // the fixed codes (RFC 1951 3.2.6)
+        for (int k = tid; k < kLitSyms + kDistSyms; k += kThreads) {
+            if (k < kLitSyms) {
                 s.lit_len[k]  = (uint8_t)fixed_lit_len(k);
                 s.lit_code[k] = (uint16_t)reverse_bits(fixed_lit_code(k), fixed_lit_len(k));
+            } else {
+                s.dist_len[k - kLitSyms]  = 5;
+                s.dist_code[k - kLitSyms] = (uint16_t)reverse_bits(k - kLitSyms, 5);
             }
-            for (int k = 0; k < kDistSyms; k++) {
-                s.dist_len[k]  = 5;
-                s.dist_code[k] = (uint16_t)reverse_bits(k, 5);
-            }
-            s.header_bits = 3;
-        } else if (bt == 2) {
-            build_codes(s.lit_len, kLitSyms, s.lit_code);
-            build_codes(s.dist_len, kDistSyms, s.dist_code);
-            build_codes(s.cl_len, kClSyms, s.cl_code);
         }
+    } else if (s.btype == 2) {  // canonical codes (RFC 1951 3.2.2) of the three alphabets
+        const uint8_t* lens[3] = {s.lit_len, s.dist_len, s.cl_len};
+        uint16_t* codes[3]     = {s.lit_code, s.dist_code, s.cl_code};
+        const int nsym[3]      = {kLitSyms, kDistSyms, kClSyms};
+        for (int k = tid; k < kLitSyms + kDistSyms + kClSyms; k += kThreads) {
+            const int a = k < kLitSyms ? 0 : (k < kLitSyms + kDistSyms ? 1 : 2);
+            const int i = k - (a == 0 ? 0 : a == 1 ? kLitSyms : kLitSyms + kDistSyms);
+            if (lens[a][i]) atomicAdd(&s.cnt[a][lens[a][i]], 1u);
+        }
+        __syncthreads();
+        if (tid < 3) {
+            uint32_t c = 0;
+            s.next[tid][0] = 0;
+            for (int l = 1; l < 16; l++) {
+                c              = (c + (l > 1 ? s.cnt[tid][l - 1] : 0u)) << 1;
+                s.next[tid][l] = c;
+            }
+        }
+        __syncthreads();
+        for (int k = tid; k < kLitSyms + kDistSyms + kClSyms; k += kThreads) {
+            const int a  = k < kLitSyms ? 0 : (k < kLitSyms + kDistSyms ? 1 : 2);
+            const int i  = k - (a == 0 ? 0 : a == 1 ? kLitSyms : kLitSyms + kDistSyms);
+            const int l  = lens[a][i];
+            uint32_t rnk = 0;  // symbols before i with the same length
+            if (l)
+                for (int j = 0; j < i; j++) rnk += lens[a][j] == l;
+            codes[a][i] = l ? (uint16_t)reverse_bits(s.next[a][l] + rnk, l) : 0;
+        }
+        (void)nsym;
     }
     __syncthreads();
     const int bt = s.btype;
