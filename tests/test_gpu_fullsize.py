@@ -48,6 +48,63 @@ def test_cesm_fullsize_matches_oracle(cuda):
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(oa, 8, 1024).view(np.uint32))
 
 
+def test_field_beyond_2_32_elements(cuda):
+    """2048 x 2048 x 1032 (4.33e9 elements, 17.3 GB): element indices, byte offsets and payload bit
+    offsets all pass 2^32.  Every plane from z = 1024 on starts at element index >= 2^32.  In abs
+    mode a Lorenzo block's codes and reconstruction depend only on its own values, so block-aligned
+    sub-boxes of the reconstruction must be bit-identical to the oracle's round trip of the same
+    sub-box.  One of them straddles index 2^32 and one is at the field's end, both with outliers.
+    The whole field is checked against the error bound."""
+    torch = cuda
+    nx, ny, nz = 2048, 2048, 1032
+    n = nx * ny * nz
+    assert n > 1 << 32
+    if torch.cuda.mem_get_info()[0] < 160 * 2**30:
+        pytest.skip("needs 160 GB of free device memory")
+    eb = 1e-3
+    z = torch.arange(nz, device="cuda", dtype=torch.float32).view(nz, 1, 1)
+    y = torch.arange(ny, device="cuda", dtype=torch.float32).view(1, ny, 1)
+    x = torch.arange(nx, device="cuda", dtype=torch.float32).view(1, 1, nx)
+    xt = (torch.sin(x * 0.0123) + torch.cos(y * 0.0071)) * (1.0 + 0.5 * torch.sin(z * 0.0037))
+    del x, y, z
+    flat = xt.view(-1)
+    flat[torch.arange(0, n, 999983, device="cuda")] += 1000.0  # outliers all over the field
+    boxes = [(slice(1016, 1032), slice(1000, 1064), slice(512, 768)),  # planes both sides of 2^32
+             (slice(1024, 1032), slice(1984, 2048), slice(1792, 2048))]  # the field's last block row
+    for zz, yy, xx in boxes:
+        xt[zz.start + 3, yy.start + 9, xx.start + 17] += 500.0
+        xt[zz.stop - 2, yy.stop - 5, xx.stop - 30] -= 300.0
+
+    codec = V.DeviceCodec((nx, ny, nz), eb=eb, mode="abs", dict_size=1024, block_size=8)
+    codec.compress(flat)
+    a1 = codec.archive_bytes()
+    r = codec.result_host()
+    assert r.n_outlier > n // 999983 and r.payload_bits > 1 << 32
+    codec.prepare_decompress(a1)
+    d_arch = torch.from_numpy(np.concatenate([np.frombuffer(a1, np.uint8), np.zeros(64, np.uint8)])).cuda()
+    del a1
+    out = torch.empty_like(flat)
+    codec.decompress(d_arch, out)
+    assert codec.decompress_status() == 0
+
+    step = 1 << 28
+    for s in range(0, n, step):
+        xs = flat[s: s + step].double()
+        err = (out[s: s + step].double() - xs).abs()
+        assert bool((err <= eb + 2.0 * xs.abs() * 2.0 ** -23).all()), f"error bound broken in [{s}, {s + step})"
+        del xs, err
+
+    out3 = out.view(nz, ny, nx)
+    for zz, yy, xx in boxes:
+        sub = xt[zz, yy, xx].contiguous().cpu().numpy().ravel()
+        dims = (xx.stop - xx.start, yy.stop - yy.start, zz.stop - zz.start)
+        oa, meta = O.compress(sub, dims, 8, 1024, eb, False)
+        assert meta["n_outlier"] > 0
+        want = O.decompress(oa, 8, 1024)
+        got = out3[zz, yy, xx].contiguous().cpu().numpy().ravel()
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 def test_adversarial_fullsize_matches_oracle(cuda):
     x = fields.adversarial_3d(256, 384, 384, seed=22).ravel()
     dims = (384, 384, 256)

@@ -61,6 +61,11 @@ def test_argument_checks():
     assert _bounds(bs=12)[0] == L.VSZ_ERR_UNSUPPORTED
     assert _bounds(bs=0)[0] == L.VSZ_ERR_INVALID
     assert _bounds(dims=(0, 4))[0] == L.VSZ_ERR_INVALID
+    # size limits: each dimension fits the archive's i32, at most 2^36 elements in all
+    assert _bounds(dims=(1 << 31,))[0] == L.VSZ_ERR_INVALID
+    assert _bounds(dims=((1 << 31) - 1,))[0] == L.VSZ_OK
+    assert _bounds(dims=(65536, 65536, 16))[0] == L.VSZ_OK
+    assert _bounds(dims=(65536, 65536, 17))[0] == L.VSZ_ERR_INVALID
     rc, ws, cap = _bounds(dims=(512, 512, 512))
     assert rc == 0 and ws > 512 ** 3 * 2 and cap > 512 ** 3 * 4
 
