@@ -982,13 +982,18 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 // longer than the primary table.  Decoded codes are packed in registers and stored 16 bytes per
 // lane per round.
 // ------------------------------------------------------------------------------------------
-constexpr int kWinMaxLen = 32;
-constexpr int kWinRound  = 8;
-constexpr int kWinRing   = 8;  // blocks of 16 bytes per lane
+constexpr int kWinMaxLen    = 32;
+constexpr int kWinRound     = 8;
+constexpr int kWinRing      = 8;    // blocks of 16 bytes per lane
+constexpr int kWinThreads   = 256;  // one primary table per CTA, shared by its warps
+constexpr int kWinMinBlocks = 4;
+constexpr size_t kWinSmem   = (sizeof(uint32_t) << kDecBits) + (size_t)(kWinThreads / 32) * kWinRing * 32 * 16;
 
-__global__ void __launch_bounds__(256, 4) k_huff_decode_win(HuffDecodeArgs a) {
-    __shared__ uint32_t s_table[1 << kDecBits];
-    __shared__ __align__(16) uint4 s_ring[8][kWinRing][32];
+__global__ void __launch_bounds__(kWinThreads, kWinMinBlocks) k_huff_decode_win(HuffDecodeArgs a) {
+    extern __shared__ __align__(16) uint8_t s_win_dyn[];
+    // [primary table: 1 << kDecBits words][ring: warp][slot][lane] x 16 bytes (kWinSmem bytes)
+    uint32_t* s_table                = reinterpret_cast<uint32_t*>(s_win_dyn);
+    uint4 (*s_ring)[kWinRing][32]    = reinterpret_cast<uint4 (*)[kWinRing][32]>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
     if (!a.tree_info || a.tree_info[2] > (uint32_t)kWinMaxLen) return;  // uniform: k_huff_decode_idx's trees
     for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
     __syncthreads();
@@ -1096,9 +1101,11 @@ __global__ void __launch_bounds__(256, 4) k_huff_decode_win(HuffDecodeArgs a) {
             zeros += (sy == 0u);
             off += len;
             // at most one word per codeword (len <= 32); refilled without a branch, because some
-            // lane of the warp crosses a word boundary on nearly every step
-            const bool adv    = off >= 32u;
-            const uint32_t nw = ring_word(wn);  // a slot not yet landed is read but not used
+            // lane of the warp crosses a word boundary on nearly every step.  Only the lanes that
+            // cross read the ring (a predicated load), so fewer lanes share its banks.
+            const bool adv = off >= 32u;
+            uint32_t nw    = w2;
+            if (adv) nw = ring_word(wn);
             off = adv ? off - 32u : off;
             w0  = adv ? w1 : w0;
             w1  = adv ? w2 : w1;
@@ -1566,7 +1573,9 @@ int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st) {
                          (reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0 && a.chunk_len;
     if (indexed) {
         if (a.tree_info) {
-            k_huff_decode_win<<<grid, 256, 0, st>>>(a);
+            static std::atomic<unsigned long long> attr_win{0};
+            smem_limit_once(k_huff_decode_win, (int)kWinSmem, attr_win);
+            k_huff_decode_win<<<(unsigned)((a.nchunks + kWinThreads - 1) / kWinThreads), kWinThreads, kWinSmem, st>>>(a);
             count_launch();
         }
         if (a.walk_smem) {
