@@ -776,13 +776,67 @@ def run_e2e(V, x, dims, eb, mode, dct, bs, steps, bytes_in, world, want=None, no
         ok = ok and all(bool(torch.equal(o.view(-1), w)) for o in h_outs)
     for op in ops:
         op.close()
-    return {"value": round(world * bytes_in / dt / 1e9, 2), "unit": "GB/s",
+    link = link_probe(h_ins[1 % nops], h_archs[1 % nops], h_outs[1 % nops], h_archs[2 % nops], arch_bytes, dt)
+    return {"value": round(world * bytes_in / dt / 1e9, 2), "unit": "GB/s", "link": link,
             "h2d_bytes_per_step": int(4 * n + arch_bytes), "d2h_bytes_per_step": int(arch_bytes + 4 * n),
             "ms_per_step": round(dt * 1e3, 3), "steps": steps,
             "api": f"vsz_host_op_compress / vsz_host_op_decompress on pinned host buffers, {nops} ops in a "
                    "software pipeline (step k+1's compress and step k's decompress in flight together)", "ok": ok,
             "sync": {"value": round(world * bytes_in / dt_sync / 1e9, 2), "ms_per_step": round(dt_sync * 1e3, 3),
                      "api": "vsz_compress_host_into + vsz_decompress_host_into (one call at a time)", "ok": ok_sync}}
+
+
+def link_probe(h_in, h_arch_in, h_out, h_arch_out, arch_bytes, step_s, reps=5):
+    """The host link on this machine, with one step's traffic: host to device the input and an
+    archive, device to host an archive and the output (plain stream copies between the pinned
+    buffers the step uses).  `duplex_ms` moves both directions at once, the time below which no
+    pipelined step can go; `e2e_frac` = that bound / the measured step."""
+    import torch
+    n_in = h_in.numel() * h_in.element_size()
+    d_in = torch.empty(n_in, dtype=torch.uint8, device="cuda")
+    d_ar = torch.empty(max(arch_bytes, 1), dtype=torch.uint8, device="cuda")
+    d_out = torch.empty(n_in, dtype=torch.uint8, device="cuda")
+    d_ar2 = torch.empty(max(arch_bytes, 1), dtype=torch.uint8, device="cuda")
+    hi, ho = h_in.view(torch.uint8), h_out.view(torch.uint8)
+    hai, hao = h_arch_in.view(torch.uint8)[:arch_bytes], h_arch_out.view(torch.uint8)[:arch_bytes]
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def up():
+        with torch.cuda.stream(s_up):
+            d_in.copy_(hi, non_blocking=True)
+            d_ar[:arch_bytes].copy_(hai, non_blocking=True)
+
+    def down():
+        with torch.cuda.stream(s_down):
+            hao.copy_(d_ar2[:arch_bytes], non_blocking=True)
+            ho.copy_(d_out, non_blocking=True)
+
+    def timed(fns):
+        ms = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record(s_up)
+            s_down.wait_event(e0)
+            for f in fns:
+                f()
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record(s_down)
+            s_up.wait_event(e1)
+            e2 = torch.cuda.Event(enable_timing=True)
+            e2.record(s_up)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e2))
+        return float(np.median(ms))
+
+    up_ms, down_ms, both_ms = timed([up]), timed([down]), timed([up, down])
+    nb = n_in + arch_bytes
+    del d_in, d_ar, d_out, d_ar2
+    return {"h2d_gbs": round(nb / up_ms / 1e6, 1), "d2h_gbs": round(nb / down_ms / 1e6, 1),
+            "duplex_ms": round(both_ms, 3), "duplex_gbs": round(2 * nb / both_ms / 1e6, 1),
+            "e2e_frac": round(both_ms / (step_s * 1e3), 3),
+            "what": "one step's copies (input + archive up, archive + output down) alone and both at once, "
+                    "stream copies between the step's pinned buffers"}
 
 
 def cpu_baseline(x, dims, eb, mode, dct, bs, max_bytes=None):
