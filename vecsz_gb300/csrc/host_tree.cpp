@@ -32,46 +32,67 @@ int host_huffman_build(const uint64_t* hist, int dict, uint64_t* cb_word, uint8_
     std::memset(cb_len, 0, (size_t)dict);
     info[0] = info[1] = info[2] = info[3] = 0u;
     if (nused == 0) return 1;  // the reference dereferences a null root here
-    // node freq (leaves then internal nodes in creation order), children of internal nodes
-    std::vector<uint64_t> freq((size_t)2 * nused);
+    // children of internal nodes (creation order); the heap holds (freq, node) pairs so that its
+    // comparisons read the entries themselves.  The operations and their order are the
+    // reference's (qinsert huffman.hh:169, qremove :179), so ties resolve the same way.
+    struct HeapEnt {
+        uint64_t f;
+        int32_t n;
+    };
     std::vector<int32_t> lch((size_t)nused), rch((size_t)nused);
-    std::vector<int32_t> heap((size_t)nused + 2);  // 1-based
+    // 1-based; qremove reads up to entry 4 i + 3 for a hole i with 2 i < qend <= nused + 1, so
+    // 2 nused + 6 entries (value-initialised) cover every read
+    std::vector<HeapEnt> heap(2 * (size_t)nused + 8);
     int qend = 1;
-    auto qinsert = [&](int n) {
+    auto qinsert = [&](uint64_t fn, int n) {
         int i = qend++, j;
-        const uint64_t fn = freq[n];
         while ((j = i >> 1)) {
-            if (freq[heap[j]] <= fn) break;
+            if (heap[j].f <= fn) break;
             heap[i] = heap[j];
             i       = j;
         }
-        heap[i] = n;
+        heap[i] = HeapEnt{fn, n};
     };
-    auto qremove = [&]() -> int {
-        const int n = heap[1];
+    // The hole always sinks to the bottom (no early exit), moving up the smaller child, the left
+    // one on a tie.  Two levels per pass: this level's choice and both possible choices of the
+    // next level come from loads that do not wait on each other, and only the final select does.
+    // No entry read is written in the same pass (the hole i is above its grandchildren 4 i ..
+    // 4 i + 3), so each choice sees the values the one-level loop would see.  Reads at or past
+    // qend are masked out of the choice.
+    auto qremove = [&]() -> HeapEnt {
+        const HeapEnt top = heap[1];
         qend--;
-        int i = 1, l;
-        while ((l = i << 1) < qend) {
-            if (l + 1 < qend && freq[heap[l + 1]] < freq[heap[l]]) l++;
-            heap[i] = heap[l];
-            i       = l;
+        int i = 1;
+        for (;;) {
+            const int l = i << 1;
+            if (l >= qend) break;
+            const int g   = l << 1;
+            const bool p  = (l + 1 < qend) & (heap[l + 1].f < heap[l].f);
+            const bool p0 = (g + 1 < qend) & (heap[g + 1].f < heap[g].f);
+            const bool p1 = (g + 3 < qend) & (heap[g + 3].f < heap[g + 2].f);
+            const int c   = l + (int)p;
+            heap[i]       = heap[c];
+            const int gc  = c << 1;  // g, or g + 2 when the right child moved up
+            if (gc >= qend) {
+                i = c;
+                break;
+            }
+            const int cc = gc + (int)(p ? p1 : p0);
+            heap[c]      = heap[cc];
+            i            = cc;
         }
         heap[i] = heap[qend];
-        return n;
+        return top;
     };
-    for (int i = 0; i < nused; i++) {
-        freq[i] = hist[used[i]];
-        qinsert(i);
-    }
+    for (int i = 0; i < nused; i++) qinsert(hist[used[i]], i);
     int nnodes = nused;
     while (qend > 2) {
-        const int r = qremove();
-        const int l = qremove();
-        const int v = nnodes++;
-        lch[v - nused] = l;
-        rch[v - nused] = r;
-        freq[v]        = freq[l] + freq[r];
-        qinsert(v);
+        const HeapEnt r = qremove();
+        const HeapEnt l = qremove();
+        const int v     = nnodes++;
+        lch[v - nused]  = l.n;
+        rch[v - nused]  = r.n;
+        qinsert(l.f + r.f, v);
     }
     // subtree sizes bottom-up, then preorder index / codeword / depth top-down
     const int nint = nnodes - nused;
