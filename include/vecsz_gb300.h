@@ -10,7 +10,8 @@
  * = dict_size / 2), block_size its `-b`, eb its `-e`, mode its `-m`.
  *
  * Each entry point names the reference function (szcompressor/vecSZ, file:line) it replaces.
- * The ctypes bindings a Python caller uses, and the C++ a host caller adds, are in INTEGRATION.md.
+ * The library ships a ctypes binding (vecsz_gb300/_lib.py) for Python callers; C and C++ callers
+ * include this header and link libvecsz_gb300.so.
  */
 #ifndef VECSZ_GB300_H
 #define VECSZ_GB300_H
@@ -178,10 +179,13 @@ vsz_status vsz_outlier_gather(int ndim, const size_t dims[3], const uint8_t* d_s
  * synchronisation, a plugin host that only hands over input and output buffers): it takes no
  * workspace and allocates nothing.  No counterpart in the reference.  Its scratch is a static
  * device array of about 512 KiB that every GPU loading this library holds until exit; fields with
- * more than 2^28 row segments (vsz_outlier_segments) are rejected with VSZ_ERR_CAPACITY.  The first
- * call on each device looks up the array's device address, so make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU (different streams,
- * or different host threads) race and must be serialised by the caller. */
+ * more than 2^28 row segments (vsz_outlier_segments) are rejected with VSZ_ERR_CAPACITY, and dims
+ * outside the limits of vsz_outlier_gather (each <= 2^31 - 1, at most 2^36 elements) with
+ * VSZ_ERR_INVALID.  Every call looks up the array's device address on the current device (it is
+ * not cached, so a reset device is handled); the first call on a device may load the library's
+ * device code, so make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (different streams, or different host threads) race and must be serialised
+ * by the caller. */
 vsz_status vsz_outlier_gather_noalloc(int ndim, const size_t dims[3], const uint8_t* d_seg_count,
                                       const float* d_scratch, float* d_out, uint64_t* d_count, void* stream);
 
@@ -339,8 +343,10 @@ typedef struct vsz_server vsz_server;
 vsz_status vsz_server_create(size_t budget_bytes, int slots, vsz_server** server);
 /* Non-blocking; VSZ_ERR_CAPACITY when the request could never fit in the budget. */
 vsz_status vsz_server_submit(vsz_server* server, const vsz_request* request, uint64_t* ticket);
-/* Blocks until the request completed (VSZ_ERR_TIMEOUT after timeout_s). */
+/* Blocks until the request completed (VSZ_ERR_TIMEOUT after timeout_s).  VSZ_ERR_INVALID for an
+ * unknown ticket, or when another thread releases the ticket while this one waits. */
 vsz_status vsz_server_wait(vsz_server* server, uint64_t ticket, double timeout_s, vsz_completion* done);
+/* Frees a completed request's output and forgets its ticket (VSZ_ERR_INVALID before completion). */
 vsz_status vsz_server_release(vsz_server* server, uint64_t ticket);
 /* Withdraws a request that is still queued: it completes at once with status VSZ_ERR_CANCELLED and
  * no output (wait returns it; release it as any other).  VSZ_ERR_UNSUPPORTED once the request has

@@ -32,9 +32,9 @@ def build(quiet: bool = True) -> str:
 
 
 def build_ref() -> str | None:
-    """Compile the reference itself (x86-64 with the reference sources present only)."""
-    ref_src = os.environ.get("VSZ_REFERENCE_SRC", "/root/reference")
-    if not os.path.isdir(os.path.join(ref_src, "src")):
+    """Compile the reference itself (x86-64 only) from the sources VSZ_REFERENCE_SRC points at."""
+    ref_src = os.environ.get("VSZ_REFERENCE_SRC")
+    if not ref_src or not os.path.isdir(os.path.join(ref_src, "src")):
         return None
     import platform
 

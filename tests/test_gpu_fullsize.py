@@ -1,7 +1,9 @@
 """The named single-field configurations at their full sizes, through the C ABI:
-  * 512^3 NYX-like field, r2r 1e-4 and 1e-3 -- size-independent properties (deterministic archive,
-    error bound within the reference's two-ulp overshoot, indexed and self-synchronising decoders
-    agree, the trailer-free packed block decodes to the same field);
+  * 512^3 NYX-like field, r2r 1e-4 and 1e-3 -- the benchmark's own field (seed 1000): packed block
+    byte-identical to the oracle's and reconstruction bit-identical; and on another seed the
+    size-independent properties (deterministic archive, error bound within the reference's two-ulp
+    overshoot, indexed and self-synchronising decoders agree, the trailer-free packed block decodes
+    to the same field);
   * 1800x3600 CESM-like field (abs 1e-4) and 256x384x384 adversarial field (abs 1e-6: many
     outliers, a flat histogram, long codewords) -- packed blocks byte-identical to the oracle's and
     reconstructions bit-identical."""
@@ -38,6 +40,29 @@ def test_nyx512_roundtrip_properties(cuda, eb):
     # trailer-free bytes: self-synchronising decode, same field
     y = V.decompress(a1[: r.data_size], r.data_size, 0, 1024, 8, "r2r", codec._desc.value_range)
     assert torch.equal(torch.from_numpy(y).cuda().view(torch.int32), out.view(torch.int32))
+
+
+@pytest.mark.parametrize("eb", [1e-4, 1e-3])
+def test_nyx512_bench_field_matches_oracle(cuda, eb):
+    """The field bench.py times (512^3 NYX-like, seed 1000, r2r, dict 1024, block 8)."""
+    torch = cuda
+    xt = fields.grf_3d_torch(512, 512, 512, seed=1000).reshape(-1)
+    x = xt.cpu().numpy()
+    dims = (512, 512, 512)
+    codec = V.DeviceCodec(dims, eb=eb, mode="r2r", dict_size=1024, block_size=8)
+    codec.compress(xt)
+    r = codec.result_host()
+    a1 = codec.archive_bytes()
+    oa, meta = O.compress(x, dims, 8, 1024, eb, True)
+    assert r.n_outlier == meta["n_outlier"]
+    assert a1[: r.data_size] == oa
+    codec.prepare_decompress(a1)
+    out = torch.empty_like(xt)
+    d_arch = torch.from_numpy(np.concatenate([np.frombuffer(a1, np.uint8), np.zeros(64, np.uint8)])).cuda()
+    codec.decompress(d_arch, out)
+    assert codec.decompress_status() == 0
+    want = O.decompress(oa, 8, 1024, O.value_range(x))
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), want.view(np.uint32))
 
 
 def test_cesm_fullsize_matches_oracle(cuda):

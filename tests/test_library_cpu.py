@@ -70,6 +70,16 @@ def test_argument_checks():
     assert rc == 0 and ws > 512 ** 3 * 2 and cap > 512 ** 3 * 4
 
 
+def test_noalloc_gather_refuses_dims_before_any_device_call():
+    """The allocation-free gather applies the same field limits as the allocating one, on the host,
+    before it touches the device: dims above 2^31 - 1 or a product above 2^36 elements are refused."""
+    lib = V.lib()
+    fake = C.c_void_p(16)  # never dereferenced: the checks come first
+    for dims in ((65536, 65536, 17), (1 << 31, 1, 1), (0, 5, 5), ((1 << 31) - 1, (1 << 31) - 1, 2)):
+        rc = lib.vsz_outlier_gather_noalloc(3, L.dims_arg(dims), fake, fake, fake, fake, None)
+        assert rc == L.VSZ_ERR_INVALID, dims
+
+
 @pytest.mark.parametrize("name", golden_cases())
 def test_archive_parse_matches_oracle(name):
     g = load_golden(name)

@@ -118,7 +118,8 @@ def test_oracle_b1_tail_columns_zeroed():
     assert np.all(xhat[:, :16] != 0.0)
 
 
-ref_only = pytest.mark.skipif(not (O.ref_available() or os.path.isdir("/root/reference/src")),
+ref_only = pytest.mark.skipif(not (O.ref_available() or
+                                   os.path.isdir(os.path.join(os.environ.get("VSZ_REFERENCE_SRC", ""), "src"))),
                               reason="reference sources not available (pinned by the golden fixtures instead)")
 
 

@@ -18,9 +18,9 @@
 //   2D tail columns (d0 % 8 != 0): code 0, outlier 0.0 -- the reference skips those AVX chunks
 //   and never runs its scalar tail (src/dualquant.hh:490-495).
 #include <cstdint>
-#include <mutex>
 #include <type_traits>
 
+#include "api_common.cuh"
 #include "scan.cuh"
 #include "vsz_device.cuh"
 #include "vsz_kernels.h"
@@ -1016,25 +1016,16 @@ constexpr size_t kNoAllocGatherBytes      = 256 + 8 * (kNoAllocGatherMaxTiles + 
 
 static __device__ __align__(256) uint8_t g_noalloc_gather_scratch[kNoAllocGatherBytes];
 
-namespace {
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64];  // device address of g_noalloc_gather_scratch, per device
-}  // namespace
-
-// Set-up, once per device, with that device current: the array's name is only a host-side stand-in
-// in host code, so its device address comes from cudaGetSymbolAddress.
+// The array's name is only a host-side stand-in in host code; its device address comes from
+// cudaGetSymbolAddress with the device current.  It is looked up on every call (a table lookup in
+// the runtime, no allocation), never cached: after cudaDeviceReset, or a primary context torn down
+// and recreated, the library's device code is loaded again and the array may move.  The first call
+// on a device may load that code, so make it before any stream capture.
 static int noalloc_gather_scratch(uint8_t** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return VSZ_ERR_CUDA;
-    if (dev < 0 || dev >= 64) return VSZ_ERR_NO_DEVICE;
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void* p        = nullptr;
-        cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_gather_scratch);
-        if (rc != cudaSuccess || !p) return VSZ_ERR_CUDA;
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = reinterpret_cast<uint8_t*>(g_noalloc_ptr[dev]);
+    void* p        = nullptr;
+    cudaError_t rc = cudaGetSymbolAddress(&p, g_noalloc_gather_scratch);
+    if (rc != cudaSuccess || !p) return VSZ_ERR_CUDA;
+    *out = reinterpret_cast<uint8_t*>(p);
     return VSZ_OK;
 }
 
@@ -1044,9 +1035,8 @@ extern "C" vsz_status vsz_outlier_gather_noalloc(int ndim, const size_t dims[3],
                                                  const float* d_scratch, float* d_out, uint64_t* d_count,
                                                  void* stream) {
     using namespace vsz;
-    if (ndim < 1 || ndim > 3 || !dims || !d_seg_count || !d_scratch || !d_out || !d_count) return VSZ_ERR_INVALID;
-    for (int i = 0; i < ndim; i++)
-        if (dims[i] == 0 || dims[i] > 0x7fffffffu) return VSZ_ERR_INVALID;
+    // the same field limits as vsz_outlier_gather: each dim <= 2^31 - 1, at most 2^36 elements
+    if (!api::valid_dims(ndim, dims) || !d_seg_count || !d_scratch || !d_out || !d_count) return VSZ_ERR_INVALID;
     Geometry g = make_geometry(ndim, dims);
     if (g.nseg > kNoAllocGatherMaxSegments) return VSZ_ERR_CAPACITY;  // beyond the static scratch
     uint8_t* base = nullptr;

@@ -222,8 +222,11 @@ void dispatch_loop(vsz_server* s) {
         s->slots[(size_t)slot].busy = 1;
         lk.unlock();
         int rc = launch_job(s, j);
+        // A failed launch may have queued some of its kernels and copies before the step that
+        // failed: let them finish before the job's arena memory goes to the next request.
+        if (rc != VSZ_OK) cudaStreamSynchronize(s->slots[(size_t)slot].stream);
         lk.lock();
-        if (rc != VSZ_OK) {  // nothing was enqueued behind the failure: complete it here
+        if (rc != VSZ_OK) {  // no completion function was enqueued: complete it here
             s->arena->release(j->ws_off, j->ws_bytes);
             s->arena->release(j->out_off, j->out_bytes);
             j->out_bytes = 0;
@@ -301,11 +304,18 @@ vsz_status vsz_server_submit(vsz_server* s, const vsz_request* r, uint64_t* tick
 vsz_status vsz_server_wait(vsz_server* s, uint64_t ticket, double timeout_s, vsz_completion* c) {
     if (!s || !c) return VSZ_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->jobs.find(ticket);
-    if (it == s->jobs.end()) return VSZ_ERR_INVALID;
-    Job* j = it->second;
+    if (s->jobs.find(ticket) == s->jobs.end()) return VSZ_ERR_INVALID;
+    // The job is looked up again on every wake-up: another thread may release the ticket while
+    // this one waits, and then the job no longer exists.
+    Job* j = nullptr;
     const auto until = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
-    if (!s->cv.wait_until(lk, until, [&] { return j->state == 2; })) return VSZ_ERR_TIMEOUT;
+    const bool woke  = s->cv.wait_until(lk, until, [&] {
+        auto it = s->jobs.find(ticket);
+        j       = it == s->jobs.end() ? nullptr : it->second;
+        return !j || j->state == 2;
+    });
+    if (!woke) return VSZ_ERR_TIMEOUT;
+    if (!j) return VSZ_ERR_INVALID;  // released by another thread meanwhile
     c->status    = j->status;
     c->d_out     = j->out_bytes ? s->base + j->out_off : nullptr;
     c->out_bytes = j->out_keep;
