@@ -128,6 +128,8 @@ typedef struct vsz_archive_desc {
     uint64_t index_offset;  /* trailer: byte offset of u16 bits-per-chunk, 8-byte aligned */
     uint64_t trailer_size;
     int strict;             /* trailer: written in strict error-bound mode (VSZ_FLAG_STRICT_EB) */
+    int32_t s_lo, s_hi;     /* trailer (version 2): bounds of the prequantized values, s_lo > s_hi
+                               when unknown; decompress tabulates the dequantization over them */
 } vsz_archive_desc;
 
 /* Options a decompressor needs that the packed block does not store (the reference takes them
@@ -293,6 +295,34 @@ vsz_status vsz_batch_set_task_sizes(vsz_batch* batch, int dq_units, int enc_chun
 vsz_status vsz_batch_autotune(vsz_batch* batch, int iterations, int* best_dq_units, int* best_enc_chunks,
                               void* stream);
 
+/* ---- many archives at once: the batched decompress ----------------------------------------
+ * Archives written by this library (packed block + trailer with the decode index), of any shapes,
+ * dimensionalities, error bounds and dictionary sizes, decompressed in a handful of launches: the
+ * Huffman tables one CTA per field in one launch, both index scans once over all fields' chunks,
+ * decoding and the reverse Lorenzo over block-wide tasks of many fields per launch.  Every field's
+ * output and status are the same as vsz_decompress of that archive alone.  Block size 8 without
+ * padding and without strict mode only (VSZ_ERR_UNSUPPORTED otherwise; vsz_decompress takes the
+ * rest).  No counterpart in the reference, which decompresses one field per process
+ * (Decompress, src/vecsz_interface.hh:232-374).
+ *
+ * vsz_dbatch_create lays out the caller's workspace (vsz_dbatch_workspace_bytes) and uploads the
+ * argument tables and task lists once (synchronous; it allocates them).  vsz_dbatch_decompress then
+ * only enqueues device work on `stream` -- memsets and launches, no host synchronisation and no
+ * allocation -- so it may be captured in a CUDA graph; each call decompresses the current contents
+ * of the archives' device buffers, which must still parse as `desc` says.  d_status: one int per
+ * field (device), the field's status after each call. */
+typedef struct vsz_dbatch_field {
+    const uint8_t* d_archive;  /* device archive bytes (16 readable bytes past its end) */
+    vsz_archive_desc desc;     /* vsz_archive_parse of the same bytes */
+    float* d_out;              /* device output: dims[0] * dims[1] * dims[2] floats */
+} vsz_dbatch_field;
+typedef struct vsz_dbatch vsz_dbatch;
+vsz_status vsz_dbatch_workspace_bytes(const vsz_dbatch_field* fields, int nfields, size_t* ws_bytes);
+vsz_status vsz_dbatch_create(const vsz_dbatch_field* fields, int nfields, void* d_ws, size_t ws_bytes, int* d_status,
+                             vsz_dbatch** batch);
+vsz_status vsz_dbatch_decompress(vsz_dbatch* batch, void* stream);
+void vsz_dbatch_destroy(vsz_dbatch* batch);
+
 /* GPU block-size autotuner (autotune_block_sizes, src/autotune.hh:80-96; the CLI's -a): times the
  * dual-quant kernel on a leading slab of the field (sample_percent of the slowest axis, at least 64
  * planes / rows, 64K elements in 1D) at block sizes 8, 16, 32 and 64, `iterations` runs each after
@@ -304,6 +334,33 @@ vsz_status vsz_autotune_workspace_bytes(const vsz_params* p, int ndim, const siz
 vsz_status vsz_autotune_block_size(const vsz_params* p, int ndim, const size_t dims[3], const float* d_in,
                                    double sample_percent, int iterations, void* d_ws, size_t ws_bytes,
                                    int* best_block_size, double timings_ms[4], void* stream);
+
+/* Field autotuner, extending autotune_block_sizes (src/autotune.hh:22-126): the block size changes
+ * the histogram, the tree, the encoder's and decoder's work and the archive's size, so each
+ * candidate (8, 16, 32, 64) is timed through vsz_compress and vsz_decompress on the leading slab
+ * (sample_percent of the slowest axis, at least 64 planes / rows, 64K elements in 1D), `iterations`
+ * runs each after one warm-up (CUDA events on `stream`; synchronising), and scored by
+ *     compress ms + decompress ms + archive bytes / (link_gbs GB/s)
+ * -- the time to compress, move the archive over a link and decompress (link_gbs = 0: speed
+ * alone).  The lowest score wins.  Results are cached process-wide per (dimensionality, size class
+ * ceil(log2 elements), eb class floor(2 log10 eb), mode, dictionary, link rate, flags and
+ * padding): a later field of the same class returns the cached result with cached = 1 and times
+ * nothing.  d_ws: vsz_autotune_bounds bytes. */
+typedef struct vsz_tune_result {
+    int block_size;             /* the choice */
+    int cached;                 /* 1: taken from the cache */
+    uint64_t sample_elements;   /* elements of the slab timed */
+    double compress_ms[4];      /* per candidate 8, 16, 32, 64: ms per run on the slab */
+    double decompress_ms[4];
+    uint64_t archive_bytes[4];  /* packed block bytes of the slab */
+    double score_ms[4];
+} vsz_tune_result;
+vsz_status vsz_autotune_bounds(const vsz_params* p, int ndim, const size_t dims[3], double sample_percent,
+                               size_t* ws_bytes);
+vsz_status vsz_autotune(const vsz_params* p, int ndim, const size_t dims[3], const float* d_in, double sample_percent,
+                        int iterations, double link_gbs, void* d_ws, size_t ws_bytes, vsz_tune_result* result,
+                        void* stream);
+void vsz_autotune_cache_clear(void);
 
 /* The same search on a field in host memory (copied to the device first): what the command line's
  * -a runs. */
@@ -465,6 +522,18 @@ int vsz_profile_read(double* ms, int* counts, const char** names, int max_stages
 /* Kernels this library has launched in this process, all entry points and devices together (a
  * relaxed atomic count taken at each launch).  No counterpart in the reference. */
 uint64_t vsz_launch_count(void);
+
+/* ---- test hooks: no counterpart in the reference ---------------------------------------------
+ * Every cross-CTA wait of this library (the decoupled look-back of the outlier gather, the
+ * encoder's chunk scan and the device-wide scans) polls at most a bounded number of times, then
+ * records VSZ_ERR_TIMEOUT in the call's status word and returns instead of hanging.
+ * vsz_debug_set_spin_limit sets that bound for every kernel of the library (polls <= 0: the
+ * default, 2^22); process-wide, synchronous.  vsz_debug_scan_stalled_predecessor runs the
+ * device-wide scan over n (<= 2^24) values with its tile ticket started past tile 0, so one tile
+ * waits on a predecessor that never publishes; it allocates, synchronises and stores the scan's
+ * status word (VSZ_ERR_TIMEOUT when the wait ran out) in *h_status. */
+vsz_status vsz_debug_set_spin_limit(long long polls);
+vsz_status vsz_debug_scan_stalled_predecessor(size_t n, int* h_status);
 
 #ifdef __cplusplus
 }

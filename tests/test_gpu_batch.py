@@ -111,3 +111,33 @@ def test_block_size_autotuner(cuda):
     best, t = autotune_block_size(x, (128, 80, 96), eb=1e-4, mode="r2r", sample_percent=50.0, iterations=2)
     assert best in (8, 16, 32, 64) and all(v > 0 for v in t.values())
     assert t[best] == min(t.values())
+
+
+def test_field_autotuner_scores_whole_round_trip_and_caches(cuda):
+    """vsz_autotune times compress + decompress per block size, scores the archive's transfer at
+    the given link rate, and caches the choice per field class: a second field of the same class
+    (same dimensionality, size class and eb class) returns the cached result without timing."""
+    from vecsz_gb300.api import autotune, autotune_cache_clear
+    autotune_cache_clear()
+    x = cuda.from_numpy(fields.grf_3d(96, 80, 128, seed=4).ravel()).cuda()
+    r1 = autotune(x, (128, 80, 96), eb=1e-4, mode="r2r", sample_percent=50.0, iterations=2, link_gbs=25.0)
+    assert not r1["cached"] and r1["block_size"] in (8, 16, 32, 64)
+    for k in range(4):
+        assert r1["compress_ms"][k] > 0 and r1["decompress_ms"][k] > 0 and r1["archive_bytes"][k] > 0
+        want = r1["compress_ms"][k] + r1["decompress_ms"][k] + r1["archive_bytes"][k] / 25e9 * 1e3
+        assert abs(r1["score_ms"][k] - want) < 1e-9 * max(1.0, want)
+    assert r1["score_ms"][[8, 16, 32, 64].index(r1["block_size"])] == min(r1["score_ms"])
+    # the same class (96 x 80 x 120: same log2 size class, same eb class): a cache hit, same choice
+    y = cuda.from_numpy(fields.grf_3d(80, 80, 120, seed=5).ravel()).cuda()
+    r2 = autotune(y, (120, 80, 80), eb=2e-4, mode="r2r", sample_percent=50.0, iterations=2, link_gbs=25.0)
+    assert r2["cached"] and r2["block_size"] == r1["block_size"] and r2["score_ms"] == r1["score_ms"]
+    # another class (2D): timed afresh; speed alone (no link) is a separate class too
+    z = cuda.from_numpy(fields.bump_field_2d(300, 500, seed=6).ravel()).cuda()
+    r3 = autotune(z, (500, 300), eb=1e-4, mode="r2r", sample_percent=100.0, iterations=1, link_gbs=25.0)
+    assert not r3["cached"]
+    r4 = autotune(x, (128, 80, 96), eb=1e-4, mode="r2r", sample_percent=50.0, iterations=1, link_gbs=0.0)
+    assert not r4["cached"]
+    assert r4["score_ms"] == [c + d for c, d in zip(r4["compress_ms"], r4["decompress_ms"])]
+    autotune_cache_clear()
+    r5 = autotune(x, (128, 80, 96), eb=1e-4, mode="r2r", sample_percent=50.0, iterations=1, link_gbs=25.0)
+    assert not r5["cached"]

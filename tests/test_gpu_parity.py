@@ -279,6 +279,25 @@ def test_long_codewords_general_decoder(cuda, monkeypatch):
     test_long_codewords_match_oracle(cuda)
 
 
+def test_long_codewords_dict4096_match_oracle(cuda):
+    """Dictionary 4096 and a last chunk of 265 codes: the window decoder's secondary table and its
+    tree walk, for codewords over 12 and 20 bits."""
+    rng = np.random.default_rng(78)
+    n = (1 << 21) + 777
+    k = np.minimum(rng.geometric(0.45, n) - 1, 30)
+    d = k * rng.choice(np.array([-1, 1]), n)
+    x = np.cumsum(d).astype(np.float64)
+    x = np.clip(x - np.round(x.mean()), -1e6, 1e6).astype(np.float32)
+    a_or, meta = O.compress(x, (n,), 8, 4096, 0.5, False)
+    lens, *_ = O.huffman_codebook(np.bincount(O.dualquant(x, (n,), 8, 4096, 0.5)[0], minlength=4096).astype(np.uint64),
+                                  4096)
+    assert lens.max() > 20 and lens.max() <= 32
+    c = V.compress(x, (n,), 0.5, "abs", 4096, 8)
+    assert c.data[: c.data_size] == a_or
+    y_or = O.decompress(a_or, 8, 4096)
+    np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y_or.view(np.uint32))
+
+
 @pytest.mark.parametrize("dims,bs", [((96, 40), 8), ((37, 41, 43), 8), ((5000,), 16), ((64, 64, 16), 16)])
 def test_nan_inputs_keep_reference_bits(cuda, dims, bs):
     """NaN inputs (quiet with payloads, negative, signalling): the reference's arithmetic keeps a

@@ -69,7 +69,17 @@ class ArchiveDesc(C.Structure):
                 ("data_size", C.c_uint64), ("has_trailer", C.c_int), ("eb_final", C.c_double),
                 ("value_range", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
                 ("chunk_syms", C.c_uint32), ("n_chunks", C.c_uint64), ("index_offset", C.c_uint64),
-                ("trailer_size", C.c_uint64), ("strict", C.c_int)]
+                ("trailer_size", C.c_uint64), ("strict", C.c_int), ("s_lo", C.c_int32), ("s_hi", C.c_int32)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("block_size", C.c_int), ("cached", C.c_int), ("sample_elements", C.c_uint64),
+                ("compress_ms", C.c_double * 4), ("decompress_ms", C.c_double * 4),
+                ("archive_bytes", C.c_uint64 * 4), ("score_ms", C.c_double * 4)]
+
+
+class DBatchField(C.Structure):
+    _fields_ = [("d_archive", C.c_void_p), ("desc", ArchiveDesc), ("d_out", C.c_void_p)]
 
 
 class DecompressOpts(C.Structure):
@@ -111,12 +121,21 @@ _PROTOS = {
     "vsz_huffman_build_host": ([_p, _i, _p, _p, _p], _i),
     "vsz_set_tree_builder": ([_i], _i),
     "vsz_launch_count": ([], C.c_uint64),
+    "vsz_debug_set_spin_limit": ([C.c_longlong], _i),
+    "vsz_debug_scan_stalled_predecessor": ([_sz, C.POINTER(C.c_int)], _i),
     "vsz_batch_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t)], _i),
     "vsz_batch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
     "vsz_batch_compress": ([_p, _p], _i),
     "vsz_batch_destroy": ([_p], None),
     "vsz_batch_set_task_sizes": ([_p, _i, _i], _i),
     "vsz_batch_autotune": ([_p, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _p], _i),
+    "vsz_autotune_bounds": ([_p, _i, C.POINTER(C.c_size_t), C.c_double, C.POINTER(C.c_size_t)], _i),
+    "vsz_autotune": ([_p, _i, C.POINTER(C.c_size_t), _p, C.c_double, _i, C.c_double, _p, _sz, _p, _p], _i),
+    "vsz_autotune_cache_clear": ([], None),
+    "vsz_dbatch_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t)], _i),
+    "vsz_dbatch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
+    "vsz_dbatch_decompress": ([_p, _p], _i),
+    "vsz_dbatch_destroy": ([_p], None),
     "vsz_autotune_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t), _d, C.POINTER(C.c_size_t)], _i),
     "vsz_autotune_block_size": ([_p, _i, C.POINTER(C.c_size_t), _p, _d, _i, _p, _sz, C.POINTER(C.c_int),
                                  C.POINTER(C.c_double), _p], _i),

@@ -355,6 +355,90 @@ class BatchCompressor:
             pass
 
 
+class BatchDecompressor:
+    """Many archives decompressed in one launch sequence (vsz_dbatch_*).
+
+    archives: list of archives written by this library (bytes, or CUDA uint8 tensors with 16 readable
+    bytes past the archive); block size 8, no padding, not strict.  The outputs land in per-field
+    float32 tensors (self.outputs[i]); decompress() may be called repeatedly (or captured in a CUDA
+    graph) and decodes the current contents of the archive buffers."""
+
+    def __init__(self, archives, descs=None, device="cuda"):
+        """descs (optional): vsz_archive_parse of each archive, for device archives whose bytes
+        should not be copied back to parse them."""
+        torch = _torch()
+        from ._lib import DBatchField
+        self.n = len(archives)
+        arr = (DBatchField * self.n)()
+        self.d_archives, self.outputs, self.descs = [], [], []
+        for i, a in enumerate(archives):
+            if isinstance(a, (bytes, bytearray)):
+                desc = parse_archive(a) if descs is None else descs[i]
+                d = torch.from_numpy(np.frombuffer(bytes(a) + bytes(64), np.uint8).copy()).to(device)
+            else:
+                desc = parse_archive(a.cpu().numpy().tobytes()) if descs is None else descs[i]
+                d = a
+            n = int(desc.dims[0]) * int(desc.dims[1]) * int(desc.dims[2])
+            out = torch.empty(n, dtype=torch.float32, device=device)
+            self.d_archives.append(d)
+            self.outputs.append(out)
+            self.descs.append(desc)
+            arr[i].d_archive = _ptr(d).value
+            arr[i].desc = desc
+            arr[i].d_out = _ptr(out).value
+        self._arr = arr
+        ws = C.c_size_t(0)
+        check(lib().vsz_dbatch_workspace_bytes(arr, self.n, C.byref(ws)), "dbatch_workspace_bytes")
+        self.ws = torch.empty(ws.value, dtype=torch.uint8, device=device)
+        self.status = torch.zeros(max(self.n, 1), dtype=torch.int32, device=device)
+        h = C.c_void_p(0)
+        check(lib().vsz_dbatch_create(arr, self.n, _ptr(self.ws), self.ws.numel(), _ptr(self.status), C.byref(h)),
+              "dbatch_create")
+        self._h = h
+
+    def decompress(self, stream=None) -> None:
+        check(lib().vsz_dbatch_decompress(self._h, _stream_ptr(stream)), "dbatch_decompress")
+
+    def statuses(self):
+        return [int(v) for v in self.status[: self.n].cpu().tolist()]
+
+    def close(self) -> None:
+        if self._h:
+            lib().vsz_dbatch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune(d_in, dims, eb=1e-4, mode="abs", dict_size=1024, sample_percent=10.0, iterations=2, link_gbs=0.0,
+             stream=None) -> dict:
+    """Field autotuner (vsz_autotune): each block size timed through compress + decompress on a
+    leading slab and scored with the archive's transfer time over a link of link_gbs GB/s; cached
+    per field class.  Returns the vsz_tune_result as a dict."""
+    torch = _torch()
+    from ._lib import TuneResult
+    dims = tuple(int(v) for v in dims)
+    p = make_params(eb, mode, dict_size, 8)
+    ws = C.c_size_t(0)
+    check(lib().vsz_autotune_bounds(C.byref(p), len(dims), dims_arg(dims), float(sample_percent), C.byref(ws)),
+          "autotune_bounds")
+    d_ws = torch.empty(ws.value, dtype=torch.uint8, device=d_in.device)
+    r = TuneResult()
+    check(lib().vsz_autotune(C.byref(p), len(dims), dims_arg(dims), _ptr(d_in), float(sample_percent), int(iterations),
+                             float(link_gbs), _ptr(d_ws), ws.value, C.byref(r), _stream_ptr(stream)), "autotune")
+    return {"block_size": r.block_size, "cached": bool(r.cached), "sample_elements": int(r.sample_elements),
+            "candidates": [8, 16, 32, 64], "compress_ms": list(r.compress_ms), "decompress_ms": list(r.decompress_ms),
+            "archive_bytes": [int(v) for v in r.archive_bytes], "score_ms": list(r.score_ms)}
+
+
+def autotune_cache_clear() -> None:
+    lib().vsz_autotune_cache_clear()
+
+
 def autotune_block_size(d_in, dims, eb=1e-4, mode="abs", dict_size=1024, sample_percent=10.0, iterations=3):
     """GPU block-size autotuner (vsz_autotune_block_size, the CLI's -a): (best block size,
     {8: ms, 16: ms, 32: ms, 64: ms})."""

@@ -43,11 +43,14 @@ __device__ __forceinline__ float strict_prequant(float v, uint32_t col, const Dq
     return prequant_vec(v, c.r_f);
 }
 
-template <int NDIM, bool VEC, bool PAD = false, bool REDO = false>
-__global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
-    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
-    typedef float PrevT[8][8][32];
-    PrevT* s_prev  = reinterpret_cast<PrevT*>(s_dq_dyn);  // 3D only
+typedef float DqPlane[8][8][32];  // one warp's plane of 8 x 8 blocks, [row][column][lane]
+
+// Units ui = first, first + stride, ... < end of one field (one warp each; `wib` = this warp's
+// plane in s_prev).  REDO: the units the separable kernel listed instead (end = their count,
+// read by the caller: final in stream order).
+template <int NDIM, bool VEC, bool PAD, bool REDO>
+__device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, uint32_t end, uint32_t stride,
+                                            DqPlane* s_prev, unsigned wib) {
     const Consts c = *a.consts;
     if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
     const int R           = a.R;
@@ -55,14 +58,9 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
     const float rbias     = 8388608.0f + (float)R;
     const uint32_t rpair  = (uint32_t)R | ((uint32_t)R << 16);
     const unsigned lane   = lane_id();
-    const unsigned wib    = threadIdx.x >> 5;  // warp in block (4 warps)
-    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
-    const uint32_t warp0       = blockIdx.x * (blockDim.x >> 5) + wib;
 
     // unit indices fit 32 bits (n <= 2^36 elements, 2048 per unit): 32-bit divisions only.
-    // REDO: only the units the separable kernel listed (its count is final: stream order).
-    const uint32_t nloop = REDO ? a.redo[0] : (uint32_t)a.nunits;
-    for (uint32_t ui = warp0; ui < nloop; ui += warps_total) {
+    for (uint32_t ui = first; ui < end; ui += stride) {
         const uint32_t u  = REDO ? a.redo[1 + ui] : ui;
         const uint32_t xs = u % a.nxs;
         const uint32_t r  = u / a.nxs;
@@ -152,7 +150,7 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
                             if (lo + t < q) zc += (a.codes[lo + t] == 0);
 #pragma unroll
                         for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
-                        seg_base = a.chunk_off[q >> 9] + zc;
+                        seg_base = a.chunk_off[q >> 9] - a.chunk_off[0] + zc;  // relative: batches
                     } else {
                         seg_base = a.seg_off[row * a.nxs + xs];
                     }
@@ -207,7 +205,7 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
                 for (int h = 0; h < 2; h++) {
                     float xo[4];
 #pragma unroll
-                    for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                    for (int k = 0; k < 4; k++) xo[k] = dequant_tab(C[4 * h + k], a.dq_tab, a.dq_lo, a.dq_n, c);
                     if (a.strict && zm) {  // strict outliers are output as stored
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
@@ -245,6 +243,15 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
     }
 }
 
+template <int NDIM, bool VEC, bool PAD = false, bool REDO = false>
+__global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    const unsigned wib = threadIdx.x >> 5;  // warp in block (4 warps)
+    const uint32_t end = REDO ? a.redo[0] : (uint32_t)a.nunits;
+    dq_b8_units<NDIM, VEC, PAD, REDO>(a, blockIdx.x * (blockDim.x >> 5) + wib, end, gridDim.x * (blockDim.x >> 5),
+                                      reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
+}
+
 // ------------------------------------------------------------------------------------------
 // Separable pass, 3D, block 8, zero halo (no padding), not strict.  With a zero halo the Lorenzo
 // inverse is the block's 3D inclusive prefix sum of the residuals q = code - R, so an element takes
@@ -255,21 +262,17 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
 // with a block whose values leave that range (or meet a NaN or an infinity) lists its unit in
 // a.redo, and the reference-order kernel redoes it afterwards.
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
-    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
-    typedef float PlaneT[8][8][32];
-    PlaneT* s_A    = reinterpret_cast<PlaneT*>(s_dq_dyn);  // A of the previous plane [row][column][lane]
+// Units u = first, first + stride, ... < end of one field; s_A: A of the previous plane.
+__device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first, uint32_t end, uint32_t stride,
+                                             DqPlane* s_A, unsigned wib) {
     const Consts c = *a.consts;
     if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
     const int R                = a.R;
     const float rbias          = 8388608.0f + (float)R;
     const uint32_t rpair       = (uint32_t)R | ((uint32_t)R << 16);
     const unsigned lane        = lane_id();
-    const unsigned wib         = threadIdx.x >> 5;
-    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
-    const uint32_t warp0       = blockIdx.x * (blockDim.x >> 5) + wib;
 
-    for (uint32_t u = warp0; u < (uint32_t)a.nunits; u += warps_total) {
+    for (uint32_t u = first; u < end; u += stride) {
         const uint32_t xs = u % a.nxs;
         const uint32_t r  = u / a.nxs;
         const uint32_t yb = r % a.nyb;
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
                             if (lo + t < q) zc += (a.codes[lo + t] == 0);
 #pragma unroll
                         for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
-                        seg_base = a.chunk_off[q >> 9] + zc;
+                        seg_base = a.chunk_off[q >> 9] - a.chunk_off[0] + zc;  // relative: batches
                     } else {
                         seg_base = a.seg_off[row * a.nxs + xs];
                     }
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
                     for (int h = 0; h < 2; h++) {
                         float xo[4];
 #pragma unroll
-                        for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                        for (int k = 0; k < 4; k++) xo[k] = dequant_tab(C[4 * h + k], a.dq_tab, a.dq_lo, a.dq_n, c);
                         __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
                     }
                 }
@@ -381,6 +384,13 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
             a.redo[1 + i]    = u;
         }
     }
+}
+
+__global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    const unsigned wib = threadIdx.x >> 5;
+    dq_b8s_units(a, blockIdx.x * (blockDim.x >> 5) + wib, (uint32_t)a.nunits, gridDim.x * (blockDim.x >> 5),
+                 reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -427,11 +437,11 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                 zb++;
                 xo = s;  // strict: the stored input value
                 if (a.strict) s = strict_prequant<1>(s, (uint32_t)x, a, c);
-                else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                else xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
             } else {
                 if ((x & (kDSeg - 1)) == 0) zb = 0;
                 s  = __fadd_rn(k ? prev : hx, (float)((int)cd - R));
-                xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
             }
             prev     = s;
             a.out[x] = xo;
@@ -499,10 +509,10 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                     zrun++;
                     xo = s;  // strict: the stored input value
                     if (a.strict) s = strict_prequant<NDIM>(s, x, a, c);
-                    else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                    else xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
                 } else {
                     s  = __fadd_rn(pred, (float)((int)cd - R));
-                    xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                    xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
                 }
                 a.out[row * a.d0 + x] = xo;
             }
@@ -560,15 +570,120 @@ static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
+// dequant() of the integers [lo, lo + n), by the double multiply (see dequant_tab).
+__global__ void k_dq_table(const Consts* __restrict__ consts, int lo, uint32_t n, float* __restrict__ tab) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) tab[i] = dequant_fp64((float)(lo + (int)i), consts->c_d);
+}
+
+int launch_dq_table(const Consts* consts, int lo, uint32_t n, float* tab, cudaStream_t st) {
+    if (n == 0) return VSZ_OK;
+    k_dq_table<<<(n + 255) / 256, 256, 0, st>>>(consts, lo, n, tab);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+// The table's range from an archive's prequantized-value bounds (lo > hi: none); n = 0 when they
+// are unknown or too wide for kDqTab entries, or leave |s| < 2^22.
+void dq_table_range(int s_lo, int s_hi, int* lo, uint32_t* n) {
+    *lo = 0;
+    *n  = 0;
+    if (s_lo > s_hi || s_lo <= -(1 << 22) || s_hi >= (1 << 22)) return;
+    const long long w = (long long)s_hi - s_lo + 1;
+    if (w > (long long)kDqTab) return;
+    *lo = s_lo;
+    *n  = (uint32_t)w;
+}
+
+void dq_b8_geometry(DqDecArgs& a, int ndim) {
+    a.nxs = (a.d0 + kDSeg - 1) / kDSeg;
+    a.nyb = (a.d1 + 7) / 8;
+    unsigned long long nzb = (ndim == 3) ? (a.d2 + 7) / 8 : 1;
+    a.nunits = (unsigned long long)a.nxs * (ndim >= 2 ? a.nyb : 1) * nzb;
+}
+
+bool dq_b8_vec(const DqDecArgs& a) {
+    return (a.d0 % 8 == 0) && ((reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0) &&
+           ((reinterpret_cast<uintptr_t>(a.out) & 15u) == 0);
+}
+
+bool dq_b8_separable(const DqDecArgs& a, int ndim) {
+    return ndim == 3 && dq_b8_vec(a) && a.redo && !a.strict && !a.pad.vals && a.n_outliers * 64 < a.n;
+}
+
+// ---- many fields (block size 8, no padding): tasks of (field, unit range); a CTA's 4 warps take
+// the task's units.  Per field the result is k_dq_decompress_b8 / _b8s's.
+template <int NDIM, bool VEC>
+__global__ void __launch_bounds__(128, 6)
+    k_dq_decompress_b8_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    const unsigned wib = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk = tasks[t];
+        const DqDecArgs a  = args[tk.field];
+        dq_b8_units<NDIM, VEC, false, false>(a, (uint32_t)tk.u0 + wib, (uint32_t)tk.u1, 4u,
+                                             reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
+    }
+}
+
+__global__ void __launch_bounds__(128, 6)
+    k_dq_decompress_b8s_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    const unsigned wib = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk = tasks[t];
+        const DqDecArgs a  = args[tk.field];
+        dq_b8s_units(a, (uint32_t)tk.u0 + wib, (uint32_t)tk.u1, 4u, reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
+    }
+}
+
+// The units the separable pass listed, one CTA per field (tasks carry only the field).
+__global__ void __launch_bounds__(128, 6)
+    k_dq_decompress_redo_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ __align__(16) uint8_t s_dq_dyn[];
+    const unsigned wib = threadIdx.x >> 5;
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const DqDecArgs a = args[tasks[t].field];
+        dq_b8_units<3, true, false, true>(a, wib, a.redo[0], 4u, reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
+    }
+}
+
+int launch_dq_decompress_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, bool vec,
+                               bool sep, cudaStream_t st, int num_sms) {
+    if (ntasks == 0) return VSZ_OK;
+    const uint32_t cap  = (uint32_t)num_sms * 6;
+    const uint32_t grid = ntasks < cap ? ntasks : cap;
+    const size_t smem   = (ndim == 3) ? 4 * sizeof(DqPlane) : 0;
+    static std::atomic<unsigned long long> attr[8];
+    auto go = [&](auto kern, int slot) {
+        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[slot]);
+        kern<<<grid, 128, smem, st>>>(args, tasks, ntasks);
+        count_launch();
+    };
+    if (sep) go(k_dq_decompress_b8s_batch, 0);
+    else if (ndim == 3) vec ? go(k_dq_decompress_b8_batch<3, true>, 1) : go(k_dq_decompress_b8_batch<3, false>, 2);
+    else if (ndim == 2) vec ? go(k_dq_decompress_b8_batch<2, true>, 3) : go(k_dq_decompress_b8_batch<2, false>, 4);
+    else vec ? go(k_dq_decompress_b8_batch<1, true>, 5) : go(k_dq_decompress_b8_batch<1, false>, 6);
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_dq_redo_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
+                         int num_sms) {
+    if (ntasks == 0) return VSZ_OK;
+    const uint32_t cap  = (uint32_t)num_sms * 6;
+    const uint32_t grid = ntasks < cap ? ntasks : cap;
+    static std::atomic<unsigned long long> attr{0};
+    smem_limit_once(k_dq_decompress_redo_batch, (int)(4 * sizeof(DqPlane)), attr);
+    k_dq_decompress_redo_batch<<<grid, 128, 4 * sizeof(DqPlane), st>>>(args, tasks, ntasks);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms) {
     if (a.n == 0) return VSZ_OK;
     if (bs == 8 && !force_general) {
-        a.nxs = (a.d0 + kDSeg - 1) / kDSeg;
-        a.nyb = (a.d1 + 7) / 8;
-        unsigned long long nzb = (ndim == 3) ? (a.d2 + 7) / 8 : 1;
-        a.nunits = (unsigned long long)a.nxs * (ndim >= 2 ? a.nyb : 1) * nzb;
-        const bool vec = (a.d0 % 8 == 0) && ((reinterpret_cast<uintptr_t>(a.codes) & 15u) == 0) &&
-                         ((reinterpret_cast<uintptr_t>(a.out) & 15u) == 0);
+        dq_b8_geometry(a, ndim);
+        const bool vec = dq_b8_vec(a);
         long long want = (long long)((a.nunits + 3) / 4);
         long long cap  = (long long)num_sms * 16;
         int grid = (int)(want < cap ? want : cap);
@@ -586,7 +701,7 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
             if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true, true>, 3) : go(k_dq_decompress_b8<3, false, true>, 3);
             else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true, true>, 2) : go(k_dq_decompress_b8<2, false, true>, 2);
             else vec ? go(k_dq_decompress_b8<1, true, true>, 1) : go(k_dq_decompress_b8<1, false, true>, 1);
-        } else if (ndim == 3 && vec && a.redo && !a.strict && a.n_outliers * 64 < a.n) {
+        } else if (dq_b8_separable(a, ndim)) {
             // separable pass, then the reference-order kernel over the units it listed
             if (cudaMemsetAsync(a.redo, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
             go(k_dq_decompress_b8s, 3);

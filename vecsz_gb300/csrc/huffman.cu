@@ -12,6 +12,7 @@
 //                   bit is known (from this library's chunk index, or found by self-synchronising
 //                   rounds k_huff_sync_* for archives written by the reference).
 #include <cstdint>
+#include <cstdlib>
 
 #include "scan.cuh"
 #include "vsz_device.cuh"
@@ -666,7 +667,8 @@ __device__ __forceinline__ uint32_t rd_index(const uint8_t* p, int w) {
     return v;
 }
 
-__global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
+// The decode tables of one field, by the whole CTA (1024 threads; returns are block-uniform).
+__device__ __forceinline__ void huff_table_run(const HuffTableArgs& a) {
     const uint8_t* h = a.huff;
     __shared__ uint32_t s_nc;
     __shared__ int s_bad;
@@ -839,6 +841,17 @@ __global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) {
     }
 }
 
+__global__ void __launch_bounds__(1024) k_huff_table(HuffTableArgs a) { huff_table_run(a); }
+
+// Many fields: one CTA per field (grid-stride); a field whose status is already set is skipped.
+__global__ void __launch_bounds__(1024) k_huff_table_batch(const HuffTableArgs* __restrict__ args, uint32_t nfields) {
+    for (uint32_t f = blockIdx.x; f < nfields; f += gridDim.x) {
+        const HuffTableArgs a = args[f];
+        if (*a.status == VSZ_OK) huff_table_run(a);
+        __syncthreads();  // the next field reuses the shared arrays
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // K4b: chunk decoder
 // ------------------------------------------------------------------------------------------
@@ -989,17 +1002,10 @@ constexpr int kWinThreads   = 256;  // one primary table per CTA, shared by its 
 constexpr int kWinMinBlocks = 4;
 constexpr size_t kWinSmem   = (sizeof(uint32_t) << kDecBits) + (size_t)(kWinThreads / 32) * kWinRing * 32 * 16;
 
-__global__ void __launch_bounds__(kWinThreads, kWinMinBlocks) k_huff_decode_win(HuffDecodeArgs a) {
-    extern __shared__ __align__(16) uint8_t s_win_dyn[];
-    // [primary table: 1 << kDecBits words][ring: warp][slot][lane] x 16 bytes (kWinSmem bytes)
-    uint32_t* s_table                = reinterpret_cast<uint32_t*>(s_win_dyn);
-    uint4 (*s_ring)[kWinRing][32]    = reinterpret_cast<uint4 (*)[kWinRing][32]>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
-    if (!a.tree_info || a.tree_info[2] > (uint32_t)kWinMaxLen) return;  // uniform: k_huff_decode_idx's trees
-    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
-    __syncthreads();
-    if (*a.status != VSZ_OK) return;  // no block barrier below
+// Lane j of the calling warp decodes chunk j (the table is in s_table; no block barrier inside).
+__device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t j, const uint32_t* s_table,
+                                                uint4 (*s_ring)[kWinRing][32]) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const size_t j      = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (j - lane >= a.nchunks) return;
     const unsigned long long out0 = (unsigned long long)j * kChunkSyms;
     uint32_t cnt = 0;
@@ -1023,7 +1029,8 @@ __global__ void __launch_bounds__(kWinThreads, kWinMinBlocks) k_huff_decode_win(
     unsigned long long cb = 0, wn = 0, breq = 0;
     uint32_t off = 0;
     if (cnt) {
-        const unsigned long long sb = a.start_bit[j];
+        // offsets relative to the field's first chunk (a batch scans all fields' indexes at once)
+        const unsigned long long sb = a.start_bit[j] - a.start_bit[0];
         cb = a.chunk_len[j];
         if (sb + cb > a.payload_bits) bad = true;
         const unsigned long long pos0 = base0 + sb;
@@ -1130,23 +1137,35 @@ __global__ void __launch_bounds__(kWinThreads, kWinMinBlocks) k_huff_decode_win(
     if (j < a.nchunks && a.chunk_zero) a.chunk_zero[j] = zeros;
 }
 
+__global__ void __launch_bounds__(kWinThreads, kWinMinBlocks) k_huff_decode_win(HuffDecodeArgs a) {
+    extern __shared__ __align__(16) uint8_t s_win_dyn[];
+    // [primary table: 1 << kDecBits words][ring: warp][slot][lane] x 16 bytes (kWinSmem bytes)
+    uint32_t* s_table             = reinterpret_cast<uint32_t*>(s_win_dyn);
+    uint4 (*s_ring)[kWinRing][32] = reinterpret_cast<uint4 (*)[kWinRing][32]>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
+    if (!a.tree_info || a.tree_info[2] > (uint32_t)kWinMaxLen) return;  // uniform: k_huff_decode_idx's trees
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+    __syncthreads();
+    if (*a.status != VSZ_OK) return;  // no block barrier below
+    decode_win_lane(a, blockIdx.x * (size_t)blockDim.x + threadIdx.x, s_table, s_ring);
+}
+
 constexpr int kDecRound = 16;                 // codes per lane staged before the coalesced store
 constexpr int kDecParts = kDecRound / 8;      // 16-byte pieces per staged row
 
+// Shared memory of the general indexed decoder (the walk array, when in shared memory, follows).
+struct IdxSmem {
+    uint32_t table[1 << kDecBits];
+    __align__(16) uint16_t stage[8][32][kDecRound + 8];  // +8: keep rows 16-byte aligned
+    __align__(16) uint4 ring[8][4][32];                   // per lane: 4 blocks of its stream
+};
+
+// Lane j of the calling warp decodes chunk j of a tree with codewords over kWinMaxLen bits.
 template <bool WALK_SMEM>
-__global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
-    __shared__ uint32_t s_table[1 << kDecBits];
-    __shared__ __align__(16) uint16_t s_stage[8][32][kDecRound + 8];  // +8: keep rows 16-byte aligned
-    __shared__ __align__(16) uint4 s_ring[8][4][32];                   // per lane: 4 blocks of its stream
-    extern __shared__ uint32_t s_walk[];                               // WALK_SMEM: a.nodes entries
-    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
-    if (WALK_SMEM)
-        for (uint32_t i = threadIdx.x; i < a.nodes; i += blockDim.x) s_walk[i] = a.walk[i];
-    __syncthreads();
-    if (*a.status != VSZ_OK) return;
-    if (a.tree_info && a.tree_info[2] <= (uint32_t)kWinMaxLen) return;  // k_huff_decode_win's trees
+__device__ __forceinline__ void decode_idx_lane(const HuffDecodeArgs& a, size_t j, IdxSmem& sm, const uint32_t* s_walk) {
+    auto& s_table = sm.table;
+    auto& s_stage = sm.stage;
+    auto& s_ring  = sm.ring;
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const size_t j      = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const size_t jw0    = j - lane;  // first chunk of this warp
     if (jw0 >= a.nchunks) return;
     const bool active   = j < a.nchunks;
@@ -1193,7 +1212,7 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
     unsigned long long buf = 0;
     int nbits = 0;
     if (cnt) {
-        const unsigned long long sb = a.start_bit[j], cb = a.chunk_len[j];
+        const unsigned long long sb = a.start_bit[j] - a.start_bit[0], cb = a.chunk_len[j];
         if (sb + cb > a.payload_bits) bad = true;
         pos = base0 + sb;
         end = pos + cb;
@@ -1319,6 +1338,96 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
     if (cnt && !bad && pos != end) bad = true;  // the chunk must fill exactly its indexed length
     if (bad) set_status(a.status, VSZ_ERR_CORRUPT);
     if (active && a.chunk_zero) a.chunk_zero[j] = zeros;
+}
+
+template <bool WALK_SMEM>
+__global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
+    __shared__ IdxSmem sm;
+    extern __shared__ uint32_t s_walk[];  // WALK_SMEM: a.nodes entries
+    for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) sm.table[i] = a.table[i];
+    if (WALK_SMEM)
+        for (uint32_t i = threadIdx.x; i < a.nodes; i += blockDim.x) s_walk[i] = a.walk[i];
+    __syncthreads();
+    if (*a.status != VSZ_OK) return;
+    if (a.tree_info && a.tree_info[2] <= (uint32_t)kWinMaxLen) return;  // k_huff_decode_win's trees
+    decode_idx_lane<WALK_SMEM>(a, blockIdx.x * (size_t)blockDim.x + threadIdx.x, sm, s_walk);
+}
+
+// ---- many fields: tasks of (field, chunk range [256 k, 256 k + 256) of its index), one CTA
+// each; lane t of the CTA decodes chunk u0 + t.  A kernel takes the tasks of the fields whose trees
+// are of its kind (read from k_huff_table's results, so uniform over the CTA) and skips the rest.
+__global__ void __launch_bounds__(kWinThreads, kWinMinBlocks)
+    k_huff_decode_win_batch(const HuffDecodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    extern __shared__ __align__(16) uint8_t s_win_dyn[];
+    uint32_t* s_table             = reinterpret_cast<uint32_t*>(s_win_dyn);
+    uint4 (*s_ring)[kWinRing][32] = reinterpret_cast<uint4 (*)[kWinRing][32]>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk     = tasks[t];
+        const HuffDecodeArgs a = args[tk.field];
+        if (a.tree_info[2] > (uint32_t)kWinMaxLen) continue;
+        for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
+        __syncthreads();
+        if (*a.status == VSZ_OK) decode_win_lane(a, tk.u0 + threadIdx.x, s_table, s_ring);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_huff_decode_idx_batch(const HuffDecodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    __shared__ IdxSmem sm;
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk     = tasks[t];
+        const HuffDecodeArgs a = args[tk.field];
+        if (a.tree_info[2] <= (uint32_t)kWinMaxLen) continue;
+        for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) sm.table[i] = a.table[i];
+        __syncthreads();
+        if (*a.status == VSZ_OK) decode_idx_lane<false>(a, tk.u0 + threadIdx.x, sm, nullptr);
+        __syncthreads();
+    }
+}
+
+// One-symbol trees: every code of the chunk is the symbol (src/huffman.hh:348-352); zero counts
+// per chunk for the outlier ranks.
+__global__ void __launch_bounds__(256)
+    k_huff_const_batch(const HuffDecodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        const BatchTask tk     = tasks[t];
+        const HuffDecodeArgs a = args[tk.field];
+        if (*a.status != VSZ_OK) continue;
+        const uint16_t c = (uint16_t)a.tree_info[1];
+        const size_t lo = tk.u0 * (size_t)kChunkSyms, hi = min((size_t)a.n, (size_t)(tk.u1 * kChunkSyms));
+        for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) a.codes[i] = c;
+        for (size_t j = tk.u0 + threadIdx.x; j < tk.u1; j += blockDim.x)
+            a.chunk_zero[j] = c == 0 ? (uint32_t)min((size_t)kChunkSyms, (size_t)(a.n - j * kChunkSyms)) : 0u;
+    }
+}
+
+int launch_huff_table_batch(const HuffTableArgs* args, uint32_t nfields, cudaStream_t st, int num_sms) {
+    if (nfields == 0) return VSZ_OK;
+    const uint32_t grid = nfields < (uint32_t)num_sms ? nfields : (uint32_t)num_sms;
+    k_huff_table_batch<<<grid, 1024, 0, st>>>(args, nfields);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+int launch_huff_decode_batch(const HuffDecodeArgs* args, const BatchTask* tasks, uint32_t ntasks,
+                             const BatchTask* const_tasks, uint32_t nconst, cudaStream_t st, int num_sms) {
+    if (ntasks) {
+        const uint32_t cap  = (uint32_t)num_sms * kWinMinBlocks;
+        const uint32_t grid = ntasks < cap ? ntasks : cap;
+        static std::atomic<unsigned long long> attr{0};
+        smem_limit_once(k_huff_decode_win_batch, (int)kWinSmem, attr);
+        k_huff_decode_win_batch<<<grid, kWinThreads, kWinSmem, st>>>(args, tasks, ntasks);
+        count_launch();
+        k_huff_decode_idx_batch<<<grid, 256, 0, st>>>(args, tasks, ntasks);
+        count_launch();
+    }
+    if (nconst) {
+        const uint32_t cap = (uint32_t)num_sms * 8;
+        k_huff_const_batch<<<nconst < cap ? nconst : cap, 256, 0, st>>>(args, const_tasks, nconst);
+        count_launch();
+    }
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
 // Constant fill for a one-symbol tree (src/huffman.hh:348-352).
@@ -1643,5 +1752,43 @@ int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsig
 }
 
 size_t scan_tmp_tiles(size_t n) { return (n + 4095) / 4096; }
+
+int set_spin_limit_huffman(long long polls) { return set_spin_limit_this_unit(polls); }
+
+// Test hook: the device-wide scan of n ones with its tile ticket started at 1 instead of 0, so no
+// tile takes ticket 0 and the tile after it waits on a predecessor that never publishes.  That
+// wait gives up after the current spin limit and records VSZ_ERR_TIMEOUT, which *status_out
+// receives; the scan's later tiles then finish.  Allocates and synchronises (testing only).
+int debug_scan_stalled(size_t n, int* status_out) {
+    if (n == 0 || n > (1u << 24) || !status_out) return VSZ_ERR_INVALID;
+    const size_t ntiles = (n + 4095) / 4096;
+    uint32_t* in = nullptr;
+    unsigned long long *out = nullptr, *ts = nullptr;
+    uint32_t* tc = nullptr;
+    int* st      = nullptr;
+    int rc       = VSZ_ERR_NOMEM;
+    if (cudaMalloc(reinterpret_cast<void**>(&in), 4 * n) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&out), 8 * n) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&ts), 8 * (ntiles + 2)) == cudaSuccess &&  // ticket ntiles publishes too
+        cudaMalloc(reinterpret_cast<void**>(&tc), 4) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&st), 4) == cudaSuccess) {
+        const uint32_t one = 1;
+        rc = VSZ_ERR_CUDA;
+        if (cudaMemset(in, 0, 4 * n) == cudaSuccess && cudaMemset(ts, 0, 8 * (ntiles + 2)) == cudaSuccess &&
+            cudaMemset(st, 0, 4) == cudaSuccess && cudaMemcpy(tc, &one, 4, cudaMemcpyHostToDevice) == cudaSuccess) {
+            k_scan_excl<uint32_t><<<(unsigned)ntiles, 256>>>(in, out, n, ts, tc, nullptr, st);
+            count_launch();
+            if (cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
+                cudaMemcpy(status_out, st, 4, cudaMemcpyDeviceToHost) == cudaSuccess)
+                rc = VSZ_OK;
+        }
+    }
+    cudaFree(in);
+    cudaFree(out);
+    cudaFree(ts);
+    cudaFree(tc);
+    cudaFree(st);
+    return rc;
+}
 
 }  // namespace vsz

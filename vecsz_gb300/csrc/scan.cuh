@@ -1,12 +1,20 @@
 // Single-pass decoupled look-back (Merrill & Garland, 2016) used by the outlier compaction, the
 // Huffman encoder and the generic device-wide exclusive scan.  Tiles take their index from an
 // atomic ticket, so a tile only ever waits on tiles that are already running; every wait is
-// bounded by kSpinLimit and reports VSZ_ERR_TIMEOUT instead of hanging.
+// bounded by g_spin_limit polls and reports VSZ_ERR_TIMEOUT instead of hanging.
 #pragma once
 
 #include "vsz_device.cuh"
 
 namespace vsz {
+
+// Polls a look-back wait makes before it gives up: kSpinLimit unless the test hook
+// vsz_debug_set_spin_limit lowers it.  A static device variable, so every translation unit that
+// includes this header has its own copy, which set_spin_limit_this_unit sets.
+static __device__ long long g_spin_limit = kSpinLimit;
+[[maybe_unused]] static int set_spin_limit_this_unit(long long polls) {
+    return cudaMemcpyToSymbol(g_spin_limit, &polls, sizeof(polls)) == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
 
 constexpr unsigned long long kFlagAgg = 1ull << 62;
 constexpr unsigned long long kFlagPre = 2ull << 62;
@@ -28,7 +36,7 @@ __device__ __forceinline__ unsigned long long lookback_publish(unsigned long lon
         unsigned long long s = ld_acquire_u64(&tile_status[t]);
         unsigned long long f = s & (3ull << 62);
         if (f == 0) {
-            if (++spins > kSpinLimit) {
+            if (++spins > g_spin_limit) {
                 set_status(status, VSZ_ERR_TIMEOUT);
                 break;
             }
@@ -66,7 +74,7 @@ __device__ __forceinline__ unsigned long long lookback_publish_warp(unsigned lon
         const int first_p    = pmask ? (__ffs(pmask) - 1) : 32;
         const unsigned need  = (first_p >= 31) ? 0xffffffffu : ((2u << first_p) - 1u);
         if (zmask & need) {
-            if (++spins > kSpinLimit) {  // a predecessor never published: give up, report
+            if (++spins > g_spin_limit) {  // a predecessor never published: give up, report
                 if (lane == 0) set_status(status, VSZ_ERR_TIMEOUT);
                 break;
             }

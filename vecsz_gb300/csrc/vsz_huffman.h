@@ -19,10 +19,13 @@ constexpr int kDec2Max     = 8;    // widest secondary table: codewords of up to
 //   (node << 8)                walk the tree bit by bit from `node` after kDecBits bits
 // Secondary table2 entries: (sym << 8) | total length, or (node << 8) to walk from `node` after
 // kDecBits + w2 bits (codewords longer than kDecBits + kDec2Max).  A zero entry is not a codeword.
-// Capacity: every secondary table hangs off a distinct internal node at depth kDecBits.
+// Capacity: every secondary table hangs off a distinct internal node at depth kDecBits, and one
+// with L leaves below it is at most 2^min(kDec2Max, L - 1) entries wide (a subtree of depth D has
+// at least D + 1 leaves), so a tree of `leaves` leaves needs at most 256 / 9 entries per leaf.
+// k_huff_table leaves the walk entries in place of secondary tables that would not fit.
 __host__ __device__ inline size_t table2_capacity(uint32_t max_nodes) {
-    const uint32_t p = max_nodes < (1u << kDecBits) ? max_nodes : (1u << kDecBits);
-    return (size_t)p << kDec2Max;
+    const size_t leaves = ((size_t)max_nodes + 1) / 2;
+    return ((size_t)(1u << kDec2Max) * leaves + 8) / 9 + 256;
 }
 constexpr int kChunkSyms   = 512;  // codewords per entry of this library's decode index
 constexpr int kSyncBits    = 8192; // chunk size (bits) of the self-synchronising decoder
@@ -96,7 +99,7 @@ struct HuffDecodeArgs {
     const uint32_t* walk;                 // packed children (k_huff_table), when walk_smem
     int walk_smem;                        // 1: dict <= 16384, the walk array is copied to shared memory
     uint32_t nodes;                       // node count of the tree
-    const unsigned long long* start_bit;  // per chunk
+    const unsigned long long* start_bit;  // per chunk, relative to start_bit[0] (indexed path)
     const uint16_t* chunk_len;            // indexed path: bits of each chunk
     uint32_t* chunk_zero;                 // indexed path: zero codes per chunk (may be null)
     const unsigned long long* out_begin;  // per chunk, or null: chunk * chunk_syms
@@ -145,6 +148,13 @@ void huff_build_prepare();  // one-time kernel attributes of launch_huff_build (
 size_t huff_build_scratch_bytes(int dict);
 int launch_huff_encode(HuffEncodeArgs a, cudaStream_t st, int num_sms);
 int launch_huff_table(HuffTableArgs a, cudaStream_t st);
+// Many fields: decode tables one CTA per field; decoding over tasks of (field, 256-chunk range
+// of the field's index), every field's tree by the decoder of its kind (the window decoder for
+// codewords up to 32 bits, the general one beyond), and const_tasks (one-symbol trees) by a
+// constant fill.
+int launch_huff_table_batch(const HuffTableArgs* args, uint32_t nfields, cudaStream_t st, int num_sms);
+int launch_huff_decode_batch(const HuffDecodeArgs* args, const BatchTask* tasks, uint32_t ntasks,
+                             const BatchTask* const_tasks, uint32_t nconst, cudaStream_t st, int num_sms);
 int launch_huff_decode(HuffDecodeArgs a, cudaStream_t st);
 int launch_huff_const(uint16_t* codes, size_t n, const uint32_t* info, uint32_t* seg_zero, uint32_t d0, uint32_t nxs,
                       const int* status, cudaStream_t st, int num_sms);
@@ -156,5 +166,8 @@ int launch_scan_u16(const uint16_t* in, unsigned long long* out, size_t n, unsig
 int launch_scan_u32(const uint32_t* in, unsigned long long* out, size_t n, unsigned long long* tile_status,
                     uint32_t* tile_counter, unsigned long long* total, int* status, cudaStream_t st);
 size_t scan_tmp_tiles(size_t n);
+// Test hooks (vsz_debug_*): this unit's look-back spin limit; a scan whose first tile never runs.
+int set_spin_limit_huffman(long long polls);
+int debug_scan_stalled(size_t n, int* status_out);
 
 }  // namespace vsz

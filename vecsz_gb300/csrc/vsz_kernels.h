@@ -136,7 +136,8 @@ struct DqDecArgs {
     unsigned long long n_outliers;       // entries of `outliers`; a rank past it is VSZ_ERR_CORRUPT
     int* status;
     const unsigned long long* seg_off;   // exclusive zero-code offsets per 256-wide row segment, or
-    const unsigned long long* chunk_off; // exclusive zero-code offsets per 512-code chunk (block 8)
+    const unsigned long long* chunk_off; // exclusive zero-code offsets per 512-code chunk (block 8),
+                                         // relative to chunk_off[0]
     const Consts* consts;
     float* out;
     uint32_t d0, d1, d2;
@@ -151,9 +152,26 @@ struct DqDecArgs {
     PadView pad;                         // padded archive: the halo of each block (vals = pad section)
     uint32_t* redo;                      // 3D block 8, separable pass: [0] count, then units whose
                                          // values left the exact range (null: reference order only)
+    const float* dq_tab;                 // dequant() of the integers [dq_lo, dq_lo + dq_n) (dq_n = 0:
+    int dq_lo;                           // no table; see dequant_tab)
+    uint32_t dq_n;
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
+// Block size 8: unit geometry (nxs, nyb, nunits), whether the 16-byte row path applies, and
+// whether the separable pass does (3D, vector rows, not strict, no padding, under 1 outlier in 64).
+void dq_b8_geometry(DqDecArgs& a, int ndim);
+// The dequantization table of a decompress (dq_table_range: from the archive's bounds).
+void dq_table_range(int s_lo, int s_hi, int* lo, uint32_t* n);
+int launch_dq_table(const Consts* consts, int lo, uint32_t n, float* tab, cudaStream_t st);
+bool dq_b8_vec(const DqDecArgs& a);
+bool dq_b8_separable(const DqDecArgs& a, int ndim);
+// Many fields of one class (ndim, vec, separable), block size 8, no padding: tasks of (field,
+// unit range).  A separable class is followed by launch_dq_redo_batch over its fields.
+int launch_dq_decompress_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, bool vec,
+                               bool sep, cudaStream_t st, int num_sms);
+int launch_dq_redo_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
+                         int num_sms);
 int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* seg_zero, cudaStream_t st,
                        int num_sms);
 
@@ -189,6 +207,7 @@ int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_
 int launch_outlier_gather_batch(const GatherArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
                                 int num_sms);
 size_t gather_tmp_bytes(size_t nseg);
+int set_spin_limit_dq(long long polls);  // test hook: this unit's look-back spin limit
 
 // Geometry helpers shared by compress and decompress.
 struct Geometry {
