@@ -128,8 +128,6 @@ typedef struct vsz_archive_desc {
     uint64_t index_offset;  /* trailer: byte offset of u16 bits-per-chunk, 8-byte aligned */
     uint64_t trailer_size;
     int strict;             /* trailer: written in strict error-bound mode (VSZ_FLAG_STRICT_EB) */
-    int32_t s_lo, s_hi;     /* trailer (version 2): bounds of the prequantized values, s_lo > s_hi
-                               when unknown; decompress tabulates the dequantization over them */
 } vsz_archive_desc;
 
 /* Options a decompressor needs that the packed block does not store (the reference takes them

@@ -69,7 +69,7 @@ class ArchiveDesc(C.Structure):
                 ("data_size", C.c_uint64), ("has_trailer", C.c_int), ("eb_final", C.c_double),
                 ("value_range", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
                 ("chunk_syms", C.c_uint32), ("n_chunks", C.c_uint64), ("index_offset", C.c_uint64),
-                ("trailer_size", C.c_uint64), ("strict", C.c_int), ("s_lo", C.c_int32), ("s_hi", C.c_int32)]
+                ("trailer_size", C.c_uint64), ("strict", C.c_int)]
 
 
 class TuneResult(C.Structure):

@@ -16,11 +16,8 @@ int num_sms();  // of the current device (cached)
 namespace api {
 
 constexpr uint32_t kTrailerMagic   = 0x545A5356u;  // "VSZT"
-// Trailer version 2 appends the prequantized-value bounds (two i32 at byte 64) to version 1's 64
-// fixed bytes; decoders read both versions.
-constexpr uint32_t kTrailerVersion = 2;
-constexpr uint32_t kTrailerFixed   = 72;
-constexpr uint32_t kTrailerFixedV1 = 64;
+constexpr uint32_t kTrailerVersion = 1;
+constexpr uint32_t kTrailerFixed   = 64;
 
 #define VSZ_TRY(x)                        \
     do {                                  \
@@ -189,8 +186,6 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
         unsigned long long nch = f.n_chunks, tsz = trailer;
         put_bytes(t + 48, &nch, 8);
         put_bytes(t + 56, &tsz, 8);
-        int32_t sb[2] = {f.consts->s_lo, f.consts->s_hi};
-        put_bytes(t + 64, sb, 8);
         for (size_t i = kTrailerFixed; i < pad; i++) t[i] = 0;
         unsigned long long* r = f.result;
         r[0] = data_size;

@@ -118,18 +118,6 @@ __device__ __forceinline__ void consts_of(int mode, double eb, const uint32_t* _
     };
     c->dq_fast = normal(ch) && (cl == 0.0f || normal(cl));
     c->status  = status;
-    // r2r: every prequantized value lies in [rint(min r_f), rint(max r_f)] (the AVX form; the
-    // scalar form of 3D tail columns may differ by one), so a decompressor can tabulate dequant()
-    c->s_lo = 1;
-    c->s_hi = 0;
-    if (mode == VSZ_MODE_R2R && status == VSZ_OK) {
-        const float mn = key2f(mm[1]), mx = key2f(mm[0]);
-        const float a = rintf(__fmul_rn(mn, c->r_f)), b = rintf(__fmul_rn(mx, c->r_f));
-        if (fabsf(a) < 4194304.0f && fabsf(b) < 4194304.0f) {  // 2^22; false for NaN and infinity
-            c->s_lo = (int)a - 1;
-            c->s_hi = (int)b + 1;
-        }
-    }
     if (status != VSZ_OK && status_word) set_status(status_word, status);
 }
 

@@ -205,7 +205,7 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
                 for (int h = 0; h < 2; h++) {
                     float xo[4];
 #pragma unroll
-                    for (int k = 0; k < 4; k++) xo[k] = dequant_tab(C[4 * h + k], a.dq_tab, a.dq_lo, a.dq_n, c);
+                    for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
                     if (a.strict && zm) {  // strict outliers are output as stored
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
@@ -372,7 +372,7 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
                     for (int h = 0; h < 2; h++) {
                         float xo[4];
 #pragma unroll
-                        for (int k = 0; k < 4; k++) xo[k] = dequant_tab(C[4 * h + k], a.dq_tab, a.dq_lo, a.dq_n, c);
+                        for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
                         __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
                     }
                 }
@@ -437,11 +437,11 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                 zb++;
                 xo = s;  // strict: the stored input value
                 if (a.strict) s = strict_prequant<1>(s, (uint32_t)x, a, c);
-                else xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
+                else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
             } else {
                 if ((x & (kDSeg - 1)) == 0) zb = 0;
                 s  = __fadd_rn(k ? prev : hx, (float)((int)cd - R));
-                xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
+                xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
             }
             prev     = s;
             a.out[x] = xo;
@@ -509,10 +509,10 @@ __global__ void __launch_bounds__(128) k_dq_decompress_gen(DqDecArgs a) {
                     zrun++;
                     xo = s;  // strict: the stored input value
                     if (a.strict) s = strict_prequant<NDIM>(s, x, a, c);
-                    else xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
+                    else xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
                 } else {
                     s  = __fadd_rn(pred, (float)((int)cd - R));
-                    xo = dequant_tab(s, a.dq_tab, a.dq_lo, a.dq_n, c);
+                    xo = dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
                 }
                 a.out[row * a.d0 + x] = xo;
             }
@@ -568,31 +568,6 @@ static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
         count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
-}
-
-// dequant() of the integers [lo, lo + n), by the double multiply (see dequant_tab).
-__global__ void k_dq_table(const Consts* __restrict__ consts, int lo, uint32_t n, float* __restrict__ tab) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) tab[i] = dequant_fp64((float)(lo + (int)i), consts->c_d);
-}
-
-int launch_dq_table(const Consts* consts, int lo, uint32_t n, float* tab, cudaStream_t st) {
-    if (n == 0) return VSZ_OK;
-    k_dq_table<<<(n + 255) / 256, 256, 0, st>>>(consts, lo, n, tab);
-    count_launch();
-    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
-}
-
-// The table's range from an archive's prequantized-value bounds (lo > hi: none); n = 0 when they
-// are unknown or too wide for kDqTab entries, or leave |s| < 2^22.
-void dq_table_range(int s_lo, int s_hi, int* lo, uint32_t* n) {
-    *lo = 0;
-    *n  = 0;
-    if (s_lo > s_hi || s_lo <= -(1 << 22) || s_hi >= (1 << 22)) return;
-    const long long w = (long long)s_hi - s_lo + 1;
-    if (w > (long long)kDqTab) return;
-    *lo = s_lo;
-    *n  = (uint32_t)w;
 }
 
 void dq_b8_geometry(DqDecArgs& a, int ndim) {

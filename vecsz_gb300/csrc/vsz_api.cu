@@ -149,7 +149,6 @@ struct DecompressWs {
     int* s_changed;
     float* outliers;
     uint32_t* redo;  // units of the separable reverse Lorenzo that the reference-order kernel redoes
-    float* dq_tab;   // the dequantization table (kDqTab entries)
     size_t bytes;
 };
 
@@ -194,7 +193,6 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
         const size_t units8 = (size_t)nxs * ((g.d1 + 7) / 8) * ((g.d2 + 7) / 8);  // block-8 warp units
         w.redo = b.take<uint32_t>(units8 + 2);
     }
-    w.dq_tab       = b.take<float>(kDqTab);
     w.bytes        = b.off + 256;
     return w;
 }
@@ -959,16 +957,11 @@ static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* 
     d->payload_bytes = d->huff_bytes - 8 - d->tree_bytes;
     d->outlier_offset = d->huff_offset + d->huff_bytes;
     // this library's trailer
-    d->s_lo = 1;
-    d->s_hi = 0;
-    if (len >= d->data_size + kTrailerFixedV1) {
+    if (len >= d->data_size + kTrailerFixed) {
         const uint8_t* t = split ? tail : h + d->data_size;
         uint32_t u32[4];
         memcpy(u32, t, 16);
-        const bool v1 = u32[1] == 1 && u32[2] == kTrailerFixedV1;
-        const bool v2 = u32[1] == kTrailerVersion && u32[2] == kTrailerFixed && len >= d->data_size + kTrailerFixed;
-        if (u32[0] == kTrailerMagic && (v1 || v2)) {
-            const uint32_t fixed = u32[2];
+        if (u32[0] == kTrailerMagic && u32[1] == kTrailerVersion && u32[2] == kTrailerFixed) {
             d->chunk_syms = u32[3];
             memcpy(&d->eb_final, t + 16, 8);
             memcpy(&d->value_range, t + 24, 8);
@@ -984,17 +977,11 @@ static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* 
             memcpy(&d->trailer_size, t + 56, 8);
             uint64_t n = d->dims[0] * d->dims[1] * d->dims[2];
             bool ok = d->chunk_syms == (uint32_t)kChunkSyms && d->n_chunks == (n + kChunkSyms - 1) / kChunkSyms &&
-                      pad >= fixed && d->data_size + pad + 2 * d->n_chunks <= len &&
+                      pad >= kTrailerFixed && d->data_size + pad + 2 * d->n_chunks <= len &&
                       ((d->data_size + pad) % 8) == 0 && valid_dict(d->dict_size) && valid_bs(d->block_size);
             if (ok) {
                 d->has_trailer = 1;
                 d->index_offset = d->data_size + pad;
-                if (v2) {
-                    int32_t sb[2];
-                    memcpy(sb, t + 64, 8);
-                    d->s_lo = sb[0];
-                    d->s_hi = sb[1];
-                }
             }
         }
     }
@@ -1130,11 +1117,8 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
     a.pad    = pad_view_of(d, bs, d_archive);
     a.redo   = w.redo;
-    a.dq_tab = w.dq_tab;
-    dq_table_range(d->has_trailer ? d->s_lo : 1, d->has_trailer ? d->s_hi : 0, &a.dq_lo, &a.dq_n);
     {
         StageTimer t(kStLorenzoDecompress, st);
-        VSZ_TRY(launch_dq_table(w.consts, a.dq_lo, a.dq_n, w.dq_tab, st));
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));
     }
     if (d_status) {

@@ -66,8 +66,6 @@ struct DField {
     double ebf;
     size_t nch;
     size_t units;  // block-8 warp units
-    int dq_lo;      // dequantization table (dq_n = 0: none)
-    uint32_t dq_n;
     bool sep, vec, konst;
 };
 
@@ -76,16 +74,6 @@ struct DqClass {
     bool vec, sep;
     uint32_t task_off, ntasks;
 };
-
-// Every field's dequantization table (one CTA per field, grid-stride), after its constants.
-__global__ void k_dbatch_dq_table(const DqDecArgs* __restrict__ args, uint32_t nfields) {
-    for (uint32_t f = blockIdx.x; f < nfields; f += gridDim.x) {
-        const DqDecArgs a = args[f];
-        float* tab        = const_cast<float*>(a.dq_tab);
-        for (uint32_t i = threadIdx.x; i < a.dq_n; i += blockDim.x)
-            tab[i] = dequant_fp64((float)(a.dq_lo + (int)i), a.consts->c_d);
-    }
-}
 
 __global__ void k_dbatch_init(const DCheck* __restrict__ c, uint32_t nfields) {
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -153,7 +141,6 @@ int field_of(const vsz_dbatch_field& F, DField& out) {
     out.nch   = (out.g.n + kChunkSyms - 1) / kChunkSyms;
     if (d.n_chunks != out.nch) return VSZ_ERR_CORRUPT;
     out.konst = d.node_count == 1;
-    dq_table_range(d.s_lo, d.s_hi, &out.dq_lo, &out.dq_n);
     DqDecArgs a{};
     a.d0 = out.g.d0;
     a.d1 = out.g.d1;
@@ -173,7 +160,7 @@ struct DLayout {
     uint32_t* scan_counter;
     std::vector<uint32_t*> table, table2, child, node_sym, parent, walk, redo;
     std::vector<uint16_t*> code;
-    std::vector<float*> outliers, dq_tab;
+    std::vector<float*> outliers;
     std::vector<size_t> chunk_base;
     size_t bytes;
 };
@@ -207,7 +194,6 @@ DLayout layout_dbatch(const std::vector<DField>& fs, const vsz_dbatch_field* fie
         L.code.push_back(b.take<uint16_t>(f.g.n + 8));
         L.outliers.push_back(b.take<float>(fields[i].desc.n_outlier + 4));
         L.redo.push_back(f.sep ? b.take<uint32_t>(f.units + 2) : nullptr);
-        L.dq_tab.push_back(f.dq_n ? b.take<float>(f.dq_n) : nullptr);
     }
     L.bytes = b.off + 256;
     return L;
@@ -355,9 +341,6 @@ vsz_status vsz_dbatch_create(const vsz_dbatch_field* fields, int nfields, void* 
         q.R           = d.dict_size / 2;
         q.xtail       = (G.g.ndim == 3 && (G.g.d0 % 8) != 0) ? (G.g.d0 & ~7u) : G.g.d0;
         q.redo        = L.redo[f];
-        q.dq_tab      = L.dq_tab[f];
-        q.dq_lo       = G.dq_lo;
-        q.dq_n        = G.dq_n;
         dq_b8_geometry(q, G.g.ndim);
 
         ci[f] = DCopy{F.d_archive + d.index_offset, reinterpret_cast<uint8_t*>(L.all_bits + base), status};
@@ -495,8 +478,6 @@ vsz_status vsz_dbatch_decompress(vsz_dbatch* B, void* stream) {
     }
     {
         StageTimer t(kStLorenzoDecompress, st);
-        k_dbatch_dq_table<<<std::min<uint32_t>(nf, (uint32_t)sms * 4), 256, 0, st>>>(B->dq, nf);
-        count_launch();
         for (const DqClass& c : B->classes)
             VSZ_TRY(launch_dq_decompress_batch(B->dq, B->tasks + c.task_off, c.ntasks, c.ndim, c.vec, c.sep, st, sms));
         VSZ_TRY(launch_dq_redo_batch(B->dq, B->tasks + B->redo_off, B->redo_n, st, sms));

@@ -55,8 +55,6 @@ struct Consts {
     float c_lo;       // (float)(c_d - c_hi)
     int dq_fast;      // 1 when c_hi and c_lo are normal floats, so dequant() may take its FP32 path
     int status;       // VSZ_OK, or why the constants are unusable (zero value range)
-    int s_lo, s_hi;   // r2r: bounds of the prequantized values (from the field's min and max, one
-                      // either side for the scalar form); s_lo > s_hi when unknown (abs mode)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -116,18 +114,6 @@ __device__ __forceinline__ float dequant(float s, double c_d, float c_hi, float 
     }
     if (ok) return y;
     return dequant_fp64(s, c_d);
-}
-
-// Dequantization by table: a decompressor with the field's prequantized-value bounds memoises
-// dequant() for the integers s in [lo, lo + n) (n <= kDqTab), computed by the double multiply
-// itself (k_dq_table).  s + 1.5 * 2^23 is exact for integer-valued |s| < 2^22 and its bits minus
-// those of 1.5 * 2^23 are s; any other s (fractional, larger, non-finite) lands outside [0, n) and
-// takes dequant().  Zeros take dequant() too, which keeps the sign of a negative zero.
-constexpr uint32_t kDqTab = 8192;
-__device__ __forceinline__ float dequant_tab(float s, const float* __restrict__ tab, int lo, uint32_t n, const Consts& c) {
-    const int si = __float_as_int(__fadd_rn(s, 12582912.0f)) - (0x4B400000 + lo);
-    if ((uint32_t)si < n && s != 0.0f) return __ldg(&tab[si]);
-    return dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
 }
 
 // Order-preserving map of floats onto unsigned integers (NaNs are skipped by the caller).

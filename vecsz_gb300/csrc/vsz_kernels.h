@@ -152,18 +152,12 @@ struct DqDecArgs {
     PadView pad;                         // padded archive: the halo of each block (vals = pad section)
     uint32_t* redo;                      // 3D block 8, separable pass: [0] count, then units whose
                                          // values left the exact range (null: reference order only)
-    const float* dq_tab;                 // dequant() of the integers [dq_lo, dq_lo + dq_n) (dq_n = 0:
-    int dq_lo;                           // no table; see dequant_tab)
-    uint32_t dq_n;
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
 // Block size 8: unit geometry (nxs, nyb, nunits), whether the 16-byte row path applies, and
 // whether the separable pass does (3D, vector rows, not strict, no padding, under 1 outlier in 64).
 void dq_b8_geometry(DqDecArgs& a, int ndim);
-// The dequantization table of a decompress (dq_table_range: from the archive's bounds).
-void dq_table_range(int s_lo, int s_hi, int* lo, uint32_t* n);
-int launch_dq_table(const Consts* consts, int lo, uint32_t n, float* tab, cudaStream_t st);
 bool dq_b8_vec(const DqDecArgs& a);
 bool dq_b8_separable(const DqDecArgs& a, int ndim);
 // Many fields of one class (ndim, vec, separable), block size 8, no padding: tasks of (field,
