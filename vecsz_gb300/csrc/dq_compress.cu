@@ -224,6 +224,13 @@ __device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t x
     }
 }
 
+// (int)(e + R) for an integer-valued residual with |e| < R <= 32768: e + R + 1.5 * 2^23 is exact
+// (an integer below 2^24), and its bits minus those of 1.5 * 2^23 are e + R -- two full-rate
+// instructions instead of a float-to-int conversion.  rmagic = (float)R + 1.5 * 2^23.
+__device__ __forceinline__ int code_of(float e, float rmagic) {
+    return __float_as_int(__fadd_rn(e, rmagic)) - 0x4B400000;
+}
+
 template <int NDIM, bool TAIL>
 __device__ __forceinline__ float prequant_at(float v, uint32_t col, uint32_t xtail, float r_f, double r_d) {
     if (NDIM == 3 && TAIL && col >= xtail) return prequant_scalar(v, r_d);
@@ -301,6 +308,7 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
     const float r_f     = c.r_f;
     const double r_d    = c.r_d;
     const float Rf      = (float)a.R;
+    const float rmagic  = Rf + 12582912.0f;
     const unsigned lane = lane_id();
     const unsigned wib  = threadIdx.x >> 5;
     const bool xbound   = ((lane * 4) % BS) == 0;  // my first column starts a Lorenzo block
@@ -400,7 +408,7 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
                         }
                         const float e = __fsub_rn(cur, pred);
                         const bool q  = fabsf(e) < Rf;
-                        code[j]       = q ? (int)__fadd_rn(e, Rf) : 0;
+                        code[j]       = q ? code_of(e, rmagic) : 0;
                         outv[j]       = cur;
                         if (STRICT) {
                             const float xr = j == 0 ? raw.x : (j == 1 ? raw.y : (j == 2 ? raw.z : raw.w));
@@ -495,6 +503,7 @@ __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, uns
                                            unsigned long long ustep, uint32_t* s_hist, HistAcc& h) {
     const float r_f     = c.r_f;
     const float Rf      = (float)a.R;
+    const float rmagic  = Rf + 12582912.0f;
     const unsigned lane = lane_id();
     const bool xbound   = ((lane * 4) % BS) == 0;
     constexpr int U     = 4;
@@ -539,7 +548,8 @@ __device__ __forceinline__ void dq1d_units(const DqArgs& a, const Consts& c, uns
                     continue;
                 }
                 const bool q     = fabsf(e) < Rf;
-                code[j]          = q ? (int)__fadd_rn(e, Rf) : 0;
+                // (1D block / edge pads make e fractional here: truncation, as the reference's scalar form)
+                code[j]          = q ? (PAD ? (int)__fadd_rn(e, Rf) : code_of(e, rmagic)) : 0;
                 outv[j]          = S[t][j];
                 if (STRICT) {
                     const float4 rw = RW[STRICT ? t : 0];
