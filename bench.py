@@ -344,7 +344,9 @@ def run_ours(args):
         same = all(bool(torch.equal(o.view(torch.int32), out.view(torch.int32))) for o in outs[1:])
         same = same and all(c2.decompress_status() == 0 for c2 in codecs)
         pipe = {"inflight": args.inflight, "outputs_identical": same}
-        del codecs[1:], outs[1:]
+        del codecs, streams, outs, c2, s2
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
     t_wall1 = time.time()
     time.sleep(0.3)
     clocks.stop()

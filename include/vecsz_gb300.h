@@ -128,6 +128,7 @@ typedef struct vsz_archive_desc {
     uint64_t index_offset;  /* trailer: byte offset of u16 bits-per-chunk, 8-byte aligned */
     uint64_t trailer_size;
     int strict;             /* trailer: written in strict error-bound mode (VSZ_FLAG_STRICT_EB) */
+    int f64;                /* trailer: an f64 field (vsz_compress_f64); n_outlier counts 8-byte values */
 } vsz_archive_desc;
 
 /* Options a decompressor needs that the packed block does not store (the reference takes them
@@ -520,6 +521,35 @@ int vsz_profile_read(double* ms, int* counts, const char** names, int max_stages
 /* Kernels this library has launched in this process, all entry points and devices together (a
  * relaxed atomic count taken at each launch).  No counterpart in the reference. */
 uint64_t vsz_launch_count(void);
+
+/* ---- f64 fields ----------------------------------------------------------------------------
+ * The reference parses -t f64 (src/argument_parser/argparse.cc:454-462) but reads its input as
+ * float (src/vecsz.cc:32) and its dual-quant loops are float AVX code (src/dualquant.hh:86-92), so
+ * it has no f64 arithmetic to match.  These entry points run the same pipeline in double precision
+ * with the error bound guaranteed, as the strict mode does for f32: prequantized values
+ * s = rint(x / 2eb) are exact integers, the Lorenzo predictor is integer arithmetic, an element
+ * keeps its code only if s * 2eb is within eb of x (and |x / 2eb| < 2^59), and every other element
+ * is an outlier stored as its 8-byte input value.  So |x - xhat| <= eb everywhere (checked in
+ * double), outliers (NaN and infinities included) come back bit for bit.  abs and r2r modes,
+ * dictionaries and block sizes as for f32; no padding (VSZ_ERR_UNSUPPORTED).  The archive is the
+ * packed-block layout with 8-byte outliers, counted as two 32-bit words in the header's outlier
+ * count, and the trailer marks it (vsz_archive_desc.f64); vsz_decompress refuses it and
+ * vsz_decompress_f64 takes only it.  Device entry points are stream-ordered as vsz_compress /
+ * vsz_decompress; the host ones allocate device memory per call and synchronise (-L zstd / gzip
+ * through the host library, the trailer after the frame). */
+vsz_status vsz_compress_f64_bounds(const vsz_params* p, int ndim, const size_t dims[3], size_t* ws_bytes,
+                                   size_t* archive_capacity);
+vsz_status vsz_compress_f64(const vsz_params* p, int ndim, const size_t dims[3], const double* d_in, void* d_ws,
+                            size_t ws_bytes, uint8_t* d_archive, size_t archive_capacity, uint64_t* d_result,
+                            void* stream);
+vsz_status vsz_decompress_f64_bounds(const vsz_archive_desc* desc, size_t* ws_bytes);
+vsz_status vsz_decompress_f64(const vsz_archive_desc* desc, const uint8_t* d_archive, void* d_ws, size_t ws_bytes,
+                              double* d_out, int* d_status, void* stream);
+vsz_status vsz_compress_host_f64(const vsz_params* p, int ndim, const size_t dims[3], const double* h_in,
+                                 uint8_t** h_out, size_t* out_bytes, size_t* data_size, size_t* lossless_size,
+                                 size_t* n_outlier);
+vsz_status vsz_decompress_host_f64(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
+                                   double** h_out, size_t* n);
 
 /* ---- test hooks: no counterpart in the reference ---------------------------------------------
  * Every cross-CTA wait of this library (the decoupled look-back of the outlier gather, the

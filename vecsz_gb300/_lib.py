@@ -69,7 +69,7 @@ class ArchiveDesc(C.Structure):
                 ("data_size", C.c_uint64), ("has_trailer", C.c_int), ("eb_final", C.c_double),
                 ("value_range", C.c_double), ("mode", C.c_int), ("dict_size", C.c_int), ("block_size", C.c_int),
                 ("chunk_syms", C.c_uint32), ("n_chunks", C.c_uint64), ("index_offset", C.c_uint64),
-                ("trailer_size", C.c_uint64), ("strict", C.c_int)]
+                ("trailer_size", C.c_uint64), ("strict", C.c_int), ("f64", C.c_int)]
 
 
 class TuneResult(C.Structure):
@@ -132,6 +132,15 @@ _PROTOS = {
     "vsz_autotune_bounds": ([_p, _i, C.POINTER(C.c_size_t), C.c_double, C.POINTER(C.c_size_t)], _i),
     "vsz_autotune": ([_p, _i, C.POINTER(C.c_size_t), _p, C.c_double, _i, C.c_double, _p, _sz, _p, _p], _i),
     "vsz_autotune_cache_clear": ([], None),
+    "vsz_compress_f64_bounds": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t),
+                                 C.POINTER(C.c_size_t)], _i),
+    "vsz_compress_f64": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), _p, _p, _sz, _p, _sz, _p, _p], _i),
+    "vsz_decompress_f64_bounds": ([C.POINTER(ArchiveDesc), C.POINTER(C.c_size_t)], _i),
+    "vsz_decompress_f64": ([C.POINTER(ArchiveDesc), _p, _p, _sz, _p, _p, _p], _i),
+    "vsz_compress_host_f64": ([C.POINTER(Params), _i, C.POINTER(C.c_size_t), _p, C.POINTER(C.c_void_p),
+                               C.POINTER(C.c_size_t),
+                               C.POINTER(C.c_size_t), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)], _i),
+    "vsz_decompress_host_f64": ([_p, _sz, _sz, _sz, C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)], _i),
     "vsz_dbatch_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t)], _i),
     "vsz_dbatch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
     "vsz_dbatch_decompress": ([_p, _p], _i),

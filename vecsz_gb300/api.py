@@ -63,9 +63,27 @@ class Compressed:
 
 
 def compress(data: np.ndarray, dims=None, eb: float = 1e-4, mode="abs", dict_size: int = 4096, block_size: int = 8,
-             lossless=None, strict: bool = False, padding=None) -> Compressed:
-    """Compress a float32 field held in host memory (vecsz::interface::Compress).  padding: the
-    reference's -p string, see make_params."""
+             lossless=None, strict: bool = False, padding=None, dtype: str = "f32") -> Compressed:
+    """Compress a field held in host memory (vecsz::interface::Compress).  padding: the
+    reference's -p string, see make_params.  dtype "f64": the data are float64 and go through the
+    f64 path (vsz_compress_host_f64: error bound guaranteed, 8-byte outliers)."""
+    if dtype == "f64":
+        x = np.ascontiguousarray(data, dtype=np.float64)
+        if dims is None:
+            dims = tuple(reversed(x.shape))
+        p = make_params(eb, mode, dict_size, block_size, lossless, strict, padding)
+        out = C.c_void_p(0)
+        ob, ds, ls, no = C.c_size_t(0), C.c_size_t(0), C.c_size_t(0), C.c_size_t(0)
+        check(lib().vsz_compress_host_f64(C.byref(p), len(dims), dims_arg(dims), x.ctypes.data_as(C.c_void_p),
+                                          C.byref(out), C.byref(ob), C.byref(ds), C.byref(ls), C.byref(no)),
+              "compress_f64")
+        try:
+            buf = C.string_at(out.value, ob.value)
+        finally:
+            lib().vsz_free_host(out)
+        return Compressed(buf, ds.value, ls.value, no.value)
+    if dtype != "f32":
+        raise ValueError(f"dtype must be 'f32' or 'f64', not {dtype!r}")
     x = np.ascontiguousarray(data, dtype=np.float32)
     if dims is None:
         dims = tuple(reversed(x.shape))  # numpy (z, y, x) -> reference (x, y, z)
@@ -88,6 +106,16 @@ def decompress(archive, data_size: int = 0, lossless_size: int = 0, dict_size: i
     if isinstance(archive, Compressed):
         data_size, lossless_size, archive = archive.data_size, archive.lossless_size, archive.data
     a = np.frombuffer(archive, np.uint8)
+    if _is_f64_archive(archive, data_size, lossless_size):
+        out = C.c_void_p(0)
+        n = C.c_size_t(0)
+        check(lib().vsz_decompress_host_f64(a.ctypes.data_as(C.c_void_p), a.size, int(data_size), int(lossless_size),
+                                            C.byref(out), C.byref(n)), "decompress_f64")
+        try:
+            res = np.frombuffer(C.string_at(out.value, n.value * 8), np.float64).copy()
+        finally:
+            lib().vsz_free_host(out)
+        return res
     o = DecompressOpts(int(dict_size), int(block_size), _MODES[mode] if isinstance(mode, str) else int(mode),
                        float(value_range))
     out = C.c_void_p(0)
@@ -99,6 +127,16 @@ def decompress(archive, data_size: int = 0, lossless_size: int = 0, dict_size: i
     finally:
         lib().vsz_free_host(out)
     return res
+
+
+def _is_f64_archive(archive, data_size: int, lossless_size: int) -> bool:
+    """Whether this library's trailer (after the packed block, or after the lossless frame) marks an
+    f64 field: its mode word's bit 9."""
+    t = int(lossless_size) if lossless_size else int(data_size)
+    b = bytes(archive[t: t + 48]) if t else b""
+    if len(b) < 48 or b[:4] != b"VSZT":
+        return False
+    return bool(int.from_bytes(b[32:36], "little") & 0x200)
 
 
 def parse_archive(buf) -> ArchiveDesc:

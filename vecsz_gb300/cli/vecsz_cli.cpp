@@ -38,7 +38,7 @@ void usage(bool full) {
         "  -z, --compress, --zip        compress the input file\n"
         "  -x, --decompress, --unzip    decompress a .sz file\n"
         "  -r, --dry-run                compress, decompress and report the error metrics\n"
-        "  -t, --dtype f32|f64          data type (the data are read as f32, as the reference does)\n"
+        "  -t, --dtype f32|f64          data type (f64: the double-precision path, error bound guaranteed)\n"
         "  -m, --mode abs|r2r           error-bound mode (default abs)\n"
         "  -e, --eb <value>             error bound (default 1e-4)\n"
         "  -l, --len x[,y[,z]]          dimensions, fastest first\n"
@@ -298,7 +298,8 @@ vsz_params params_of(const Args& a) {
 
 // error metrics of a reconstruction (max absolute error and its index, value range, PSNR,
 // NRMSE, correlation), as the reference's dry run prints them
-void print_metrics(const float* o, const float* x, size_t n, size_t archive_bytes) {
+template <typename T>
+void print_metrics(const T* o, const T* x, size_t n, size_t archive_bytes) {
     double mn = o[0], mx = o[0], s0 = 0, sx = 0;
     for (size_t i = 0; i < n; i++) {
         mn = std::min(mn, (double)o[i]);
@@ -335,7 +336,8 @@ void print_metrics(const float* o, const float* x, size_t n, size_t archive_byte
     std::printf("\n");
 }
 
-void print_histogram(const char* title, const float* v, size_t n, int bins) {
+template <typename T>
+void print_histogram(const char* title, const T* v, size_t n, int bins) {
     double mn = v[0], mx = v[0];
     for (size_t i = 0; i < n; i++) mn = std::min(mn, (double)v[i]), mx = std::max(mx, (double)v[i]);
     std::vector<size_t> h(bins, 0);
@@ -358,16 +360,47 @@ size_t element_count(const Args& a) {
     return n;
 }
 
-std::vector<float> read_field(const Args& a, size_t n) {
+template <typename T = float>
+std::vector<T> read_field(const Args& a, size_t n) {
     std::vector<uint8_t> raw = read_file(a.input);
-    if (raw.size() < 4 * n) {
+    if (raw.size() < sizeof(T) * n) {
         std::fprintf(stderr, "[error] %s holds %zu bytes, the dimensions need %zu\n", a.input.c_str(), raw.size(),
-                     4 * n);
+                     sizeof(T) * n);
         std::exit(-1);
     }
-    std::vector<float> x(n);
-    std::memcpy(x.data(), raw.data(), 4 * n);
+    std::vector<T> x(n);
+    std::memcpy(x.data(), raw.data(), sizeof(T) * n);
     return x;
+}
+
+// -t f64: the f64 path (error bound guaranteed, 8-byte outliers); the reference reads f32 here
+std::vector<uint8_t> compress_f64(const Args& a, vsz_params& p, const double* x, size_t* data_size,
+                                  size_t* lossless_size) {
+    const size_t dims[3] = {(size_t)a.dims[0], (size_t)a.dims[1], (size_t)a.dims[2]};
+    if (a.autotune) std::fprintf(stderr, "[warn] -a: the block-size autotuner takes f32 fields; -b %d kept\n", p.block_size);
+    uint8_t* out = nullptr;
+    size_t ob = 0, no = 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int st  = vsz_compress_host_f64(&p, a.ndim, dims, x, &out, &ob, data_size, lossless_size, &no);
+    if (st != VSZ_OK) fail("compress", st);
+    std::vector<uint8_t> payload(out, out + ob);
+    vsz_free_host(out);
+    if (a.verbose)
+        std::printf("[dbg] compress (f64): %zu outliers, packed block %zu bytes, lossless %zu bytes, %.6f s\n", no,
+                    *data_size, *lossless_size, seconds_since(t0));
+    return payload;
+}
+
+std::vector<double> decompress_f64(const Args& a, const uint8_t* payload, size_t len, size_t data_size,
+                                   size_t lossless_size) {
+    double* out   = nullptr;
+    size_t n      = 0;
+    const int st  = vsz_decompress_host_f64(payload, len, data_size, lossless_size, &out, &n);
+    if (st != VSZ_OK) fail("decompress", st);
+    std::vector<double> y(out, out + n);
+    vsz_free_host(out);
+    if (a.verbose) std::printf("[dbg] decompress (f64): %zu values\n", n);
+    return y;
 }
 
 // compress: returns the payload main() writes after its 16-byte header
@@ -410,6 +443,7 @@ std::vector<float> decompress(const Args& a, const uint8_t* payload, size_t len,
     size_t n              = 0;
     const auto t0         = std::chrono::steady_clock::now();
     const int st          = vsz_decompress_host(payload, len, data_size, lossless_size, &o, &out, &n);
+    if (st == VSZ_ERR_UNSUPPORTED) return {};  // an f64 archive: the caller takes decompress_f64
     if (st != VSZ_OK) fail("decompress", st);
     if (a.verbose) std::printf("[dbg] decompress: %zu values, %.6f s\n", n, seconds_since(t0));
     std::vector<float> y(out, out + n);
@@ -432,7 +466,28 @@ int main(int argc, char** argv) {
         std::printf("[cfg] Lossless pass:       %s\n", a.lossless_pass ? a.lossless.c_str() : "no");
         std::printf("[cfg] Library:             %s\n", vsz_version());
     }
-    if (a.dtype == "f64") std::fprintf(stderr, "[warn] -t f64: the data are read as f32, as the reference's main does\n");
+    if (a.dtype == "f64" && (a.compress || a.dryrun)) {
+        const size_t n        = element_count(a);
+        std::vector<double> x = read_field<double>(a, n);
+        vsz_params p          = params_of(a);
+        size_t ds = 0, ls = 0;
+        std::vector<uint8_t> payload = compress_f64(a, p, x.data(), &ds, &ls);
+        if (a.compress) {
+            if (!a.skip_write) {
+                const uint64_t head[2] = {(uint64_t)ls, (uint64_t)ds};
+                write_file(a.output, {{head, sizeof(head)}, {payload.data(), payload.size()}});
+            }
+            return 0;
+        }
+        std::vector<double> y = decompress_f64(a, payload.data(), payload.size(), ds, ls);
+        if (!a.skip_write) write_file(a.output, {{y.data(), 8 * y.size()}});
+        if (a.show_histo) {
+            print_histogram("original datum", x.data(), n, 16);
+            print_histogram("reconstructed data", y.data(), n, 16);
+        }
+        print_metrics(x.data(), y.data(), n, ds);
+        return 0;
+    }
 
     if (a.compress) {
         const size_t n       = element_count(a);
@@ -456,6 +511,11 @@ int main(int argc, char** argv) {
         uint64_t head[2];
         std::memcpy(head, f.data(), 16);
         std::vector<float> y = decompress(a, f.data() + 16, f.size() - 16, head[1], head[0]);
+        if (y.empty()) {  // an f64 archive (its trailer says so): doubles out
+            std::vector<double> z = decompress_f64(a, f.data() + 16, f.size() - 16, head[1], head[0]);
+            if (!a.skip_write) write_file(a.output, {{z.data(), 8 * z.size()}});
+            return 0;
+        }
         if (!a.skip_write) write_file(a.output, {{y.data(), 4 * y.size()}});
         return 0;
     }

@@ -131,6 +131,7 @@ struct FinalizeArgs {
     unsigned long long* result;             // vsz_result
     const uint16_t* chunk_bits;
     unsigned long long n_chunks;
+    int f64;  // an f64 field: 8-byte outliers, counted as two 32-bit words in the header
 };
 
 __device__ __forceinline__ void put_bytes(uint8_t* d, const void* src, int n) {
@@ -150,7 +151,8 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
     const unsigned long long nout = *f.n_out;
     const uint32_t tree           = f.build_info[1];
     const size_t huff_bytes       = 8 + (size_t)tree + (size_t)((bits + 7) >> 3);
-    const size_t data_size        = f.hdr + 4 * f.npad + huff_bytes + 4 * (size_t)nout;
+    const unsigned long long owords = f.f64 ? 2 * nout : nout;  // outlier section in 32-bit words
+    const size_t data_size        = f.hdr + 4 * f.npad + huff_bytes + 4 * (size_t)owords;
     const size_t pad              = trailer_index_pad(data_size);
     const size_t trailer          = ((pad + 2 * (size_t)f.n_chunks) + 7) & ~(size_t)7;
     uint8_t* t                    = f.archive + data_size;
@@ -171,7 +173,7 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
             put_bytes(f.archive + 4 * (1 + i), &d, 4);
         }
         put_bytes(f.archive + 4 * (f.ndim + 1), &f.eb, 8);
-        unsigned long long lens[3] = {(unsigned long long)f.npad, (unsigned long long)huff_bytes, nout};
+        unsigned long long lens[3] = {(unsigned long long)f.npad, (unsigned long long)huff_bytes, owords};
         put_bytes(f.archive + 4 * (f.ndim + 1) + 8, lens, 24);
         // trailer fixed part
         uint32_t u32[4] = {kTrailerMagic, kTrailerVersion, kTrailerFixed, (uint32_t)kChunkSyms};
@@ -179,7 +181,8 @@ __device__ __forceinline__ void finalize_field(const FinalizeArgs& f, unsigned b
         double ebf = f.consts->eb_final, vr = f.consts->range;
         put_bytes(t + 16, &ebf, 8);
         put_bytes(t + 24, &vr, 8);
-        int32_t i32[3] = {f.mode | (f.strict ? 0x100 : 0), f.dict, f.bs};  // bit 8: strict error-bound mode
+        // bit 8: strict error-bound mode; bit 9: an f64 field
+        int32_t i32[3] = {f.mode | (f.strict ? 0x100 : 0) | (f.f64 ? 0x200 : 0), f.dict, f.bs};
         put_bytes(t + 32, i32, 12);
         uint32_t padu = (uint32_t)pad;
         put_bytes(t + 44, &padu, 4);

@@ -969,6 +969,7 @@ static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* 
             memcpy(i32, t + 32, 12);
             d->mode = i32[0] & 0xff;
             d->strict = (i32[0] >> 8) & 1;
+            const int f64 = (i32[0] >> 9) & 1;
             d->dict_size = i32[1];
             d->block_size = i32[2];
             uint32_t pad;
@@ -979,9 +980,12 @@ static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* 
             bool ok = d->chunk_syms == (uint32_t)kChunkSyms && d->n_chunks == (n + kChunkSyms - 1) / kChunkSyms &&
                       pad >= kTrailerFixed && d->data_size + pad + 2 * d->n_chunks <= len &&
                       ((d->data_size + pad) % 8) == 0 && valid_dict(d->dict_size) && valid_bs(d->block_size);
+            if (f64 && (d->n_outlier & 1)) ok = false;  // 8-byte outliers: an even word count
             if (ok) {
                 d->has_trailer = 1;
                 d->index_offset = d->data_size + pad;
+                d->f64 = f64;
+                if (f64) d->n_outlier /= 2;
             }
         }
     }
@@ -990,6 +994,7 @@ static vsz_status parse_split(const uint8_t* h, size_t head_len, const uint8_t* 
 
 static int resolve_decode_params(const vsz_archive_desc* d, const vsz_decompress_opts* o, int* dict, int* bs,
                                  double* ebf) {
+    if (d->f64) return VSZ_ERR_UNSUPPORTED;  // vsz_decompress_f64
     if (d->has_trailer) {
         *dict = d->dict_size;
         *bs = d->block_size;
@@ -1137,5 +1142,397 @@ vsz_status vsz_debug_set_spin_limit(long long polls) {
 }
 
 vsz_status vsz_debug_scan_stalled_predecessor(size_t n, int* h_status) { return debug_scan_stalled(n, h_status); }
+
+}  // extern "C"
+
+// =================================================================================================
+// f64 fields (dq_f64.cu): the same pipeline in double precision, error bound guaranteed
+// =================================================================================================
+namespace {
+
+struct CompressF64Ws {
+    Consts* consts;
+    unsigned long long* mm;
+    int* status;
+    unsigned long long* hist;
+    long long* s;
+    uint16_t* code;
+    uint32_t* seg_zero;
+    unsigned long long* seg_off;
+    unsigned long long* g_scan;
+    uint32_t* g_counter;
+    unsigned long long* n_out;
+    uint8_t* build_scratch;
+    uint8_t* cb_block;
+    unsigned long long* cb_word;
+    uint8_t* cb_len;
+    uint32_t* build_info;
+    size_t n_chunks;
+    unsigned long long* e_chunk_off;
+    unsigned long long* e_scan_status;
+    unsigned long long* e_edge_idx;
+    uint32_t* e_edge_bits;
+    uint32_t* e_counter;
+    unsigned long long* total_bits;
+    uint16_t* chunk_bits;
+    size_t bytes;
+};
+
+CompressF64Ws layout_compress_f64(const Geometry& g, int dict, uint8_t* base, size_t cap) {
+    Bump b{base, cap};
+    CompressF64Ws w{};
+    const size_t nsegd = g.nrows * ((g.d0 + 255) / 256);
+    w.consts    = b.take<Consts>(1);
+    w.mm        = b.take<unsigned long long>(2);
+    w.status    = b.take<int>(4);
+    w.hist      = b.take<unsigned long long>(dict);
+    w.s         = b.take<long long>(g.n);
+    w.code      = b.take<uint16_t>(g.n + 8);
+    w.seg_zero  = b.take<uint32_t>(nsegd + 1);
+    w.seg_off   = b.take<unsigned long long>(nsegd + 1);
+    w.g_scan    = b.take<unsigned long long>(scan_tmp_tiles(nsegd) + 1);
+    w.g_counter = b.take<uint32_t>(4);
+    w.n_out     = b.take<unsigned long long>(1);
+    w.build_scratch = b.take<uint8_t>(huff_build_scratch_bytes(dict));
+    uint8_t* cb  = b.take<uint8_t>(codebook_block_bytes(dict));
+    w.cb_block   = cb;
+    w.cb_word    = reinterpret_cast<unsigned long long*>(cb);
+    w.build_info = cb ? reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict) : nullptr;
+    w.cb_len     = cb ? cb + 8 * (size_t)dict + 16 : nullptr;
+    w.n_chunks   = (g.n + kChunkSyms - 1) / kChunkSyms;
+    w.e_chunk_off   = b.take<unsigned long long>(w.n_chunks + 1);
+    w.e_scan_status = b.take<unsigned long long>(scan_tmp_tiles(w.n_chunks) + 1);
+    w.e_edge_idx    = b.take<unsigned long long>(2 * w.n_chunks + 2);
+    w.e_edge_bits   = b.take<uint32_t>(2 * w.n_chunks + 2);
+    w.e_counter     = b.take<uint32_t>(4);
+    w.total_bits    = b.take<unsigned long long>(1);
+    w.chunk_bits    = b.take<uint16_t>(w.n_chunks + 8);
+    w.bytes         = b.off + 256;
+    return w;
+}
+
+// the packed block with 8-byte outliers, and the trailer
+size_t archive_capacity_f64(const Geometry& g, int dict) { return archive_capacity(g, dict) + 4 * g.n; }
+
+int check_params_f64(const vsz_params* p, int ndim, const size_t dims[3]) {
+    VSZ_TRY(check_params(p, ndim, dims));
+    // padding keeps the reference's f32 pad section; the f64 path always bounds the error as the
+    // strict mode does, so the strict flag changes nothing
+    if (p->pad_mode != VSZ_PAD_NONE) return VSZ_ERR_UNSUPPORTED;
+    return VSZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+vsz_status vsz_compress_f64_bounds(const vsz_params* p, int ndim, const size_t dims[3], size_t* ws_bytes,
+                                   size_t* archive_cap) {
+    VSZ_TRY(check_params_f64(p, ndim, dims));
+    Geometry g = make_geometry(ndim, dims);
+    if (ws_bytes) *ws_bytes = layout_compress_f64(g, p->dict_size, nullptr, 0).bytes;
+    if (archive_cap) *archive_cap = archive_capacity_f64(g, p->dict_size);
+    return VSZ_OK;
+}
+
+vsz_status vsz_compress_f64(const vsz_params* p, int ndim, const size_t dims[3], const double* d_in, void* d_ws,
+                            size_t ws_bytes, uint8_t* d_archive, size_t archive_cap, uint64_t* d_result,
+                            void* stream) {
+    VSZ_TRY(check_params_f64(p, ndim, dims));
+    if (!d_in || !d_ws || !d_archive || !d_result) return VSZ_ERR_INVALID;
+    Geometry g     = make_geometry(ndim, dims);
+    const int dict = p->dict_size;
+    CompressF64Ws w = layout_compress_f64(g, dict, reinterpret_cast<uint8_t*>(d_ws), ws_bytes);
+    if (w.bytes > ws_bytes) return VSZ_ERR_CAPACITY;
+    if (archive_cap < archive_capacity_f64(g, dict)) return VSZ_ERR_CAPACITY;
+    cudaStream_t st       = S(stream);
+    const size_t hdr      = hdr_bytes(ndim);
+    const size_t huff_off = hdr;
+    VSZ_CUDA(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+    VSZ_CUDA(cudaMemsetAsync(w.hist, 0, sizeof(unsigned long long) * dict, st));
+    VSZ_CUDA(cudaMemsetAsync(w.build_info, 0, 4 * sizeof(uint32_t), st));
+    VSZ_CUDA(cudaMemsetAsync(w.total_bits, 0, sizeof(unsigned long long), st));
+    VSZ_CUDA(cudaMemsetAsync(w.n_out, 0, sizeof(unsigned long long), st));
+    {
+        StageTimer t(kStEbSetup, st);
+        VSZ_TRY(launch_eb_setup_f64(p->mode, p->eb, d_in, g.n, w.consts, w.mm, w.status, st, num_sms()));
+    }
+    F64Args a{};
+    a.x       = d_in;
+    a.s       = w.s;
+    a.code    = w.code;
+    a.hist    = w.hist;
+    a.consts  = w.consts;
+    a.status  = w.status;
+    a.n       = g.n;
+    a.d0      = g.d0;
+    a.d1      = g.d1;
+    a.d2      = g.d2;
+    a.bs      = p->block_size;
+    a.dict    = dict;
+    a.archive = d_archive;
+    {
+        StageTimer t(kStDualquant, st);
+        VSZ_TRY(launch_dq_compress_f64(a, ndim, st, num_sms()));
+    }
+    HuffBuildArgs hb{};
+    hb.hist     = w.hist;
+    hb.dict     = dict;
+    hb.hdr_dict = dict;
+    hb.cb_word  = w.cb_word;
+    hb.cb_len   = w.cb_len;
+    hb.out      = d_archive + huff_off;
+    hb.info     = w.build_info;
+    hb.scratch  = w.build_scratch;
+    hb.status   = w.status;
+    {
+        StageTimer t(kStHuffBuild, st);
+        if (tree_builder() == VSZ_TREE_HOST && !stream_capturing(st)) {
+            huff_build_prepare();
+            VSZ_TRY(enqueue_host_tree(w.hist, dict, dict, w.cb_block, d_archive + huff_off, st));
+        } else
+            VSZ_TRY(launch_huff_build(hb, st));
+    }
+    HuffEncodeArgs he{};
+    he.codes        = w.code;
+    he.n            = g.n;
+    he.cb_word      = w.cb_word;
+    he.cb_len       = w.cb_len;
+    he.dict         = dict;
+    he.out          = d_archive;
+    he.out_off      = DevOffset{huff_off + 8, w.build_info + 1, nullptr};
+    he.total_bits   = w.total_bits;
+    he.chunk_bits   = w.chunk_bits;
+    he.chunk_off    = w.e_chunk_off;
+    he.scan_status  = w.e_scan_status;
+    he.scan_counter = w.e_counter;
+    he.edge_idx     = w.e_edge_idx;
+    he.edge_bits    = w.e_edge_bits;
+    he.status       = w.status;
+    he.build_info   = w.build_info;
+    VSZ_TRY(launch_huff_encode(he, st, num_sms()));
+    {
+        // outliers (code 0) in row-major order after the bitstream: zero codes per 256-wide row
+        // segment, their exclusive scan (the total is the outlier count), then the copy
+        StageTimer t(kStOutlierGather, st);
+        const size_t nsegd = g.nrows * ((g.d0 + 255) / 256);
+        VSZ_TRY(launch_count_zeros(w.code, g.d0, g.nrows, w.seg_zero, st, num_sms()));
+        VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.g_scan, w.g_counter, w.n_out, w.status, st));
+        VSZ_TRY(launch_gather_f64(a, w.seg_off, DevOffset{huff_off + 8, w.build_info + 1, w.total_bits}, st,
+                                  num_sms()));
+    }
+    FinalizeArgs f{};
+    f.archive      = d_archive;
+    f.ndim         = ndim;
+    f.dims[0]      = g.d0;
+    f.dims[1]      = g.d1;
+    f.dims[2]      = g.d2;
+    f.eb           = p->eb;
+    f.mode         = p->mode;
+    f.dict         = dict;
+    f.bs           = p->block_size;
+    f.hdr          = hdr;
+    f.consts       = w.consts;
+    f.build_info   = w.build_info;
+    f.payload_bits = w.total_bits;
+    f.n_out        = w.n_out;
+    f.status       = w.status;
+    f.result       = reinterpret_cast<unsigned long long*>(d_result);
+    f.chunk_bits   = w.chunk_bits;
+    f.n_chunks     = w.n_chunks;
+    f.f64          = 1;
+    int fg = (int)((w.n_chunks + 255) / 256);
+    if (fg < 1) fg = 1;
+    if (fg > num_sms() * 4) fg = num_sms() * 4;
+    {
+        StageTimer t(kStFinalize, st);
+        k_finalize<<<fg, 256, 0, st>>>(f);
+        count_launch();
+    }
+    VSZ_CUDA(cudaGetLastError());
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress_f64_bounds(const vsz_archive_desc* d, size_t* ws_bytes) {
+    if (!d) return VSZ_ERR_INVALID;
+    if (!d->f64 || !d->has_trailer) return VSZ_ERR_UNSUPPORTED;
+    size_t dims[3] = {d->dims[0], d->dims[1], d->dims[2]};
+    if (!valid_dims(d->ndim, dims) || !valid_dict(d->dict_size) || !valid_bs(d->block_size)) return VSZ_ERR_CORRUPT;
+    Geometry g = make_geometry(d->ndim, dims);
+    if (ws_bytes) *ws_bytes = layout_decompress(g, d->dict_size, d->payload_bytes, 0, d->n_chunks, nullptr, 0).bytes;
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress_f64(const vsz_archive_desc* d, const uint8_t* d_archive, void* d_ws, size_t ws_bytes,
+                              double* d_out, int* d_status, void* stream) {
+    if (!d || !d_archive || !d_ws || !d_out) return VSZ_ERR_INVALID;
+    if (!d->f64 || !d->has_trailer) return VSZ_ERR_UNSUPPORTED;  // f32 archives: vsz_decompress
+    size_t dims[3] = {d->dims[0], d->dims[1], d->dims[2]};
+    if (!valid_dims(d->ndim, dims) || !valid_dict(d->dict_size) || !valid_bs(d->block_size) || !(d->eb_final > 0))
+        return VSZ_ERR_CORRUPT;
+    const int dict = d->dict_size;
+    if (d->node_count > (uint32_t)(2 * dict - 1)) return VSZ_ERR_CORRUPT;
+    Geometry g     = make_geometry(d->ndim, dims);
+    DecompressWs w = layout_decompress(g, dict, d->payload_bytes, 0, d->n_chunks, reinterpret_cast<uint8_t*>(d_ws),
+                                       ws_bytes);
+    if (w.bytes > ws_bytes) return VSZ_ERR_CAPACITY;
+    cudaStream_t st    = S(stream);
+    const size_t nsegd = g.nrows * ((g.d0 + 255) / 256);
+    VSZ_CUDA(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+    VSZ_TRY(launch_eb_setup_f64(VSZ_MODE_ABS, d->eb_final, nullptr, 0, w.consts,
+                                reinterpret_cast<unsigned long long*>(w.mm), w.status, st, num_sms()));
+    const uint16_t* idx = reinterpret_cast<const uint16_t*>(d_archive + d->index_offset);
+    VSZ_TRY(decode_codes(d_archive + d->huff_offset, d->huff_bytes, d->node_count, d->tree_bytes, g.n, dict, idx,
+                         d->n_chunks, d->chunk_syms, w, nullptr, g.d0, st));
+    {
+        StageTimer t(kStZeroScan, st);
+        VSZ_TRY(launch_count_zeros(w.code, g.d0, g.nrows, w.seg_zero, st, num_sms()));
+        VSZ_TRY(launch_scan_u32(w.seg_zero, w.seg_off, nsegd, w.scan_status, w.scan_counter, w.scan_total, w.status,
+                                st));
+        k_check_zeros<<<1, 1, 0, st>>>(w.scan_total, d->n_outlier, w.status);
+        count_launch();
+    }
+    F64Args a{};
+    a.code     = w.code;
+    a.consts   = w.consts;
+    a.status   = w.status;
+    a.n        = g.n;
+    a.d0       = g.d0;
+    a.d1       = g.d1;
+    a.d2       = g.d2;
+    a.bs       = d->block_size;
+    a.dict     = dict;
+    a.outliers = d_archive + d->outlier_offset;
+    a.n_out    = d->n_outlier;
+    a.out      = d_out;
+    {
+        StageTimer t(kStLorenzoDecompress, st);
+        VSZ_TRY(launch_dq_decompress_f64(a, d->ndim, w.seg_off, st));
+    }
+    if (d_status) {
+        k_copy_status<<<1, 1, 0, st>>>(w.status, w.consts, d_status);
+        count_launch();
+    }
+    VSZ_CUDA(cudaGetLastError());
+    return VSZ_OK;
+}
+
+// Host buffers: device buffers allocated per call, synchronous.
+vsz_status vsz_compress_host_f64(const vsz_params* p, int ndim, const size_t dims[3], const double* h_in,
+                                 uint8_t** h_out, size_t* out_bytes, size_t* data_size, size_t* lossless_size,
+                                 size_t* n_outlier) {
+    if (!p || !h_in || !h_out) return VSZ_ERR_INVALID;
+    *h_out = nullptr;
+    size_t ws = 0, cap = 0;
+    VSZ_TRY(vsz_compress_f64_bounds(p, ndim, dims, &ws, &cap));
+    if (p->lossless != VSZ_LOSSLESS_NONE && p->lossless != VSZ_LOSSLESS_ZSTD && p->lossless != VSZ_LOSSLESS_GZIP)
+        return VSZ_ERR_UNSUPPORTED;
+    const Geometry g = make_geometry(ndim, dims);
+    uint8_t *d_in = nullptr, *d_ws = nullptr, *d_arch = nullptr;
+    uint64_t* d_res = nullptr;
+    std::vector<uint8_t> arch;
+    uint64_t res[8] = {};
+    int rc = VSZ_ERR_NOMEM;
+    if (cudaMalloc(reinterpret_cast<void**>(&d_in), 8 * g.n) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&d_ws), ws) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&d_arch), cap + 64) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&d_res), 64) == cudaSuccess) {
+        rc = VSZ_ERR_CUDA;
+        if (cudaMemcpy(d_in, h_in, 8 * g.n, cudaMemcpyHostToDevice) == cudaSuccess) {
+            rc = vsz_compress_f64(p, ndim, dims, reinterpret_cast<const double*>(d_in), d_ws, ws, d_arch, cap, d_res,
+                                  nullptr);
+            if (rc == VSZ_OK) rc = cudaMemcpy(res, d_res, 64, cudaMemcpyDeviceToHost) == cudaSuccess ? (int)res[5] : VSZ_ERR_CUDA;
+            if (rc == VSZ_OK) {
+                arch.resize(res[0] + res[1]);
+                if (cudaMemcpy(arch.data(), d_arch, arch.size(), cudaMemcpyDeviceToHost) != cudaSuccess) rc = VSZ_ERR_CUDA;
+            }
+        }
+    }
+    cudaFree(d_in);
+    cudaFree(d_ws);
+    cudaFree(d_arch);
+    cudaFree(d_res);
+    if (rc != VSZ_OK) return rc;
+    size_t ls = 0;
+    uint8_t* out = nullptr;
+    size_t total = 0;
+    if (p->lossless != VSZ_LOSSLESS_NONE) {
+        uint8_t* frame = nullptr;
+        VSZ_TRY(vsz_lossless_compress(p->lossless, arch.data(), res[0], &frame, &ls));
+        total = ls + res[1];
+        out   = static_cast<uint8_t*>(malloc(total ? total : 1));
+        if (!out) {
+            vsz_free_host(frame);
+            return VSZ_ERR_NOMEM;
+        }
+        memcpy(out, frame, ls);
+        memcpy(out + ls, arch.data() + res[0], res[1]);  // the trailer follows the frame
+        vsz_free_host(frame);
+    } else {
+        total = arch.size();
+        out   = static_cast<uint8_t*>(malloc(total ? total : 1));
+        if (!out) return VSZ_ERR_NOMEM;
+        memcpy(out, arch.data(), total);
+    }
+    *h_out = out;
+    if (out_bytes) *out_bytes = total;
+    if (data_size) *data_size = res[0];
+    if (lossless_size) *lossless_size = ls;
+    if (n_outlier) *n_outlier = res[2];
+    return VSZ_OK;
+}
+
+vsz_status vsz_decompress_host_f64(const uint8_t* h_archive, size_t len, size_t data_size, size_t lossless_size,
+                                   double** h_out, size_t* n) {
+    if (!h_archive || !h_out) return VSZ_ERR_INVALID;
+    *h_out = nullptr;
+    std::vector<uint8_t> arch;
+    if (lossless_size) {  // [frame][trailer]: undo the lossless pass, keep the trailer after the block
+        if (lossless_size > len) return VSZ_ERR_CORRUPT;
+        uint8_t* block = nullptr;
+        size_t blen    = 0;
+        VSZ_TRY(vsz_lossless_decompress(h_archive, lossless_size, data_size, &block, &blen));
+        arch.assign(block, block + blen);
+        vsz_free_host(block);
+        arch.insert(arch.end(), h_archive + lossless_size, h_archive + len);
+    } else {
+        arch.assign(h_archive, h_archive + len);
+    }
+    vsz_archive_desc d{};
+    VSZ_TRY(vsz_archive_parse(arch.data(), arch.size(), &d));
+    size_t ws = 0;
+    VSZ_TRY(vsz_decompress_f64_bounds(&d, &ws));
+    const size_t count = d.dims[0] * d.dims[1] * d.dims[2];
+    uint8_t *d_arch = nullptr, *d_ws = nullptr;
+    double* d_out = nullptr;
+    int* d_st     = nullptr;
+    int rc = VSZ_ERR_NOMEM, st = VSZ_OK;
+    double* out = static_cast<double*>(malloc(8 * (count ? count : 1)));
+    if (out && cudaMalloc(reinterpret_cast<void**>(&d_arch), arch.size() + 64) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&d_ws), ws) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&d_out), 8 * count) == cudaSuccess &&
+        cudaMalloc(reinterpret_cast<void**>(&d_st), 4) == cudaSuccess) {
+        rc = VSZ_ERR_CUDA;
+        if (cudaMemset(d_arch + arch.size(), 0, 64) == cudaSuccess &&
+            cudaMemcpy(d_arch, arch.data(), arch.size(), cudaMemcpyHostToDevice) == cudaSuccess) {
+            rc = vsz_decompress_f64(&d, d_arch, d_ws, ws, d_out, d_st, nullptr);
+            if (rc == VSZ_OK && (cudaMemcpy(&st, d_st, 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                                 cudaMemcpy(out, d_out, 8 * count, cudaMemcpyDeviceToHost) != cudaSuccess))
+                rc = VSZ_ERR_CUDA;
+            if (rc == VSZ_OK) rc = st;
+        }
+    }
+    cudaFree(d_arch);
+    cudaFree(d_ws);
+    cudaFree(d_out);
+    cudaFree(d_st);
+    if (rc != VSZ_OK) {
+        free(out);
+        return rc;
+    }
+    *h_out = out;
+    if (n) *n = count;
+    return VSZ_OK;
+}
 
 }  // extern "C"

@@ -132,7 +132,7 @@ int field_of(const vsz_dbatch_field& F, DField& out) {
     // the batch needs this library's index (trailer) and the block-8 kernels; padded and strict
     // archives go through vsz_decompress
     if (!d.has_trailer || d.chunk_syms != (uint32_t)kChunkSyms) return VSZ_ERR_UNSUPPORTED;
-    if (d.block_size != 8 || d.n_pad != 0 || d.strict) return VSZ_ERR_UNSUPPORTED;
+    if (d.block_size != 8 || d.n_pad != 0 || d.strict || d.f64) return VSZ_ERR_UNSUPPORTED;
     if (!valid_dict(d.dict_size) || !(d.eb_final > 0)) return VSZ_ERR_CORRUPT;
     out.g    = make_geometry(d.ndim, dims);
     out.nsym = d.dict_size;

@@ -169,6 +169,28 @@ int launch_dq_redo_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t
 int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* seg_zero, cudaStream_t st,
                        int num_sms);
 
+// ---- f64 fields (dq_f64.cu) ---------------------------------------------------------------
+struct F64Args {
+    const double* x;          // compress: the field
+    long long* s;             // compress: prequantized values (n)
+    uint16_t* code;           // codes (n): written by compress, read by decompress and the gather
+    unsigned long long* hist; // compress: dict bins
+    const Consts* consts;
+    int* status;
+    size_t n;
+    uint32_t d0, d1, d2;
+    int bs, dict;
+    uint8_t* archive;             // compress: the archive (the gather writes its outlier section)
+    const uint8_t* outliers;      // decompress: the archive's outlier section (8 bytes each, any alignment)
+    unsigned long long n_out;     // decompress: outliers in it
+    double* out;                  // decompress: the field
+};
+int launch_eb_setup_f64(int mode, double eb, const double* d_in, size_t n, Consts* c, unsigned long long* mm,
+                        int* status, cudaStream_t st, int num_sms);
+int launch_dq_compress_f64(F64Args a, int ndim, cudaStream_t st, int num_sms);
+int launch_gather_f64(F64Args a, const unsigned long long* seg_off, DevOffset out_off, cudaStream_t st, int num_sms);
+int launch_dq_decompress_f64(F64Args a, int ndim, const unsigned long long* seg_off, cudaStream_t st);
+
 int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_consts, uint32_t* d_mm,
                     cudaStream_t st, int* status_word = nullptr);
 int launch_dq_compress(DqArgs a, int ndim, int bs, cudaStream_t st, int num_sms);
