@@ -43,7 +43,7 @@ def _smooth(dims, seed):
     if len(dims) == 2:
         return fields.bump_field_2d(dims[1], dims[0], seed=seed).astype(np.float64).ravel() * 1.0e4
     g = fields.grf_3d(dims[2], dims[1], dims[0], seed=seed).astype(np.float64)
-    return (g * np.pi + 1.0e-3 * g * g).ravel()  # a log-normal field, not representable in f32 as is
+    return (g * np.pi + 1.0e-3 * g * g).ravel()  # full double mantissas: not representable in f32 as is
 
 
 @pytest.mark.parametrize("dims", [(100003,), (257, 131), (70, 33, 21), (64, 64, 32)])
