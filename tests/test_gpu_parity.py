@@ -298,11 +298,13 @@ def test_long_codewords_dict4096_match_oracle(cuda):
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y_or.view(np.uint32))
 
 
-@pytest.mark.parametrize("dims,bs", [((96, 40), 8), ((37, 41, 43), 8), ((5000,), 16), ((64, 64, 16), 16)])
-def test_nan_inputs_keep_reference_bits(cuda, dims, bs):
+@pytest.mark.parametrize("dims,bs,mode", [((96, 40), 8, "abs"), ((37, 41, 43), 8, "abs"), ((5000,), 16, "abs"),
+                                          ((64, 64, 16), 16, "abs"), ((37, 41, 43), 8, "r2r"), ((64, 64, 16), 16, "r2r")])
+def test_nan_inputs_keep_reference_bits(cuda, dims, bs, mode):
     """NaN inputs (quiet with payloads, negative, signalling): the reference's arithmetic keeps a
     NaN operand's bits, quieted, where the GPU's would give its canonical NaN; outliers and
-    reconstructions must carry the reference's bits."""
+    reconstructions must carry the reference's bits, in abs and r2r mode (whose value range skips
+    the NaNs)."""
     rng = np.random.default_rng(sum(dims) + bs)
     n = int(np.prod(dims))
     x = (np.cumsum(rng.standard_normal(n)) * 0.1).astype(np.float32)
@@ -312,11 +314,14 @@ def test_nan_inputs_keep_reference_bits(cuda, dims, bs):
     bits[idx[4:8]] = 0xffc00001
     bits[idx[8:]] = 0x7f800005   # signalling
     bits[0] = 0x7fc0beef
-    c = V.compress(x, dims, eb=1e-3, dict_size=1024, block_size=bs)
-    oa, _ = O.compress(x, dims, bs, 1024, 1e-3, False)
+    if mode == "r2r":
+        bits[0] = x.view(np.uint32)[1]  # a finite first value: the range skips NaNs after it
+    c = V.compress(x, dims, eb=1e-3, mode=mode, dict_size=1024, block_size=bs)
+    oa, _ = O.compress(x, dims, bs, 1024, 1e-3, mode == "r2r")
     assert c.data[:c.data_size] == oa
     y = V.decompress(c)
-    np.testing.assert_array_equal(y.view(np.uint32), O.decompress(oa, bs, 1024).view(np.uint32))
+    vr = O.value_range(x) if mode == "r2r" else 0.0
+    np.testing.assert_array_equal(y.view(np.uint32), O.decompress(oa, bs, 1024, vr).view(np.uint32))
 
 
 def test_host_ops_match_host_entry_points(cuda):

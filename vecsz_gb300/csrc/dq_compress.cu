@@ -116,8 +116,10 @@ __device__ __forceinline__ void consts_of(int mode, double eb, const uint32_t* _
         uint32_t e = __float_as_uint(f) & 0x7f800000u;
         return e != 0u && e != 0x7f800000u;
     };
-    c->dq_fast = normal(ch) && (cl == 0.0f || normal(cl));
-    c->status  = status;
+    c->dq_fast  = normal(ch) && (cl == 0.0f || normal(cl));
+    c->status   = status;
+    c->dq_mul   = 0;  // until k_dq_mul_verify has checked the two-operation dequantization
+    c->dq_exc   = 0.f;
     if (status != VSZ_OK && status_word) set_status(status_word, status);
 }
 
@@ -185,9 +187,20 @@ __device__ __forceinline__ void emit_row(const DqArgs& a, size_t row, uint32_t x
         for (int j = 0; j < 4; j++)
             if (in[j]) crow[xb + j] = (uint16_t)code[j];
     }
+    if (s_hist) {
+        // predicated, not branched: the zero-residual code counts in a register, the others in the
+        // block's shared histogram
 #pragma unroll
-    for (int j = 0; j < 4; j++)
-        if (in[j]) h.add(code[j], a.R, s_hist, a.dict, a.hist);
+        for (int j = 0; j < 4; j++) {
+            const bool hot = code[j] == a.R;
+            h.c1 += (in[j] && hot) ? 1u : 0u;
+            if (in[j] && !hot) atomicAdd(&s_hist[code[j]], 1u);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (in[j]) h.add(code[j], a.R, s_hist, a.dict, a.hist);
+    }
     // Outlier ranking inside the row segment: element (lane, j) precedes (lane', j') iff
     // 4 lane + j < 4 lane' + j'.  Most rows of a smooth field have none: one vote decides.
     bool o[4];

@@ -372,7 +372,7 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
                     for (int h = 0; h < 2; h++) {
                         float xo[4];
 #pragma unroll
-                        for (int k = 0; k < 4; k++) xo[k] = dequant(C[4 * h + k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                        for (int k = 0; k < 4; k++) xo[k] = dequant_small(C[4 * h + k], c);
                         __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
                     }
                 }
@@ -384,6 +384,43 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
             a.redo[1 + i]    = u;
         }
     }
+}
+
+// Checks, for every integer 0 < s < 2^21, the two-operation dequantization of dequant_small()
+// against the reference's (float)((double)s * c_d), and sets c->dq_mul (negative s follow: both
+// forms are odd).  scratch: 3 words, zero on entry (mismatches, one mismatching s, block ticket);
+// the last block to finish sets the mode and zeroes scratch[0] again.
+__global__ void __launch_bounds__(256) k_dq_mul_verify(Consts* __restrict__ c, uint32_t* __restrict__ scratch) {
+    __shared__ uint32_t s_bad;
+    const Consts k = *c;
+    if (threadIdx.x == 0) s_bad = 0;
+    __syncthreads();
+    uint32_t bad = 0, which = 0;
+    if (k.status == VSZ_OK) {
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x + 1; i < (1u << 21); i += gridDim.x * blockDim.x) {
+            const float s   = (float)i;  // exact
+            const float y1  = __fmaf_rn(s, k.c_hi, __fmul_rn(s, k.c_lo));
+            const float y2  = __double2float_rn(__dmul_rn((double)i, k.c_d));
+            const bool diff = __float_as_uint(y1) != __float_as_uint(y2);
+            bad += diff ? 1u : 0u;
+            which = diff ? i : which;
+        }
+    }
+    if (bad) {
+        atomicAdd(&s_bad, bad);
+        atomicExch(&scratch[1], which);
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    if (s_bad) atomicAdd(&scratch[0], s_bad);
+    __threadfence();
+    if (atomicAdd(&scratch[2], 1u) != gridDim.x - 1) return;
+    __threadfence();
+    const uint32_t nbad = atomicAdd(&scratch[0], 0u), s1 = atomicAdd(&scratch[1], 0u);
+    const int mode      = k.status != VSZ_OK ? 0 : nbad == 0 ? 1 : nbad == 1 ? 2 : 0;
+    c->dq_exc   = mode == 2 ? (float)s1 : 0.f;
+    c->dq_mul   = mode;
+    scratch[0]  = 0u;  // the separable pass counts its redo units here
 }
 
 __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
@@ -654,6 +691,9 @@ int launch_dq_redo_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
+// Fields from this size on check the two-operation dequantization before the separable pass.
+constexpr size_t kDqVerifyMin = (size_t)1 << 22;
+
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms) {
     if (a.n == 0) return VSZ_OK;
     if (bs == 8 && !force_general) {
@@ -677,8 +717,15 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
             else if (ndim == 2) vec ? go(k_dq_decompress_b8<2, true, true>, 2) : go(k_dq_decompress_b8<2, false, true>, 2);
             else vec ? go(k_dq_decompress_b8<1, true, true>, 1) : go(k_dq_decompress_b8<1, false, true>, 1);
         } else if (dq_b8_separable(a, ndim)) {
-            // separable pass, then the reference-order kernel over the units it listed
-            if (cudaMemsetAsync(a.redo, 0, sizeof(uint32_t), st) != cudaSuccess) return VSZ_ERR_CUDA;
+            // separable pass, then the reference-order kernel over the units it listed.  A large
+            // field first checks the cheaper dequantization (a few microseconds, all SMs).
+            const bool verify = a.consts_rw && a.n >= kDqVerifyMin;
+            if (cudaMemsetAsync(a.redo, 0, (verify ? 3 : 1) * sizeof(uint32_t), st) != cudaSuccess)
+                return VSZ_ERR_CUDA;
+            if (verify) {
+                k_dq_mul_verify<<<(unsigned)num_sms * 4, 256, 0, st>>>(a.consts_rw, a.redo);
+                count_launch();
+            }
             go(k_dq_decompress_b8s, 3);
             go(k_dq_decompress_b8<3, true, false, true>, 3);
         } else {

@@ -370,9 +370,14 @@ __device__ __forceinline__ void count_chunks(const HuffEncodeArgs& a, size_t c, 
     for (; c < c1; c += cstep) {
         const Codes16 cc = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
         uint32_t bits    = 0;
+        if (cc.nvalid == (uint32_t)kEncPerThread) {  // all but the field's last lanes
 #pragma unroll
-        for (int k = 0; k < kEncPerThread; k++)
-            if ((uint32_t)k < cc.nvalid) bits += cl[code_k(cc, k)];
+            for (int k = 0; k < kEncPerThread; k++) bits += cl[code_k(cc, k)];
+        } else {
+#pragma unroll
+            for (int k = 0; k < kEncPerThread; k++)
+                if ((uint32_t)k < cc.nvalid) bits += cl[code_k(cc, k)];
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) bits += __shfl_xor_sync(0xffffffffu, bits, o);
         if (lane == 0) a.chunk_bits[c] = (uint16_t)bits;  // <= 512 x 64
@@ -508,7 +513,11 @@ __device__ __forceinline__ void pack_chunks(const HuffEncodeArgs& a, size_t c, s
 
 // Codewords of at most kPackFastLen bits: the codebook is one u32 per symbol in shared memory,
 // (codeword << 6) | length, and a lane appends its 16 codewords to a right-aligned 64-bit
-// accumulator with no per-code branches but the word flush -- the same words as pack_chunks.
+// accumulator with no branch at all: the word a codeword completes is stored under a predicate.
+// A word is completed -- and stored, with a plain store -- by exactly one lane, the one holding
+// its last bit; the bits of it that earlier lanes hold are their unfinished tails, OR-ed in after
+// a warp barrier.  The chunk's last word may be completed by nobody, so it alone is zeroed
+// first.  Same words as pack_chunks.
 constexpr uint32_t kPackFastLen = 26;
 
 __device__ __forceinline__ void pack_chunks_fast(const HuffEncodeArgs& a, size_t c, size_t c1, size_t cstep,
@@ -527,15 +536,24 @@ __device__ __forceinline__ void pack_chunks_fast(const HuffEncodeArgs& a, size_t
     uint32_t* gw         = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(out) & ~(uintptr_t)3);
     const unsigned long long off0 = a.chunk_off[0];
     Codes16 nxt                   = load_codes16(a, c * kEncChunk + lane * kEncPerThread);
+    unsigned long long nxt_off    = c < c1 ? a.chunk_off[c] : 0ull;
     for (; c < c1; c += cstep) {
         const Codes16 cc = nxt;
-        if (c + cstep < c1) nxt = load_codes16(a, (c + cstep) * kEncChunk + lane * kEncPerThread);
-        uint32_t e[kEncPerThread], bits = 0;
-#pragma unroll
-        for (int k = 0; k < kEncPerThread; k++) {
-            e[k] = ((uint32_t)k < cc.nvalid) ? s_tab[code_k(cc, k)] : 0u;
-            bits += e[k] & 63u;
+        const unsigned long long coff = nxt_off;
+        if (c + cstep < c1) {
+            nxt     = load_codes16(a, (c + cstep) * kEncChunk + lane * kEncPerThread);
+            nxt_off = a.chunk_off[c + cstep];
         }
+        uint32_t e[kEncPerThread], bits = 0;
+        if (cc.nvalid == (uint32_t)kEncPerThread) {  // all but the field's last lanes
+#pragma unroll
+            for (int k = 0; k < kEncPerThread; k++) e[k] = s_tab[code_k(cc, k)];
+        } else {
+#pragma unroll
+            for (int k = 0; k < kEncPerThread; k++) e[k] = ((uint32_t)k < cc.nvalid) ? s_tab[code_k(cc, k)] : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kEncPerThread; k++) bits += e[k] & 63u;
         uint32_t incl = bits;  // warp inclusive scan of lane bit counts
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -543,33 +561,30 @@ __device__ __forceinline__ void pack_chunks_fast(const HuffEncodeArgs& a, size_t
             if (lane >= (unsigned)o) incl += t;
         }
         const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-        const unsigned long long gstart = base0 + (a.chunk_off[c] - off0);
+        const unsigned long long gstart = base0 + (coff - off0);  // chunk's first bit on the word grid
         const uint32_t r0               = (uint32_t)(gstart & 31u);
         const unsigned long long F      = gstart >> 5;
         const uint32_t nwords           = tot ? (r0 + tot + 31) >> 5 : 0u;
-        for (uint32_t i = lane; i < nwords; i += 32) sw[i] = 0u;
+        if (lane == 0 && nwords) sw[nwords - 1] = 0u;
         __syncwarp();
-        if (bits) {
-            const uint32_t pos = r0 + incl - bits;
-            uint32_t wi        = pos >> 5;
-            uint32_t nb        = pos & 31u;  // bits pending in acc; the leading ones belong to the lane before
-            const bool shared0 = nb != 0;    // my first word is shared with the lane before
-            unsigned long long acc = 0;      // right-aligned pending bits
+        const uint32_t pos = r0 + incl - bits;
+        uint32_t wi        = pos >> 5;
+        uint32_t nb        = pos & 31u;  // bits pending in hi:lo; the leading ones belong to earlier lanes
+        uint32_t hi = 0, lo = 0;         // right-aligned pending bits (above them: spent bits)
 #pragma unroll
-            for (int k = 0; k < kEncPerThread; k++) {
-                const uint32_t l = e[k] & 63u;
-                acc = (acc << l) | (e[k] >> 6);
-                nb += l;
-                if (nb >= 32) {
-                    nb -= 32;
-                    const uint32_t w = (uint32_t)(acc >> nb);
-                    if (shared0 && wi == (pos >> 5)) atomicOr(&sw[wi], w);
-                    else sw[wi] = w;
-                    wi++;
-                }
-            }
-            if (nb > 0) atomicOr(&sw[wi], (uint32_t)(acc << (32 - nb)));
+        for (int k = 0; k < kEncPerThread; k++) {
+            const uint32_t l = e[k] & 63u;  // <= 26: 32-bit funnel shifts move the 64-bit pair
+            hi = __funnelshift_l(lo, hi, l);
+            lo = (lo << l) | (e[k] >> 6);
+            nb += l;
+            const bool done  = nb >= 32u;
+            const uint32_t w = __funnelshift_r(lo, hi, nb - 32u);  // nb <= 57
+            if (done) sw[wi] = w;
+            wi += done ? 1u : 0u;
+            nb -= done ? 32u : 0u;
         }
+        __syncwarp();
+        if (bits && nb > 0) atomicOr(&sw[wi], lo << (32 - nb));
         __syncwarp();
         const bool first_partial = (r0 != 0);
         const bool last_partial  = ((r0 + tot) & 31u) != 0;
@@ -606,7 +621,11 @@ __global__ void __launch_bounds__(kEncThreads, 4)
         const BatchTask tk      = tasks[t];
         const HuffEncodeArgs& a = args[tk.field];
         if (*a.status != VSZ_OK) continue;  // no kernel of this launch writes it
-        pack_chunks(a, tk.u0 + (threadIdx.x >> 5), tk.u1, kEncThreads / 32, s_dyn);
+        // the field's longest codeword: uniform over the task
+        if (a.cb_in_smem && a.build_info && a.build_info[2] <= kPackFastLen)
+            pack_chunks_fast(a, tk.u0 + (threadIdx.x >> 5), tk.u1, kEncThreads / 32, s_dyn);
+        else
+            pack_chunks(a, tk.u0 + (threadIdx.x >> 5), tk.u1, kEncThreads / 32, s_dyn);
         __syncthreads();
     }
 }
@@ -991,20 +1010,22 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 // most one word, so the move and the ring read are predicated, not branched.  Words come from a
 // per-lane ring of kWinRing 16-byte blocks in shared memory that cp.async keeps filled ahead of
 // the window: one round reads at most kWinRound * 32 bits = 8 words, and the blocks holding them
-// have landed at the round's start.  The warp diverges only on codewords
-// longer than the primary table.  Decoded codes are packed in registers and stored 16 bytes per
-// lane per round.
+// have landed at the round's start.  Block and word counters are 32-bit and relative to the
+// chunk's first 16-byte block.  The warp diverges only on codewords longer than the primary
+// table.  Decoded codes are packed in registers and stored 16 bytes per lane per round.
 // ------------------------------------------------------------------------------------------
 constexpr int kWinMaxLen    = 32;
 constexpr int kWinRound     = 8;
 constexpr int kWinRing      = 8;    // blocks of 16 bytes per lane
+constexpr int kWinLaneWords = kWinRing * 4 + 4;  // a lane's ring, padded: lanes 8 apart share banks
 constexpr int kWinThreads   = 256;  // one primary table per CTA, shared by its warps
 constexpr int kWinMinBlocks = 4;
-constexpr size_t kWinSmem   = (sizeof(uint32_t) << kDecBits) + (size_t)(kWinThreads / 32) * kWinRing * 32 * 16;
+constexpr size_t kWinSmem   = (sizeof(uint32_t) << kDecBits) + (size_t)kWinThreads * kWinLaneWords * 4;
+typedef uint32_t WinRing[32][kWinLaneWords];  // one warp's rings, [lane][word]
 
 // Lane j of the calling warp decodes chunk j (the table is in s_table; no block barrier inside).
 __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t j, const uint32_t* s_table,
-                                                uint4 (*s_ring)[kWinRing][32]) {
+                                                WinRing* s_ring) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     if (j - lane >= a.nchunks) return;
     const unsigned long long out0 = (unsigned long long)j * kChunkSyms;
@@ -1014,31 +1035,32 @@ __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t 
     const uint8_t* g16   = reinterpret_cast<const uint8_t*>(reinterpret_cast<uintptr_t>(a.payload) & ~(uintptr_t)15);
     // readable bytes from g16: the payload plus the 8 bytes past its end that callers provide
     const unsigned long long readable = base0 / 8u + (a.payload_bits + 7) / 8 + 8;
-    uint4* ring           = &s_ring[warp][0][lane];
-    const uint32_t* ringw = reinterpret_cast<const uint32_t*>(ring);  // word k of slot s: ringw[128 s + k]
-    auto fetch = [&](unsigned long long b) {  // block b into slot b % kWinRing, one commit group
-        const unsigned long long o = b * 16;
-        const uint32_t nb = o >= readable ? 0u : (uint32_t)min(16ull, readable - o);
-        cp_async16_zfill(ring + 32 * (uint32_t)(b % kWinRing), g16 + (nb ? o : 0), nb);
-        cp_async_commit();
-    };
-    auto ring_word = [&](unsigned long long w) -> uint32_t {
-        return bswap32(ringw[128u * ((uint32_t)(w >> 2) % kWinRing) + ((uint32_t)w & 3u)]);
-    };
+    uint32_t* ring = s_ring[warp][lane];
     bool bad = false;
-    unsigned long long cb = 0, wn = 0, breq = 0;
-    uint32_t off = 0;
+    unsigned long long cb = 0;
+    const uint8_t* gb = g16;  // the chunk's first 16-byte block
+    uint32_t rem = 0;         // readable bytes from gb (clamped)
+    uint32_t off = 0, wn = 0, breq = 0;  // bit offset in w0; next word to enter the window; next block
     if (cnt) {
         // offsets relative to the field's first chunk (a batch scans all fields' indexes at once)
         const unsigned long long sb = a.start_bit[j] - a.start_bit[0];
         cb = a.chunk_len[j];
         if (sb + cb > a.payload_bits) bad = true;
         const unsigned long long pos0 = base0 + sb;
-        off  = (uint32_t)(pos0 & 31u);
-        wn   = pos0 >> 5;  // next word to enter the window
-        breq = wn >> 2;
+        const unsigned long long b0   = pos0 >> 7;
+        gb  = g16 + b0 * 16;
+        rem = b0 * 16 >= readable ? 0u : (uint32_t)min(readable - b0 * 16, 0x7fffffffull);
+        off = (uint32_t)(pos0 & 31u);
+        wn  = (uint32_t)(pos0 >> 5) & 3u;
     }
     const bool live = cnt && !bad;
+    auto fetch = [&](uint32_t b) {  // block b into slot b % kWinRing, one commit group
+        const uint32_t o  = b * 16u;
+        const uint32_t nb = o >= rem ? 0u : min(16u, rem - o);
+        cp_async16_zfill(ring + 4u * (b % (uint32_t)kWinRing), gb + (nb ? o : 0u), nb);
+        cp_async_commit();
+    };
+    auto ring_word = [&](uint32_t w) -> uint32_t { return bswap32(ring[w % (uint32_t)(4 * kWinRing)]); };
     // blocks [wn / 4, wn / 4 + kWinRing - 1) stay requested: the slot a fetch overwrites held a
     // block whose words entered the window at least one block earlier; with kWinRing / 2 groups
     // allowed in flight, blocks wn / 4 .. + 2 (at least 9 words from wn) have landed
@@ -1052,13 +1074,13 @@ __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t 
         w2 = ring_word(wn + 2);
         wn += 3;
     }
-    const unsigned long long pos_first = wn * 32ull + off;  // the first bit (wn counts the 3 window words)
+    const uint32_t pos_first = wn * 32u + off;  // the first bit (wn counts the 3 window words)
     uint32_t zeros = 0;
     uint16_t* dst = a.codes + out0;
     for (uint32_t r0 = 0; r0 < (uint32_t)kChunkSyms; r0 += kWinRound) {
         const uint32_t m = (live && cnt > r0) ? min((uint32_t)kWinRound, cnt - r0) : 0u;
         if (m) {
-            const unsigned long long bneed = (wn >> 2) + kWinRing - 1;
+            const uint32_t bneed = (wn >> 2) + kWinRing - 1;
             while (breq < bneed) fetch(breq++);
         }
         cp_async_wait<kWinRing / 2>();
@@ -1131,17 +1153,17 @@ __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t 
         }
     }
     cp_async_wait<0>();  // no copy into this CTA's shared memory may outlive it
-    // bits consumed: the position now minus the first
-    const unsigned long long used = live ? wn * 32ull + off - pos_first : 0ull;
+    // bits consumed: the position now minus the first (a chunk spans < 2^32 bits)
+    const unsigned long long used = live ? (unsigned long long)(wn * 32u + off - pos_first) : 0ull;
     if (cnt && (bad || used != cb)) set_status(a.status, VSZ_ERR_CORRUPT);  // must fill exactly its length
     if (j < a.nchunks && a.chunk_zero) a.chunk_zero[j] = zeros;
 }
 
 __global__ void __launch_bounds__(kWinThreads, kWinMinBlocks) k_huff_decode_win(HuffDecodeArgs a) {
     extern __shared__ __align__(16) uint8_t s_win_dyn[];
-    // [primary table: 1 << kDecBits words][ring: warp][slot][lane] x 16 bytes (kWinSmem bytes)
-    uint32_t* s_table             = reinterpret_cast<uint32_t*>(s_win_dyn);
-    uint4 (*s_ring)[kWinRing][32] = reinterpret_cast<uint4 (*)[kWinRing][32]>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
+    // [primary table: 1 << kDecBits words][rings: warp][lane][kWinLaneWords] (kWinSmem bytes)
+    uint32_t* s_table = reinterpret_cast<uint32_t*>(s_win_dyn);
+    WinRing* s_ring   = reinterpret_cast<WinRing*>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
     if (!a.tree_info || a.tree_info[2] > (uint32_t)kWinMaxLen) return;  // uniform: k_huff_decode_idx's trees
     for (int i = threadIdx.x; i < (1 << kDecBits); i += blockDim.x) s_table[i] = a.table[i];
     __syncthreads();
@@ -1359,8 +1381,8 @@ __global__ void __launch_bounds__(256) k_huff_decode_idx(HuffDecodeArgs a) {
 __global__ void __launch_bounds__(kWinThreads, kWinMinBlocks)
     k_huff_decode_win_batch(const HuffDecodeArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
     extern __shared__ __align__(16) uint8_t s_win_dyn[];
-    uint32_t* s_table             = reinterpret_cast<uint32_t*>(s_win_dyn);
-    uint4 (*s_ring)[kWinRing][32] = reinterpret_cast<uint4 (*)[kWinRing][32]>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
+    uint32_t* s_table = reinterpret_cast<uint32_t*>(s_win_dyn);
+    WinRing* s_ring = reinterpret_cast<WinRing*>(s_win_dyn + (sizeof(uint32_t) << kDecBits));
     for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
         const BatchTask tk     = tasks[t];
         const HuffDecodeArgs a = args[tk.field];

@@ -1122,6 +1122,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
     a.pad    = pad_view_of(d, bs, d_archive);
     a.redo   = w.redo;
+    a.consts_rw = w.consts;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

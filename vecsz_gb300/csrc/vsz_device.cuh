@@ -55,6 +55,9 @@ struct Consts {
     float c_lo;       // (float)(c_d - c_hi)
     int dq_fast;      // 1 when c_hi and c_lo are normal floats, so dequant() may take its FP32 path
     int status;       // VSZ_OK, or why the constants are unusable (zero value range)
+    int dq_mul;       // dequant_small(): 0 dequant(); 1 fmaf(s, c_hi, s * c_lo) is exact for every
+                      // integer |s| < 2^21; 2 the same except at s = +-dq_exc (k_dq_mul_verify)
+    float dq_exc;     // the one s > 0 where the two-operation form differs (dq_mul 2)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -114,6 +117,17 @@ __device__ __forceinline__ float dequant(float s, double c_d, float c_hi, float 
     }
     if (ok) return y;
     return dequant_fp64(s, c_d);
+}
+
+// Dequantization of an integer |s| < 2^21 (the separable reverse Lorenzo's values; larger ones are
+// redone through dequant()).  When k_dq_mul_verify has compared, for every such s, the
+// two-operation form RN32(s * c_hi + RN32(s * c_lo)) with the reference's (float)((double)s * c_d)
+// and found them equal (or equal but at one pair +-dq_exc), that form is used; both are odd in s.
+__device__ __forceinline__ float dequant_small(float s, const Consts& c) {
+    if (c.dq_mul == 0) return dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+    float y = __fmaf_rn(s, c.c_hi, __fmul_rn(s, c.c_lo));
+    if (c.dq_mul == 2 && fabsf(s) == c.dq_exc) y = dequant_fp64(s, c.c_d);
+    return y;
 }
 
 // Order-preserving map of floats onto unsigned integers (NaNs are skipped by the caller).

@@ -152,6 +152,8 @@ struct DqDecArgs {
     PadView pad;                         // padded archive: the halo of each block (vals = pad section)
     uint32_t* redo;                      // 3D block 8, separable pass: [0] count, then units whose
                                          // values left the exact range (null: reference order only)
+    Consts* consts_rw;                   // the same constants when writable: the separable pass of a
+                                         // large field records its dequantization check there (or null)
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
