@@ -120,6 +120,7 @@ __device__ __forceinline__ void consts_of(int mode, double eb, const uint32_t* _
     c->status   = status;
     c->dq_mul   = 0;  // until k_dq_mul_verify has checked the two-operation dequantization
     c->dq_exc   = 0.f;
+    c->dq_exc_y = 0.f;
     if (status != VSZ_OK && status_word) set_status(status_word, status);
 }
 
@@ -466,7 +467,7 @@ __device__ __forceinline__ void dq23_units(const DqArgs& a, const Consts& c, uns
 }
 
 template <int NDIM, int BS, bool VEC, bool TAIL, bool STRICT = false, bool PAD = false>
-__global__ void __launch_bounds__(256, 3) k_dq_compress_23d(DqArgs a) {
+__global__ void __launch_bounds__(256, 4) k_dq_compress_23d(DqArgs a) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
     uint32_t* s_hist = a.smem_hist ? s_dyn : nullptr;
     PrevRows* s_prev = reinterpret_cast<PrevRows*>(s_dyn + (a.smem_hist ? ((a.dict + 3) & ~3) : 0));

@@ -305,6 +305,13 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
                 const bool all_in = row_in && col_in;
                 const uint4 cv    = cv_next;
                 cv_next           = (y < 7) ? load_row(zz, y + 1) : load_row(zz + 1, 0);
+                {  // the row 4 ahead into L2 (rows of this unit only): the load one row ahead then hits L2
+                    const int za = y < 4 ? zz : zz + 1, ya = (y + 4) & 7;
+                    if (col_in && za < nz && ya < ny) {
+                        const size_t rowa = (size_t)(z0 + za) * a.d1 + (y0 + ya);
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.codes + rowa * a.d0 + x0));
+                    }
+                }
                 const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
                 auto code_at = [&](int k) -> uint32_t { return (cw[k >> 1] >> (16 * (k & 1))) & 0xffffu; };
                 // outliers of this row segment, ranked in row-major order (as k_dq_decompress_b8)
@@ -419,6 +426,7 @@ __global__ void __launch_bounds__(256) k_dq_mul_verify(Consts* __restrict__ c, u
     const uint32_t nbad = atomicAdd(&scratch[0], 0u), s1 = atomicAdd(&scratch[1], 0u);
     const int mode      = k.status != VSZ_OK ? 0 : nbad == 0 ? 1 : nbad == 1 ? 2 : 0;
     c->dq_exc   = mode == 2 ? (float)s1 : 0.f;
+    c->dq_exc_y = mode == 2 ? __double2float_rn(__dmul_rn((double)s1, k.c_d)) : 0.f;
     c->dq_mul   = mode;
     scratch[0]  = 0u;  // the separable pass counts its redo units here
 }

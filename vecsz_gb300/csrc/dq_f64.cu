@@ -91,6 +91,7 @@ __global__ void k_consts_f64(int mode, double eb, const unsigned long long* __re
     c->dq_fast  = 0;
     c->dq_mul   = 0;
     c->dq_exc   = 0.f;
+    c->dq_exc_y = 0.f;
     if (status == VSZ_OK && !(c->r_d > 0.0 && isfinite(c->r_d) && isfinite(c->c_d))) status = VSZ_ERR_INVALID;
     c->status = status;
     if (status != VSZ_OK && status_word) set_status(status_word, status);

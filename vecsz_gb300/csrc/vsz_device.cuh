@@ -58,6 +58,7 @@ struct Consts {
     int dq_mul;       // dequant_small(): 0 dequant(); 1 fmaf(s, c_hi, s * c_lo) is exact for every
                       // integer |s| < 2^21; 2 the same except at s = +-dq_exc (k_dq_mul_verify)
     float dq_exc;     // the one s > 0 where the two-operation form differs (dq_mul 2)
+    float dq_exc_y;   // (float)((double)dq_exc * c_d)
 };
 
 // ------------------------------------------------------------------------------------------
@@ -126,7 +127,7 @@ __device__ __forceinline__ float dequant(float s, double c_d, float c_hi, float 
 __device__ __forceinline__ float dequant_small(float s, const Consts& c) {
     if (c.dq_mul == 0) return dequant(s, c.c_d, c.c_hi, c.c_lo, c.dq_fast);
     float y = __fmaf_rn(s, c.c_hi, __fmul_rn(s, c.c_lo));
-    if (c.dq_mul == 2 && fabsf(s) == c.dq_exc) y = dequant_fp64(s, c.c_d);
+    if (c.dq_mul == 2 && fabsf(s) == c.dq_exc) y = copysignf(c.dq_exc_y, s);
     return y;
 }
 
