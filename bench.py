@@ -3,7 +3,7 @@
 
 A step is one compress of the workload field (device-resident input) followed by one decompress of
 the archive it produced.  `value` is input bytes (4 N) per second of step time over all ranks, with
---inflight (default 2) steps in flight at once, each on its own stream with its own workspace,
+--inflight (default 4) steps in flight at once, each on its own stream with its own workspace,
 archive and output, so that one step's host tree step and small kernels overlap another's kernels;
 `serial` is the same K steps one after another on one stream, and `compress_gbs` /
 `decompress_gbs`, the stage table and the roofline come from that serial pass.  `e2e` is the same round trip through the
@@ -62,10 +62,10 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="nyx512")
-    ap.add_argument("--inflight", type=int, default=2,
+    ap.add_argument("--inflight", type=int, default=4,
                     help="round trips in flight in the timed pass, each on its own stream (1: one stream)")
     ap.add_argument("--e2e-steps", type=int, default=40)
-    ap.add_argument("--e2e-ops", type=int, default=5, help="host operations in flight in the e2e pipeline")
+    ap.add_argument("--e2e-ops", type=int, default=3, help="host operations in flight in the e2e pipeline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain mixed field set")

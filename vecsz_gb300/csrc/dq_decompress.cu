@@ -271,6 +271,8 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
     const float rbias          = 8388608.0f + (float)R;
     const uint32_t rpair       = (uint32_t)R | ((uint32_t)R << 16);
     const unsigned lane        = lane_id();
+    // rows start on 32-byte boundaries (d0 % 8 == 0) when the output does
+    const bool out32           = (reinterpret_cast<uintptr_t>(a.out) & 31u) == 0;
 
     for (uint32_t u = first; u < end; u += stride) {
         const uint32_t xs = u % a.nxs;
@@ -375,12 +377,19 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
                 else row_pass(std::false_type{});
                 if (all_in) {
                     float* orow = a.out + row * a.d0;
+                    float xo[8];
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        float xo[4];
+                    for (int k = 0; k < 8; k++) xo[k] = dequant_small(C[k], c);
+                    if (out32) {  // the lane's 8 values are one 32-byte sector: one 256-bit store
+                        asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(orow + x0),
+                                     "f"(xo[0]), "f"(xo[1]), "f"(xo[2]), "f"(xo[3]), "f"(xo[4]), "f"(xo[5]), "f"(xo[6]),
+                                     "f"(xo[7])
+                                     : "memory");
+                    } else {
 #pragma unroll
-                        for (int k = 0; k < 4; k++) xo[k] = dequant_small(C[4 * h + k], c);
-                        __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h), make_float4(xo[0], xo[1], xo[2], xo[3]));
+                        for (int h = 0; h < 2; h++)
+                            __stcs(reinterpret_cast<float4*>(orow + x0 + 4 * h),
+                                   make_float4(xo[4 * h], xo[4 * h + 1], xo[4 * h + 2], xo[4 * h + 3]));
                     }
                 }
             }

@@ -576,12 +576,12 @@ __device__ __forceinline__ void pack_chunks_fast(const HuffEncodeArgs& a, size_t
             const uint32_t l = e[k] & 63u;  // <= 26: 32-bit funnel shifts move the 64-bit pair
             hi = __funnelshift_l(lo, hi, l);
             lo = (lo << l) | (e[k] >> 6);
-            nb += l;
-            const bool done  = nb >= 32u;
-            const uint32_t w = __funnelshift_r(lo, hi, nb - 32u);  // nb <= 57
+            nb += l;                         // <= 57
+            const bool done  = nb >= 32u;    // word wi is complete: the 32 bits above the nb - 32 newest
+            const uint32_t w = __funnelshift_r(lo, hi, nb);  // shift nb & 31, which is nb - 32 when done
             if (done) sw[wi] = w;
             wi += done ? 1u : 0u;
-            nb -= done ? 32u : 0u;
+            nb &= 31u;
         }
         __syncwarp();
         if (bits && nb > 0) atomicOr(&sw[wi], lo << (32 - nb));
@@ -1017,9 +1017,15 @@ __global__ void __launch_bounds__(256) k_huff_decode(HuffDecodeArgs a) {
 constexpr int kWinMaxLen    = 32;
 constexpr int kWinRound     = 8;
 constexpr int kWinRing      = 8;    // blocks of 16 bytes per lane
+constexpr int kWinWait      = 4;    // copy groups left in flight at a round's start
 constexpr int kWinLaneWords = kWinRing * 4 + 4;  // a lane's ring, padded: lanes 8 apart share banks
 constexpr int kWinThreads   = 256;  // one primary table per CTA, shared by its warps
 constexpr int kWinMinBlocks = 4;
+// Blocks wn / 4 .. wn / 4 + kWinRing - 2 are requested and all but the newest kWinWait have landed
+// at a round's start: at least 4 (kWinRing - 1 - kWinWait) - 3 words from wn, and a round of
+// kWinRound codewords of <= 32 bits moves the window by at most kWinRound words.
+static_assert(4 * (kWinRing - 1 - kWinWait) - 3 >= kWinRound, "a round may read words still in flight");
+static_assert((kWinRing & (kWinRing - 1)) == 0 && (kWinRound == 8 || kWinRound == 4), "ring and round shapes");
 constexpr size_t kWinSmem   = (sizeof(uint32_t) << kDecBits) + (size_t)kWinThreads * kWinLaneWords * 4;
 typedef uint32_t WinRing[32][kWinLaneWords];  // one warp's rings, [lane][word]
 
@@ -1062,11 +1068,10 @@ __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t 
     };
     auto ring_word = [&](uint32_t w) -> uint32_t { return bswap32(ring[w % (uint32_t)(4 * kWinRing)]); };
     // blocks [wn / 4, wn / 4 + kWinRing - 1) stay requested: the slot a fetch overwrites held a
-    // block whose words entered the window at least one block earlier; with kWinRing / 2 groups
-    // allowed in flight, blocks wn / 4 .. + 2 (at least 9 words from wn) have landed
+    // block whose words entered the window at least one block earlier
     if (live)
         for (int k = 0; k < kWinRing - 1; k++) fetch(breq++);
-    cp_async_wait<kWinRing / 2>();
+    cp_async_wait<kWinWait>();
     uint32_t w0 = 0, w1 = 0, w2 = 0;
     if (live) {
         w0 = ring_word(wn);
@@ -1077,14 +1082,27 @@ __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t 
     const uint32_t pos_first = wn * 32u + off;  // the first bit (wn counts the 3 window words)
     uint32_t zeros = 0;
     uint16_t* dst = a.codes + out0;
+    // full rounds are stored in pairs, a whole 32-byte sector at a time: the lanes of a warp write
+    // 32 different chunks, and a sector written in halves far apart can leave L2 half written
+    uint32_t pkp[kWinRound / 2] = {};
+    bool pend = false;  // pkp holds the full round before this one, not yet stored
+    // a pair of rounds starts on a 32-byte boundary of the chunk (1024 bytes); so of the field's
+    // codes when those are 32-byte aligned (workspace arrays are 256-byte aligned)
+    const bool sector_store = (reinterpret_cast<uintptr_t>(a.codes) & 31u) == 0;
+    auto store_round = [&](uint32_t at, const uint32_t* q) {
+        if constexpr (kWinRound == 8)
+            *reinterpret_cast<uint4*>(dst + at) = make_uint4(q[0], q[1], q[kWinRound / 2 - 2], q[kWinRound / 2 - 1]);
+        else
+            *reinterpret_cast<uint2*>(dst + at) = make_uint2(q[0], q[1]);
+    };
     for (uint32_t r0 = 0; r0 < (uint32_t)kChunkSyms; r0 += kWinRound) {
         const uint32_t m = (live && cnt > r0) ? min((uint32_t)kWinRound, cnt - r0) : 0u;
         if (m) {
             const uint32_t bneed = (wn >> 2) + kWinRing - 1;
             while (breq < bneed) fetch(breq++);
         }
-        cp_async_wait<kWinRing / 2>();
-        uint32_t pk[kWinRound / 2] = {0u, 0u, 0u, 0u};
+        cp_async_wait<kWinWait>();
+        uint32_t pk[kWinRound / 2] = {};
         // one codeword; a full round (m == kWinRound) runs it without per-code guards
         auto step = [&](int k) {
             const uint32_t win = __funnelshift_l(w1, w0, off);  // 32 bits from the current position
@@ -1144,14 +1162,36 @@ __device__ __forceinline__ void decode_win_lane(const HuffDecodeArgs& a, size_t 
         if (m == (uint32_t)kWinRound) {
 #pragma unroll
             for (int k = 0; k < kWinRound; k++) step(k);
-            *reinterpret_cast<uint4*>(dst + r0) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            if (pend) {
+                if constexpr (kWinRound == 8) {
+                    if (sector_store) {  // one 256-bit store: the whole sector in one request
+                        asm volatile("st.global.v8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(dst + r0 - kWinRound),
+                                     "r"(pkp[0]), "r"(pkp[1]), "r"(pkp[2]), "r"(pkp[3]), "r"(pk[0]), "r"(pk[1]),
+                                     "r"(pk[2]), "r"(pk[3])
+                                     : "memory");
+                    } else {
+                        store_round(r0 - kWinRound, pkp);
+                        store_round(r0, pk);
+                    }
+                } else {
+                    store_round(r0 - kWinRound, pkp);
+                    store_round(r0, pk);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < kWinRound / 2; k++) pkp[k] = pk[k];
+            }
+            pend = !pend;
         } else {
+            if (pend) store_round(r0 - kWinRound, pkp);
+            pend = false;
 #pragma unroll
             for (int k = 0; k < kWinRound; k++)
                 if ((uint32_t)k < m) step(k);
             for (uint32_t k = 0; k < m; k++) dst[r0 + k] = (uint16_t)(pk[k >> 1] >> (16 * (k & 1)));
         }
     }
+    if (pend) store_round((uint32_t)kChunkSyms - kWinRound, pkp);  // not reached: 512 / kWinRound is even
     cp_async_wait<0>();  // no copy into this CTA's shared memory may outlive it
     // bits consumed: the position now minus the first (a chunk spans < 2^32 bits)
     const unsigned long long used = live ? (unsigned long long)(wn * 32u + off - pos_first) : 0ull;
