@@ -12,6 +12,7 @@ import pytest
 
 import oracle as O
 import vecsz_gb300 as V
+from vecsz_gb300 import _lib as L
 from vecsz_gb300 import fields
 
 pytestmark = pytest.mark.gpu
@@ -138,3 +139,32 @@ def test_adversarial_fullsize_matches_oracle(cuda):
     assert c.n_outlier == meta["n_outlier"] and c.n_outlier > 0
     assert c.data[: c.data_size] == oa
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(oa, 8, 1024).view(np.uint32))
+
+
+def test_dequant_check_cached_per_workspace(cuda):
+    """Fields of 2^22 elements and more check the separable pass's two-operation dequantization
+    once per error bound and keep the result in the decompress workspace: decompressing through one
+    workspace fields with the same bound (a hit), another bound (a new check) and the first bound
+    again gives the oracle's reconstruction each time; bytes planted where the result is kept, with
+    a wrong check word, are not taken for a result."""
+    torch = cuda
+    dims = (256, 256, 256)
+    cases = [(fields.grf_3d(256, 256, 256, seed=s).ravel() * 0.01, eb) for s, eb in ((1, 1e-4), (2, 1e-4), (3, 1e-3))]
+    cases.append(cases[0])
+    codec = V.DeviceCodec(dims, eb=1e-4, mode="abs", dict_size=1024, block_size=8)
+    for i, (x, eb) in enumerate(cases + [cases[1]]):
+        oa, meta = O.compress(x, dims, 8, 1024, eb, False)
+        want = O.decompress(oa, 8, 1024)
+        c = V.compress(x, dims, eb=eb, mode="abs", dict_size=1024, block_size=8)
+        assert c.data[: c.data_size] == oa
+        codec.prepare_decompress(c.data, L.DecompressOpts(1024, 8, 0, 0.0))
+        if i == len(cases):
+            # the slot after the constants (workspace offset 256): c_d's bits, a mode, a bad check word
+            key = np.array([2.0 * eb], np.float64).view(np.uint64)[0]
+            junk = np.array([key, 1, 0, 12345], np.uint64).view(np.uint8)
+            codec._dws[256:288].copy_(torch.from_numpy(junk.copy()))
+        out = torch.empty(x.size, dtype=torch.float32, device="cuda")
+        d_arch = torch.from_numpy(np.concatenate([np.frombuffer(c.data, np.uint8), np.zeros(64, np.uint8)])).cuda()
+        codec.decompress(d_arch, out)
+        assert codec.decompress_status() == 0
+        np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), want.view(np.uint32))

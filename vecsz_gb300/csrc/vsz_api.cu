@@ -149,6 +149,7 @@ struct DecompressWs {
     int* s_changed;
     float* outliers;
     uint32_t* redo;  // units of the separable reverse Lorenzo that the reference-order kernel redoes
+    unsigned long long* dq_cache;  // the last dequantization check (k_dq_mul_verify), at a fixed offset
     size_t bytes;
 };
 
@@ -158,6 +159,7 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
     DecompressWs w{};
     uint32_t maxn = (uint32_t)(2 * dict);
     w.consts   = b.take<Consts>(1);
+    w.dq_cache = b.take<unsigned long long>(4);  // offset 256 whatever the field: kept across calls
     w.mm       = b.take<uint32_t>(4);
     w.status   = b.take<int>(4);
     w.table    = b.take<uint32_t>(1u << kDecBits);
@@ -1123,6 +1125,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.pad    = pad_view_of(d, bs, d_archive);
     a.redo   = w.redo;
     a.consts_rw = w.consts;
+    a.dq_cache  = w.dq_cache;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

@@ -154,6 +154,8 @@ struct DqDecArgs {
                                          // values left the exact range (null: reference order only)
     Consts* consts_rw;                   // the same constants when writable: the separable pass of a
                                          // large field records its dequantization check there (or null)
+    unsigned long long* dq_cache;        // 4 words kept across calls: the last check's c_d and result
+                                         // (or null)
 };
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
