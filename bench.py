@@ -864,7 +864,20 @@ def run_serving(V, seconds, rate, seed, budget_gb=120, slots=8, pool=48, items=N
     t_last = max(d for _, d, _ in done)
     total = sum(nb for _, _, nb in done)
     offered = sum(items[p]["bytes"] for p in picks) / max(t_sub, 1e-9)
-    return {"requests": n_req, "compress": int(kinds.sum()), "decompress": int(n_req - kinds.sum()),
+    minutes = []
+    if seconds >= 120:  # a long run: latency and throughput per minute of submissions (drift, leaks)
+        sub = np.array([s for s, _, _ in done])
+        nbs = np.array([nb for _, _, nb in done], dtype=np.float64)
+        for m in range(int(seconds // 60)):
+            sel = (sub >= t_first + 60 * m) & (sub < t_first + 60 * (m + 1))
+            if sel.any():
+                minutes.append({"minute": m, "requests": int(sel.sum()),
+                                "p50_ms": round(float(np.percentile(lat[sel], 50)), 3),
+                                "p99_ms": round(float(np.percentile(lat[sel], 99)), 3),
+                                "max_ms": round(float(lat[sel].max()), 3),
+                                "gbs": round(float(nbs[sel].sum()) / 60.0 / 1e9, 2)})
+    extra = {"per_minute": minutes} if minutes else {}
+    return {**extra, "requests": n_req, "compress": int(kinds.sum()), "decompress": int(n_req - kinds.sum()),
             "rate_req_s": rate, "arrival_seconds": round(t_sub, 3), "p50_ms": round(float(np.percentile(lat, 50)), 3),
             "p99_ms": round(float(np.percentile(lat, 99)), 3), "max_ms": round(float(lat.max()), 3),
             "sustained_gbs": round(total / (t_last - t_first) / 1e9, 2), "offered_gbs": round(offered / 1e9, 2),
