@@ -48,3 +48,39 @@ def test_dequant_special_values(cuda, eb):
         want = (s.astype(np.float64) * (2.0 * eb)).astype(np.float32)
     same = (got.view(np.uint32) == want.view(np.uint32)) | (np.isnan(got) & np.isnan(want))
     assert same.all(), f"eb={eb}: {np.count_nonzero(~same)} mismatches, e.g. {s[~same][:5]}"
+
+
+# Error bounds whose c_d = 2 eb makes the separable pass's two-operation dequantization,
+# RN32(s c_hi + RN32(s c_lo)), differ from the reference's (float)((double)s c_d) at exactly one
+# pair +-s with 0 < s < 2^21 (kept as the check's exception), and one where it differs at several
+# (the check falls back to the checked FP32 path).  Found by an exhaustive C loop over s with a
+# correctly rounded fmaf.
+ONE_PAIR = [(0.00013056223589487476, 1698755), (0.00019158748290109797, 1478839)]
+MANY = [0.00011538630910934243]
+
+
+@pytest.mark.parametrize("eb,s_exc", ONE_PAIR + [(e, None) for e in MANY])
+def test_separable_dequant_exception_and_fallback(cuda, eb, s_exc):
+    """A 2^22-element 3D field (the size from which decompress checks the two-operation form)
+    whose prequantized values pass through the exception value +-s_exc (or, for the fallback bound,
+    a comparable range): archive and reconstruction bit-identical to the oracle's."""
+    import oracle as O
+    import vecsz_gb300 as V
+    nz, ny, nx = 128, 128, 256
+    z, y, xx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    g = (np.sin(xx / 9.0) * np.cos(y / 7.0) + 0.3 * np.sin(z / 5.0 + xx / 13.0)).ravel() / 1.3  # [-1, 1]
+    centre = (s_exc if s_exc else 1500000) * 2.0 * eb
+    half = g.size // 2
+    x = np.empty(g.size, np.float64)
+    x[:half] = centre + g[:half] * 1000 * 2.0 * eb   # about +-1000 quanta around +s
+    x[half:] = -centre + g[half:] * 1000 * 2.0 * eb  # and around -s
+    x = x.astype(np.float32)
+    if s_exc:
+        s = np.rint(x * np.float32(1.0 / (2.0 * eb)))  # the AVX prequantization, float32
+        assert (s == s_exc).any() and (s == -s_exc).any()
+    dims = (nx, ny, nz)
+    c = V.compress(x, dims, eb=eb, mode="abs", dict_size=1024, block_size=8)
+    oa, meta = O.compress(x, dims, 8, 1024, eb, False)
+    assert c.data[: c.data_size] == oa
+    assert meta["n_outlier"] * 64 < x.size  # the separable pass is taken
+    np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(oa, 8, 1024).view(np.uint32))
