@@ -435,3 +435,19 @@ def test_infinite_and_huge_inputs_match_oracle(cuda, dims, bs, mode):
     oa, _ = O.compress(x, dims, bs, 1024, 1e-3, mode == "r2r")
     assert c.data[:c.data_size] == oa
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(oa, bs, 1024).view(np.uint32))
+
+
+def test_growing_dictionaries_in_one_process(cuda):
+    """Dictionaries that grow from call to call in one process (3D: shared histogram + previous
+    planes up to 96 KB of shared memory; 1D: histogram up to 64 KB): every launch still fits its
+    kernel's shared-memory opt-in, and archives and reconstructions match the oracle."""
+    rng = np.random.default_rng(31)
+    x3 = fields.grf_3d(24, 40, 64, seed=5).ravel()
+    x1 = (np.cumsum(rng.standard_normal(70001)) * 0.05).astype(np.float32)
+    for dct in (2048, 8192, 16384):
+        for x, dims in ((x3, (64, 40, 24)), (x1, (70001,))):
+            c = V.compress(x, dims, eb=1e-4, mode="r2r", dict_size=dct, block_size=8)
+            oa, _ = O.compress(x, dims, 8, dct, 1e-4, True)
+            assert c.data[: c.data_size] == oa
+            y = O.decompress(oa, 8, dct, O.value_range(x))
+            np.testing.assert_array_equal(V.decompress(c).view(np.uint32), y.view(np.uint32))

@@ -860,6 +860,11 @@ int launch_eb_setup(int mode, double eb, const float* d_in, size_t n, Consts* d_
     return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
 }
 
+// The most dynamic shared memory a dual-quant kernel takes: a shared histogram of up to 16384
+// bins and the 3D previous planes.  Every kernel is opted in to it once, so that a later launch
+// with a larger dictionary than the first still fits.
+constexpr int kDqSmemMax = 16384 * 4 + 8 * (int)sizeof(PrevRows);
+
 template <int NDIM, int BS>
 static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
     // tail columns exist only when d0 % 8 != 0 (and then never with 16-byte rows)
@@ -869,7 +874,7 @@ static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStr
     if (NDIM == 3) smem += 8 * 8 * 4 * 32 * sizeof(float);
     static std::atomic<unsigned long long> attr[4];
     auto go = [&](auto kern, std::atomic<unsigned long long>& at) {
-        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, at);
+        smem_limit_once(kern, kDqSmemMax, at);
         kern<<<grid, 256, smem, st>>>(a);
     };
     static std::atomic<unsigned long long> attr_strict{0}, attr_pad{0};
@@ -885,10 +890,15 @@ static void launch_23d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStr
 
 template <int BS>
 static void launch_1d(const DqArgs& a, bool vec, int grid, size_t smem, cudaStream_t st) {
-    if (a.strict) k_dq_compress_1d<BS, false, true><<<grid, 256, smem, st>>>(a);
-    else if (a.pad.vals) k_dq_compress_1d<BS, false, false, true><<<grid, 256, smem, st>>>(a);
-    else if (vec) k_dq_compress_1d<BS, true><<<grid, 256, smem, st>>>(a);
-    else k_dq_compress_1d<BS, false><<<grid, 256, smem, st>>>(a);
+    static std::atomic<unsigned long long> attr[4];
+    auto go = [&](auto kern, std::atomic<unsigned long long>& at) {
+        smem_limit_once(kern, kDqSmemMax, at);
+        kern<<<grid, 256, smem, st>>>(a);
+    };
+    if (a.strict) go(k_dq_compress_1d<BS, false, true>, attr[0]);
+    else if (a.pad.vals) go(k_dq_compress_1d<BS, false, false, true>, attr[1]);
+    else if (vec) go(k_dq_compress_1d<BS, true>, attr[2]);
+    else go(k_dq_compress_1d<BS, false>, attr[3]);
     count_launch();
 }
 
@@ -967,11 +977,11 @@ int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_
     const uint32_t grid = ntasks < cap ? ntasks : cap;
     int rc = VSZ_OK;
     auto go23 = [&](auto kern, std::atomic<unsigned long long>& attr) {
-        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr);
+        smem_limit_once(kern, kDqSmemMax, attr);
         kern<<<grid, 256, smem, st>>>(args, tasks, ntasks, hist_words);
     };
     auto go1 = [&](auto kern, std::atomic<unsigned long long>& attr) {
-        if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr);
+        smem_limit_once(kern, kDqSmemMax, attr);
         kern<<<grid, 256, smem, st>>>(args, tasks, ntasks);
     };
     auto pick = [&](auto nd_c, auto bs_c) {
