@@ -60,18 +60,36 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
     const uint32_t rpair  = (uint32_t)R | ((uint32_t)R << 16);
     const unsigned lane   = lane_id();
 
+    // Narrow rows (a.ygrp > 1, rows of at most 16 blocks): the warp takes ygrp consecutive
+    // y-blocks of one z-block, a group of nbx8 lanes per y-block (lanes past ygrp * nbx8 idle), so
+    // that its lanes are not spent on columns past the row's end.  A lane still reconstructs one
+    // whole block; the lanes of a group share a row, and outliers are ranked per group.
+    const uint32_t G   = (REDO || PAD || NDIM == 1) ? 1u : a.ygrp;
+    const uint32_t gw  = G > 1 ? a.nbx8 : 32u;  // lanes per group
+    const uint32_t grp = G > 1 ? lane / gw : 0u;
+    const uint32_t gl0 = grp * gw;              // the group's first lane
+    const uint32_t lbx = lane - gl0;            // this lane's block along x in its segment
+
     // unit indices fit 32 bits (n <= 2^36 elements, 2048 per unit): 32-bit divisions only.
     for (uint32_t ui = first; ui < end; ui += stride) {
         const uint32_t u  = REDO ? a.redo[1 + ui] : ui;
-        const uint32_t xs = u % a.nxs;
-        const uint32_t r  = u / a.nxs;
-        const uint32_t yb = (NDIM >= 2) ? r % a.nyb : 0u;
-        const uint32_t zb = (NDIM == 3) ? r / a.nyb : 0u;
-        const uint32_t x0 = xs * kDSeg + lane * 8;
+        uint32_t xs, yb, zb;
+        if (G > 1) {  // units: (group of G y-blocks, z-block)
+            xs = 0;
+            yb = (u % a.nyb_g) * G + grp;
+            zb = (NDIM == 3) ? u / a.nyb_g : 0u;
+        } else {
+            xs = u % a.nxs;
+            const uint32_t r = u / a.nxs;
+            yb = (NDIM >= 2) ? r % a.nyb : 0u;
+            zb = (NDIM == 3) ? r / a.nyb : 0u;
+        }
+        const bool blk_in = grp < G && (NDIM < 2 || yb < a.nyb);  // my block exists
+        const uint32_t x0 = xs * kDSeg + lbx * 8;
         const uint32_t y0 = yb * 8, z0 = zb * 8;
-        const int ny = (NDIM >= 2) ? (int)min(8u, a.d1 - y0) : 1;
+        const int ny = (NDIM >= 2) ? (blk_in ? (int)min(8u, a.d1 - y0) : 0) : 1;
         const int nz = (NDIM == 3) ? (int)min(8u, a.d2 - z0) : 1;
-        const bool col_in = x0 < a.d0;  // VEC: d0 % 8 == 0, so all 8 columns or none
+        const bool col_in = blk_in && x0 < a.d0;  // VEC: d0 % 8 == 0, so all 8 columns or none
         // halo of my block (zero without padding): x-, y- and z-halo cells; in 3D the (x-1, y-1)
         // cell of a halo row is the y-halo's, in 2D the x-halo's
         float hx = 0.f, hy = 0.f, hz = 0.f;
@@ -131,27 +149,38 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
                     for (int k = 0; k < 8; k++) zm |= (code_at(k) == 0u) ? (1u << k) : 0u;
                 }
                 unsigned long long obase = 0;
-                if (__any_sync(0xffffffffu, zm != 0u)) {
+                const unsigned zlanes = __ballot_sync(0xffffffffu, zm != 0u);
+                if (zlanes) {
                     uint32_t cnt = __popc(zm), incl = cnt;
 #pragma unroll
                     for (int o = 1; o < 32; o <<= 1) {
                         uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
                         if (lane >= (unsigned)o) incl += t;
                     }
-                    unsigned long long seg_base;
+                    if (G > 1) {  // ranks within my group's row: less the lanes of earlier groups
+                        const uint32_t before = __shfl_sync(0xffffffffu, incl, gl0 ? gl0 - 1 : 0);
+                        if (gl0) incl -= before;
+                    }
+                    unsigned long long seg_base = 0;
                     if (a.chunk_off) {
                         // zeros before this row segment: the chunk's offset plus the zeros between the
-                        // chunk start and the segment start, counted by the warp (at most 511 codes)
-                        const unsigned long long q  = row * a.d0 + (unsigned long long)xs * kDSeg;
-                        const unsigned long long c0 = q & ~511ull;
-                        uint32_t zc = 0;
-                        const unsigned long long lo = c0 + (unsigned long long)lane * 16;
+                        // chunk start and the segment start, counted by the warp (at most 511 codes),
+                        // once for each group that has an outlier in this row
+                        const unsigned long long q = row * a.d0 + (unsigned long long)xs * kDSeg;
+                        for (uint32_t g = 0; g < G; g++) {
+                            const unsigned gmask = (gw >= 32u) ? 0xffffffffu : (((1u << gw) - 1u) << (g * gw));
+                            if (!(zlanes & gmask)) continue;  // the same for the whole warp
+                            const unsigned long long qg = __shfl_sync(0xffffffffu, q, g * gw);
+                            const unsigned long long c0 = qg & ~511ull;
+                            uint32_t zc = 0;
+                            const unsigned long long lo = c0 + (unsigned long long)lane * 16;
 #pragma unroll
-                        for (int t = 0; t < 16; t++)
-                            if (lo + t < q) zc += (a.codes[lo + t] == 0);
+                            for (int t = 0; t < 16; t++)
+                                if (lo + t < qg) zc += (a.codes[lo + t] == 0);
 #pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
-                        seg_base = a.chunk_off[q >> 9] - a.chunk_off[0] + zc;  // relative: batches
+                            for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
+                            if (g == grp) seg_base = a.chunk_off[qg >> 9] - a.chunk_off[0] + zc;  // relative: batches
+                        }
                     } else {
                         seg_base = a.seg_off[row * a.nxs + xs];
                     }
@@ -666,10 +695,21 @@ static int launch_gen(const DqDecArgs& a, cudaStream_t st) {
 }
 
 void dq_b8_geometry(DqDecArgs& a, int ndim) {
-    a.nxs = (a.d0 + kDSeg - 1) / kDSeg;
-    a.nyb = (a.d1 + 7) / 8;
+    a.nxs   = (a.d0 + kDSeg - 1) / kDSeg;
+    a.nyb   = (a.d1 + 7) / 8;
+    a.nbx8  = (a.d0 + 7) / 8;
+    a.ygrp  = 1;
+    a.nyb_g = a.nyb;
     unsigned long long nzb = (ndim == 3) ? (a.d2 + 7) / 8 : 1;
     a.nunits = (unsigned long long)a.nxs * (ndim >= 2 ? a.nyb : 1) * nzb;
+}
+
+void dq_b8_narrow(DqDecArgs& a, int ndim) {
+    if (ndim < 2 || a.nbx8 == 0 || a.nbx8 > 16) return;
+    a.ygrp  = 32 / a.nbx8;
+    a.nyb_g = (a.nyb + a.ygrp - 1) / a.ygrp;
+    const unsigned long long nzb = (ndim == 3) ? (a.d2 + 7) / 8 : 1;
+    a.nunits = (unsigned long long)a.nyb_g * nzb;
 }
 
 bool dq_b8_vec(const DqDecArgs& a) {
@@ -757,6 +797,7 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
     if (bs == 8 && !force_general) {
         dq_b8_geometry(a, ndim);
         const bool vec = dq_b8_vec(a);
+        if (!a.pad.vals && !dq_b8_separable(a, ndim)) dq_b8_narrow(a, ndim);  // the reference-order kernel
         long long want = (long long)((a.nunits + 3) / 4);
         long long cap  = (long long)num_sms * 16;
         int grid = (int)(want < cap ? want : cap);

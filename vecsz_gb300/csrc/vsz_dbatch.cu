@@ -215,6 +215,15 @@ int dfields(const vsz_dbatch_field* fields, int nfields, std::vector<DField>& ou
         a.redo       = reinterpret_cast<uint32_t*>(1);
         f.vec        = dq_b8_vec(a);
         f.sep        = dq_b8_separable(a, f.g.ndim);
+        if (!f.sep) {  // the reference-order kernel groups narrow rows: its own unit count
+            DqDecArgs t{};
+            t.d0 = f.g.d0;
+            t.d1 = f.g.d1;
+            t.d2 = f.g.d2;
+            dq_b8_geometry(t, f.g.ndim);
+            dq_b8_narrow(t, f.g.ndim);
+            f.units = t.nunits;
+        }
         out.push_back(f);
     }
     return VSZ_OK;
@@ -342,6 +351,7 @@ vsz_status vsz_dbatch_create(const vsz_dbatch_field* fields, int nfields, void* 
         q.xtail       = (G.g.ndim == 3 && (G.g.d0 % 8) != 0) ? (G.g.d0 & ~7u) : G.g.d0;
         q.redo        = L.redo[f];
         dq_b8_geometry(q, G.g.ndim);
+        if (!G.sep) dq_b8_narrow(q, G.g.ndim);
 
         ci[f] = DCopy{F.d_archive + d.index_offset, reinterpret_cast<uint8_t*>(L.all_bits + base), status};
         co[f] = DCopy{F.d_archive + d.outlier_offset, reinterpret_cast<uint8_t*>(L.outliers[f]), status};

@@ -145,6 +145,9 @@ struct DqDecArgs {
     int R;
     uint32_t nxs;                        // 256-wide segments per row
     uint32_t nyb;                        // Lorenzo blocks along y
+    uint32_t nbx8;                       // block 8: Lorenzo blocks along x
+    uint32_t ygrp;                       // block 8: y-blocks per warp (narrow rows, dq_b8_narrow), else 1
+    uint32_t nyb_g;                      // block 8: groups of ygrp y-blocks along y
     uint32_t nbx;                        // Lorenzo blocks along x (general kernel)
     unsigned long long nunits;
     int strict;                          // strict archive: outliers are input values (re-prequantized)
@@ -162,6 +165,9 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
 // Block size 8: unit geometry (nxs, nyb, nunits), whether the 16-byte row path applies, and
 // whether the separable pass does (3D, vector rows, not strict, no padding, under 1 outlier in 64).
 void dq_b8_geometry(DqDecArgs& a, int ndim);
+// Block size 8, the reference-order kernel, rows of at most 16 blocks (2D / 3D): a warp takes
+// 32 / nbx8 y-blocks side by side, and the unit count is recomputed for that.
+void dq_b8_narrow(DqDecArgs& a, int ndim);
 bool dq_b8_vec(const DqDecArgs& a);
 bool dq_b8_separable(const DqDecArgs& a, int ndim);
 // Many fields of one class (ndim, vec, separable), block size 8, no padding: tasks of (field,
