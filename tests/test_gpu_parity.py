@@ -145,6 +145,22 @@ def test_edge_shapes_match_oracle(cuda, dims):
         np.testing.assert_array_equal(y.view(np.uint32), O.decompress(a_or, bs, 1024).view(np.uint32))
 
 
+@pytest.mark.parametrize("d0", [5, 8, 13, 40, 64, 100, 128, 136, 200, 256, 264])
+def test_outlier_dense_rows_match_oracle(cuda, d0):
+    """At least a tenth of the codes are outliers, on rows that one warp covers whole (d0 <= 256:
+    an outlier's rank is carried from row to row; d0 <= 128: several y-blocks per warp) and on
+    wider rows, 16-byte aligned rows or not, in 2D and 3D."""
+    rng = np.random.default_rng(d0)
+    for dims, sigma in (((d0, 37, 19), 0.03), ((d0, 150), 0.04)):
+        x = (rng.standard_normal(int(np.prod(dims))) * sigma).astype(np.float32)
+        a_or, meta = O.compress(x, dims, 8, 1024, 1e-4, False)
+        assert meta["n_outlier"] > 0.1 * x.size  # all of them for 2D rows of d0 < 8
+        c = V.compress(x, dims, 1e-4, "abs", 1024, 8)
+        assert c.data[: c.data_size] == a_or
+        y = V.decompress(c)
+        np.testing.assert_array_equal(y.view(np.uint32), O.decompress(a_or, 8, 1024).view(np.uint32))
+
+
 def test_large_3d_roundtrip_properties(cuda):
     """256^3 r2r field: deterministic archive, error bound (reference overshoot <= 2 ulp),
     indexed and self-synchronising decoders agree."""

@@ -484,15 +484,25 @@ __global__ void __launch_bounds__(256, 4) k_dq_compress_23d(DqArgs a) {
     hist_flush_block(a, s_hist, h);
 }
 
-// Many fields in one launch: block-wide tasks (one field, a range of its warp units) taken in
-// grid-stride order.  hist_words = shared-memory histogram words reserved before the planes.
+// Many fields in one launch: block-wide tasks (one field, a range of its warp units), each taken
+// by the next free block (`next`: the launch's task counter, zero at launch), so that blocks do
+// not idle behind uneven tasks.  hist_words = shared-memory histogram words reserved before the
+// planes.
+__device__ __forceinline__ uint32_t dq_block_next_task(uint32_t* next, uint32_t* s_task) {
+    __syncthreads();  // every thread has read the previous task number
+    if (threadIdx.x == 0) *s_task = atomicAdd(next, 1u);
+    __syncthreads();
+    return *s_task;
+}
+
 template <int NDIM, int BS, bool VEC, bool TAIL>
 __global__ void __launch_bounds__(256, 3)
     k_dq_compress_23d_batch(const DqArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks,
-                            uint32_t hist_words) {
+                            uint32_t hist_words, uint32_t* __restrict__ next) {
     extern __shared__ __align__(16) uint32_t s_dyn[];
+    __shared__ uint32_t s_task;
     PrevRows* s_prev = reinterpret_cast<PrevRows*>(s_dyn + hist_words);
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    for (uint32_t t = dq_block_next_task(next, &s_task); t < ntasks; t = dq_block_next_task(next, &s_task)) {
         const BatchTask tk = tasks[t];
         const DqArgs& a    = args[tk.field];  // read-only table: loads stay cached
         const Consts c     = *a.consts;
@@ -596,9 +606,11 @@ __global__ void __launch_bounds__(256) k_dq_compress_1d(DqArgs a) {
 
 template <int BS, bool VEC>
 __global__ void __launch_bounds__(256)
-    k_dq_compress_1d_batch(const DqArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    k_dq_compress_1d_batch(const DqArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks,
+                           uint32_t* __restrict__ next) {
     extern __shared__ uint32_t s_hist_dyn[];
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    __shared__ uint32_t s_task;
+    for (uint32_t t = dq_block_next_task(next, &s_task); t < ntasks; t = dq_block_next_task(next, &s_task)) {
         const BatchTask tk = tasks[t];
         const DqArgs& a    = args[tk.field];
         const Consts c     = *a.consts;
@@ -969,7 +981,7 @@ int launch_consts_batch(const ConstsField* f, uint32_t nfields, cudaStream_t st)
 }
 
 int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, int bs, bool vec,
-                             bool tail, uint32_t hist_words, cudaStream_t st, int num_sms) {
+                             bool tail, uint32_t hist_words, uint32_t* next, cudaStream_t st, int num_sms) {
     if (ntasks == 0) return VSZ_OK;
     size_t smem = (size_t)hist_words * sizeof(uint32_t);
     if (ndim == 3) smem += sizeof(PrevRows) * 8;
@@ -978,11 +990,11 @@ int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_
     int rc = VSZ_OK;
     auto go23 = [&](auto kern, std::atomic<unsigned long long>& attr) {
         smem_limit_once(kern, kDqSmemMax, attr);
-        kern<<<grid, 256, smem, st>>>(args, tasks, ntasks, hist_words);
+        kern<<<grid, 256, smem, st>>>(args, tasks, ntasks, hist_words, next);
     };
     auto go1 = [&](auto kern, std::atomic<unsigned long long>& attr) {
         smem_limit_once(kern, kDqSmemMax, attr);
-        kern<<<grid, 256, smem, st>>>(args, tasks, ntasks);
+        kern<<<grid, 256, smem, st>>>(args, tasks, ntasks, next);
     };
     auto pick = [&](auto nd_c, auto bs_c) {
         constexpr int ND = decltype(nd_c)::value, B = decltype(bs_c)::value;

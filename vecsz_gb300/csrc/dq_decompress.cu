@@ -69,6 +69,12 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
     const uint32_t grp = G > 1 ? lane / gw : 0u;
     const uint32_t gl0 = grp * gw;              // the group's first lane
     const uint32_t lbx = lane - gl0;            // this lane's block along x in its segment
+    const uint32_t gll = min(gl0 + gw - 1u, 31u);  // the group's last lane
+    const unsigned gmy = (gw >= 32u) ? 0xffffffffu : (((1u << gw) - 1u) << gl0);  // my group's lanes
+    // When a unit spans whole rows (one segment per row), the rows of a block in one plane are
+    // consecutive in the field, so the outlier rank at a row's start is the one at the previous
+    // row's start plus that row's zeros: the zeros from the chunk start are counted once per plane.
+    const bool carry = NDIM >= 2 && a.chunk_off != nullptr && a.nxs == 1u;
 
     // unit indices fit 32 bits (n <= 2^36 elements, 2048 per unit): 32-bit divisions only.
     for (uint32_t ui = first; ui < end; ui += stride) {
@@ -100,14 +106,22 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
             hz = hv.z;
         }
 
-        // VEC: the 8 codes of this lane's columns in one 16-byte load; rows outside the field
-        // read as R (no zero codes, so they never enter the outlier path)
+        // the 8 codes of this lane's columns (VEC: one 16-byte load), a row ahead of their use;
+        // cells outside the field read as R (no zero codes, so they never enter the outlier path)
         auto load_row = [&](int zz, int y) -> uint4 {
-            if (!(col_in && y < ny && zz < nz)) return make_uint4(rpair, rpair, rpair, rpair);
             const size_t row = (size_t)(z0 + zz) * a.d1 + (y0 + y);
-            return __ldcs(reinterpret_cast<const uint4*>(a.codes + row * a.d0 + x0));
+            if (VEC) {
+                if (!(col_in && y < ny && zz < nz)) return make_uint4(rpair, rpair, rpair, rpair);
+                return __ldcs(reinterpret_cast<const uint4*>(a.codes + row * a.d0 + x0));
+            }
+            const bool rin       = y < ny && zz < nz;
+            const uint16_t* crow = a.codes + row * a.d0;
+            uint32_t t[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) t[k] = (rin && x0 + k < a.d0) ? (uint32_t)crow[x0 + k] : (uint32_t)R;
+            return make_uint4(t[0] | (t[1] << 16), t[2] | (t[3] << 16), t[4] | (t[5] << 16), t[6] | (t[7] << 16));
         };
-        uint4 cv_next = VEC ? load_row(0, 0) : make_uint4(0u, 0u, 0u, 0u);
+        uint4 cv_next = load_row(0, 0);
 
         if (NDIM == 3) {
 #pragma unroll
@@ -121,22 +135,15 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
             float Zm[8], Zn[8];  // 3D: row y - 1 and row y of plane z - 1
 #pragma unroll
             for (int k = 0; k < 8; k++) Cm[k] = hy;
+            unsigned long long rbase = 0;  // carry: my group's rank at the next row's start, once known
+            bool rknown = false;
 #pragma unroll 2
             for (int y = 0; y < 8; y++) {
                 const bool row_in = y < ny;
                 const size_t row  = ((size_t)(z0 + zz) * a.d1 + (y0 + y));
                 const bool all_in = row_in && (x0 + 7 < a.d0);
-                uint4 cv;
-                if (VEC) {
-                    cv      = cv_next;
-                    cv_next = (y < 7) ? load_row(zz, y + 1) : load_row(zz + 1, 0);
-                } else {
-                    const uint16_t* crow = a.codes + row * a.d0;
-                    uint32_t t[8];
-#pragma unroll
-                    for (int k = 0; k < 8; k++) t[k] = (row_in && x0 + k < a.d0) ? (uint32_t)crow[x0 + k] : (uint32_t)R;
-                    cv = make_uint4(t[0] | (t[1] << 16), t[2] | (t[3] << 16), t[4] | (t[5] << 16), t[6] | (t[7] << 16));
-                }
+                const uint4 cv    = cv_next;
+                cv_next           = (y < 7) ? load_row(zz, y + 1) : load_row(zz + 1, 0);
                 const uint32_t cw[4] = {cv.x, cv.y, cv.z, cv.w};
                 auto code_at = [&](int k) -> uint32_t { return (cw[k >> 1] >> (16 * (k & 1))) & 0xffffu; };
                 auto in_at   = [&](int k) -> bool { return all_in || (row_in && x0 + (uint32_t)k < a.d0); };
@@ -161,15 +168,16 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
                         const uint32_t before = __shfl_sync(0xffffffffu, incl, gl0 ? gl0 - 1 : 0);
                         if (gl0) incl -= before;
                     }
-                    unsigned long long seg_base = 0;
+                    unsigned long long seg_base = rbase;
                     if (a.chunk_off) {
                         // zeros before this row segment: the chunk's offset plus the zeros between the
                         // chunk start and the segment start, counted by the warp (at most 511 codes),
-                        // once for each group that has an outlier in this row
+                        // once for each group that has an outlier in this row and no carried rank
                         const unsigned long long q = row * a.d0 + (unsigned long long)xs * kDSeg;
+                        const unsigned need = carry ? __ballot_sync(0xffffffffu, zm != 0u && !rknown) : zlanes;
                         for (uint32_t g = 0; g < G; g++) {
                             const unsigned gmask = (gw >= 32u) ? 0xffffffffu : (((1u << gw) - 1u) << (g * gw));
-                            if (!(zlanes & gmask)) continue;  // the same for the whole warp
+                            if (!(need & gmask)) continue;  // the same for the whole warp
                             const unsigned long long qg = __shfl_sync(0xffffffffu, q, g * gw);
                             const unsigned long long c0 = qg & ~511ull;
                             uint32_t zc = 0;
@@ -180,6 +188,13 @@ __device__ __forceinline__ void dq_b8_units(const DqDecArgs& a, uint32_t first, 
 #pragma unroll
                             for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
                             if (g == grp) seg_base = a.chunk_off[qg >> 9] - a.chunk_off[0] + zc;  // relative: batches
+                        }
+                        if (carry) {  // the next row starts this row's zeros later
+                            const uint32_t tot = __shfl_sync(0xffffffffu, incl, gll);
+                            if (zlanes & gmy) {
+                                rbase  = seg_base + tot;
+                                rknown = true;
+                            }
                         }
                     } else {
                         seg_base = a.seg_off[row * a.nxs + xs];
@@ -293,6 +308,8 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8(DqDecArgs a) {
 // a.redo, and the reference-order kernel redoes it afterwards.
 // ------------------------------------------------------------------------------------------
 // Units u = first, first + stride, ... < end of one field; s_A: A of the previous plane.
+// CARRY: rows of one segment carry their outlier rank (checked at run time).
+template <bool CARRY>
 __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first, uint32_t end, uint32_t stride,
                                              DqPlane* s_A, unsigned wib) {
     const Consts c = *a.consts;
@@ -303,6 +320,9 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
     const unsigned lane        = lane_id();
     // rows start on 32-byte boundaries (d0 % 8 == 0) when the output does
     const bool out32           = (reinterpret_cast<uintptr_t>(a.out) & 31u) == 0;
+    // one segment per row: a row's outlier rank is the previous row's plus its zeros (as
+    // k_dq_decompress_b8)
+    const bool carry           = CARRY && a.chunk_off != nullptr && a.nxs == 1u;
 
     for (uint32_t u = first; u < end; u += stride) {
         const uint32_t xs = u % a.nxs;
@@ -331,6 +351,8 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
             float Bm[8];  // B of the row above (zero above the block)
 #pragma unroll
             for (int k = 0; k < 8; k++) Bm[k] = 0.f;
+            unsigned long long rbase = 0;  // carry: the rank at the next row's start, once known
+            bool rknown = false;
 #pragma unroll 2
             for (int y = 0; y < 8; y++) {
                 const bool row_in = y < ny;
@@ -361,18 +383,24 @@ __device__ __forceinline__ void dq_b8s_units(const DqDecArgs& a, uint32_t first,
                         uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
                         if (lane >= (unsigned)o) incl += t;
                     }
-                    unsigned long long seg_base;
+                    unsigned long long seg_base = rbase;
                     if (a.chunk_off) {
-                        const unsigned long long q  = row * a.d0 + (unsigned long long)xs * kDSeg;
-                        const unsigned long long c0 = q & ~511ull;
-                        uint32_t zc = 0;
-                        const unsigned long long lo = c0 + (unsigned long long)lane * 16;
+                        if (!rknown) {  // the same for the whole warp
+                            const unsigned long long q  = row * a.d0 + (unsigned long long)xs * kDSeg;
+                            const unsigned long long c0 = q & ~511ull;
+                            uint32_t zc = 0;
+                            const unsigned long long lo = c0 + (unsigned long long)lane * 16;
 #pragma unroll
-                        for (int t = 0; t < 16; t++)
-                            if (lo + t < q) zc += (a.codes[lo + t] == 0);
+                            for (int t = 0; t < 16; t++)
+                                if (lo + t < q) zc += (a.codes[lo + t] == 0);
 #pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
-                        seg_base = a.chunk_off[q >> 9] - a.chunk_off[0] + zc;  // relative: batches
+                            for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(0xffffffffu, zc, o);
+                            seg_base = a.chunk_off[q >> 9] - a.chunk_off[0] + zc;  // relative: batches
+                        }
+                        if (carry) {
+                            rbase  = seg_base + __shfl_sync(0xffffffffu, incl, 31);
+                            rknown = true;
+                        }
                     } else {
                         seg_base = a.seg_off[row * a.nxs + xs];
                     }
@@ -510,10 +538,11 @@ __global__ void __launch_bounds__(256) k_dq_mul_verify(Consts* __restrict__ c, u
     }
 }
 
+template <bool CARRY>
 __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     const unsigned wib = threadIdx.x >> 5;
-    dq_b8s_units(a, blockIdx.x * (blockDim.x >> 5) + wib, (uint32_t)a.nunits, gridDim.x * (blockDim.x >> 5),
+    dq_b8s_units<CARRY>(a, blockIdx.x * (blockDim.x >> 5) + wib, (uint32_t)a.nunits, gridDim.x * (blockDim.x >> 5),
                  reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
 }
 
@@ -721,29 +750,36 @@ bool dq_b8_separable(const DqDecArgs& a, int ndim) {
     return ndim == 3 && dq_b8_vec(a) && a.redo && !a.strict && !a.pad.vals && a.n_outliers * 64 < a.n;
 }
 
-// ---- many fields (block size 8, no padding): tasks of (field, unit range); a CTA's 4 warps take
-// the task's units.  Per field the result is k_dq_decompress_b8 / _b8s's.
+// ---- many fields (block size 8, no padding): tasks of (field, unit range), taken one at a time
+// by whichever warp is free (`next`: the class's task counter, zero at launch), so that warps do
+// not idle behind uneven tasks.  Per field the result is k_dq_decompress_b8 / _b8s's.
+__device__ __forceinline__ uint32_t dq_next_task(uint32_t* next) {
+    uint32_t t = 0;
+    if (lane_id() == 0) t = atomicAdd(next, 1u);
+    return __shfl_sync(0xffffffffu, t, 0);
+}
+
 template <int NDIM, bool VEC>
 __global__ void __launch_bounds__(128, 6)
-    k_dq_decompress_b8_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    k_dq_decompress_b8_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks,
+                             uint32_t* __restrict__ next) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     const unsigned wib = threadIdx.x >> 5;
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
-        const BatchTask tk = tasks[t];
-        const DqDecArgs a  = args[tk.field];
-        dq_b8_units<NDIM, VEC, false, false>(a, (uint32_t)tk.u0 + wib, (uint32_t)tk.u1, 4u,
+    for (uint32_t t = dq_next_task(next); t < ntasks; t = dq_next_task(next)) {
+        const BatchTask tk = tasks[t];  // the field's arguments are read in place (a copy spills)
+        dq_b8_units<NDIM, VEC, false, false>(args[tk.field], (uint32_t)tk.u0, (uint32_t)tk.u1, 1u,
                                              reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
     }
 }
 
 __global__ void __launch_bounds__(128, 6)
-    k_dq_decompress_b8s_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks) {
+    k_dq_decompress_b8s_batch(const DqDecArgs* __restrict__ args, const BatchTask* __restrict__ tasks, uint32_t ntasks,
+                              uint32_t* __restrict__ next) {
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     const unsigned wib = threadIdx.x >> 5;
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+    for (uint32_t t = dq_next_task(next); t < ntasks; t = dq_next_task(next)) {
         const BatchTask tk = tasks[t];
-        const DqDecArgs a  = args[tk.field];
-        dq_b8s_units(a, (uint32_t)tk.u0 + wib, (uint32_t)tk.u1, 4u, reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
+        dq_b8s_units<true>(args[tk.field], (uint32_t)tk.u0, (uint32_t)tk.u1, 1u, reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
     }
 }
 
@@ -753,21 +789,22 @@ __global__ void __launch_bounds__(128, 6)
     extern __shared__ __align__(16) uint8_t s_dq_dyn[];
     const unsigned wib = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
-        const DqDecArgs a = args[tasks[t].field];
+        const DqDecArgs& a = args[tasks[t].field];  // read in place: fewer registers than a copy
         dq_b8_units<3, true, false, true>(a, wib, a.redo[0], 4u, reinterpret_cast<DqPlane*>(s_dq_dyn), wib);
     }
 }
 
 int launch_dq_decompress_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, bool vec,
-                               bool sep, cudaStream_t st, int num_sms) {
+                               bool sep, uint32_t* next, cudaStream_t st, int num_sms) {
     if (ntasks == 0) return VSZ_OK;
-    const uint32_t cap  = (uint32_t)num_sms * 6;
-    const uint32_t grid = ntasks < cap ? ntasks : cap;
+    const uint32_t cap  = (uint32_t)num_sms * 6;  // resident CTAs of 4 warps
+    const uint32_t want = (ntasks + 3) / 4;
+    const uint32_t grid = want < cap ? want : cap;
     const size_t smem   = (ndim == 3) ? 4 * sizeof(DqPlane) : 0;
     static std::atomic<unsigned long long> attr[8];
     auto go = [&](auto kern, int slot) {
         if (smem > 48 * 1024) smem_limit_once(kern, (int)smem, attr[slot]);
-        kern<<<grid, 128, smem, st>>>(args, tasks, ntasks);
+        kern<<<grid, 128, smem, st>>>(args, tasks, ntasks, next);
         count_launch();
     };
     if (sep) go(k_dq_decompress_b8s_batch, 0);
@@ -825,7 +862,8 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
                 k_dq_mul_verify<<<(unsigned)num_sms * 4, 256, 0, st>>>(a.consts_rw, a.redo, a.dq_cache);
                 count_launch();
             }
-            go(k_dq_decompress_b8s, 3);
+            // fields of one segment per row carry outlier ranks; wider ones keep the lighter kernel
+            a.nxs == 1 ? go(k_dq_decompress_b8s<true>, 3) : go(k_dq_decompress_b8s<false>, 3);
             go(k_dq_decompress_b8<3, true, false, true>, 3);
         } else {
             if (ndim == 3) vec ? go(k_dq_decompress_b8<3, true>, 3) : go(k_dq_decompress_b8<3, false>, 3);

@@ -34,6 +34,10 @@ constexpr size_t kCtlInfo    = 80;   // u32[4] tree info
 constexpr size_t kCtlBits    = 96;   // u64 payload bits
 constexpr size_t kCtlNOut    = 104;  // u64 outliers
 constexpr size_t kCtlTicket  = 112;  // u32 gather look-back ticket
+// after the per-field records: the batch status, then one dual-quant task counter per class
+// (dimensionality x block size x aligned or not x tail or not: at most 48)
+constexpr size_t kDqNextOff  = 64;
+static_assert(kDqNextOff + 4 * 48 <= 256, "the counters fit the control tail");
 
 // Work per task (defaults; vsz_batch_autotune searches the first two): dual-quant warp units,
 // encoder chunks, min/max elements.
@@ -522,9 +526,12 @@ vsz_status vsz_batch_compress(vsz_batch* B, void* stream) {
     }
     {
         StageTimer t(kStDualquant, st);
-        for (const DqGroup& g : B->dq_groups)
+        uint32_t* next = reinterpret_cast<uint32_t*>(B->ctl + (size_t)nf * kCtlBytes + kDqNextOff);
+        for (size_t i = 0; i < B->dq_groups.size(); i++) {
+            const DqGroup& g = B->dq_groups[i];
             VSZ_TRY(launch_dq_compress_batch(B->dq, B->tasks + g.task_off, g.ntasks, g.ndim, g.bs, g.vec, g.tail,
-                                             g.hist_words, st, sms));
+                                             g.hist_words, next + i, st, sms));
+        }
     }
     {
         StageTimer t(kStHuffBuild, st);

@@ -39,7 +39,9 @@ constexpr size_t kDCtlInfo   = 80;  // u32[4] tree info (k_huff_table)
 
 constexpr uint64_t kDecTaskChunks = 256;      // one decoder CTA: lane t decodes chunk u0 + t
 constexpr uint64_t kCopyTaskBytes = 1 << 18;  // index and outlier copies
-constexpr uint64_t kDqTaskUnits   = 16;       // reverse-Lorenzo warp units per task
+constexpr uint64_t kDqTaskUnits   = 1;        // reverse-Lorenzo warp units per task (one warp's)
+constexpr size_t kDqNextOff       = 64;       // after the batch status in the control tail: one
+constexpr size_t kDqMaxClasses    = 16;       // task counter per reverse-Lorenzo class
 
 // A byte range copied into an aligned buffer (the archive's index and outlier sections).
 struct DCopy {
@@ -374,6 +376,11 @@ vsz_status vsz_dbatch_create(const vsz_dbatch_field* fields, int nfields, void* 
     B->out_n = (uint32_t)tasks.size() - B->out_off;
     std::map<std::tuple<int, bool, bool>, std::vector<uint32_t>> classes;
     for (uint32_t f = 0; f < nf; f++) classes[std::make_tuple(fs[f].g.ndim, fs[f].vec, fs[f].sep)].push_back(f);
+    static_assert(kDqNextOff + 4 * kDqMaxClasses <= 256, "the counters fit the control tail");
+    if (classes.size() > kDqMaxClasses) {  // 3 dimensionalities x aligned or not x separable or not
+        delete B;
+        return VSZ_ERR_INVALID;
+    }
     for (auto& kv : classes) {
         DqClass c{};
         std::tie(c.ndim, c.vec, c.sep) = kv.first;
@@ -488,8 +495,12 @@ vsz_status vsz_dbatch_decompress(vsz_dbatch* B, void* stream) {
     }
     {
         StageTimer t(kStLorenzoDecompress, st);
-        for (const DqClass& c : B->classes)
-            VSZ_TRY(launch_dq_decompress_batch(B->dq, B->tasks + c.task_off, c.ntasks, c.ndim, c.vec, c.sep, st, sms));
+        uint32_t* next = reinterpret_cast<uint32_t*>(B->ctl + B->nfields * kDCtlBytes + kDqNextOff);
+        for (size_t i = 0; i < B->classes.size(); i++) {
+            const DqClass& c = B->classes[i];
+            VSZ_TRY(launch_dq_decompress_batch(B->dq, B->tasks + c.task_off, c.ntasks, c.ndim, c.vec, c.sep, next + i,
+                                               st, sms));
+        }
         VSZ_TRY(launch_dq_redo_batch(B->dq, B->tasks + B->redo_off, B->redo_n, st, sms));
     }
     k_dbatch_status<<<fb, 128, 0, st>>>(B->check, nf);

@@ -171,9 +171,10 @@ void dq_b8_narrow(DqDecArgs& a, int ndim);
 bool dq_b8_vec(const DqDecArgs& a);
 bool dq_b8_separable(const DqDecArgs& a, int ndim);
 // Many fields of one class (ndim, vec, separable), block size 8, no padding: tasks of (field,
-// unit range).  A separable class is followed by launch_dq_redo_batch over its fields.
+// unit range), one warp each, handed out through the counter `next` (zero on entry; the class's
+// own word).  A separable class is followed by launch_dq_redo_batch over its fields.
 int launch_dq_decompress_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, bool vec,
-                               bool sep, cudaStream_t st, int num_sms);
+                               bool sep, uint32_t* next, cudaStream_t st, int num_sms);
 int launch_dq_redo_batch(const DqDecArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
                          int num_sms);
 int launch_count_zeros(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* seg_zero, cudaStream_t st,
@@ -225,11 +226,12 @@ int launch_pad_values(const PadArgs& a, cudaStream_t st, int num_sms);
 
 // Batched launchers (device arrays of per-field arguments and of tasks).  A dual-quant batch
 // holds fields of one kernel class: ndim, block size, vec (d0 % 4 == 0 and aligned), tail
-// (d0 % 8 != 0); hist_words = shared-memory histogram words (0 when no field uses one).
+// (d0 % 8 != 0); hist_words = shared-memory histogram words (0 when no field uses one); next =
+// the launch's task counter (zero on entry), through which free blocks take tasks.
 int launch_minmax_batch(const MinmaxField* f, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st, int num_sms);
 int launch_consts_batch(const ConstsField* f, uint32_t nfields, cudaStream_t st);
 int launch_dq_compress_batch(const DqArgs* args, const BatchTask* tasks, uint32_t ntasks, int ndim, int bs, bool vec,
-                             bool tail, uint32_t hist_words, cudaStream_t st, int num_sms);
+                             bool tail, uint32_t hist_words, uint32_t* next, cudaStream_t st, int num_sms);
 int launch_outlier_gather_batch(const GatherArgs* args, const BatchTask* tasks, uint32_t ntasks, cudaStream_t st,
                                 int num_sms);
 size_t gather_tmp_bytes(size_t nseg);
