@@ -563,11 +563,13 @@ vsz_status vsz_decompress_host_f64(const uint8_t* h_archive, size_t len, size_t 
 vsz_status vsz_debug_set_spin_limit(long long polls);
 vsz_status vsz_debug_scan_stalled_predecessor(size_t n, int* h_status);
 
-/* Two environment variables, read by vsz_decompress on every call, make it take another of its
+/* Three environment variables, read by vsz_decompress on every call, make it take another of its
  * kernels for the same result, so that tests can compare the kernels on one archive:
- * VSZ_DECODE_NO_WINDOW (set: the general indexed decoder instead of the window decoder) and
+ * VSZ_DECODE_NO_WINDOW (set: the general indexed decoder instead of the window decoder),
  * VSZ_FORCE_GENERAL_DECOMPRESS (set: the per-block-row reverse Lorenzo for block size 8 instead of
- * the block-8 kernels).  Unset, the library picks its fastest exact kernel. */
+ * the block-8 kernels) and VSZ_DQ_NO_WAVEFRONT (set: the block-8 kernels also for 3D fields of at
+ * most 2^24 elements, which otherwise take the wavefront kernel).  Unset, the library picks its
+ * fastest exact kernel. */
 
 #ifdef __cplusplus
 }

@@ -60,12 +60,13 @@ MANY = [0.00011538630910934243]
 
 
 @pytest.mark.parametrize("eb,s_exc", ONE_PAIR + [(e, None) for e in MANY])
-def test_separable_dequant_exception_and_fallback(cuda, eb, s_exc):
+def test_separable_dequant_exception_and_fallback(cuda, eb, s_exc, monkeypatch):
     """A 2^22-element 3D field (the size from which decompress checks the two-operation form)
     whose prequantized values pass through the exception value +-s_exc (or, for the fallback bound,
     a comparable range): archive and reconstruction bit-identical to the oracle's."""
     import oracle as O
     import vecsz_gb300 as V
+    monkeypatch.setenv("VSZ_DQ_NO_WAVEFRONT", "1")  # a field this small else takes the wavefront pass
     nz, ny, nx = 128, 128, 256
     z, y, xx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
     g = (np.sin(xx / 9.0) * np.cos(y / 7.0) + 0.3 * np.sin(z / 5.0 + xx / 13.0)).ravel() / 1.3  # [-1, 1]

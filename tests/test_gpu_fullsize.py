@@ -141,13 +141,14 @@ def test_adversarial_fullsize_matches_oracle(cuda):
     np.testing.assert_array_equal(V.decompress(c).view(np.uint32), O.decompress(oa, 8, 1024).view(np.uint32))
 
 
-def test_dequant_check_cached_per_workspace(cuda):
+def test_dequant_check_cached_per_workspace(cuda, monkeypatch):
     """Fields of 2^22 elements and more check the separable pass's two-operation dequantization
     once per error bound and keep the result in the decompress workspace: decompressing through one
     workspace fields with the same bound (a hit), another bound (a new check) and the first bound
     again gives the oracle's reconstruction each time; bytes planted where the result is kept, with
     a wrong check word, are not taken for a result."""
     torch = cuda
+    monkeypatch.setenv("VSZ_DQ_NO_WAVEFRONT", "1")  # 2^24 elements: else the wavefront pass
     dims = (256, 256, 256)
     cases = [(fields.grf_3d(256, 256, 256, seed=s).ravel() * 0.01, eb) for s, eb in ((1, 1e-4), (2, 1e-4), (3, 1e-3))]
     cases.append(cases[0])

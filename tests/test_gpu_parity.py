@@ -117,8 +117,17 @@ def _random_case(seed):
     return dims, bs, dct, eb, r2r, x
 
 
+@pytest.fixture(params=["wavefront", "block"])
+def dq_kernel(request, monkeypatch):
+    """Small 3D fields run the wavefront reverse Lorenzo, or (VSZ_DQ_NO_WAVEFRONT) the block-8
+    kernels that larger fields take."""
+    if request.param == "block":
+        monkeypatch.setenv("VSZ_DQ_NO_WAVEFRONT", "1")
+    return request.param
+
+
 @pytest.mark.parametrize("seed", range(24))
-def test_random_settings_match_oracle(cuda, seed):
+def test_random_settings_match_oracle(cuda, seed, dq_kernel):
     dims, bs, dct, eb, r2r, x = _random_case(seed)
     if r2r and O.value_range(x) == 0:
         r2r = False
@@ -134,7 +143,7 @@ def test_random_settings_match_oracle(cuda, seed):
 
 @pytest.mark.parametrize("dims", [(1,), (7,), (128,), (129,), (1, 1), (3, 1), (1, 9), (130, 2), (8, 8), (9, 9),
                                   (1, 1, 1), (2, 3, 5), (1, 1, 9), (129, 1, 1), (8, 8, 8), (9, 9, 9)])
-def test_edge_shapes_match_oracle(cuda, dims):
+def test_edge_shapes_match_oracle(cuda, dims, dq_kernel):
     rng = np.random.default_rng(sum(dims))
     x = np.cumsum(rng.standard_normal(int(np.prod(dims)))).astype(np.float32)
     for bs in (8, 16):
@@ -146,7 +155,7 @@ def test_edge_shapes_match_oracle(cuda, dims):
 
 
 @pytest.mark.parametrize("d0", [5, 8, 13, 40, 64, 100, 128, 136, 200, 256, 264])
-def test_outlier_dense_rows_match_oracle(cuda, d0):
+def test_outlier_dense_rows_match_oracle(cuda, d0, dq_kernel):
     """At least a tenth of the codes are outliers, on rows that one warp covers whole (d0 <= 256:
     an outlier's rank is carried from row to row; d0 <= 128: several y-blocks per warp) and on
     wider rows, 16-byte aligned rows or not, in 2D and 3D."""
@@ -388,10 +397,11 @@ def test_host_ops_match_host_entry_points(cuda):
 
 
 @pytest.mark.parametrize("offset", ["none", "all", "half", "nan"])
-def test_separable_reverse_lorenzo_matches_oracle(cuda, offset):
-    """3D block-8 fields with few outliers take the separable reverse Lorenzo; blocks whose values
-    reach 2^21 (here: a large offset at abs 1e-3, all or half of the field) or hold a NaN are redone
-    in the reference's order.  Every case must match the oracle bit for bit."""
+def test_separable_reverse_lorenzo_matches_oracle(cuda, offset, dq_kernel):
+    """3D block-8 fields with few outliers take the separable reverse Lorenzo (block kernels; a
+    field this small takes the wavefront pass unless VSZ_DQ_NO_WAVEFRONT is set); blocks whose
+    values reach 2^21 (here: a large offset at abs 1e-3, all or half of the field) or hold a NaN
+    are redone in the reference's order.  Every case must match the oracle bit for bit."""
     nz, ny, nx = 40, 48, 64
     z, y, xx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
     x = (np.sin(xx / 9.0) * np.cos(y / 7.0) + 0.3 * np.sin(z / 5.0 + xx / 13.0)).astype(np.float64)
@@ -412,7 +422,7 @@ def test_separable_reverse_lorenzo_matches_oracle(cuda, offset):
 
 
 @pytest.mark.parametrize("case", ["small", "offset", "nan", "abs", "bs16", "bs32_tail"])
-def test_3d_value_scales_match_oracle(cuda, case):
+def test_3d_value_scales_match_oracle(cuda, case, dq_kernel):
     """3D fields over value scales (prequantized values far below and far above 2^21, a NaN, abs
     and r2r) and block sizes 8, 16 and 32 with tail columns: archives byte-identical to the
     oracle's, reconstructions bit-identical."""

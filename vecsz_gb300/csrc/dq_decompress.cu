@@ -13,6 +13,7 @@
 // order: seg_off[row segment of 256 columns] (an exclusive scan of the zero counts the Huffman
 // decoder produced) plus the zeros before it inside the segment.
 #include <cstdint>
+#include <cstdlib>
 #include <type_traits>
 
 #include "vsz_device.cuh"
@@ -547,6 +548,155 @@ __global__ void __launch_bounds__(128, 6) k_dq_decompress_b8s(DqDecArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------
+// Wavefront pass, 3D, block 8, no padding, fields of at most kW8MaxN elements.  The block-8
+// kernels give each lane a whole 8 x 8 x 8 block, 512 elements one after another; a field with
+// fewer warp units than the GPU holds then takes that chain's latency (0.1-0.3 ms) whatever its
+// size.  Here a block has 8 lanes, one per row y, and lane y runs one plane behind lane y - 1: at
+// step t it reconstructs row (y, z = t - y) from its own row of plane z - 1 (in registers) and
+// lane y - 1's rows of planes z and z - 1 (shuffled one lane up after each step).  15 steps of 8
+// elements per lane instead of 512; the predictor is the reference's, in its FP32 order, so the
+// values are the same bits.  A warp holds 4 blocks along x.  Outliers are ranked from blk_off
+// (zero codes before each row's x-block), so no lane waits on another for a rank.
+// ------------------------------------------------------------------------------------------
+template <bool VEC>
+__global__ void __launch_bounds__(128, 4) k_dq_decompress_w8(DqDecArgs a) {
+    const Consts c = *a.consts;
+    if (c.status != VSZ_OK || *a.status != VSZ_OK) return;
+    const int R           = a.R;
+    const float rbias     = 8388608.0f + (float)R;
+    const uint32_t rpair  = (uint32_t)R | ((uint32_t)R << 16);
+    const unsigned lane   = lane_id();
+    const int y           = (int)(lane & 7u);  // row of the block
+    const uint32_t nxq    = (a.nbx8 + 3) / 4;  // groups of 4 blocks along x
+    const bool ranks      = a.n_outliers != 0;
+    const unsigned long long wtot = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    for (unsigned long long u = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+         u < a.nunits; u += wtot) {
+        const uint32_t xq = (uint32_t)(u % nxq);
+        const unsigned long long r = u / nxq;
+        const uint32_t yb = (uint32_t)(r % a.nyb), zb = (uint32_t)(r / a.nyb);
+        const uint32_t bx = xq * 4 + (lane >> 3);
+        const uint32_t x0 = bx * 8, z0 = zb * 8, yr = yb * 8 + (uint32_t)y;
+        const int nz        = (int)min(8u, a.d2 - z0);  // the same for the whole warp
+        const bool row_in   = bx < a.nbx8 && yr < a.d1;  // this lane's row exists (in every plane)
+        const bool all_in   = row_in && x0 + 7 < a.d0;
+        auto row_of = [&](int zz) -> size_t { return (size_t)(z0 + zz) * a.d1 + yr; };
+        // the 8 codes of the lane's row in plane zz (cells outside the field read R: never an
+        // outlier, and their values only feed other cells outside the field)
+        auto load_row = [&](int zz) -> uint4 {
+            if (!(row_in && zz < nz)) return make_uint4(rpair, rpair, rpair, rpair);
+            const uint16_t* crow = a.codes + row_of(zz) * a.d0;
+            if (VEC) return __ldcs(reinterpret_cast<const uint4*>(crow + x0));
+            uint32_t t[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) t[k] = (x0 + k < a.d0) ? (uint32_t)crow[x0 + k] : (uint32_t)R;
+            return make_uint4(t[0] | (t[1] << 16), t[2] | (t[3] << 16), t[4] | (t[5] << 16), t[6] | (t[7] << 16));
+        };
+        auto load_off = [&](int zz) -> unsigned long long {
+            return (ranks && row_in && zz < nz) ? a.blk_off[row_of(zz) * a.nbx8 + bx] : 0ull;
+        };
+        float Zp[8], Y[8], Yp[8];  // own row of plane z - 1; rows y - 1 of planes z and z - 1
+#pragma unroll
+        for (int k = 0; k < 8; k++) Zp[k] = Y[k] = Yp[k] = 0.f;
+        uint4 cv               = load_row(0);
+        unsigned long long off = load_off(0);
+        for (int t = 0; t < nz + 7; t++) {
+            float up[8];  // lane y - 1's newest row (row y - 1 of the plane this lane takes now)
+#pragma unroll
+            for (int k = 0; k < 8; k++) up[k] = __shfl_up_sync(0xffffffffu, Zp[k], 1);
+            const int zz = t - y;
+            if (zz >= 0 && zz < nz) {
+                const uint4 cw4 = cv;
+                const unsigned long long obase = off;
+                cv  = load_row(zz + 1);
+                off = load_off(zz + 1);
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    Yp[k] = Y[k];
+                    Y[k]  = y ? up[k] : 0.f;
+                }
+                const uint32_t cw[4] = {cw4.x, cw4.y, cw4.z, cw4.w};
+                auto code_at = [&](int k) -> uint32_t { return (cw[k >> 1] >> (16 * (k & 1))) & 0xffffu; };
+                uint32_t zm = 0;
+                if (zero_halves(cw4.x) | zero_halves(cw4.y) | zero_halves(cw4.z) | zero_halves(cw4.w)) {
+#pragma unroll
+                    for (int k = 0; k < 8; k++) zm |= (code_at(k) == 0u) ? (1u << k) : 0u;
+                }
+                float C[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const float X   = k ? C[k - 1] : 0.f;
+                    const float XY  = k ? Y[k - 1] : 0.f;
+                    const float XZ  = k ? Zp[k - 1] : 0.f;
+                    const float XYZ = k ? Yp[k - 1] : 0.f;
+                    const float pred =
+                        __fadd_rn(__fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(XYZ, XY), XZ), Yp[k]), X), Y[k]), Zp[k]);
+                    float s = __fadd_rn(pred, __fsub_rn(__uint_as_float(0x4B000000u | code_at(k)), rbias));
+                    if (zm & (1u << k)) {
+                        const unsigned long long oi = obase + __popc(zm & ((1u << k) - 1u));
+                        s = 0.f;
+                        if (oi < a.n_outliers) s = a.outliers[oi];
+                        else set_status(a.status, VSZ_ERR_CORRUPT);
+                        if (a.strict) s = strict_prequant<3>(s, x0 + (uint32_t)k, a, c);
+                    }
+                    C[k] = s;
+                }
+                float xo[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    xo[k] = dequant(C[k], c.c_d, c.c_hi, c.c_lo, c.dq_fast);
+                    if (a.strict && (zm & (1u << k))) {  // strict outliers are output as stored
+                        const unsigned long long oi = obase + __popc(zm & ((1u << k) - 1u));
+                        xo[k] = oi < a.n_outliers ? a.outliers[oi] : 0.f;
+                    }
+                }
+                float* orow = a.out + row_of(zz) * a.d0;
+                if (VEC && all_in) {
+                    __stcs(reinterpret_cast<float4*>(orow + x0), make_float4(xo[0], xo[1], xo[2], xo[3]));
+                    __stcs(reinterpret_cast<float4*>(orow + x0 + 4), make_float4(xo[4], xo[5], xo[6], xo[7]));
+                } else if (row_in) {
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        if (x0 + (uint32_t)k < a.d0) orow[x0 + k] = xo[k];
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) Zp[k] = C[k];
+            }
+        }
+    }
+}
+
+// Zero codes per (row, x-block of 8) in row-major order, for k_dq_decompress_w8's ranks.
+__global__ void __launch_bounds__(256) k_count_zeros_b8(const uint16_t* __restrict__ codes, uint32_t d0, uint32_t nbx8,
+                                                        size_t m, uint32_t* __restrict__ blk_zero) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t row     = i / nbx8;
+        const uint32_t x0    = (uint32_t)(i - row * nbx8) * 8u;
+        const uint16_t* crow = codes + row * d0;
+        uint32_t z = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; k++) z += (x0 + k < d0 && crow[x0 + k] == 0) ? 1u : 0u;
+        blk_zero[i] = z;
+    }
+}
+
+int launch_count_zeros_b8(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* blk_zero, cudaStream_t st,
+                          int num_sms) {
+    const uint32_t nbx8 = (d0 + 7) / 8;
+    const size_t m      = nrows * nbx8;
+    if (m == 0) return VSZ_OK;
+    long long want = (long long)((m + 255) / 256), cap = (long long)num_sms * 8;
+    k_count_zeros_b8<<<(int)(want < cap ? want : cap), 256, 0, st>>>(codes, d0, nbx8, m, blk_zero);
+    count_launch();
+    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+}
+
+bool dq_w8_applies(const DqDecArgs& a, int ndim) {
+    return ndim == 3 && !a.pad.vals && a.n <= kW8MaxN && (a.blk_off || a.n_outliers == 0) &&
+           getenv("VSZ_DQ_NO_WAVEFRONT") == nullptr;
+}
+
+// ------------------------------------------------------------------------------------------
 // General block sizes (16, 32, 64; also 8): one thread per block row, skewed pipeline.
 // Thread t (row y = t of the block) visits its elements in (z, x) order one step behind thread
 // t - 1, so every neighbour it reads was written in an earlier step; planes alternate between
@@ -834,6 +984,15 @@ int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cuda
     if (bs == 8 && !force_general) {
         dq_b8_geometry(a, ndim);
         const bool vec = dq_b8_vec(a);
+        if (dq_w8_applies(a, ndim)) {  // small 3D field: the wavefront pass
+            a.nunits = (unsigned long long)((a.nbx8 + 3) / 4) * a.nyb * ((a.d2 + 7) / 8);
+            const long long want = (long long)((a.nunits + 3) / 4), cap = (long long)num_sms * 16;
+            const int grid = (int)(want < cap ? want : cap);
+            if (vec) k_dq_decompress_w8<true><<<grid, 128, 0, st>>>(a);
+            else k_dq_decompress_w8<false><<<grid, 128, 0, st>>>(a);
+            count_launch();
+            return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+        }
         if (!a.pad.vals && !dq_b8_separable(a, ndim)) dq_b8_narrow(a, ndim);  // the reference-order kernel
         long long want = (long long)((a.nunits + 3) / 4);
         long long cap  = (long long)num_sms * 16;

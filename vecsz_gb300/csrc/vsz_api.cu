@@ -148,6 +148,8 @@ struct DecompressWs {
     unsigned long long* s_out_begin;
     int* s_changed;
     float* outliers;
+    uint32_t* blk_zero;             // zero codes per (row, x-block of 8): small 3D fields only
+    unsigned long long* blk_off;    // their exclusive scan (outlier rank of each row's block)
     uint32_t* redo;  // units of the separable reverse Lorenzo that the reference-order kernel redoes
     unsigned long long* dq_cache;  // the last dequantization check (k_dq_mul_verify), at a fixed offset
     size_t bytes;
@@ -176,8 +178,11 @@ DecompressWs layout_decompress(const Geometry& g, int dict, size_t payload_bytes
     w.seg_off  = b.take<unsigned long long>(nsegd + 1);
     w.chunk_zero = b.take<uint32_t>(n_index_chunks + 1);
     w.chunk_off  = b.take<unsigned long long>(n_index_chunks + 1);
+    const size_t nblk = (g.ndim == 3 && g.n <= kW8MaxN) ? g.nrows * ((g.d0 + 7) / 8) : 0;
+    w.blk_zero = b.take<uint32_t>(nblk + 1);
+    w.blk_off  = b.take<unsigned long long>(nblk + 1);
     size_t nsync = (payload_bytes * 8 + kSyncBits - 1) / kSyncBits + 1;
-    size_t scan_n = nsegd;
+    size_t scan_n = nsegd > nblk ? nsegd : nblk;
     if (n_index_chunks > scan_n) scan_n = n_index_chunks;
     if (nsync > scan_n) scan_n = nsync;
     w.scan_status  = b.take<unsigned long long>(scan_tmp_tiles(scan_n) + 1);
@@ -1088,9 +1093,20 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     // outliers (over 1 in 1024 elements) the per-segment zero counts are cheaper
     const bool dense_outliers = d->n_outlier > g.n / 1024;
     const bool chunk_rank     = idx != nullptr && bs == 8 && d->node_count > 1 && !force_general && !dense_outliers;
+    // small 3D fields (the wavefront pass): zeros before each row's x-block of 8
+    DqDecArgs probe{};
+    probe.n          = g.n;
+    probe.n_outliers = d->n_outlier;
+    probe.blk_off    = w.blk_off;
+    probe.pad        = pad_view_of(d, bs, d_archive);
+    const bool blk_rank = bs == 8 && !force_general && d->n_outlier != 0 && dq_w8_applies(probe, g.ndim);
     {
         StageTimer t(kStZeroScan, st);
-        if (chunk_rank) {
+        if (blk_rank) {
+            VSZ_TRY(launch_count_zeros_b8(w.code, g.d0, g.nrows, w.blk_zero, st, num_sms()));
+            VSZ_TRY(launch_scan_u32(w.blk_zero, w.blk_off, g.nrows * ((g.d0 + 7) / 8), w.scan_status, w.scan_counter,
+                                    w.scan_total, w.status, st));
+        } else if (chunk_rank) {
             VSZ_TRY(launch_scan_u32(w.chunk_zero, w.chunk_off, d->n_chunks, w.scan_status, w.scan_counter,
                                     w.scan_total, w.status, st));
         } else {
@@ -1126,6 +1142,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     a.redo   = w.redo;
     a.consts_rw = w.consts;
     a.dq_cache  = w.dq_cache;
+    a.blk_off   = blk_rank ? w.blk_off : nullptr;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

@@ -159,7 +159,13 @@ struct DqDecArgs {
                                          // large field records its dequantization check there (or null)
     unsigned long long* dq_cache;        // 4 words kept across calls: the last check's c_d and result
                                          // (or null)
+    const unsigned long long* blk_off;   // 3D block 8, fields of at most kW8MaxN elements: exclusive
+                                         // zero-code offsets per (row, x-block of 8), or null
 };
+
+// 3D block-8 fields up to this many elements take the wavefront reverse Lorenzo
+// (k_dq_decompress_w8), which ranks outliers from per-(row, x-block) zero offsets.
+constexpr size_t kW8MaxN = size_t(1) << 24;
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
 // Block size 8: unit geometry (nxs, nyb, nunits), whether the 16-byte row path applies, and
@@ -170,6 +176,12 @@ void dq_b8_geometry(DqDecArgs& a, int ndim);
 void dq_b8_narrow(DqDecArgs& a, int ndim);
 bool dq_b8_vec(const DqDecArgs& a);
 bool dq_b8_separable(const DqDecArgs& a, int ndim);
+// The wavefront pass applies: 3D, no padding, at most kW8MaxN elements, blk_off given (or no
+// outliers), and VSZ_DQ_NO_WAVEFRONT unset.
+bool dq_w8_applies(const DqDecArgs& a, int ndim);
+// Zero codes per (row, x-block of 8), row-major: nrows * ceil(d0 / 8) counts.
+int launch_count_zeros_b8(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* blk_zero, cudaStream_t st,
+                          int num_sms);
 // Many fields of one class (ndim, vec, separable), block size 8, no padding: tasks of (field,
 // unit range), one warp each, handed out through the counter `next` (zero on entry; the class's
 // own word).  A separable class is followed by launch_dq_redo_batch over its fields.
