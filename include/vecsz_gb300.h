@@ -208,9 +208,9 @@ vsz_status vsz_huffman_build(const uint64_t* d_hist, int dict_size, void* d_code
 vsz_status vsz_huffman_build_host(const uint64_t* h_hist, int dict_size, void* h_codebook, uint8_t* h_huff_head,
                                   uint32_t h_info[4]);
 
-/* Where vsz_compress builds the Huffman tree.  VSZ_TREE_HOST (the default): the histogram is
- * copied to pinned host memory, a host function enqueued on the same stream builds the tree, and
- * async copies bring the codebook and tree back -- stream-ordered, no synchronisation of the
+/* Where vsz_compress builds the Huffman tree.  VSZ_TREE_HOST (the default): a kernel on the same
+ * stream posts the histogram in pinned host memory, a library host thread builds the tree there,
+ * and the kernel brings the codebook and tree back -- stream-ordered, no synchronisation of the
  * calling thread.  Streams under graph capture always use the device builder.  VSZ_TREE_DEVICE: the
  * one-CTA device builder (vsz_huffman_build).  The environment variable VSZ_TREE_BUILD=device
  * selects the device builder at load.  Process-wide; returns the previous setting (a negative
@@ -562,6 +562,14 @@ vsz_status vsz_decompress_host_f64(const uint8_t* h_archive, size_t len, size_t 
  * status word (VSZ_ERR_TIMEOUT when the wait ran out) in *h_status. */
 vsz_status vsz_debug_set_spin_limit(long long polls);
 vsz_status vsz_debug_scan_stalled_predecessor(size_t n, int* h_status);
+
+/* The host tree build of vsz_compress is a handoff: a kernel posts the histogram in pinned memory
+ * and waits for a host worker thread's answer, at most a bounded time (2 s), then records
+ * VSZ_ERR_TIMEOUT in the call's status word and returns.  vsz_debug_tree_hold(1) makes the worker
+ * leave new requests unanswered (0: answer them again, the held ones too);
+ * vsz_debug_set_tree_wait_ns sets the kernel's bound for later calls (ns <= 0: the default). */
+vsz_status vsz_debug_tree_hold(int hold);
+vsz_status vsz_debug_set_tree_wait_ns(long long ns);
 
 /* Three environment variables, read by vsz_decompress on every call, make it take another of its
  * kernels for the same result, so that tests can compare the kernels on one archive:

@@ -49,3 +49,27 @@ def test_spin_limit_argument_checks(cuda):
     assert lib.vsz_debug_scan_stalled_predecessor(0, C.byref(st)) == L.VSZ_ERR_INVALID
     assert lib.vsz_debug_scan_stalled_predecessor((1 << 24) + 1, C.byref(st)) == L.VSZ_ERR_INVALID
     assert lib.vsz_debug_set_spin_limit(0) == L.VSZ_OK
+
+
+def test_tree_handoff_wait_runs_out_and_reports_timeout(cuda):
+    """The host tree build is a handoff: a kernel posts the histogram and waits, bounded, for the
+    host worker's answer.  With the worker holding its answers and the bound lowered to 50 ms, a
+    compress records VSZ_ERR_TIMEOUT instead of hanging; once the worker answers again, the next
+    compress is the oracle's archive."""
+    lib = L.lib()
+    x = fields.grf_3d(16, 24, 40, seed=6).ravel()
+    dims = (40, 24, 16)
+    L.check(lib.vsz_debug_set_tree_wait_ns(50_000_000), "set tree wait")
+    L.check(lib.vsz_debug_tree_hold(1), "hold")
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(V.VszError) as e:
+            V.compress(x, dims, eb=1e-3, mode="r2r", dict_size=1024, block_size=8)
+        assert e.value.status == L.VSZ_ERR_TIMEOUT
+        assert time.perf_counter() - t0 < 10.0
+    finally:
+        L.check(lib.vsz_debug_tree_hold(0), "release")
+        L.check(lib.vsz_debug_set_tree_wait_ns(0), "restore tree wait")
+    c = V.compress(x, dims, eb=1e-3, mode="r2r", dict_size=1024, block_size=8)
+    oa, _ = O.compress(x, dims, 8, 1024, 1e-3, True)
+    assert c.data[: c.data_size] == oa

@@ -123,6 +123,8 @@ _PROTOS = {
     "vsz_launch_count": ([], C.c_uint64),
     "vsz_debug_set_spin_limit": ([C.c_longlong], _i),
     "vsz_debug_scan_stalled_predecessor": ([_sz, C.POINTER(C.c_int)], _i),
+    "vsz_debug_tree_hold": ([C.c_int], _i),
+    "vsz_debug_set_tree_wait_ns": ([C.c_longlong], _i),
     "vsz_batch_workspace_bytes": ([_p, _i, C.POINTER(C.c_size_t)], _i),
     "vsz_batch_create": ([_p, _i, _p, _sz, _p, C.POINTER(C.c_void_p)], _i),
     "vsz_batch_compress": ([_p, _p], _i),

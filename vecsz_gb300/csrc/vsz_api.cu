@@ -1,12 +1,15 @@
 // C ABI of the library (include/vecsz_gb300.h): argument checks, workspace layout and the
 // stream-ordered compress / decompress pipelines built from the kernels in dq_*.cu and huffman.cu.
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "api_common.cuh"
@@ -317,15 +320,18 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
 // The tree build replays the reference's binary heap one operation at a time: ~20k dependent,
 // branchy steps on a few KB for a 1024-symbol dictionary.  One GPU thread runs that chain at
 // shared-memory latency; a host core runs it from L1, several times faster.  The step stays in
-// stream order: the histogram comes down by an async copy, a host function on the stream builds
-// the tree into pinned staging, and two async copies put the codebook into the workspace and the
-// serialised tree into the archive.  Nothing returns to the caller's thread and nothing
-// synchronises.  Under stream capture (a CUDA graph) the device builder k_huff_build is used.
+// stream order as one kernel, k_tree_handoff: it writes the histogram into mapped pinned staging,
+// posts a request number there and waits (bounded) for the host worker thread, which polls the
+// staging areas of queued requests, builds the tree and answers with the same number; the kernel
+// then copies the codebook into the workspace and the serialised tree into the archive.  Nothing
+// returns to the caller's thread and nothing synchronises.  Under stream capture (a CUDA graph)
+// the device builder k_huff_build is used.
 //
-// The three small transfers are made by a kernel's loads and stores to the mapped pinned area,
-// not by the copy engines: a copy engine serves its queue in order, so with several streams in
-// flight a few-KB histogram or codebook copy would wait behind another stream's field-sized
-// transfer, and the Huffman stage of this compress with it.
+// A stream host function (cudaLaunchHostFunc) between two copy kernels did the same at 0.12 ms a
+// build; the handoff takes 0.056 ms.  The small transfers are loads and stores of a kernel to the
+// mapped area, not copy-engine copies: a copy engine serves its queue in order, so with several
+// streams in flight a few-KB histogram or codebook copy would wait behind another stream's
+// field-sized transfer, and the Huffman stage of this compress with it.
 
 std::atomic<int> g_tree_builder{-1};
 
@@ -340,8 +346,11 @@ int tree_builder() {
     return v;
 }
 
-// One pinned staging area: [hist dict x u64][codebook block][tree head].  A slot is reused once the
-// event recorded after its last upload has completed.
+// One pinned staging area: [hist dict x u64][codebook block][tree head][flags: request, answer].
+// The stream hands the histogram to the host and takes the codebook and tree back in one kernel
+// (k_tree_handoff): it posts the histogram and a request number in the staging area and waits,
+// bounded, for a host worker thread to answer with the same number.  A slot is reused once the
+// event recorded after its kernel has completed and the worker has let it go.
 struct TreeSlot {
     int device    = -1;
     int dict_cap  = 0;
@@ -351,41 +360,163 @@ struct TreeSlot {
     uint8_t* pinned = nullptr;
     uint8_t* pinned_dev = nullptr;  // the same area as the device addresses it
     cudaEvent_t done = nullptr;
-    size_t hist_off = 0, cb_off = 0, head_off = 0;
+    size_t hist_off = 0, cb_off = 0, head_off = 0, flags_off = 0;
+    uint32_t seq = 0;                    // this use's request number (never 0)
+    std::atomic<bool> in_worker{false};  // queued to the worker, not yet answered or dropped
+    std::atomic<bool> cancel{false};     // the enqueue failed: the worker drops the request
 };
 
-__global__ void __launch_bounds__(256) k_link_copy(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
-                                                   size_t bytes) {
-    const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const size_t nt  = (size_t)gridDim.x * blockDim.x;
-    size_t head      = 0;
-    if ((((uintptr_t)dst | (uintptr_t)src) & 15) == 0) {
-        head = bytes & ~(size_t)15;
-        for (size_t i = tid; i < head / 16; i += nt)
-            reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
-    }
-    for (size_t i = head + tid; i < bytes; i += nt) dst[i] = src[i];
-    __threadfence_system();
-}
+// Copies the histogram (hist_bytes) into the staging area, posts `seq` in flags[0], waits until the
+// host answers `seq` in flags[1] (or wait_ns pass: VSZ_ERR_TIMEOUT, nothing copied back), then
+// copies the codebook block and the tree head to the device.  One block of kHandoffThreads: every
+// thread issues all its reads of host memory before it stores anything, in 16-byte pieces, so
+// the answer crosses the host link in about one round trip even when bulk copies of other
+// streams queue ahead of it.
+constexpr int kHandoffThreads = 1024;
+constexpr int kHandoffUnroll  = 4;
 
-int launch_link_copy(void* dst, const void* src, size_t bytes, cudaStream_t st) {
-    if (bytes == 0) return VSZ_OK;
-    const unsigned blocks = (unsigned)std::min<size_t>(32, (bytes + 4095) / 4096);
-    k_link_copy<<<blocks, 256, 0, st>>>(static_cast<uint8_t*>(dst), static_cast<const uint8_t*>(src), bytes);
-    count_launch();
-    return cudaGetLastError() == cudaSuccess ? VSZ_OK : VSZ_ERR_CUDA;
+__global__ void __launch_bounds__(kHandoffThreads)
+    k_tree_handoff(const uint8_t* __restrict__ hist, uint8_t* pin, size_t hist_off, size_t hist_bytes, size_t cb_off,
+                   uint8_t* __restrict__ cb_block, size_t cb_bytes, size_t head_off, uint8_t* __restrict__ huff_out,
+                   size_t head_bytes, size_t flags_off, uint32_t seq, long long wait_ns, int* status) {
+    __shared__ int s_ok;
+    const unsigned t = threadIdx.x;
+    // 8-byte histogram words into the 256-byte aligned staging block (bytes from a workspace that
+    // the caller did not align)
+    if ((reinterpret_cast<uintptr_t>(hist) & 7u) == 0) {
+        for (size_t i = t; i < hist_bytes / 8; i += blockDim.x)
+            reinterpret_cast<unsigned long long*>(pin + hist_off)[i] = reinterpret_cast<const unsigned long long*>(hist)[i];
+    } else {
+        for (size_t i = t; i < hist_bytes; i += blockDim.x) pin[hist_off + i] = hist[i];
+    }
+    __threadfence_system();
+    __syncthreads();
+    volatile uint32_t* flags = reinterpret_cast<volatile uint32_t*>(pin + flags_off);
+    if (t == 0) {
+        flags[0] = seq;
+        __threadfence_system();
+        unsigned long long t0, now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        bool ok = false;
+        for (;;) {
+            if (flags[1] == seq) {
+                ok = true;
+                break;
+            }
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+            if ((long long)(now - t0) > wait_ns) break;
+            __nanosleep(500);
+        }
+        __threadfence_system();
+        if (!ok) set_status(status, VSZ_ERR_TIMEOUT);
+        s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    // the answer, read past the caches (the host wrote it after the kernel started): the codebook
+    // block (16-byte aligned at both ends but its tail) and the head (aligned in the staging area,
+    // not in the archive: stored byte by byte)
+    const bool cb16       = (reinterpret_cast<uintptr_t>(cb_block) & 15u) == 0;
+    const uint4* cb_src   = reinterpret_cast<const uint4*>(pin + cb_off);
+    const uint4* head_src = reinterpret_cast<const uint4*>(pin + head_off);
+    const size_t n_cb = cb_bytes / 16, n_head = (head_bytes + 15) / 16, n_all = n_cb + n_head;
+    for (size_t base = 0; base < n_all; base += (size_t)kHandoffUnroll * blockDim.x) {
+        uint4 v[kHandoffUnroll];
+#pragma unroll
+        for (int u = 0; u < kHandoffUnroll; u++) {
+            const size_t i = base + (size_t)u * blockDim.x + t;
+            if (i < n_all) v[u] = __ldcv(i < n_cb ? cb_src + i : head_src + (i - n_cb));
+        }
+#pragma unroll
+        for (int u = 0; u < kHandoffUnroll; u++) {
+            const size_t i = base + (size_t)u * blockDim.x + t;
+            const uint32_t w[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+            if (i < n_cb && cb16) {
+                reinterpret_cast<uint4*>(cb_block)[i] = v[u];
+            } else if (i < n_cb) {
+#pragma unroll
+                for (int k = 0; k < 16; k++) cb_block[i * 16 + k] = (uint8_t)(w[k >> 2] >> (8 * (k & 3)));
+            } else if (i < n_all) {
+                const size_t o = (i - n_cb) * 16;
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    if (o + k < head_bytes) huff_out[o + k] = (uint8_t)(w[k >> 2] >> (8 * (k & 3)));
+            }
+        }
+    }
+    for (size_t i = n_cb * 16 + t; i < cb_bytes; i += blockDim.x)
+        cb_block[i] = __ldcv(reinterpret_cast<const unsigned char*>(pin + cb_off) + i);
 }
 
 std::mutex g_slot_mu;
 std::vector<TreeSlot*> g_slots;
+std::atomic<long long> g_tree_wait_ns{2000000000ll};  // the handoff's bound: 2 s
 
-void host_tree_callback(void* p) {
-    TreeSlot* s    = static_cast<TreeSlot*>(p);
+// The host side of the handoff: one thread for the process, started on first use and never
+// destroyed (it may outlive static destructors).  While requests are queued it polls their
+// request words and builds each tree as soon as its stream has posted the histogram.
+struct TreeWorker {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<TreeSlot*> queued;
+    std::atomic<int> hold{0};  // test hook: leave requests unanswered while set
+};
+
+void answer_tree(TreeSlot* s) {
     const int dict = s->dict;
     uint8_t* cb    = s->pinned + s->cb_off;
     host_huffman_build(reinterpret_cast<const uint64_t*>(s->pinned + s->hist_off), dict,
                        reinterpret_cast<uint64_t*>(cb), cb + 8 * (size_t)dict + 16,
                        reinterpret_cast<uint32_t*>(cb + 8 * (size_t)dict), s->pinned + s->head_off, s->hdr_dict);
+    __atomic_store_n(reinterpret_cast<uint32_t*>(s->pinned + s->flags_off) + 1, s->seq, __ATOMIC_RELEASE);
+}
+
+void tree_worker_loop(TreeWorker* w) {
+    using clk = std::chrono::steady_clock;
+    std::vector<std::pair<TreeSlot*, clk::time_point>> mine;
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(w->mu);
+            if (mine.empty()) w->cv.wait(lk, [&] { return !w->queued.empty(); });
+            for (TreeSlot* s : w->queued) mine.emplace_back(s, clk::now());
+            w->queued.clear();
+        }
+        bool progress = false;
+        for (size_t i = 0; i < mine.size();) {
+            TreeSlot* s    = mine[i].first;
+            bool drop      = s->cancel.load(std::memory_order_acquire);
+            const uint32_t req = __atomic_load_n(reinterpret_cast<uint32_t*>(s->pinned + s->flags_off), __ATOMIC_ACQUIRE);
+            if (!drop && req == s->seq && !w->hold.load(std::memory_order_relaxed)) {
+                answer_tree(s);
+                drop = true;
+            } else if (!drop && clk::now() - mine[i].second > std::chrono::seconds(1)) {
+                // not posted after a second: keep waiting unless the stream failed for good (the
+                // event was recorded at enqueue; a kernel that ran would have posted first)
+                cudaSetDevice(s->device);
+                const cudaError_t e = cudaEventQuery(s->done);
+                if (e != cudaErrorNotReady && e != cudaSuccess) drop = true;
+                mine[i].second = clk::now();
+            }
+            if (drop) {
+                s->in_worker.store(false, std::memory_order_release);
+                mine[i] = mine.back();
+                mine.pop_back();
+                progress = true;
+            } else {
+                i++;
+            }
+        }
+        if (!progress) std::this_thread::yield();
+    }
+}
+
+TreeWorker* tree_worker() {
+    static TreeWorker* w = [] {
+        TreeWorker* t = new TreeWorker();
+        std::thread(tree_worker_loop, t).detach();
+        return t;
+    }();
+    return w;
 }
 
 TreeSlot* acquire_tree_slot(int dict) {
@@ -394,7 +525,8 @@ TreeSlot* acquire_tree_slot(int dict) {
     std::lock_guard<std::mutex> g(g_slot_mu);
     for (TreeSlot* s : g_slots) {
         if (s->reserved || s->device != dev || s->dict_cap < dict) continue;
-        if (cudaEventQuery(s->done) != cudaSuccess) continue;  // an upload from it is still queued
+        if (s->in_worker.load(std::memory_order_acquire)) continue;  // the worker still holds it
+        if (cudaEventQuery(s->done) != cudaSuccess) continue;         // its kernel is still queued
         s->reserved = true;
         return s;
     }
@@ -404,11 +536,13 @@ TreeSlot* acquire_tree_slot(int dict) {
     s->hist_off   = 0;
     s->cb_off     = (8 * (size_t)dict + 255) & ~(size_t)255;
     s->head_off   = (s->cb_off + codebook_block_bytes(dict) + 255) & ~(size_t)255;
-    size_t bytes  = s->head_off + tree_head_max(dict);
+    s->flags_off  = (s->head_off + tree_head_max(dict) + 255) & ~(size_t)255;
+    size_t bytes  = s->flags_off + 64;
     if (cudaHostAlloc(reinterpret_cast<void**>(&s->pinned), bytes, cudaHostAllocDefault) != cudaSuccess) {
         delete s;
         return nullptr;
     }
+    memset(s->pinned + s->flags_off, 0, 64);
     if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->pinned_dev), s->pinned, 0) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
@@ -430,18 +564,31 @@ void release_tree_slot(TreeSlot* s) {
 // [BE nc][BE hdr_dict][tree] at huff_out (device archive; up to tree_head_max(dict) bytes are
 // written, the bytes past the tree are overwritten by the encoder that follows).
 int enqueue_host_tree(const unsigned long long* hist, int dict, int hdr_dict, uint8_t* cb_block, uint8_t* huff_out,
-                      cudaStream_t st) {
-    TreeSlot* s = acquire_tree_slot(dict);
+                      int* status, cudaStream_t st) {
+    TreeWorker* w = tree_worker();
+    TreeSlot* s   = acquire_tree_slot(dict);
     if (!s) return VSZ_ERR_CUDA;
     s->dict     = dict;
     s->hdr_dict = hdr_dict;
-    int rc  = VSZ_OK;
-    if (launch_link_copy(s->pinned_dev + s->hist_off, hist, 8 * (size_t)dict, st) != VSZ_OK ||
-        cudaLaunchHostFunc(st, host_tree_callback, s) != cudaSuccess ||
-        launch_link_copy(cb_block, s->pinned_dev + s->cb_off, codebook_block_bytes(dict), st) != VSZ_OK ||
-        launch_link_copy(huff_out, s->pinned_dev + s->head_off, tree_head_max(dict), st) != VSZ_OK)
+    if (++s->seq == 0) s->seq = 1;
+    s->cancel.store(false, std::memory_order_relaxed);
+    s->in_worker.store(true, std::memory_order_release);
+    {
+        std::lock_guard<std::mutex> g(w->mu);
+        w->queued.push_back(s);
+    }
+    w->cv.notify_one();
+    int rc = VSZ_OK;
+    k_tree_handoff<<<1, kHandoffThreads, 0, st>>>(reinterpret_cast<const uint8_t*>(hist), s->pinned_dev, s->hist_off,
+                                      8 * (size_t)dict, s->cb_off, cb_block, codebook_block_bytes(dict), s->head_off,
+                                      huff_out, tree_head_max(dict), s->flags_off, s->seq,
+                                      g_tree_wait_ns.load(std::memory_order_relaxed), status);
+    count_launch();
+    if (cudaGetLastError() != cudaSuccess) {
+        s->cancel.store(true, std::memory_order_release);
         rc = VSZ_ERR_CUDA;
-    // recorded even after a failed enqueue, so the slot is not reused while anything queued reads it
+    }
+    // recorded even after a failed launch, so the slot is not reused while anything queued reads it
     if (cudaEventRecord(s->done, st) != cudaSuccess) rc = VSZ_ERR_CUDA;
     release_tree_slot(s);
     return rc;
@@ -831,7 +978,7 @@ vsz_status vsz_compress(const vsz_params* p, int ndim, const size_t dims[3], con
         StageTimer t(kStHuffBuild, st);
         if (tree_builder() == VSZ_TREE_HOST && !stream_capturing(st)) {
             huff_build_prepare();  // a later captured call takes the device builder
-            VSZ_TRY(enqueue_host_tree(w.hist, nsym, dict, w.cb_block, d_archive + huff_off, st));
+            VSZ_TRY(enqueue_host_tree(w.hist, nsym, dict, w.cb_block, d_archive + huff_off, w.status, st));
         } else
             VSZ_TRY(launch_huff_build(hb, st));
     }
@@ -1164,6 +1311,16 @@ vsz_status vsz_debug_set_spin_limit(long long polls) {
 
 vsz_status vsz_debug_scan_stalled_predecessor(size_t n, int* h_status) { return debug_scan_stalled(n, h_status); }
 
+vsz_status vsz_debug_tree_hold(int hold) {
+    tree_worker()->hold.store(hold ? 1 : 0, std::memory_order_relaxed);
+    return VSZ_OK;
+}
+
+vsz_status vsz_debug_set_tree_wait_ns(long long ns) {
+    g_tree_wait_ns.store(ns > 0 ? ns : 2000000000ll, std::memory_order_relaxed);
+    return VSZ_OK;
+}
+
 }  // extern "C"
 
 // =================================================================================================
@@ -1310,7 +1467,7 @@ vsz_status vsz_compress_f64(const vsz_params* p, int ndim, const size_t dims[3],
         StageTimer t(kStHuffBuild, st);
         if (tree_builder() == VSZ_TREE_HOST && !stream_capturing(st)) {
             huff_build_prepare();
-            VSZ_TRY(enqueue_host_tree(w.hist, dict, dict, w.cb_block, d_archive + huff_off, st));
+            VSZ_TRY(enqueue_host_tree(w.hist, dict, dict, w.cb_block, d_archive + huff_off, w.status, st));
         } else
             VSZ_TRY(launch_huff_build(hb, st));
     }
