@@ -692,8 +692,11 @@ int launch_count_zeros_b8(const uint16_t* codes, uint32_t d0, size_t nrows, uint
 }
 
 bool dq_w8_applies(const DqDecArgs& a, int ndim) {
-    return ndim == 3 && !a.pad.vals && a.n <= kW8MaxN && (a.blk_off || a.n_outliers == 0) &&
-           getenv("VSZ_DQ_NO_WAVEFRONT") == nullptr;
+    if (ndim != 3 || a.pad.vals || a.n > kW8MaxN || !(a.blk_off || a.n_outliers == 0)) return false;
+    if (getenv("VSZ_DQ_NO_WAVEFRONT") != nullptr) return false;
+    // the separable pass catches up with the wavefront between 160^3 and 256^3 (measured: 0.123
+    // vs 0.060 ms at 160^3, 0.099 vs 0.127 ms at 256^3, zero scans included)
+    return a.n <= kW8MaxSeparableN || !dq_b8_separable(a, ndim);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -687,6 +687,8 @@ __device__ __forceinline__ uint32_t rd_index(const uint8_t* p, int w) {
 }
 
 // The decode tables of one field, by the whole CTA (1024 threads; returns are block-uniform).
+constexpr int kTableSmemNodes = 4096;
+
 __device__ __forceinline__ void huff_table_run(const HuffTableArgs& a) {
     const uint8_t* h = a.huff;
     __shared__ uint32_t s_nc;
@@ -710,7 +712,11 @@ __device__ __forceinline__ void huff_table_run(const HuffTableArgs& a) {
     const uint8_t* pR = pL + (size_t)w * nc;
     const uint8_t* pC = pR + (size_t)w * nc;
     const uint8_t* pT = pC + 4 * (size_t)nc;
-    uint32_t* parent  = a.parent;  // nc entries: parent << 1 | side; 0xffffffff = none
+    // nc entries: parent << 1 | side; 0xffffffff = none.  In shared memory for trees of up to
+    // kTableSmemNodes nodes (dictionaries up to 2048 symbols): every node's depth and code come
+    // from a walk up to the root, one dependent read per level, twice.
+    __shared__ uint32_t s_parent[kTableSmemNodes];
+    uint32_t* parent  = nc <= (uint32_t)kTableSmemNodes ? s_parent : a.parent;
     for (uint32_t i = threadIdx.x; i < nc; i += blockDim.x) parent[i] = 0xffffffffu;
     for (uint32_t i = threadIdx.x; i < (1u << kDecBits); i += blockDim.x) a.table[i] = 0u;
     __syncthreads();
@@ -781,6 +787,7 @@ __device__ __forceinline__ void huff_table_run(const HuffTableArgs& a) {
         }
         return true;
     };
+    const bool table16 = (reinterpret_cast<uintptr_t>(a.table) & 15u) == 0;
     // pass 1: primary entries; width of the secondary table below every depth-kDecBits prefix
     for (uint32_t i = threadIdx.x; i < (1u << kDecBits); i += blockDim.x) s_w2[i] = 0u;
     if (threadIdx.x == 0) s_maxlen = 0u;
@@ -798,7 +805,14 @@ __device__ __forceinline__ void huff_table_run(const HuffTableArgs& a) {
             uint32_t lo = (uint32_t)(code << (kDecBits - depth));
             uint32_t hi = lo + (1u << (kDecBits - depth));
             uint32_t e  = ((a.node_sym[i] & 0xffffu) << 8) | depth;
-            for (uint32_t t = lo; t < hi; t++) a.table[t] = e;
+            // a short codeword fills up to 2^(kDecBits - 1) entries: 16 bytes at a time (lo and hi
+            // are multiples of 4 when depth <= kDecBits - 2)
+            if (hi - lo >= 4 && table16) {
+                const uint4 e4 = make_uint4(e, e, e, e);
+                for (uint32_t t = lo; t < hi; t += 4) *reinterpret_cast<uint4*>(a.table + t) = e4;
+            } else {
+                for (uint32_t t = lo; t < hi; t++) a.table[t] = e;
+            }
         } else if (!leaf && depth == (uint32_t)kDecBits) {
             a.table[(uint32_t)code] = (i << 8);  // walk from node i (until a secondary table replaces it)
         } else if (leaf && depth > (uint32_t)kDecBits) {

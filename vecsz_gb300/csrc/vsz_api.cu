@@ -25,6 +25,10 @@ using namespace vsz::api;
 static_assert(sizeof(Consts) <= VSZ_CONSTS_BYTES, "Consts must fit VSZ_CONSTS_BYTES");
 
 namespace vsz {
+// A tree builder for the calling thread's next compress calls (VSZ_TREE_HOST / _DEVICE), or -1
+// for the process setting: the host-buffer operations take the device builder (vsz_host.cu).
+thread_local int t_tree_builder = -1;
+void set_thread_tree_builder(int which) { t_tree_builder = which; }
 int g_sms[64];
 int num_sms() {
     int dev = 0;
@@ -336,6 +340,7 @@ int decode_codes(const uint8_t* d_huff, size_t huff_bytes, uint32_t node_count, 
 std::atomic<int> g_tree_builder{-1};
 
 int tree_builder() {
+    if (t_tree_builder >= 0) return t_tree_builder;
     int v = g_tree_builder.load(std::memory_order_relaxed);
     if (v < 0) {
         v               = VSZ_TREE_HOST;
@@ -1240,13 +1245,30 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
     // outliers (over 1 in 1024 elements) the per-segment zero counts are cheaper
     const bool dense_outliers = d->n_outlier > g.n / 1024;
     const bool chunk_rank     = idx != nullptr && bs == 8 && d->node_count > 1 && !force_general && !dense_outliers;
+    // the reverse Lorenzo's arguments (the outlier rank source is set after the zero scan)
+    DqDecArgs a{};
+    a.codes = w.code;
+    a.outliers = w.outliers;
+    a.n_outliers = d->n_outlier;
+    a.status = w.status;
+    a.seg_off = w.seg_off;
+    a.chunk_off = chunk_rank ? w.chunk_off : nullptr;
+    a.consts = w.consts;
+    a.out = d_out;
+    a.d0 = g.d0;
+    a.d1 = g.d1;
+    a.d2 = g.d2;
+    a.n = g.n;
+    a.R = dict / 2;
+    a.strict = d->has_trailer ? d->strict : 0;
+    a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
+    a.pad    = pad_view_of(d, bs, d_archive);
+    a.redo   = w.redo;
+    a.consts_rw = w.consts;
+    a.dq_cache  = w.dq_cache;
     // small 3D fields (the wavefront pass): zeros before each row's x-block of 8
-    DqDecArgs probe{};
-    probe.n          = g.n;
-    probe.n_outliers = d->n_outlier;
-    probe.blk_off    = w.blk_off;
-    probe.pad        = pad_view_of(d, bs, d_archive);
-    const bool blk_rank = bs == 8 && !force_general && d->n_outlier != 0 && dq_w8_applies(probe, g.ndim);
+    a.blk_off = w.blk_off;
+    const bool blk_rank = bs == 8 && !force_general && d->n_outlier != 0 && dq_w8_applies(a, g.ndim);
     {
         StageTimer t(kStZeroScan, st);
         if (blk_rank) {
@@ -1269,27 +1291,7 @@ vsz_status vsz_decompress(const vsz_archive_desc* d, const vsz_decompress_opts* 
         VSZ_CUDA(cudaMemcpyAsync(w.outliers, d_archive + d->outlier_offset, 4 * d->n_outlier, cudaMemcpyDeviceToDevice,
                                  st));
     }
-    DqDecArgs a{};
-    a.codes = w.code;
-    a.outliers = w.outliers;
-    a.n_outliers = d->n_outlier;
-    a.status = w.status;
-    a.seg_off = w.seg_off;
-    a.chunk_off = chunk_rank ? w.chunk_off : nullptr;
-    a.consts = w.consts;
-    a.out = d_out;
-    a.d0 = g.d0;
-    a.d1 = g.d1;
-    a.d2 = g.d2;
-    a.n = g.n;
-    a.R = dict / 2;
-    a.strict = d->has_trailer ? d->strict : 0;
-    a.xtail  = (g.ndim == 3 && (g.d0 % 8) != 0) ? (g.d0 & ~7u) : g.d0;
-    a.pad    = pad_view_of(d, bs, d_archive);
-    a.redo   = w.redo;
-    a.consts_rw = w.consts;
-    a.dq_cache  = w.dq_cache;
-    a.blk_off   = blk_rank ? w.blk_off : nullptr;
+    a.blk_off = blk_rank ? w.blk_off : nullptr;
     {
         StageTimer t(kStLorenzoDecompress, st);
         VSZ_TRY(launch_dq_decompress(a, d->ndim, bs, force_general, st, num_sms()));

@@ -166,6 +166,8 @@ struct DqDecArgs {
 // 3D block-8 fields up to this many elements take the wavefront reverse Lorenzo
 // (k_dq_decompress_w8), which ranks outliers from per-(row, x-block) zero offsets.
 constexpr size_t kW8MaxN = size_t(1) << 24;
+// ... and those that would take the separable pass only up to this many.
+constexpr size_t kW8MaxSeparableN = size_t(1) << 23;
 
 int launch_dq_decompress(DqDecArgs a, int ndim, int bs, bool force_general, cudaStream_t st, int num_sms);
 // Block size 8: unit geometry (nxs, nyb, nunits), whether the 16-byte row path applies, and
@@ -176,8 +178,8 @@ void dq_b8_geometry(DqDecArgs& a, int ndim);
 void dq_b8_narrow(DqDecArgs& a, int ndim);
 bool dq_b8_vec(const DqDecArgs& a);
 bool dq_b8_separable(const DqDecArgs& a, int ndim);
-// The wavefront pass applies: 3D, no padding, at most kW8MaxN elements, blk_off given (or no
-// outliers), and VSZ_DQ_NO_WAVEFRONT unset.
+// The wavefront pass applies: 3D, no padding, at most kW8MaxN elements (kW8MaxSeparableN for a
+// field the separable pass takes), blk_off given (or no outliers), VSZ_DQ_NO_WAVEFRONT unset.
 bool dq_w8_applies(const DqDecArgs& a, int ndim);
 // Zero codes per (row, x-block of 8), row-major: nrows * ceil(d0 / 8) counts.
 int launch_count_zeros_b8(const uint16_t* codes, uint32_t d0, size_t nrows, uint32_t* blk_zero, cudaStream_t st,
