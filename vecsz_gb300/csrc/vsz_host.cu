@@ -644,8 +644,8 @@ vsz_status vsz_host_op_compress(vsz_host_op* op, const vsz_params* p, int ndim, 
     VSZ_CUDA(cudaMemcpyAsync(op->in.p, h_in, n * sizeof(float), cudaMemcpyHostToDevice, op->stream));
     // The device tree builder: host operations run beside other operations' field-sized transfers
     // over the host link, and the host builder's few-KB exchange with the host then waits behind
-    // them (pipelined round trips measured at 76-81 GB/s in some runs against 117 with this
-    // builder's ~0.7 ms, which the transfers hide).
+    // them (pipelined round trips of a 512^3 field: 76, 81, 117 and 117 GB/s over four runs with
+    // the host builder; 97, 120 and 120 with this one, whose ~0.7 ms the transfers hide).
     vsz::set_thread_tree_builder(VSZ_TREE_DEVICE);
     const int rc = vsz_compress(p, ndim, dims, (const float*)op->in.p, op->ws.p, op->ws.cap, (uint8_t*)op->archive.p,
                                 op->archive.cap, (uint64_t*)op->result.p, op->stream);
