@@ -524,6 +524,11 @@ TreeWorker* tree_worker() {
     return w;
 }
 
+// Slots are made kTreeSlotBatch at a time from one pinned allocation, so that a burst of
+// concurrent compresses (a request server's slots) does not pin host memory on its critical path:
+// the first compress of a dictionary size makes them all.
+constexpr int kTreeSlotBatch = 16;
+
 TreeSlot* acquire_tree_slot(int dict) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
@@ -535,29 +540,40 @@ TreeSlot* acquire_tree_slot(int dict) {
         s->reserved = true;
         return s;
     }
-    TreeSlot* s   = new TreeSlot();
-    s->device     = dev;
-    s->dict_cap   = dict;
-    s->hist_off   = 0;
-    s->cb_off     = (8 * (size_t)dict + 255) & ~(size_t)255;
-    s->head_off   = (s->cb_off + codebook_block_bytes(dict) + 255) & ~(size_t)255;
-    s->flags_off  = (s->head_off + tree_head_max(dict) + 255) & ~(size_t)255;
-    size_t bytes  = s->flags_off + 64;
-    if (cudaHostAlloc(reinterpret_cast<void**>(&s->pinned), bytes, cudaHostAllocDefault) != cudaSuccess) {
-        delete s;
+    const size_t cb_off    = (8 * (size_t)dict + 255) & ~(size_t)255;
+    const size_t head_off  = (cb_off + codebook_block_bytes(dict) + 255) & ~(size_t)255;
+    const size_t flags_off = (head_off + tree_head_max(dict) + 255) & ~(size_t)255;
+    const size_t stride    = (flags_off + 64 + 255) & ~(size_t)255;
+    uint8_t *pinned = nullptr, *pinned_dev = nullptr;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&pinned), stride * kTreeSlotBatch, cudaHostAllocDefault) != cudaSuccess)
         return nullptr;
-    }
-    memset(s->pinned + s->flags_off, 0, 64);
-    if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->pinned_dev), s->pinned, 0) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&pinned_dev), pinned, 0) != cudaSuccess) {
         cudaGetLastError();
-        cudaFreeHost(s->pinned);
-        delete s;
+        cudaFreeHost(pinned);
         return nullptr;
     }
-    s->reserved = true;
-    g_slots.push_back(s);
-    return s;
+    TreeSlot* first = nullptr;
+    for (int k = 0; k < kTreeSlotBatch; k++) {
+        TreeSlot* s   = new TreeSlot();
+        s->device     = dev;
+        s->dict_cap   = dict;
+        s->pinned     = pinned + k * stride;
+        s->pinned_dev = pinned_dev + k * stride;
+        s->hist_off   = 0;
+        s->cb_off     = cb_off;
+        s->head_off   = head_off;
+        s->flags_off  = flags_off;
+        memset(s->pinned + s->flags_off, 0, 64);
+        if (cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            delete s;  // the slots made so far stay usable; the pinned block stays allocated
+            break;
+        }
+        g_slots.push_back(s);
+        if (!first) first = s;
+    }
+    if (first) first->reserved = true;
+    return first;
 }
 
 void release_tree_slot(TreeSlot* s) {
