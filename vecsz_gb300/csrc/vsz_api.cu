@@ -524,10 +524,12 @@ TreeWorker* tree_worker() {
     return w;
 }
 
-// Slots are made kTreeSlotBatch at a time from one pinned allocation, so that a burst of
-// concurrent compresses (a request server's slots) does not pin host memory on its critical path:
-// the first compress of a dictionary size makes them all.
-constexpr int kTreeSlotBatch = 16;
+// Slots are made up to kTreeSlotBatch at a time from one pinned allocation (at most
+// kTreeSlotBatchBytes, at least 2 slots), so that a burst of concurrent compresses (a request
+// server's slots) does not pin host memory on its critical path: the first compress of a
+// dictionary size makes them.  A 1024-symbol slot takes ~37 KB, a 65536-symbol one ~2.6 MB.
+constexpr int kTreeSlotBatch         = 16;
+constexpr size_t kTreeSlotBatchBytes = size_t(8) << 20;
 
 TreeSlot* acquire_tree_slot(int dict) {
     int dev = 0;
@@ -544,8 +546,9 @@ TreeSlot* acquire_tree_slot(int dict) {
     const size_t head_off  = (cb_off + codebook_block_bytes(dict) + 255) & ~(size_t)255;
     const size_t flags_off = (head_off + tree_head_max(dict) + 255) & ~(size_t)255;
     const size_t stride    = (flags_off + 64 + 255) & ~(size_t)255;
+    const int batch = (int)std::max<size_t>(2, std::min<size_t>(kTreeSlotBatch, kTreeSlotBatchBytes / stride));
     uint8_t *pinned = nullptr, *pinned_dev = nullptr;
-    if (cudaHostAlloc(reinterpret_cast<void**>(&pinned), stride * kTreeSlotBatch, cudaHostAllocDefault) != cudaSuccess)
+    if (cudaHostAlloc(reinterpret_cast<void**>(&pinned), stride * batch, cudaHostAllocDefault) != cudaSuccess)
         return nullptr;
     if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&pinned_dev), pinned, 0) != cudaSuccess) {
         cudaGetLastError();
@@ -553,7 +556,7 @@ TreeSlot* acquire_tree_slot(int dict) {
         return nullptr;
     }
     TreeSlot* first = nullptr;
-    for (int k = 0; k < kTreeSlotBatch; k++) {
+    for (int k = 0; k < batch; k++) {
         TreeSlot* s   = new TreeSlot();
         s->device     = dev;
         s->dict_cap   = dict;
