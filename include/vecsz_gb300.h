@@ -463,7 +463,10 @@ void vsz_free_host(void* p);
  *               out_capacity from vsz_compress_host_bound) and h_result (the 8-u64 vsz_result:
  *               data_size + trailer_size bytes of h_out are valid; status VSZ_ERR_CAPACITY when
  *               they did not fit).  The archive's size is known only on the device: a kernel
- *               copies exactly those bytes into h_out.
+ *               copies exactly those bytes into h_out.  The Huffman tree is built on the device
+ *               (as VSZ_TREE_DEVICE), whatever vsz_set_tree_builder says: these operations share
+ *               the host link with other operations' field-sized transfers, which the host
+ *               builder's small exchange would wait behind; the archive is the same.
  *   decompress: h_archive (len bytes, complete: the host parses its header) -> h_out (n floats),
  *               *h_status = VSZ_OK or the device-side error.
  *   wait:       blocks until the op's enqueued work is done; returns VSZ_ERR_CUDA if it failed. */
