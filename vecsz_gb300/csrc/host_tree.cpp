@@ -1,5 +1,6 @@
 // Heap-tree Huffman codebook built on the host, for the stream-ordered host-build mode of
-// vsz_compress (a cudaLaunchHostFunc step between the histogram and the encoder).
+// vsz_compress (the library's tree thread answers k_tree_handoff between the histogram and the
+// encoder).
 //
 // Same result as k_huff_build (huffman.cu): the reference's binary-heap priority queue replayed
 // operation for operation (src/huffman.hh:169-192, 248-262; the first qremove() of a merge is the
