@@ -686,7 +686,7 @@ def run_batch(V, n_fields, seed, reps, sample_every=25):
             "workload": f"{n_fields} mixed fields: 1D/2D/3D 20/40/40 %, 16K-16M elements log-uniform, random "
                         f"aspect ratios, k^-11/3 or smooth-bump fields, r2r eb log-uniform 1e-5..1e-2, dict 1024, "
                         f"block 8 (seed {seed})",
-            "plain_path": "vsz_compress per field on one stream (18 launches + host tree step each)",
+            "plain_path": "vsz_compress per field on one stream (11 kernel launches each, the tree by the host thread)",
             "batched_path": "vsz_batch_compress captured in a CUDA graph (one launch per stage / kernel class, "
                             "device tree build, one CTA per field)"}
 
