@@ -367,6 +367,7 @@ struct TreeSlot {
     cudaEvent_t done = nullptr;
     size_t hist_off = 0, cb_off = 0, head_off = 0, flags_off = 0;
     uint32_t seq = 0;                    // this use's request number (never 0)
+    bool dead    = false;                // its event failed (e.g. the device was reset): never reused
     std::atomic<bool> in_worker{false};  // queued to the worker, not yet answered or dropped
     std::atomic<bool> cancel{false};     // the enqueue failed: the worker drops the request
 };
@@ -499,7 +500,10 @@ void tree_worker_loop(TreeWorker* w) {
                 // event was recorded at enqueue; a kernel that ran would have posted first)
                 cudaSetDevice(s->device);
                 const cudaError_t e = cudaEventQuery(s->done);
-                if (e != cudaErrorNotReady && e != cudaSuccess) drop = true;
+                if (e != cudaErrorNotReady && e != cudaSuccess) {
+                    cudaGetLastError();
+                    drop = true;
+                }
                 mine[i].second = clk::now();
             }
             if (drop) {
@@ -536,9 +540,15 @@ TreeSlot* acquire_tree_slot(int dict) {
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
     std::lock_guard<std::mutex> g(g_slot_mu);
     for (TreeSlot* s : g_slots) {
-        if (s->reserved || s->device != dev || s->dict_cap < dict) continue;
+        if (s->dead || s->reserved || s->device != dev || s->dict_cap < dict) continue;
         if (s->in_worker.load(std::memory_order_acquire)) continue;  // the worker still holds it
-        if (cudaEventQuery(s->done) != cudaSuccess) continue;         // its kernel is still queued
+        const cudaError_t e = cudaEventQuery(s->done);
+        if (e == cudaErrorNotReady) continue;  // its kernel is still queued
+        if (e != cudaSuccess) {                 // a context torn down under it: retire the slot
+            cudaGetLastError();                 // and leave no error behind for the caller
+            s->dead = true;
+            continue;
+        }
         s->reserved = true;
         return s;
     }
